@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""Throughput of the plmDCA per-locus solve: target loci solved per second.
+
+Workload: the seeded 3000-sequence x 94,000-locus coalescent-tree alignment
+(synthetic stand-in for a genome alignment of that shape), unit sequence
+weights (SuperDCA's --no-reweighting path), automatic lambdas, gradient
+threshold 1e-3, zero start.  A step solves one batch of target loci to
+convergence (L-BFGS + More-Thuente, every locus independent); steps take
+disjoint loci.  The alignment (282 MB) and the per-slot solver state are far
+larger than the 129 MB L2, so no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+
+--impl engine (default) prints one JSON line with:
+  value       loci/s over all ranks, inputs resident in HBM, device time from
+              CUDA events around each solve (max over ranks)
+  e2e         the same metric through the C ABI with host buffers: each step
+              uploads the alignment from pinned host memory and reads the
+              score rows back
+  roofline    for the kernel class with the most device time
+  cpu_baseline the FP64 C oracle on this host's cores (rank 0, N=1)
+--impl reference times the CPU reference path (the FP64 C oracle restating
+SuperDCA's solve) on all host cores, on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+Q = 4
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--workload", default="tree-3000x94000")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--loci-per-step", type=int, default=0, help="default: batch")
+    ap.add_argument("--form", default="gather", choices=["gather", "tc"])
+    ap.add_argument("--history-bf16", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    return ap.parse_args()
+
+
+def dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device), "-f", self.path], stdout=subprocess.DEVNULL,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        try:
+            for line in open(self.path):
+                p = [v.strip() for v in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+            os.unlink(self.path)
+        except Exception:
+            return None
+        if not rows:
+            return None
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return float("nan")
+
+        sm = np.array([num(r[1]) for r in rows])
+        mx = np.array([num(r[2]) for r in rows])
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        load = sm[sm > 0.5 * np.nanmax(sm)] if np.isfinite(sm).any() else sm
+        return {"sm_mhz": float(np.nanmedian(load)) if len(load) else None,
+                "sm_max_mhz": float(np.nanmax(mx)) if np.isfinite(mx).any() else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def load_workload(args):
+    from superdca_gb300 import synthetic
+
+    st, cols, _ = synthetic.workload(args.workload, seed=args.seed)
+    return st
+
+
+def roofline(prof_tot, N, L, Dp, m, hist_bytes):
+    """Roofline of the kernel class with the most device time.
+
+    Work per unit (one target locus through one launch of the class):
+      forward / backward contraction: 2 N L q^2 FLOP (the one-hot GEMM
+        X . J or X^T . R for one locus: bound by the tensor pipe);
+      history dots: (2k+2) Dp elements read, direction (2k+2) Dp read and Dp
+        written, accept 3 Dp read/written + Dp history: bound by HBM, with k
+        the history depth (m when full)."""
+    hbm, tflops, src = measured_peaks()
+    ms, units, launches = prof_tot["kernel_ms"], prof_tot["kernel_units"], prof_tot["kernel_launches"]
+    cls = max(ms, key=lambda k: ms[k])
+    t = ms[cls] / 1e3
+    if units[cls] == 0 or t <= 0:
+        return None, cls
+    per_launch_units = units[cls] / max(1, launches[cls] / (2 if cls in ("forward", "backward", "accept") else 1))
+    if cls in ("forward", "backward"):
+        work = 2.0 * N * L * Q * Q * units[cls]
+        ach = work / t / 1e12
+        return dict(bound="tensor", achieved=round(ach, 3), peak=tflops, unit="TFLOP/s",
+                    frac=round(ach / tflops, 5), traffic=None, kernel=cls,
+                    work_per_launch=2.0 * N * L * Q * Q * per_launch_units,
+                    peak_source=src), cls
+    k = m
+    if cls == "history":
+        byts = (2 * k * hist_bytes + 2 * 4) * Dp * units[cls]
+    elif cls == "direction":
+        byts = (2 * k * hist_bytes + 3 * 4) * Dp * units[cls]
+    elif cls == "accept":
+        byts = (3 * 4 + hist_bytes) * Dp * units[cls]
+    else:
+        return None, cls
+    ach = byts / t / 1e9
+    return dict(bound="hbm", achieved=round(ach, 1), peak=hbm, unit="GB/s", frac=round(ach / hbm, 4),
+                traffic=None, kernel=cls, peak_source=src), cls
+
+
+def cpu_eval_rate(st, seconds, threads, seed=5):
+    """Full-size FP64 objective+gradient evaluations on `threads` host
+    threads (distinct loci, zero start): returns seconds per evaluation per
+    thread and the number of evaluations timed."""
+    from oracle import oracle as O
+
+    O.build()
+    N, L = st.shape
+    w = np.ones(N)
+    lh, lJ, _ = O.lambdas(w)
+    P = O.Problem(st, w, lh, lJ)
+    rng = np.random.default_rng(seed)
+    x = np.zeros(O.dim(L))
+    done, t_all = 0, 0.0
+    while t_all < seconds:
+        loci = rng.choice(L, size=threads, replace=False).astype(np.int64)
+        t0 = time.time()
+        P.eval_many(loci, x, threads=threads)
+        t_all += time.time() - t0
+        done += threads
+    return t_all * threads / done, done, t_all
+
+
+def nfeval_reference(workload):
+    path = os.path.join(ROOT, "oracle", f"nfeval_{workload}.json")
+    with open(path) as fh:
+        d = json.load(fh)
+    return float(np.median(d["nfeval"])), d
+
+
+def engine_arm(args):
+    world, rank, local = dist()
+    import torch
+
+    if world > 1:
+        import torch.distributed as tdist
+
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from superdca_gb300 import Engine, FORM_GATHER, FORM_TC
+
+    st = load_workload(args)
+    N, L = st.shape
+    w = np.ones(N)
+    B = args.batch
+    per_step = args.loci_per_step or B
+    form = FORM_TC if args.form == "tc" else FORM_GATHER
+    E = Engine(N, L, batch=B, device=local, form=form, history_bf16=args.history_bf16)
+    E.set_alignment(st, w)
+
+    def loci_for(step):
+        base = (step * world + rank) * per_step
+        return (np.arange(base, base + per_step) * 7919) % L  # spread over the genome
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(local)
+
+    for s in range(args.warmup):
+        E.solve(loci_for(s), want_scores=True)
+    keys = ["forward", "backward", "linesearch", "history", "direction", "accept", "score", "other"]
+    tot = dict(kernel_ms={k: 0.0 for k in keys}, kernel_units={k: 0 for k in keys},
+               kernel_launches={k: 0 for k in keys})
+    launches = 0
+    dev_ms = 0.0
+    nfe, iters, contr, statuses = [], [], [], []
+    clocks = Clocks(local)
+    barrier()
+    clocks.start()
+    t0 = time.time()
+    for s in range(args.steps):
+        res = E.solve(loci_for(args.warmup + s), want_scores=True)
+        p = E.profile()
+        dev_ms += p["solve_ms"]
+        launches += p["gpu_launches"]
+        for k in keys:
+            tot["kernel_ms"][k] += p["kernel_ms"][k]
+            tot["kernel_units"][k] += p["kernel_units"][k]
+            tot["kernel_launches"][k] += p["kernel_launches"][k]
+        nfe += res.nfeval.tolist(); iters += res.iterations.tolist()
+        contr += res.contractions.tolist(); statuses += res.status.tolist()
+    barrier()
+    wall = time.time() - t0
+    clk = clocks.stop()
+    t_dev = dev_ms / 1e3
+    if world > 1:
+        tt = torch.tensor([t_dev], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    total_loci = args.steps * per_step * world
+    value = total_loci / t_dev
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        pinned = torch.empty((N, L), dtype=torch.uint8, pin_memory=True)
+        pinned.numpy()[:] = st
+        hst = pinned.numpy()
+        barrier()
+        t1 = time.time()
+        for s in range(args.steps):
+            E.set_alignment(hst, w)
+            E.solve(loci_for(args.warmup + args.steps + s), want_scores=True)
+        barrier()
+        t_e2e = time.time() - t1
+        if world > 1:
+            tt = torch.tensor([t_e2e], dtype=torch.float64, device=f"cuda:{local}")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            t_e2e = float(tt.item())
+        e2e = dict(value=round(args.steps * per_step * world / t_e2e, 4), unit="loci/s",
+                   h2d_bytes_per_step=int(N * L + 8 * N), d2h_bytes_per_step=int(per_step * L * 4 + per_step * 32))
+
+    Dp = ((16 * L + 4 + 63) // 64) * 64
+    rf, dom = roofline(tot, N, L, Dp, 10, 2 if args.history_bf16 else 4)
+    if rf is not None:
+        rf["avg_launch_ms"] = round(tot["kernel_ms"][dom] / max(1, tot["kernel_launches"][dom]), 4)
+    out = {
+        "metric": "loci/s at N=3000,L=94k (per-locus plmDCA solve, gradient threshold 1e-3)",
+        "value": round(value, 4), "unit": "loci/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t_dev * 1e3 / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded coalescent-tree alignment)",
+        "config": {"workload": f"{args.workload} seed {args.seed}", "N": int(N), "L": int(L),
+                   "batch": B, "loci_per_step": per_step, "form": args.form,
+                   "history": "bf16" if args.history_bf16 else "fp32",
+                   "weights": "unit (--no-reweighting)", "gradient_threshold": 1e-3,
+                   "l2": "inputs larger than L2 (282 MB alignment, per-slot solver state)",
+                   "parallelism": f"loci sharded over {world} rank(s)"},
+        "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": rf,
+        "kernel_ms": {k: round(v, 2) for k, v in tot["kernel_ms"].items()},
+        "solver": {"median_nfeval": float(np.median(nfe)), "median_iterations": float(np.median(iters)),
+                   "median_contractions": float(np.median(contr)),
+                   "status_counts": {str(k): statuses.count(k) for k in sorted(set(statuses))},
+                   "wall_s": round(wall, 2)},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        spe, n_eval, t_cpu = cpu_eval_rate(st, args.cpu_seconds, threads)
+        nf = float(np.median(nfe))
+        out["cpu_baseline"] = {
+            "value": round(threads / (spe * nf), 6), "unit": "loci/s", "cores": threads,
+            "kind": "port",
+            "sample": (f"{n_eval} full-size FP64 objective+gradient evaluations ({t_cpu:.1f} s) on "
+                       f"{threads} threads, {spe:.3f} s each; loci/s = threads / (s per evaluation x "
+                       f"{nf:.0f} evaluations per locus, SuperDCA counting, median of this run)")}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    E.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def reference_arm(args):
+    world, rank, local = dist()
+    if rank != 0:
+        return
+    st = load_workload(args)
+    N, L = st.shape
+    threads = os.cpu_count() or 1
+    nf, meta = nfeval_reference(args.workload)
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_eval_rate(st, 0.0, threads)
+    vals, spes = [], []
+    t0 = time.time()
+    for _ in range(args.steps):
+        spe, n_eval, t = cpu_eval_rate(st, per_step, threads)
+        spes.append(spe)
+        vals.append(threads / (spe * nf))
+    wall = time.time() - t0
+    value = float(np.mean(vals))
+    sample = (f"each step: >= {per_step:.0f} s of full-size FP64 objective+gradient evaluations on "
+              f"{threads} threads ({np.mean(spes):.3f} s each); loci/s = threads / (s per evaluation x "
+              f"{nf:.0f} evaluations per locus, median of full oracle solves of {len(meta['loci'])} loci, "
+              f"oracle/nfeval_{args.workload}.json)")
+    out = {
+        "metric": "loci/s at N=3000,L=94k (per-locus plmDCA solve, gradient threshold 1e-3)",
+        "value": round(value, 6), "unit": "loci/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(wall * 1e3 / args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+        "data": "synthetic (seeded coalescent-tree alignment)", "impl": "reference",
+        "config": {"workload": f"{args.workload} seed {args.seed}", "N": int(N), "L": int(L),
+                   "weights": "unit (--no-reweighting)", "gradient_threshold": 1e-3},
+        "cpu_baseline": {"value": round(value, 6), "unit": "loci/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 6), "unit": "loci/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        engine_arm(args)
+
+
+if __name__ == "__main__":
+    main()

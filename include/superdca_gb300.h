@@ -1,0 +1,161 @@
+/* superdca_gb300.h -- C ABI of the GB300 plmDCA per-locus solve engine.
+ *
+ * One handle owns one GPU stream and all device memory of one alignment.  The
+ * caller owns every host buffer.  Every function returns 0 on success and a
+ * negative SDCA_E* code otherwise; sdca_last_error() gives the message.  A
+ * handle is not thread-safe; separate handles are independent.
+ *
+ * The entry points replace SuperDCA's only solve boundary, the template call
+ *   run_plmDCA<double, triallelic_state_t>(alignments, loci_list)
+ * (SuperDCA/include/plmDCA.hpp:436-437, called from SuperDCA/src/SuperDCA.cpp:408),
+ * together with the option getters it reads (SuperDCA/include/plmDCA_options.h).
+ * File output, FASTA parsing and filtering stay with the caller.
+ *
+ * Parameter vectors crossing this ABI (x, g) use SuperDCA's own layout,
+ * D = q*q*L + q doubles: J_r in 16-locus blocks, STATES order inside a block
+ * (SuperDCA/include/Matrix_kernel_access_order.hpp:28-34,
+ *  SuperDCA/include/Coupling_matrix_view.hpp:156-168), then h_r
+ * (SuperDCA/include/plmDCA_optimizer_parameters.hpp:219-247).
+ */
+#ifndef SUPERDCA_GB300_H
+#define SUPERDCA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SDCA_ABI_VERSION 1
+
+/* status codes */
+#define SDCA_OK 0
+#define SDCA_E_ARG (-1)       /* invalid argument */
+#define SDCA_E_CUDA (-2)      /* CUDA runtime error */
+#define SDCA_E_STATE (-3)     /* call out of order (e.g. no alignment yet) */
+#define SDCA_E_NOMEM (-4)     /* device allocation failed */
+#define SDCA_E_NUMERIC (-5)   /* non-finite objective or gradient */
+#define SDCA_E_UNSUPPORTED (-6)
+
+/* contraction forms (sdca_config.form) */
+#define SDCA_FORM_GATHER 0    /* plain form: FP32 gather/scatter on CUDA cores */
+#define SDCA_FORM_TC 1        /* tcgen05 one-hot GEMMs, BF16 hi+lo, FP32 accumulate */
+
+/* sdca_config.flags */
+#define SDCA_FLAG_HISTORY_BF16 0x1 /* keep L-BFGS (s, y) history in BF16 */
+
+typedef struct sdca_handle sdca_handle;
+
+typedef struct {
+    int64_t n_seqs;            /* N: sequences */
+    int64_t n_loci;            /* L: loci (columns) */
+    int32_t q;                 /* states per locus: 4 (SuperDCA triallelic envelope) */
+    int32_t gap_state;         /* state left out of the coupling norm (3) */
+    double lambda_h;           /* --lambda-h option value; < 0 selects the automatic rule */
+    double lambda_J;           /* --lambda-J option value; < 0 selects the automatic rule */
+    double gradient_threshold; /* --gradient-threshold (1e-3): stop on max-norm of g */
+    int32_t max_iterations;    /* L-BFGS iteration limit (2000) */
+    int32_t history;           /* L-BFGS history length m (10) */
+    int32_t batch;             /* loci solved concurrently (slots) */
+    int32_t form;              /* SDCA_FORM_* */
+    int32_t flags;             /* SDCA_FLAG_* */
+    int32_t device;            /* CUDA device ordinal */
+    void *stream;              /* cudaStream_t to run on, or NULL for a private stream */
+} sdca_config;
+
+typedef struct {
+    double f;                  /* objective at the returned point (FP64 reduction) */
+    double gnorm;              /* max-norm of the gradient there */
+    int32_t iterations;        /* L-BFGS iterations */
+    int32_t nfeval;            /* objective evaluations as SuperDCA counts them */
+    int32_t contractions;      /* forward + backward contraction passes run */
+    int32_t status;            /* 0 gradient tolerance, 1 iteration limit,
+                                  2 relative-epsilon stop, -1 non-finite */
+} sdca_locus_stat;
+
+typedef struct {
+    double solve_ms;           /* device time of the last sdca_solve* call (CUDA events) */
+    double kernel_ms[8];       /* device time per kernel class (see SDCA_K_*) */
+    int64_t kernel_launches[8];/* kernels launched per class */
+    int64_t kernel_units[8];   /* slot-passes per class: one unit = one target locus
+                                  through one launch of that class */
+    int64_t gpu_launches;      /* all kernels launched by the last call */
+    int64_t iterations;        /* summed over loci of the last solve */
+    int64_t contractions;
+    int64_t h2d_bytes;
+    int64_t d2h_bytes;
+} sdca_profile;
+
+/* kernel classes in sdca_profile */
+#define SDCA_K_FORWARD 0       /* u = X . d (logit direction) */
+#define SDCA_K_BACKWARD 1      /* g = X^T R + 2 lambda x (gradient) */
+#define SDCA_K_LINESEARCH 2    /* per-trial softmax, objective and g.d */
+#define SDCA_K_HISTORY 3       /* L-BFGS history dot products */
+#define SDCA_K_DIRECTION 4     /* L-BFGS direction */
+#define SDCA_K_ACCEPT 5        /* iterate update and history push */
+#define SDCA_K_SCORE 6         /* Ising gauge + Frobenius scoring */
+#define SDCA_K_OTHER 7
+
+/* Defaults: q=4, gap 3, lambdas automatic, threshold 1e-3, 2000 iterations,
+ * m=10, batch 64, gather form.  Replaces the option defaults of
+ * SuperDCA/src/plmDCA_options.cpp:30-61 and plmDCA.hpp:218-221. */
+int sdca_config_default(sdca_config *cfg);
+
+/* Create a handle on cfg->device. */
+int sdca_create(const sdca_config *cfg, sdca_handle **out);
+
+/* Upload the encoded alignment (N x L row-major state codes 0..q-1) and the
+ * sequence weights (N doubles; SuperDCA computes them in calculate_weights,
+ * SuperDCA/include/plmDCA_optimizer_parameters.hpp:39-98, or uses 1.0 with
+ * --no-reweighting, plmDCA.hpp:541-544).  Sets B_eff and the lambdas
+ * (plmDCA_optimizer_parameters.hpp:257-284). */
+int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weights);
+
+/* Sequence reweighting on the GPU: weights of SuperDCA's calculate_weights
+ * (plmDCA_optimizer_parameters.hpp:39-98) with identity = (L - d_ij)/L, d_ij
+ * the number of loci whose codes differ.  mult: per-sequence multiplicities
+ * or NULL. */
+int sdca_compute_weights(sdca_handle *h, const uint8_t *states, const double *mult,
+                         double threshold, double *weights_out);
+
+/* B_eff and the absolute regularisation strengths in force. */
+int sdca_get_lambdas(const sdca_handle *h, double *lambda_h, double *lambda_J,
+                     double *b_eff);
+
+/* Solve the listed target loci (the per-locus loop of plmDCA_solver,
+ * SuperDCA/include/plmDCA.hpp:277-396, over tbb::parallel_reduce,
+ * plmDCA.hpp:581-586).  scores: n_loci x L floats, row k holds S[loci[k]][n]
+ * = ||gauge(J_rn)||_F without GAP for n != r and NaN at n == r
+ * (plmDCA.hpp:366-394); may be NULL.  stats: n_loci records; may be NULL. */
+int sdca_solve(sdca_handle *h, const uint32_t *loci, size_t n_loci, float *scores,
+               sdca_locus_stat *stats);
+
+/* As sdca_solve, with optional start points x_init (n_loci x D, reference
+ * layout; NULL = zero start as in plmDCA.hpp:298) and optional solutions
+ * x_out (n_loci x D). */
+int sdca_solve_ex(sdca_handle *h, const uint32_t *loci, size_t n_loci, const double *x_init,
+                  double *x_out, float *scores, sdca_locus_stat *stats);
+
+/* One objective evaluation for target locus r at x (reference layout):
+ * plmDCA_objective_fval_and_gradient (SuperDCA/include/plmDCA_objective.hpp:
+ * 38-249) as reached through value_and_gradient
+ * (SuperDCA/include/LBFGS_interface_CppNumericalSolvers.hpp:111-117).
+ * g may be NULL. */
+int sdca_eval(sdca_handle *h, uint32_t r, const double *x, double *f, double *g);
+
+/* Device timings and counters of the last sdca_solve* call. */
+int sdca_get_profile(const sdca_handle *h, sdca_profile *out);
+
+/* Message of the last failed call on h (or of the last failed sdca_create
+ * when h is NULL). */
+const char *sdca_last_error(const sdca_handle *h);
+
+int sdca_destroy(sdca_handle *h);
+
+int sdca_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

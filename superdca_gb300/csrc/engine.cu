@@ -1,0 +1,1112 @@
+// engine.cu -- host driver and C ABI of the GB300 plmDCA solve engine.
+//
+// What it replaces in SuperDCA:
+//   run_plmDCA / plmDCA_solver::operator()   SuperDCA/include/plmDCA.hpp:277-396, 436-587
+//   plmDCA_optimizer_parameters (lambdas)    SuperDCA/include/plmDCA_optimizer_parameters.hpp:257-295
+//   LbfgsSolver + MoreThuente (absent)       driven as in plmDCA.hpp:218-221, 298-304
+//   tbb::parallel_reduce over loci           plmDCA.hpp:581-586
+//
+// A batch of `batch` slots holds one target locus each.  Per L-BFGS iteration
+// the engine runs, for all active slots together:
+//   A. line-search rounds: one k_trial launch per round for every slot still
+//      searching (O(N q) per slot, no contraction), the More-Thuente state
+//      machine on the host between rounds;
+//   B. accept (x += stp d, push s), backward contraction (gradient, push y),
+//      convergence tests, history dots, compact-form coefficients, direction,
+//      forward contraction u = X . d for the next search.
+// Slots whose locus converged are scored and refilled from the queue, so loci
+// retire and enter independently.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "lbfgs_host.h"
+#include "linesearch.h"
+
+using namespace sdca;
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_create_err;
+
+enum Phase {
+    PH_EMPTY = 0,
+    PH_INIT,        // needs the evaluation at its start point
+    PH_LS,          // line search: needs a trial at ls.stp
+    PH_FINAL_EVAL,  // search ended without a trial at its step: evaluate there
+    PH_READY_INIT,  // start point evaluated, waiting for the gradient pass
+    PH_READY_STEP,  // step accepted, waiting for the gradient pass
+    PH_FINALIZE,    // converged: logits refreshed, needs the final evaluation
+};
+
+struct SlotHost {
+    int phase = PH_EMPTY;
+    int64_t k = -1;          // index in the caller's loci list
+    int32_t locus = -1;
+    int iter = 0;            // pairs since the last restart (bounded by m)
+    int iterations = 0;
+    int64_t nfeval = 0;
+    int64_t contractions = 0;
+    int status = 0;
+    double gamma = 1.0;      // H0 scaling s.y / y.y
+    std::deque<int> hist;    // ring positions, oldest first
+    double SY[MAXHIST + 1][MAXHIST + 1];
+    double YY[MAXHIST + 1][MAXHIST + 1];
+    double f = 0, gmax = 0, g2 = 0, x2J = 0, x2H = 0;
+    double gd = 0, ddJ = 0, ddH = 0, xdJ = 0, xdH = 0;
+    double stp = 0;
+    int trials = 0;
+    bool use_u = false;
+    bool push = false;
+    int ring_new = -1;
+    int gcur = 0;
+    double rs[Q] = {0, 0, 0, 0};
+    double f_final = 0;
+    MoreThuente ls;
+};
+
+struct ProfRec {
+    int cls;
+    int kernels;
+    int64_t units;
+    cudaEvent_t a, b;
+};
+
+} // namespace
+
+struct sdca_handle {
+    sdca_config cfg{};
+    std::string err;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    Problem P;
+    bool has_alignment = false;
+    std::vector<double> w_host;
+
+    // device memory
+    std::vector<void *> allocs;
+    uint8_t *X = nullptr, *XT = nullptr, *rstate = nullptr;
+    double *w = nullptr;
+    float *wa = nullptr, *d = nullptr, *gpool = nullptr, *u = nullptr, *R = nullptr;
+    float *partial = nullptr, *rows = nullptr;
+    void *Spool = nullptr, *Ypool = nullptr;
+    double *lbase = nullptr, *acc = nullptr, *dots = nullptr;
+    SlotDev *sd = nullptr;
+    int32_t *list = nullptr;
+    int *flag = nullptr;
+    // pinned host mirrors
+    SlotDev *sd_h = nullptr;
+    int32_t *list_h = nullptr;
+    double *acc_h = nullptr, *dots_h = nullptr;
+    float *rows_h = nullptr;
+    int *flag_h = nullptr;
+    int hist_bf16 = 0;
+
+    std::vector<SlotHost> slots;
+
+    // profiling
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<ProfRec> recs;
+    sdca_profile prof{};
+};
+
+namespace {
+
+int fail(sdca_handle *h, int code, const std::string &msg)
+{
+    if (h) h->err = msg;
+    else {
+        std::lock_guard<std::mutex> lk(g_err_mu);
+        g_create_err = msg;
+    }
+    return code;
+}
+
+#define CK(call)                                                                         \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            return fail(h, SDCA_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CKL()                                                                            \
+    do {                                                                                 \
+        cudaError_t e_ = cudaGetLastError();                                             \
+        if (e_ != cudaSuccess)                                                           \
+            return fail(h, SDCA_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
+
+cudaEvent_t take_event(sdca_handle *h)
+{
+    if (h->ev_used == h->ev_pool.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        h->ev_pool.push_back(e);
+    }
+    return h->ev_pool[h->ev_used++];
+}
+
+// Times the kernels launched in its scope: `kernels` launches working on
+// `units` target loci each.
+struct Timed {
+    sdca_handle *h;
+    ProfRec rec;
+    Timed(sdca_handle *hh, int cls, int kernels, int64_t units) : h(hh)
+    {
+        rec.cls = cls;
+        rec.kernels = kernels;
+        rec.units = units;
+        h->prof.gpu_launches += kernels;
+        rec.a = take_event(h);
+        rec.b = take_event(h);
+        if (rec.a) cudaEventRecord(rec.a, h->stream);
+    }
+    ~Timed()
+    {
+        if (rec.b) cudaEventRecord(rec.b, h->stream);
+        if (rec.a && rec.b) h->recs.push_back(rec);
+    }
+};
+
+void prof_reset(sdca_handle *h)
+{
+    h->ev_used = 0;
+    h->recs.clear();
+    std::memset(&h->prof, 0, sizeof(h->prof));
+}
+
+void prof_collect(sdca_handle *h)
+{
+    for (auto &r : h->recs) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            h->prof.kernel_ms[r.cls] += ms;
+            h->prof.kernel_launches[r.cls] += r.kernels;
+            h->prof.kernel_units[r.cls] += r.units;
+        }
+    }
+    h->recs.clear();
+}
+
+template <typename T> int dalloc(sdca_handle *h, T **p, size_t count)
+{
+    void *q = nullptr;
+    const size_t bytes = std::max<size_t>(count * sizeof(T), 256);
+    if (cudaMalloc(&q, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(h, SDCA_E_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed");
+    }
+    if (cudaMemsetAsync(q, 0, bytes, h->stream) != cudaSuccess)
+        return fail(h, SDCA_E_CUDA, "cudaMemsetAsync failed");
+    h->allocs.push_back(q);
+    *p = static_cast<T *>(q);
+    return SDCA_OK;
+}
+
+template <typename T> int halloc(sdca_handle *h, T **p, size_t count)
+{
+    void *q = nullptr;
+    if (cudaMallocHost(&q, std::max<size_t>(count * sizeof(T), 64)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(h, SDCA_E_NOMEM, "pinned host allocation failed");
+    }
+    std::memset(q, 0, std::max<size_t>(count * sizeof(T), 64));
+    *p = static_cast<T *>(q);
+    return SDCA_OK;
+}
+
+void free_all(sdca_handle *h)
+{
+    for (void *p : h->allocs) cudaFree(p);
+    h->allocs.clear();
+    if (h->sd_h) cudaFreeHost(h->sd_h);
+    if (h->list_h) cudaFreeHost(h->list_h);
+    if (h->acc_h) cudaFreeHost(h->acc_h);
+    if (h->dots_h) cudaFreeHost(h->dots_h);
+    if (h->rows_h) cudaFreeHost(h->rows_h);
+    if (h->flag_h) cudaFreeHost(h->flag_h);
+    h->sd_h = nullptr; h->list_h = nullptr; h->acc_h = nullptr; h->dots_h = nullptr;
+    h->rows_h = nullptr; h->flag_h = nullptr;
+    h->X = h->XT = h->rstate = nullptr;
+    h->has_alignment = false;
+}
+
+// X [N][Lx] -> XT [L][Nx]; flags codes >= Q
+__global__ void k_transpose(const uint8_t *__restrict__ X, int64_t Lx, int N, int L,
+                            uint8_t *__restrict__ XT, int64_t Nx, int *__restrict__ bad)
+{
+    __shared__ uint8_t tile[64][65];
+    const int n0 = blockIdx.x * 64, i0 = blockIdx.y * 64;
+    for (int k = threadIdx.x; k < 64 * 64; k += blockDim.x) {
+        const int ii = k / 64, nn = k % 64;
+        const int i = i0 + ii, n = n0 + nn;
+        uint8_t v = 0;
+        if (i < N && n < L) {
+            v = X[(int64_t)i * Lx + n];
+            if (v >= Q) atomicOr(bad, 1);
+        }
+        tile[ii][nn] = v;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 64 * 64; k += blockDim.x) {
+        const int nn = k / 64, ii = k % 64;
+        const int i = i0 + ii, n = n0 + nn;
+        if (n < L && i < (int)Nx) XT[(int64_t)n * Nx + i] = (i < N) ? tile[ii][nn] : 0;
+    }
+}
+
+// reference layout (double, 16-locus STATES blocks) <-> engine layout (float)
+int64_t ref_index(int64_t L, int64_t n, int s, int a)
+{
+    const int64_t b = n / 16, p = n % 16, nfull = L / 16;
+    const int64_t e = b < nfull ? 16 : L % 16;
+    return b * 16 * QQ + ((int64_t)s * e + p) * Q + a;
+}
+
+void ref_to_engine(const Problem &P, int64_t r, const double *x, float *out)
+{
+    std::memset(out, 0, sizeof(float) * P.Dp);
+    for (int64_t n = 0; n < P.L; ++n) {
+        if (n == r) continue;  // J_rr never enters the objective
+        for (int s = 0; s < Q; ++s)
+            for (int a = 0; a < Q; ++a) out[n * QQ + s * Q + a] = (float)x[ref_index(P.L, n, s, a)];
+    }
+    for (int a = 0; a < Q; ++a) out[QQ * P.L + a] = (float)x[QQ * P.L + a];
+}
+
+void engine_to_ref(const Problem &P, const float *v, double *out)
+{
+    for (int64_t n = 0; n < P.L; ++n)
+        for (int s = 0; s < Q; ++s)
+            for (int a = 0; a < Q; ++a) out[ref_index(P.L, n, s, a)] = v[n * QQ + s * Q + a];
+    for (int a = 0; a < Q; ++a) out[QQ * P.L + a] = v[QQ * P.L + a];
+}
+
+int upload_list(sdca_handle *h, const std::vector<int32_t> &lst)
+{
+    if (lst.empty()) return SDCA_OK;
+    std::memcpy(h->list_h, lst.data(), sizeof(int32_t) * lst.size());
+    CK(cudaMemcpyAsync(h->list, h->list_h, sizeof(int32_t) * lst.size(), cudaMemcpyHostToDevice,
+                       h->stream));
+    return SDCA_OK;
+}
+
+// copy the host slot parameters of `lst` into the device mirror
+int upload_slots(sdca_handle *h, const std::vector<int32_t> &lst)
+{
+    for (int b : lst) {
+        SlotHost &S = h->slots[b];
+        SlotDev &D = h->sd_h[b];
+        D.locus = S.locus;
+        D.gcur = S.gcur;
+        D.ring_new = S.ring_new;
+        D.nhist = (int)S.hist.size();
+        for (int j = 0; j < D.nhist; ++j) D.ring[j] = S.hist[j];
+        D.flags = (S.use_u ? SLOT_F_USE_U : 0) | (S.push ? SLOT_F_PUSH : 0);
+        D.stp = S.stp;
+        for (int a = 0; a < Q; ++a) D.rs[a] = S.rs[a];
+    }
+    // the mirror is small; copy it whole
+    CK(cudaMemcpyAsync(h->sd, h->sd_h, sizeof(SlotDev) * h->P.Bmax, cudaMemcpyHostToDevice,
+                       h->stream));
+    return upload_list(h, lst);
+}
+
+int zero_acc(sdca_handle *h)
+{
+    CK(cudaMemsetAsync(h->acc, 0, sizeof(double) * NACC * h->P.Bmax, h->stream));
+    return SDCA_OK;
+}
+
+int fetch_acc(sdca_handle *h)
+{
+    CK(cudaMemcpyAsync(h->acc_h, h->acc, sizeof(double) * NACC * h->P.Bmax, cudaMemcpyDeviceToHost,
+                       h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return SDCA_OK;
+}
+
+double acc_get(sdca_handle *h, int b, int k) { return h->acc_h[(int64_t)b * NACC + k]; }
+
+// forward contraction u = X . v_J (+ v_h): into `u` (float) or `lbase` (double)
+int run_forward(sdca_handle *h, const std::vector<int32_t> &lst, const float *vecs, bool to_lbase)
+{
+    if (lst.empty()) return SDCA_OK;
+    int rc = upload_list(h, lst);
+    if (rc) return rc;
+    {
+        Timed t(h, SDCA_K_FORWARD, 2, (int64_t)lst.size());
+        launch_fwd_gather(h->P, h->X, h->list, (int)lst.size(), vecs, h->partial, h->stream);
+        launch_reduce_partial(h->P, h->list, (int)lst.size(), h->partial, vecs, 1,
+                              to_lbase ? nullptr : h->u, to_lbase ? h->lbase : nullptr, h->stream);
+    }
+    CKL();
+    for (int b : lst) h->slots[b].contractions++;
+    return SDCA_OK;
+}
+
+// begin a locus in slot b: zero or given start point, logits at the start point
+int slot_begin(sdca_handle *h, int b, int64_t k, int32_t locus, const float *x0_engine)
+{
+    SlotHost &S = h->slots[b];
+    S = SlotHost();
+    S.phase = PH_INIT;
+    S.k = k;
+    S.locus = locus;
+    S.gcur = 0;
+    const Problem &P = h->P;
+    float *wab = h->wa + (int64_t)b * P.Dp;
+    if (x0_engine)
+        CK(cudaMemcpyAsync(wab, x0_engine, sizeof(float) * P.Dp, cudaMemcpyHostToDevice, h->stream));
+    else
+        CK(cudaMemsetAsync(wab, 0, sizeof(float) * P.Dp, h->stream));
+    CK(cudaMemsetAsync(h->d + (int64_t)b * P.Dp, 0, sizeof(float) * P.Dp, h->stream));
+    CK(cudaMemcpyAsync(h->rstate + (int64_t)b * P.Nx, h->XT + (int64_t)locus * P.Nx, P.Nx,
+                       cudaMemcpyDeviceToDevice, h->stream));
+    if (!x0_engine)
+        CK(cudaMemsetAsync(h->lbase + (int64_t)b * P.Nx * 4, 0, sizeof(double) * P.Nx * 4, h->stream));
+    S.stp = 0.0;
+    S.use_u = false;
+    S.push = false;
+    S.ring_new = -1;
+    return SDCA_OK;
+}
+
+// the per-solve queue
+struct Queue {
+    const uint32_t *loci = nullptr;
+    size_t n = 0, next = 0;
+    const double *x_init = nullptr;
+    double *x_out = nullptr;
+    float *scores = nullptr;
+    sdca_locus_stat *stats = nullptr;
+    std::vector<float> xbuf;
+};
+
+int refill(sdca_handle *h, Queue &Qu)
+{
+    std::vector<int32_t> warm;
+    for (int b = 0; b < h->P.Bmax && Qu.next < Qu.n; ++b) {
+        if (h->slots[b].phase != PH_EMPTY) continue;
+        const int64_t k = (int64_t)Qu.next++;
+        const float *x0 = nullptr;
+        if (Qu.x_init) {
+            const double *xr = Qu.x_init + k * (QQ * h->P.L + Q);
+            ref_to_engine(h->P, Qu.loci[k], xr, Qu.xbuf.data());
+            x0 = Qu.xbuf.data();
+        }
+        int rc = slot_begin(h, b, k, (int32_t)Qu.loci[k], x0);
+        if (rc) return rc;
+        if (x0) {
+            // the copy reads the staging buffer: finish it before the next slot reuses it
+            CK(cudaStreamSynchronize(h->stream));
+            warm.push_back(b);
+        }
+    }
+    if (!warm.empty()) return run_forward(h, warm, h->wa, true);
+    return SDCA_OK;
+}
+
+// record the results of a finished slot and free it
+int retire(sdca_handle *h, Queue &Qu, const std::vector<int32_t> &done)
+{
+    if (done.empty()) return SDCA_OK;
+    const Problem &P = h->P;
+    int rc = upload_slots(h, done);
+    if (rc) return rc;
+    if (Qu.scores) {
+        {
+            Timed t(h, SDCA_K_SCORE, 1, (int64_t)done.size());
+            launch_score(P, h->sd, h->list, (int)done.size(), h->wa, h->cfg.gap_state, h->rows,
+                         h->stream);
+        }
+        CKL();
+        CK(cudaMemcpyAsync(h->rows_h, h->rows, sizeof(float) * P.L * done.size(),
+                           cudaMemcpyDeviceToHost, h->stream));
+        h->prof.d2h_bytes += (int64_t)sizeof(float) * P.L * done.size();
+    }
+    std::vector<float> xe;
+    if (Qu.x_out) xe.resize(P.Dp);
+    for (size_t j = 0; j < done.size(); ++j) {
+        const int b = done[j];
+        SlotHost &S = h->slots[b];
+        if (Qu.x_out) {
+            CK(cudaMemcpyAsync(xe.data(), h->wa + (int64_t)b * P.Dp, sizeof(float) * P.Dp,
+                               cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            engine_to_ref(P, xe.data(), Qu.x_out + S.k * (QQ * P.L + Q));
+            h->prof.d2h_bytes += (int64_t)sizeof(float) * P.Dp;
+        }
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    for (size_t j = 0; j < done.size(); ++j) {
+        const int b = done[j];
+        SlotHost &S = h->slots[b];
+        if (Qu.scores) std::memcpy(Qu.scores + S.k * P.L, h->rows_h + j * P.L, sizeof(float) * P.L);
+        if (Qu.stats) {
+            sdca_locus_stat &st = Qu.stats[S.k];
+            st.f = S.f_final;
+            st.gnorm = S.gmax;
+            st.iterations = S.iterations;
+            st.nfeval = (int32_t)S.nfeval;
+            st.contractions = (int32_t)S.contractions;
+            st.status = S.status;
+        }
+        h->prof.iterations += S.iterations;
+        h->prof.contractions += S.contractions;
+        S.phase = PH_EMPTY;
+    }
+    return SDCA_OK;
+}
+
+double l2_along(const Problem &P, const SlotHost &S, double stp)
+{
+    const double j2 = S.x2J + 2.0 * stp * S.xdJ + stp * stp * S.ddJ;
+    const double h2 = S.x2H + 2.0 * stp * S.xdH + stp * stp * S.ddH;
+    return P.lambda_J * j2 + P.lambda_h * h2;
+}
+
+double dl2_along(const Problem &P, const SlotHost &S, double stp)
+{
+    return 2.0 * P.lambda_J * (S.xdJ + stp * S.ddJ) + 2.0 * P.lambda_h * (S.xdH + stp * S.ddH);
+}
+
+// phase A: line-search rounds until no slot needs a trial
+int phase_trials(sdca_handle *h, Queue &Qu)
+{
+    const Problem &P = h->P;
+    for (;;) {
+        std::vector<int32_t> lst;
+        for (int b = 0; b < P.Bmax; ++b) {
+            const int ph = h->slots[b].phase;
+            if (ph == PH_INIT || ph == PH_LS || ph == PH_FINAL_EVAL || ph == PH_FINALIZE) lst.push_back(b);
+        }
+        if (lst.empty()) return SDCA_OK;
+        int rc = upload_slots(h, lst);
+        if (rc) return rc;
+        rc = zero_acc(h);
+        if (rc) return rc;
+        {
+            Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)lst.size());
+            launch_trial(P, h->sd, h->list, (int)lst.size(), h->lbase, h->u, h->rstate, h->w, h->R,
+                         h->acc, h->stream);
+        }
+        CKL();
+        rc = fetch_acc(h);
+        if (rc) return rc;
+        std::vector<int32_t> done;
+        for (int b : lst) {
+            SlotHost &S = h->slots[b];
+            const double fdata = acc_get(h, b, ACC_F);
+            for (int a = 0; a < Q; ++a) S.rs[a] = acc_get(h, b, ACC_RS0 + a);
+            if (S.phase == PH_INIT) {
+                S.f = fdata;  // the L2 part is added once |x|^2 is known
+                S.phase = PH_READY_INIT;
+            } else if (S.phase == PH_FINALIZE) {
+                S.f_final = fdata + P.lambda_J * S.x2J + P.lambda_h * S.x2H;
+                done.push_back(b);
+            } else if (S.phase == PH_FINAL_EVAL) {
+                S.f = fdata + l2_along(P, S, S.stp);
+                S.phase = PH_READY_STEP;
+            } else {  // PH_LS
+                const double f = fdata + l2_along(P, S, S.stp);
+                const double dg = acc_get(h, b, ACC_DG) + dl2_along(P, S, S.stp);
+                S.trials++;
+                if (!std::isfinite(f) || !std::isfinite(dg)) {
+                    S.f = f;
+                    S.phase = PH_READY_STEP;
+                    continue;
+                }
+                const double stp_eval = S.stp;
+                if (S.ls.feed(f, dg) == MoreThuente::DONE) {
+                    S.stp = stp_eval;  // the accepted point is the last trial
+                    S.f = f;
+                    S.phase = PH_READY_STEP;
+                } else {
+                    S.stp = S.ls.stp;
+                }
+            }
+        }
+        if (!done.empty()) {
+            rc = retire(h, Qu, done);
+            if (rc) return rc;
+            rc = refill(h, Qu);
+            if (rc) return rc;
+        }
+    }
+}
+
+// phase B: accept, gradient, tests, new direction, forward contraction
+int phase_step(sdca_handle *h)
+{
+    const Problem &P = h->P;
+    const int m = P.m;
+    std::vector<int32_t> all, steps;
+    for (int b = 0; b < P.Bmax; ++b) {
+        SlotHost &S = h->slots[b];
+        if (S.phase == PH_READY_STEP) {
+            steps.push_back(b);
+            all.push_back(b);
+            S.push = true;
+            // a ring position outside the live history (there are m + 1)
+            int pos = 0;
+            while (std::find(S.hist.begin(), S.hist.end(), pos) != S.hist.end()) ++pos;
+            S.ring_new = pos;
+        } else if (S.phase == PH_READY_INIT) {
+            all.push_back(b);
+            S.push = false;
+            S.ring_new = -1;
+        }
+    }
+    if (all.empty()) return SDCA_OK;
+    int rc = upload_slots(h, all);
+    if (rc) return rc;
+    if (!steps.empty()) {
+        rc = upload_slots(h, steps);
+        if (rc) return rc;
+        {
+            Timed t(h, SDCA_K_ACCEPT, 2, (int64_t)steps.size());
+            launch_accept(P, h->sd, h->list, (int)steps.size(), h->wa, h->d, h->Spool, h->hist_bf16,
+                          h->stream);
+            launch_lbase_update(P, h->sd, h->list, (int)steps.size(), h->lbase, h->u, h->stream);
+        }
+        CKL();
+        rc = upload_list(h, all);
+        if (rc) return rc;
+    }
+    rc = zero_acc(h);
+    if (rc) return rc;
+    {
+        Timed t(h, SDCA_K_BACKWARD, 2, (int64_t)all.size());
+        launch_bwd_gather(P, h->XT, h->sd, h->list, (int)all.size(), h->R, h->wa, h->gpool, h->Ypool,
+                          h->Spool, h->hist_bf16, h->acc, h->stream);
+        launch_hpart(P, h->sd, h->list, (int)all.size(), h->wa, h->gpool, h->Ypool, h->Spool,
+                     h->hist_bf16, h->acc, h->stream);
+    }
+    CKL();
+    rc = fetch_acc(h);
+    if (rc) return rc;
+
+    std::vector<int32_t> cont, fin;
+    for (int b : all) {
+        SlotHost &S = h->slots[b];
+        S.contractions++;
+        S.gcur = 1 - S.gcur;
+        S.g2 = acc_get(h, b, ACC_G2);
+        S.x2J = acc_get(h, b, ACC_X2J);
+        S.x2H = acc_get(h, b, ACC_X2H);
+        {
+            const double gm = acc_get(h, b, ACC_GMAX);
+            S.gmax = gm;
+        }
+        bool stop = false;
+        if (S.phase == PH_READY_INIT) {
+            S.f += P.lambda_J * S.x2J + P.lambda_h * S.x2H;
+            S.nfeval = 1;
+        } else {
+            S.iterations++;
+            S.nfeval += 2 + S.trials;
+            const double sy = acc_get(h, b, ACC_SY), yy = acc_get(h, b, ACC_YY);
+            if (sy > 0.0 && yy > 0.0 && std::isfinite(sy) && std::isfinite(yy)) {
+                if ((int)S.hist.size() == m) S.hist.pop_front();
+                S.hist.push_back(S.ring_new);
+                S.gamma = sy / yy;
+                S.iter++;
+            } else {
+                S.ring_new = -1;  // pair not usable: keep the history as it is
+            }
+            if (S.iterations > h->cfg.max_iterations) {
+                S.status = 1;
+                stop = true;
+            } else if (S.gmax < h->cfg.gradient_threshold) {
+                S.status = 0;
+                stop = true;
+            }
+        }
+        if (!std::isfinite(S.f) || !std::isfinite(S.g2) || !std::isfinite(S.gmax)) {
+            S.status = -1;
+            stop = true;
+        }
+        if (!stop) {
+            const double releps = 1e-4 * std::max(1.0, std::sqrt(S.x2J + S.x2H));
+            if (std::sqrt(S.g2) < releps) {
+                S.status = 2;
+                stop = true;
+            }
+        }
+        if (stop) fin.push_back(b);
+        else cont.push_back(b);
+    }
+
+    // converged slots: refresh their logits from the stored parameters
+    if (!fin.empty()) {
+        rc = run_forward(h, fin, h->wa, true);
+        if (rc) return rc;
+        for (int b : fin) {
+            SlotHost &S = h->slots[b];
+            S.phase = PH_FINALIZE;
+            S.stp = 0.0;
+            S.use_u = false;
+        }
+    }
+    if (cont.empty()) return SDCA_OK;
+
+    // history dots for slots with history
+    std::vector<int32_t> withh;
+    for (int b : cont)
+        if (!h->slots[b].hist.empty()) withh.push_back(b);
+    if (!withh.empty()) {
+        rc = upload_slots(h, withh);
+        if (rc) return rc;
+        CK(cudaMemsetAsync(h->dots, 0, sizeof(double) * 4 * MAXHIST * P.Bmax, h->stream));
+        {
+            Timed t(h, SDCA_K_HISTORY, 1, (int64_t)withh.size());
+            launch_hist_dots(P, h->sd, h->list, (int)withh.size(), h->gpool, h->Spool, h->Ypool,
+                             h->hist_bf16, h->dots, h->stream);
+        }
+        CKL();
+        CK(cudaMemcpyAsync(h->dots_h, h->dots, sizeof(double) * 4 * MAXHIST * P.Bmax,
+                           cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    for (int b : cont) {
+        SlotHost &S = h->slots[b];
+        SlotDev &D = h->sd_h[b];
+        const int k = (int)S.hist.size();
+        D.coef_g = -1.0;
+        if (k > 0) {
+            const double *dt = h->dots_h + (int64_t)b * 4 * MAXHIST;
+            // the newest pair supplies a new column of S^T Y and a row of Y^T Y
+            if (S.ring_new >= 0) {
+                const int pn = S.ring_new;
+                for (int j = 0; j < k; ++j) {
+                    const int pj = S.hist[j];
+                    S.SY[pj][pn] = dt[2 * MAXHIST + j];
+                    S.YY[pj][pn] = dt[3 * MAXHIST + j];
+                    S.YY[pn][pj] = dt[3 * MAXHIST + j];
+                }
+            }
+            double Rm[MAXHIST * MAXHIST], YYm[MAXHIST * MAXHIST], sg[MAXHIST], yg[MAXHIST];
+            for (int a = 0; a < k; ++a) {
+                sg[a] = dt[a];
+                yg[a] = dt[MAXHIST + a];
+                for (int c = 0; c < k; ++c) {
+                    Rm[a * k + c] = (a <= c) ? S.SY[S.hist[a]][S.hist[c]] : 0.0;
+                    YYm[a * k + c] = S.YY[S.hist[a]][S.hist[c]];
+                }
+            }
+            double cg, cS[MAXHIST], cY[MAXHIST];
+            if (lbfgs_compact_coeffs(k, Rm, YYm, sg, yg, S.gamma, &cg, cS, cY)) {
+                D.coef_g = cg;
+                for (int a = 0; a < k; ++a) {
+                    D.coefS[a] = cS[a];
+                    D.coefY[a] = cY[a];
+                }
+            } else {
+                S.hist.clear();
+                S.iter = 0;
+            }
+        }
+    }
+    // direction (the coefficient fields of the mirror are already set)
+    auto run_direction = [&](const std::vector<int32_t> &lst) -> int {
+        for (int b : lst) {
+            SlotHost &S = h->slots[b];
+            SlotDev &D = h->sd_h[b];
+            D.nhist = (int)S.hist.size();
+            for (int j = 0; j < D.nhist; ++j) D.ring[j] = S.hist[j];
+        }
+        CK(cudaMemcpyAsync(h->sd, h->sd_h, sizeof(SlotDev) * P.Bmax, cudaMemcpyHostToDevice, h->stream));
+        int r2 = upload_list(h, lst);
+        if (r2) return r2;
+        r2 = zero_acc(h);
+        if (r2) return r2;
+        {
+            Timed t(h, SDCA_K_DIRECTION, 1, (int64_t)lst.size());
+            launch_direction(P, h->sd, h->list, (int)lst.size(), h->gpool, h->Spool, h->Ypool,
+                             h->hist_bf16, h->wa, h->d, h->acc, h->stream);
+        }
+        CKL();
+        return fetch_acc(h);
+    };
+    for (int b : cont) h->sd_h[b].gcur = h->slots[b].gcur;
+    rc = run_direction(cont);
+    if (rc) return rc;
+    std::vector<int32_t> restart;
+    for (int b : cont) {
+        SlotHost &S = h->slots[b];
+        S.gd = acc_get(h, b, ACC_GD);
+        S.ddJ = acc_get(h, b, ACC_DDJ);
+        S.ddH = acc_get(h, b, ACC_DDH);
+        S.xdJ = acc_get(h, b, ACC_XDJ);
+        S.xdH = acc_get(h, b, ACC_XDH);
+        const double releps = 1e-4 * std::max(1.0, std::sqrt(S.x2J + S.x2H));
+        if (!S.hist.empty() && !(S.gd <= -1e-4 * releps)) restart.push_back(b);
+    }
+    std::vector<char> restarted(P.Bmax, 0);
+    if (!restart.empty()) {
+        // not a usable descent direction: restart from steepest descent
+        for (int b : restart) {
+            h->slots[b].hist.clear();
+            h->slots[b].iter = 0;
+            h->sd_h[b].coef_g = -1.0;
+            restarted[b] = 1;
+        }
+        rc = run_direction(restart);
+        if (rc) return rc;
+        for (int b : restart) {
+            SlotHost &S = h->slots[b];
+            S.gd = acc_get(h, b, ACC_GD);
+            S.ddJ = acc_get(h, b, ACC_DDJ);
+            S.ddH = acc_get(h, b, ACC_DDH);
+            S.xdJ = acc_get(h, b, ACC_XDJ);
+            S.xdH = acc_get(h, b, ACC_XDH);
+        }
+    }
+    rc = run_forward(h, cont, h->d, false);
+    if (rc) return rc;
+    for (int b : cont) {
+        SlotHost &S = h->slots[b];
+        const double alpha_init = restarted[b] ? 1.0 : 1.0 / std::sqrt(S.g2);
+        S.trials = 0;
+        S.use_u = true;
+        S.push = false;
+        if (S.ls.start(S.f, S.gd, alpha_init) == MoreThuente::NEED_EVAL) {
+            S.stp = S.ls.stp;
+            S.phase = PH_LS;
+        } else {
+            S.stp = alpha_init;
+            S.phase = PH_FINAL_EVAL;
+        }
+    }
+    return SDCA_OK;
+}
+
+int check_ready(sdca_handle *h)
+{
+    if (!h) return SDCA_E_ARG;
+    if (!h->has_alignment) return fail(h, SDCA_E_STATE, "no alignment set (call sdca_set_alignment)");
+    return SDCA_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int sdca_abi_version(void) { return SDCA_ABI_VERSION; }
+
+int sdca_config_default(sdca_config *cfg)
+{
+    if (!cfg) return SDCA_E_ARG;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->q = 4;
+    cfg->gap_state = 3;
+    cfg->lambda_h = -1.0;
+    cfg->lambda_J = -1.0;
+    cfg->gradient_threshold = 1e-3;
+    cfg->max_iterations = 2000;
+    cfg->history = 10;
+    cfg->batch = 64;
+    cfg->form = SDCA_FORM_GATHER;
+    cfg->flags = 0;
+    cfg->device = 0;
+    cfg->stream = nullptr;
+    return SDCA_OK;
+}
+
+int sdca_create(const sdca_config *cfg, sdca_handle **out)
+{
+    sdca_handle *h = nullptr;
+    if (!cfg || !out) return fail(nullptr, SDCA_E_ARG, "sdca_create: null argument");
+    *out = nullptr;
+    if (cfg->q != Q) return fail(nullptr, SDCA_E_UNSUPPORTED, "only q = 4 (the triallelic envelope) is supported");
+    if (cfg->n_seqs < 1 || cfg->n_loci < 2)
+        return fail(nullptr, SDCA_E_ARG, "need at least 1 sequence and 2 loci");
+    if (cfg->n_seqs > (1LL << 30) || cfg->n_loci > (1LL << 26))
+        return fail(nullptr, SDCA_E_ARG, "alignment too large");
+    if (cfg->history < 1 || cfg->history > MAXHIST)
+        return fail(nullptr, SDCA_E_ARG, "history must be in 1..10");
+    if (cfg->batch < 1 || cfg->batch > 4096) return fail(nullptr, SDCA_E_ARG, "batch must be in 1..4096");
+    if (cfg->gap_state < -1 || cfg->gap_state >= Q) return fail(nullptr, SDCA_E_ARG, "gap_state out of range");
+    if (cfg->form != SDCA_FORM_GATHER)
+        return fail(nullptr, SDCA_E_UNSUPPORTED, "contraction form not available in this build");
+    if (!(cfg->gradient_threshold >= 0.0) || cfg->max_iterations < 0)
+        return fail(nullptr, SDCA_E_ARG, "invalid stopping criteria");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(nullptr, SDCA_E_CUDA, "no CUDA device available");
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) return fail(nullptr, SDCA_E_ARG, "device ordinal out of range");
+    if (cudaSetDevice(cfg->device) != cudaSuccess) return fail(nullptr, SDCA_E_CUDA, "cudaSetDevice failed");
+    h = new (std::nothrow) sdca_handle();
+    if (!h) return fail(nullptr, SDCA_E_NOMEM, "host allocation failed");
+    h->cfg = *cfg;
+    if (cfg->stream) {
+        h->stream = static_cast<cudaStream_t>(cfg->stream);
+    } else {
+        if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete h;
+            return fail(nullptr, SDCA_E_CUDA, "cudaStreamCreate failed");
+        }
+        h->own_stream = true;
+    }
+    h->hist_bf16 = (cfg->flags & SDCA_FLAG_HISTORY_BF16) ? 1 : 0;
+    Problem &P = h->P;
+    P.N = cfg->n_seqs;
+    P.L = cfg->n_loci;
+    P.Lx = round_up(P.L, 64);
+    P.Nx = round_up(P.N, 64);
+    P.Dp = round_up(QQ * P.L + Q, 64);
+    P.m = cfg->history;
+    P.ring = P.m + 1;
+    P.Bmax = cfg->batch;
+    {
+        // locus chunks of the forward gather: enough CTAs to fill the GPU
+        const int64_t seq_tiles = (P.N + 255) / 256, slot_groups = (P.Bmax + 7) / 8;
+        int64_t want = (2 * 152 + seq_tiles * slot_groups - 1) / (seq_tiles * slot_groups);
+        want = std::max<int64_t>(1, want);
+        P.LC = round_up((P.L + want - 1) / want, 32);
+        P.LC = std::max<int64_t>(P.LC, 512);
+        P.C = (P.L + P.LC - 1) / P.LC;
+    }
+    h->slots.resize(P.Bmax);
+    int rc = SDCA_OK;
+    const size_t B = P.Bmax;
+    const size_t hsz = h->hist_bf16 ? 2 : 4;
+    if ((rc = dalloc(h, &h->X, (size_t)P.N * P.Lx)) || (rc = dalloc(h, &h->XT, (size_t)P.L * P.Nx)) ||
+        (rc = dalloc(h, &h->w, (size_t)P.Nx)) || (rc = dalloc(h, &h->rstate, B * P.Nx)) ||
+        (rc = dalloc(h, &h->wa, B * P.Dp)) || (rc = dalloc(h, &h->d, B * P.Dp)) ||
+        (rc = dalloc(h, &h->gpool, 2 * B * P.Dp)) || (rc = dalloc(h, &h->u, B * P.Nx * 4)) ||
+        (rc = dalloc(h, &h->R, B * P.Nx * 4)) || (rc = dalloc(h, &h->lbase, B * P.Nx * 4)) ||
+        (rc = dalloc(h, &h->partial, (size_t)P.C * B * P.Nx * 4)) ||
+        (rc = dalloc(h, &h->rows, B * P.L)) || (rc = dalloc(h, &h->acc, B * NACC)) ||
+        (rc = dalloc(h, &h->dots, B * 4 * MAXHIST)) || (rc = dalloc(h, &h->sd, B)) ||
+        (rc = dalloc(h, &h->list, B)) || (rc = dalloc(h, &h->flag, 4)) ||
+        (rc = dalloc(h, reinterpret_cast<uint8_t **>(&h->Spool), B * P.ring * P.Dp * hsz)) ||
+        (rc = dalloc(h, reinterpret_cast<uint8_t **>(&h->Ypool), B * P.ring * P.Dp * hsz)) ||
+        (rc = halloc(h, &h->sd_h, B)) || (rc = halloc(h, &h->list_h, B)) ||
+        (rc = halloc(h, &h->acc_h, B * NACC)) || (rc = halloc(h, &h->dots_h, B * 4 * MAXHIST)) ||
+        (rc = halloc(h, &h->rows_h, B * P.L)) || (rc = halloc(h, &h->flag_h, 4))) {
+        std::string msg = h->err;
+        free_all(h);
+        if (h->own_stream) cudaStreamDestroy(h->stream);
+        delete h;
+        return fail(nullptr, rc, msg);
+    }
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
+        free_all(h);
+        if (h->own_stream) cudaStreamDestroy(h->stream);
+        delete h;
+        return fail(nullptr, SDCA_E_CUDA, "initialisation failed");
+    }
+    *out = h;
+    return SDCA_OK;
+}
+
+int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weights)
+{
+    if (!h) return SDCA_E_ARG;
+    if (!states || !weights) return fail(h, SDCA_E_ARG, "states and weights are required");
+    Problem &P = h->P;
+    for (int64_t i = 0; i < P.N; ++i)
+        if (!(weights[i] >= 0.0) || !std::isfinite(weights[i]))
+            return fail(h, SDCA_E_ARG, "weights must be finite and non-negative");
+    CK(cudaSetDevice(h->cfg.device));
+    h->w_host.assign(weights, weights + P.N);
+    CK(cudaMemcpy2DAsync(h->X, P.Lx, states, P.L, P.L, P.N, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->w, weights, sizeof(double) * P.N, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(h->flag, 0, sizeof(int), h->stream));
+    {
+        dim3 grid((unsigned)((P.L + 63) / 64), (unsigned)((P.Nx + 63) / 64));
+        k_transpose<<<grid, 256, 0, h->stream>>>(h->X, P.Lx, (int)P.N, (int)P.L, h->XT, P.Nx, h->flag);
+    }
+    CKL();
+    CK(cudaMemcpyAsync(h->flag_h, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->flag_h[0]) {
+        h->has_alignment = false;
+        return fail(h, SDCA_E_ARG, "state codes must be in 0..q-1");
+    }
+    // B_eff and lambdas: SuperDCA/include/plmDCA_optimizer_parameters.hpp:257-284
+    double beff = 0.0;
+    for (int64_t i = 0; i < P.N; ++i) beff += weights[i];
+    const double autol = (beff > 500.0) ? 0.1 : 1.0 - ((1.0 - 0.1) * beff / 500.0);
+    P.b_eff = beff;
+    P.lambda_J = (h->cfg.lambda_J < 0.0) ? autol * beff / 2.0 : h->cfg.lambda_J * beff;
+    P.lambda_h = (h->cfg.lambda_h < 0.0) ? autol * beff : h->cfg.lambda_h * beff;
+    h->has_alignment = true;
+    h->prof.h2d_bytes = (int64_t)P.N * P.L + (int64_t)sizeof(double) * P.N;
+    return SDCA_OK;
+}
+
+int sdca_get_lambdas(const sdca_handle *h, double *lambda_h, double *lambda_J, double *b_eff)
+{
+    if (!h || !h->has_alignment) return SDCA_E_STATE;
+    if (lambda_h) *lambda_h = h->P.lambda_h;
+    if (lambda_J) *lambda_J = h->P.lambda_J;
+    if (b_eff) *b_eff = h->P.b_eff;
+    return SDCA_OK;
+}
+
+int sdca_solve_ex(sdca_handle *h, const uint32_t *loci, size_t n_loci, const double *x_init,
+                  double *x_out, float *scores, sdca_locus_stat *stats)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (n_loci > 0 && !loci) return fail(h, SDCA_E_ARG, "null loci list");
+    for (size_t k = 0; k < n_loci; ++k)
+        if ((int64_t)loci[k] >= h->P.L) return fail(h, SDCA_E_ARG, "locus index out of range");
+    CK(cudaSetDevice(h->cfg.device));
+    const int64_t h2d0 = h->prof.h2d_bytes;
+    prof_reset(h);
+    h->prof.h2d_bytes = 0;
+    (void)h2d0;
+    cudaEvent_t t0 = take_event(h), t1 = take_event(h);
+    CK(cudaEventRecord(t0, h->stream));
+    Queue Qu;
+    Qu.loci = loci;
+    Qu.n = n_loci;
+    Qu.x_init = x_init;
+    Qu.x_out = x_out;
+    Qu.scores = scores;
+    Qu.stats = stats;
+    if (x_init) Qu.xbuf.resize(h->P.Dp);
+    for (auto &S : h->slots) S.phase = PH_EMPTY;
+    rc = refill(h, Qu);
+    if (rc) return rc;
+    for (;;) {
+        bool any = false;
+        for (auto &S : h->slots)
+            if (S.phase != PH_EMPTY) any = true;
+        if (!any) break;
+        rc = phase_trials(h, Qu);
+        if (rc) return rc;
+        rc = phase_step(h);
+        if (rc) return rc;
+    }
+    CK(cudaEventRecord(t1, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, t0, t1));
+    h->prof.solve_ms = ms;
+    prof_collect(h);
+    return SDCA_OK;
+}
+
+int sdca_solve(sdca_handle *h, const uint32_t *loci, size_t n_loci, float *scores,
+               sdca_locus_stat *stats)
+{
+    return sdca_solve_ex(h, loci, n_loci, nullptr, nullptr, scores, stats);
+}
+
+int sdca_eval(sdca_handle *h, uint32_t r, const double *x, double *f, double *g)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (!x || !f) return fail(h, SDCA_E_ARG, "null argument");
+    const Problem &P = h->P;
+    if ((int64_t)r >= P.L) return fail(h, SDCA_E_ARG, "locus index out of range");
+    CK(cudaSetDevice(h->cfg.device));
+    prof_reset(h);
+    std::vector<float> xe(P.Dp);
+    ref_to_engine(P, r, x, xe.data());
+    const int b = 0;
+    rc = slot_begin(h, b, 0, (int32_t)r, xe.data());
+    if (rc) return rc;
+    std::vector<int32_t> one{b};
+    rc = run_forward(h, one, h->wa, true);
+    if (rc) return rc;
+    SlotHost &S = h->slots[b];
+    rc = upload_slots(h, one);
+    if (rc) return rc;
+    rc = zero_acc(h);
+    if (rc) return rc;
+    launch_trial(P, h->sd, h->list, 1, h->lbase, h->u, h->rstate, h->w, h->R, h->acc, h->stream);
+    CKL();
+    rc = fetch_acc(h);
+    if (rc) return rc;
+    const double fdata = acc_get(h, b, ACC_F);
+    for (int a = 0; a < Q; ++a) S.rs[a] = acc_get(h, b, ACC_RS0 + a);
+    S.push = false;
+    S.ring_new = -1;
+    rc = upload_slots(h, one);
+    if (rc) return rc;
+    rc = zero_acc(h);
+    if (rc) return rc;
+    launch_bwd_gather(P, h->XT, h->sd, h->list, 1, h->R, h->wa, h->gpool, h->Ypool, h->Spool,
+                      h->hist_bf16, h->acc, h->stream);
+    launch_hpart(P, h->sd, h->list, 1, h->wa, h->gpool, h->Ypool, h->Spool, h->hist_bf16, h->acc,
+                 h->stream);
+    CKL();
+    rc = fetch_acc(h);
+    if (rc) return rc;
+    *f = fdata + P.lambda_J * acc_get(h, b, ACC_X2J) + P.lambda_h * acc_get(h, b, ACC_X2H);
+    if (g) {
+        std::vector<float> ge(P.Dp);
+        CK(cudaMemcpyAsync(ge.data(), h->gpool + (int64_t)(2 * b + 1 - S.gcur) * P.Dp,
+                           sizeof(float) * P.Dp, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        engine_to_ref(P, ge.data(), g);
+    }
+    S.phase = PH_EMPTY;
+    return SDCA_OK;
+}
+
+int sdca_compute_weights(sdca_handle *h, const uint8_t *states, const double *mult,
+                         double threshold, double *weights_out)
+{
+    (void)states; (void)mult; (void)threshold; (void)weights_out;
+    if (!h) return SDCA_E_ARG;
+    return fail(h, SDCA_E_UNSUPPORTED, "sequence reweighting on the GPU is not in this build");
+}
+
+int sdca_get_profile(const sdca_handle *h, sdca_profile *out)
+{
+    if (!h || !out) return SDCA_E_ARG;
+    *out = h->prof;
+    return SDCA_OK;
+}
+
+const char *sdca_last_error(const sdca_handle *h)
+{
+    if (!h) {
+        std::lock_guard<std::mutex> lk(g_err_mu);
+        return g_create_err.c_str();
+    }
+    return h->err.c_str();
+}
+
+int sdca_destroy(sdca_handle *h)
+{
+    if (!h) return SDCA_OK;
+    cudaSetDevice(h->cfg.device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (auto e : h->ev_pool) cudaEventDestroy(e);
+    free_all(h);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return SDCA_OK;
+}
+
+// Test hook (not part of the public header): the compact-form coefficients.
+int sdca_internal_lbfgs_coeffs(int k, const double *R, const double *YY, const double *sg,
+                               const double *yg, double gamma, double *coef_g, double *coefS,
+                               double *coefY)
+{
+    return lbfgs_compact_coeffs(k, R, YY, sg, yg, gamma, coef_g, coefS, coefY) ? 0 : -1;
+}
+
+} // extern "C"

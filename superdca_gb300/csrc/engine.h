@@ -1,0 +1,116 @@
+// engine.h -- internal structures of the GB300 plmDCA solve engine.
+//
+// Device data layout ("engine layout"), q = 4:
+//   X   [N][Lx]  uint8 state codes, sequence-major (Lx = L rounded up to 64)
+//   XT  [L][Nx]  uint8 state codes, locus-major    (Nx = N rounded up to 64)
+//   per slot b, a parameter vector of Dp floats (Dp = 16 L + 4 rounded up to
+//   64): J_r[n][s][a] at 16 n + 4 s + a, h_r[a] at 16 L + a, zero padding.
+//   The J_rr block (n == r) is held at zero and never enters the objective,
+//   as in SuperDCA/include/plmDCA_objective.hpp:107-120,174-188,224-242.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/superdca_gb300.h"
+
+namespace sdca {
+
+constexpr int Q = 4;
+constexpr int QQ = Q * Q;
+constexpr int MAXHIST = 10;      // upper bound on the L-BFGS history length m
+
+// per-slot accumulators (doubles), zeroed by the host before each use
+enum Acc {
+    ACC_F = 0,      // sum_i w_i (lse_i - l_i[s_i(r)])             (trial)
+    ACC_DG,         // sum_i R_i . u_i                              (trial)
+    ACC_RS0,        // sum_i R_i[a], a = 0..3                       (trial)
+    ACC_RS1, ACC_RS2, ACC_RS3,
+    ACC_G2,         // ||g||^2                                      (gradient)
+    ACC_X2J,        // ||x_J||^2                                    (gradient)
+    ACC_X2H,        // ||x_h||^2                                    (gradient)
+    ACC_SY,         // s_k . y_k                                    (gradient)
+    ACC_YY,         // y_k . y_k                                    (gradient)
+    ACC_GD,         // g . d                                        (direction)
+    ACC_DDJ,        // d_J . d_J                                    (direction)
+    ACC_DDH,        // d_h . d_h                                    (direction)
+    ACC_XDJ,        // x_J . d_J                                    (direction)
+    ACC_XDH,        // x_h . d_h                                    (direction)
+    ACC_GMAX,       // max |g| (bits of a non-negative double, atomicMax) (gradient)
+    NACC = 20
+};
+
+// Per-slot parameters the kernels read; mirrored from the host before launches.
+struct SlotDev {
+    int32_t locus;          // target locus r
+    int32_t gcur;           // g buffer holding the accepted gradient (0/1)
+    int32_t ring_new;       // history position written by the last accept, -1 none
+    int32_t nhist;          // history pairs in use
+    int32_t ring[MAXHIST];  // history positions, oldest first
+    int32_t flags;          // SLOT_F_*
+    int32_t pad_;
+    double stp;             // trial (or accepted) step along d
+    double coef_g;          // direction = coef_g g + sum coefS_j s_j + coefY_j y_j
+    double coefS[MAXHIST];
+    double coefY[MAXHIST];
+    double rs[Q];           // R sums at the accepted point (h gradient)
+};
+
+enum SlotFlags {
+    SLOT_F_USE_U = 1,       // trial logits use lbase + stp u (else lbase)
+    SLOT_F_PUSH = 2,        // accept pushes an (s, y) pair into the history
+};
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+// launch configuration for the kernels of one call
+struct SlotList {
+    const int32_t *list;    // device array of slot indices
+    int n;
+};
+
+struct Problem {
+    int64_t N = 0, L = 0, Lx = 0, Nx = 0, Dp = 0, LC = 0, C = 0;
+    int m = 10;
+    int ring = 11;   // history positions per slot: m + 1 (one spare for the pending pair)
+    int Bmax = 0;
+    double lambda_h = 0, lambda_J = 0, b_eff = 0;
+};
+
+// kernel launchers (kernels_*.cu)
+void launch_fwd_gather(const Problem &P, const uint8_t *X, const int32_t *list, int n,
+                       const float *vecs, float *partial, cudaStream_t st);
+void launch_reduce_partial(const Problem &P, const int32_t *list, int n, const float *partial,
+                           const float *vecs, int add_h, float *out_f, double *out_d,
+                           cudaStream_t st);
+void launch_bwd_gather(const Problem &P, const uint8_t *XT, const SlotDev *sd,
+                       const int32_t *list, int n, const float *R, const float *wa,
+                       float *gpool, void *Ypool, const void *Spool, int hist_bf16,
+                       double *acc, cudaStream_t st);
+void launch_hpart(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                  const float *wa, float *gpool, void *Ypool, const void *Spool, int hist_bf16,
+                  double *acc, cudaStream_t st);
+void launch_trial(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                  const double *lbase, const float *u, const uint8_t *rstate, const double *w,
+                  float *R, double *acc, cudaStream_t st);
+void launch_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float *wa,
+                   const float *d, void *Spool, int hist_bf16, cudaStream_t st);
+void launch_lbase_update(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                         double *lbase, const float *u, cudaStream_t st);
+void launch_hist_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                      const float *gpool, const void *Spool, const void *Ypool, int hist_bf16,
+                      double *dots, cudaStream_t st);
+void launch_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                      const float *gpool, const void *Spool, const void *Ypool, int hist_bf16,
+                      const float *wa, float *d, double *acc, cudaStream_t st);
+void launch_score(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                  const float *wa, int gap, float *rows, cudaStream_t st);
+
+} // namespace sdca

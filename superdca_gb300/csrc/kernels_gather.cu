@@ -1,0 +1,251 @@
+// kernels_gather.cu -- the plain contraction form: FP32 gather (forward) and
+// masked accumulation (backward) on CUDA cores.
+//
+// forward   u_b[i][a] = sum_n v_b[n][X_in][a]                 (X one-hot . v_J)
+// backward  g_b[n][s][a] = sum_{i: X_in = s} R_b[i][a] + 2 lambda_J x_b[n][s][a]
+//
+// These are SuperDCA's block gather (SuperDCA/include/plmDCA_objective.hpp:86-121,
+// Coupling_matrix_view.hpp:59-86) and gradient scatter (plmDCA_objective.hpp:
+// 153-190, Coupling_matrix_view.hpp:88-111) for a batch of target loci that
+// share one alignment read.  Both are bound by shared-memory / FP32 issue
+// (one 16-byte shared load or 16 FMAs per (sequence, locus, slot)).
+#include "engine.h"
+#include "kernels_common.cuh"
+
+namespace sdca {
+
+namespace {
+
+constexpr int FWD_THREADS = 256;  // sequences per CTA
+constexpr int FWD_G = 8;          // slots per CTA
+constexpr int FWD_SUB = 32;       // loci per shared-memory sub-tile
+
+__global__ void __launch_bounds__(FWD_THREADS)
+k_fwd_gather(const uint8_t *__restrict__ X, int64_t Lx, int N, int L, int64_t LC,
+             const int32_t *__restrict__ list, int nlist, const float *__restrict__ vecs,
+             int64_t Dp, float4 *__restrict__ partial, int Bmax, int64_t Nx)
+{
+    __shared__ float4 sJ[FWD_G][FWD_SUB][Q];
+    const int i = blockIdx.x * FWD_THREADS + threadIdx.x;
+    const int c = blockIdx.z;
+    const int64_t n_begin = (int64_t)c * LC;
+    const int64_t n_end = min((int64_t)L, n_begin + LC);
+    int slot[FWD_G];
+#pragma unroll
+    for (int g = 0; g < FWD_G; ++g) {
+        const int k = blockIdx.y * FWD_G + g;
+        slot[g] = k < nlist ? list[k] : -1;
+    }
+    float4 acc[FWD_G];
+#pragma unroll
+    for (int g = 0; g < FWD_G; ++g) acc[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+
+    for (int64_t n0 = n_begin; n0 < n_end; n0 += FWD_SUB) {
+        for (int k = threadIdx.x; k < FWD_G * FWD_SUB * Q; k += FWD_THREADS) {
+            const int g = k / (FWD_SUB * Q), rem = k % (FWD_SUB * Q);
+            const int nl = rem / Q, s = rem % Q;
+            const int64_t n = n0 + nl;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (slot[g] >= 0 && n < n_end)
+                v = reinterpret_cast<const float4 *>(vecs + (int64_t)slot[g] * Dp)[n * Q + s];
+            sJ[g][nl][s] = v;
+        }
+        __syncthreads();
+        if (i < N) {
+            const uint4 *xp = reinterpret_cast<const uint4 *>(X + (int64_t)i * Lx + n0);
+            const uint4 w0 = xp[0], w1 = xp[1];
+            const uint32_t words[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+            for (int wd = 0; wd < 8; ++wd) {
+#pragma unroll
+                for (int bt = 0; bt < 4; ++bt) {
+                    const int nl = wd * 4 + bt;
+                    const int s = (words[wd] >> (8 * bt)) & 0x3;
+#pragma unroll
+                    for (int g = 0; g < FWD_G; ++g) {
+                        const float4 j = sJ[g][nl][s];
+                        acc[g].x += j.x;
+                        acc[g].y += j.y;
+                        acc[g].z += j.z;
+                        acc[g].w += j.w;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (i < N) {
+#pragma unroll
+        for (int g = 0; g < FWD_G; ++g)
+            if (slot[g] >= 0) partial[((int64_t)c * Bmax + slot[g]) * Nx + i] = acc[g];
+    }
+}
+
+__global__ void k_reduce_partial(const float4 *__restrict__ partial, int C, int Bmax, int64_t Nx,
+                                 int N, const int32_t *__restrict__ list,
+                                 const float *__restrict__ vecs, int64_t Dp, int64_t hoff,
+                                 int add_h, float4 *__restrict__ out_f, double *__restrict__ out_d)
+{
+    const int b = list[blockIdx.y];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    if (add_h) {
+        const float *h = vecs + (int64_t)b * Dp + hoff;
+        s0 = h[0]; s1 = h[1]; s2 = h[2]; s3 = h[3];
+    }
+    for (int c = 0; c < C; ++c) {
+        const float4 p = partial[((int64_t)c * Bmax + b) * Nx + i];
+        s0 += p.x; s1 += p.y; s2 += p.z; s3 += p.w;
+    }
+    const int64_t o = (int64_t)b * Nx + i;
+    if (out_f) out_f[o] = make_float4((float)s0, (float)s1, (float)s2, (float)s3);
+    if (out_d) {
+        out_d[o * 4 + 0] = s0; out_d[o * 4 + 1] = s1;
+        out_d[o * 4 + 2] = s2; out_d[o * 4 + 3] = s3;
+    }
+}
+
+constexpr int BWD_THREADS = 128;  // loci per CTA
+constexpr int BWD_G = 4;          // slots per CTA
+constexpr int BWD_SUB = 64;       // sequences per shared-memory sub-tile
+
+__global__ void __launch_bounds__(BWD_THREADS)
+k_bwd_gather(const uint8_t *__restrict__ XT, int64_t Nx, int N, int L,
+             const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int nlist,
+             const float4 *__restrict__ R, const float *__restrict__ wa, float *__restrict__ gpool,
+             void *__restrict__ Ypool, const void *__restrict__ Spool, int hist_bf16, int m,
+             int64_t Dp, double lambda_J, double *__restrict__ acc)
+{
+    __shared__ float4 sR[BWD_G][BWD_SUB];
+    const int n = blockIdx.x * BWD_THREADS + threadIdx.x;
+    int slot[BWD_G];
+#pragma unroll
+    for (int g = 0; g < BWD_G; ++g) {
+        const int k = blockIdx.y * BWD_G + g;
+        slot[g] = k < nlist ? list[k] : -1;
+    }
+    float a[BWD_G][QQ];
+#pragma unroll
+    for (int g = 0; g < BWD_G; ++g)
+#pragma unroll
+        for (int k = 0; k < QQ; ++k) a[g][k] = 0.f;
+
+    for (int i0 = 0; i0 < N; i0 += BWD_SUB) {
+        for (int k = threadIdx.x; k < BWD_G * BWD_SUB; k += BWD_THREADS) {
+            const int g = k / BWD_SUB, ii = k % BWD_SUB;
+            const int i = i0 + ii;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (slot[g] >= 0 && i < N) v = R[(int64_t)slot[g] * Nx + i];
+            sR[g][ii] = v;
+        }
+        __syncthreads();
+        if (n < L) {
+            const uint4 *xp = reinterpret_cast<const uint4 *>(XT + (int64_t)n * Nx + i0);
+#pragma unroll
+            for (int q4 = 0; q4 < BWD_SUB / 16; ++q4) {
+                const uint4 w = xp[q4];
+                const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                for (int wd = 0; wd < 4; ++wd) {
+#pragma unroll
+                    for (int bt = 0; bt < 4; ++bt) {
+                        const int ii = q4 * 16 + wd * 4 + bt;
+                        const int s = (words[wd] >> (8 * bt)) & 0x3;
+                        const float m0 = s == 0, m1 = s == 1, m2 = s == 2, m3 = s == 3;
+#pragma unroll
+                        for (int g = 0; g < BWD_G; ++g) {
+                            const float4 r = sR[g][ii];
+                            a[g][0] += m0 * r.x; a[g][1] += m0 * r.y; a[g][2] += m0 * r.z; a[g][3] += m0 * r.w;
+                            a[g][4] += m1 * r.x; a[g][5] += m1 * r.y; a[g][6] += m1 * r.z; a[g][7] += m1 * r.w;
+                            a[g][8] += m2 * r.x; a[g][9] += m2 * r.y; a[g][10] += m2 * r.z; a[g][11] += m2 * r.w;
+                            a[g][12] += m3 * r.x; a[g][13] += m3 * r.y; a[g][14] += m3 * r.z; a[g][15] += m3 * r.w;
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    // epilogue: + 2 lambda_J x, zero the J_rr block, push y, reductions
+    const float l2 = (float)(2.0 * lambda_J);
+#pragma unroll
+    for (int g = 0; g < BWD_G; ++g) {
+        if (slot[g] < 0) continue;  // uniform across the block
+        const int b = slot[g];
+        const SlotDev &S = sd[b];
+        float gmax = 0.f, g2 = 0.f, x2 = 0.f, sy = 0.f, yy = 0.f;
+        if (n < L) {
+            const float *x = wa + (int64_t)b * Dp + (int64_t)n * QQ;
+            float *gn = gpool + (int64_t)(2 * b + 1 - S.gcur) * Dp + (int64_t)n * QQ;
+            const float *go = gpool + (int64_t)(2 * b + S.gcur) * Dp + (int64_t)n * QQ;
+            const bool zero = (n == S.locus);
+            const bool push = (S.flags & SLOT_F_PUSH) && S.ring_new >= 0;
+            const int64_t hoff = ((int64_t)b * m + (push ? S.ring_new : 0)) * Dp + (int64_t)n * QQ;
+#pragma unroll
+            for (int k4 = 0; k4 < 4; ++k4) {
+                const float4 xv = reinterpret_cast<const float4 *>(x)[k4];
+                float4 gv;
+                gv.x = zero ? 0.f : a[g][4 * k4 + 0] + l2 * xv.x;
+                gv.y = zero ? 0.f : a[g][4 * k4 + 1] + l2 * xv.y;
+                gv.z = zero ? 0.f : a[g][4 * k4 + 2] + l2 * xv.z;
+                gv.w = zero ? 0.f : a[g][4 * k4 + 3] + l2 * xv.w;
+                reinterpret_cast<float4 *>(gn)[k4] = gv;
+                gmax = fmaxf(gmax, fmaxf(fmaxf(fabsf(gv.x), fabsf(gv.y)), fmaxf(fabsf(gv.z), fabsf(gv.w))));
+                g2 += dot4(gv, gv);
+                x2 += dot4(xv, xv);
+                if (push) {
+                    const float4 ov = reinterpret_cast<const float4 *>(go)[k4];
+                    float4 yv = make_float4(gv.x - ov.x, gv.y - ov.y, gv.z - ov.z, gv.w - ov.w);
+                    yv = store_hist4(Ypool, hoff + 4 * k4, yv, hist_bf16);
+                    const float4 sv = load_hist4(Spool, hoff + 4 * k4, hist_bf16);
+                    sy += dot4(sv, yv);
+                    yy += dot4(yv, yv);
+                }
+            }
+        }
+        double v[4] = {g2, x2, sy, yy};
+        const int idx[4] = {ACC_G2, ACC_X2J, ACC_SY, ACC_YY};
+        block_sum_atomic<4>(v, acc + (int64_t)b * NACC, idx);
+        const float wm = warp_max(gmax);
+        if ((threadIdx.x & 31) == 0 && wm > 0.f) atomic_max_nonneg(acc + (int64_t)b * NACC + ACC_GMAX, (double)wm);
+    }
+}
+
+} // namespace
+
+void launch_fwd_gather(const Problem &P, const uint8_t *X, const int32_t *list, int n,
+                       const float *vecs, float *partial, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 grid((unsigned)((P.N + FWD_THREADS - 1) / FWD_THREADS), (unsigned)((n + FWD_G - 1) / FWD_G),
+              (unsigned)P.C);
+    k_fwd_gather<<<grid, FWD_THREADS, 0, st>>>(X, P.Lx, (int)P.N, (int)P.L, P.LC, list, n, vecs, P.Dp,
+                                               reinterpret_cast<float4 *>(partial), P.Bmax, P.Nx);
+}
+
+void launch_reduce_partial(const Problem &P, const int32_t *list, int n, const float *partial,
+                           const float *vecs, int add_h, float *out_f, double *out_d,
+                           cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 grid((unsigned)((P.N + 255) / 256), (unsigned)n);
+    k_reduce_partial<<<grid, 256, 0, st>>>(reinterpret_cast<const float4 *>(partial), (int)P.C,
+                                           P.Bmax, P.Nx, (int)P.N, list, vecs, P.Dp, QQ * P.L, add_h,
+                                           reinterpret_cast<float4 *>(out_f), out_d);
+}
+
+void launch_bwd_gather(const Problem &P, const uint8_t *XT, const SlotDev *sd,
+                       const int32_t *list, int n, const float *R, const float *wa,
+                       float *gpool, void *Ypool, const void *Spool, int hist_bf16,
+                       double *acc, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 grid((unsigned)((P.L + BWD_THREADS - 1) / BWD_THREADS), (unsigned)((n + BWD_G - 1) / BWD_G));
+    k_bwd_gather<<<grid, BWD_THREADS, 0, st>>>(XT, P.Nx, (int)P.N, (int)P.L, sd, list, n,
+                                               reinterpret_cast<const float4 *>(R), wa, gpool, Ypool,
+                                               Spool, hist_bf16, P.ring, P.Dp, P.lambda_J, acc);
+}
+
+} // namespace sdca

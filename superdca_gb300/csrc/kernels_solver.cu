@@ -1,0 +1,390 @@
+// kernels_solver.cu -- per-slot solver kernels shared by every contraction
+// form: line-search trials, iterate update, L-BFGS history and direction,
+// and coupling scores.
+//
+// Line-search trials never run a contraction.  The logits of sequence i are
+// affine in the step along d: l_i(stp) = lbase_i + stp * u_i with
+// u_i = X_i . d_J + d_h, so a trial needs O(N q) work per slot.  This is
+// exactly SuperDCA's objective along the search line (plmDCA_objective.hpp:
+// 126-151 for the pseudo-likelihood part; the L2 part is a quadratic in stp
+// that the host evaluates from x.d and d.d).
+#include "engine.h"
+#include "kernels_common.cuh"
+
+namespace sdca {
+
+namespace {
+
+constexpr int TRIAL_THREADS = 256;
+
+__global__ void __launch_bounds__(TRIAL_THREADS)
+k_trial(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int N, int64_t Nx,
+        const double *__restrict__ lbase, const float4 *__restrict__ u,
+        const uint8_t *__restrict__ rstate, const double *__restrict__ w, float4 *__restrict__ R,
+        double *__restrict__ acc)
+{
+    const int b = list[blockIdx.y];
+    const SlotDev &S = sd[b];
+    const double stp = S.stp;
+    const bool use_u = S.flags & SLOT_F_USE_U;
+    double f = 0, dg = 0, rs0 = 0, rs1 = 0, rs2 = 0, rs3 = 0;
+    for (int i = blockIdx.x * TRIAL_THREADS + threadIdx.x; i < N; i += gridDim.x * TRIAL_THREADS) {
+        const int64_t o = (int64_t)b * Nx + i;
+        const double *lb = lbase + o * 4;
+        const float4 uu = use_u ? u[o] : make_float4(0.f, 0.f, 0.f, 0.f);
+        double l[4] = {lb[0] + stp * uu.x, lb[1] + stp * uu.y, lb[2] + stp * uu.z,
+                       lb[3] + stp * uu.w};
+        const double mx = fmax(fmax(l[0], l[1]), fmax(l[2], l[3]));
+        double e[4], z = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            e[a] = exp(l[a] - mx);
+            z += e[a];
+        }
+        const double lse = mx + log(z);
+        const int sr = rstate[o];
+        const double wi = w[i];
+        f += wi * (lse - l[sr]);
+        double r[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) r[a] = wi * (e[a] / z) - (a == sr ? wi : 0.0);
+        dg += r[0] * uu.x + r[1] * uu.y + r[2] * uu.z + r[3] * uu.w;
+        rs0 += r[0]; rs1 += r[1]; rs2 += r[2]; rs3 += r[3];
+        R[o] = make_float4((float)r[0], (float)r[1], (float)r[2], (float)r[3]);
+    }
+    double v[6] = {f, dg, rs0, rs1, rs2, rs3};
+    const int idx[6] = {ACC_F, ACC_DG, ACC_RS0, ACC_RS1, ACC_RS2, ACC_RS3};
+    block_sum_atomic<6>(v, acc + (int64_t)b * NACC, idx);
+}
+
+// x <- x + stp d; with a history push, s = x_new - x_old goes to ring_new.
+__global__ void k_accept(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list,
+                         int64_t Dp, int m, float *__restrict__ wa, const float *__restrict__ d,
+                         void *__restrict__ Spool, int hist_bf16)
+{
+    const int b = list[blockIdx.y];
+    const SlotDev &S = sd[b];
+    const float stp = (float)S.stp;
+    const bool push = (S.flags & SLOT_F_PUSH) && S.ring_new >= 0;
+    for (int64_t e = 4 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); e < Dp;
+         e += 4 * (int64_t)gridDim.x * blockDim.x) {
+        float4 *xp = reinterpret_cast<float4 *>(wa + (int64_t)b * Dp + e);
+        const float4 x = *xp;
+        const float4 dv = *reinterpret_cast<const float4 *>(d + (int64_t)b * Dp + e);
+        float4 xn;
+        xn.x = fmaf(stp, dv.x, x.x);
+        xn.y = fmaf(stp, dv.y, x.y);
+        xn.z = fmaf(stp, dv.z, x.z);
+        xn.w = fmaf(stp, dv.w, x.w);
+        if (push)
+            store_hist4(Spool, ((int64_t)b * m + S.ring_new) * Dp + e,
+                        make_float4(xn.x - x.x, xn.y - x.y, xn.z - x.z, xn.w - x.w), hist_bf16);
+        *xp = xn;
+    }
+}
+
+__global__ void k_lbase_update(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list,
+                               int N, int64_t Nx, double *__restrict__ lbase,
+                               const float4 *__restrict__ u)
+{
+    const int b = list[blockIdx.y];
+    const double stp = sd[b].stp;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N || stp == 0.0) return;
+    const int64_t o = (int64_t)b * Nx + i;
+    const float4 uu = u[o];
+    double *lb = lbase + o * 4;
+    lb[0] += stp * uu.x;
+    lb[1] += stp * uu.y;
+    lb[2] += stp * uu.z;
+    lb[3] += stp * uu.w;
+}
+
+// gradient of h_r: sum_i R_i + 2 lambda_h h (plmDCA_objective.hpp:149,198)
+__global__ void k_hpart(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list,
+                        int64_t L, int64_t Dp, int m, double lambda_h, const float *__restrict__ wa,
+                        float *__restrict__ gpool, void *__restrict__ Ypool,
+                        const void *__restrict__ Spool, int hist_bf16, double *__restrict__ acc)
+{
+    const int b = list[blockIdx.x];
+    if (threadIdx.x != 0) return;
+    const SlotDev &S = sd[b];
+    const int64_t hoff = QQ * L;
+    const float *x = wa + (int64_t)b * Dp + hoff;
+    float *gn = gpool + (int64_t)(2 * b + 1 - S.gcur) * Dp + hoff;
+    const float *go = gpool + (int64_t)(2 * b + S.gcur) * Dp + hoff;
+    const bool push = (S.flags & SLOT_F_PUSH) && S.ring_new >= 0;
+    double g2 = 0, x2 = 0, sy = 0, yy = 0, gmax = 0;
+    float4 gv, yv;
+    float *gp = &gv.x, *yp = &yv.x;
+    for (int a = 0; a < 4; ++a) {
+        const double g = S.rs[a] + 2.0 * lambda_h * (double)x[a];
+        gp[a] = (float)g;
+        gn[a] = gp[a];
+        g2 += (double)gp[a] * gp[a];
+        x2 += (double)x[a] * x[a];
+        gmax = fmax(gmax, fabs((double)gp[a]));
+        yp[a] = gp[a] - go[a];
+    }
+    if (push) {
+        const int64_t off = ((int64_t)b * m + S.ring_new) * Dp + hoff;
+        yv = store_hist4(Ypool, off, yv, hist_bf16);
+        const float4 sv = load_hist4(Spool, off, hist_bf16);
+        sy = (double)dot4(sv, yv);
+        yy = (double)dot4(yv, yv);
+    }
+    double *A = acc + (int64_t)b * NACC;
+    atomicAdd(A + ACC_G2, g2);
+    atomicAdd(A + ACC_X2H, x2);
+    if (push) {
+        atomicAdd(A + ACC_SY, sy);
+        atomicAdd(A + ACC_YY, yy);
+    }
+    if (gmax > 0) atomic_max_nonneg(A + ACC_GMAX, gmax);
+}
+
+constexpr int DOT_THREADS = 256;
+
+// dots[b] = [S_j.g | Y_j.g | S_j.y_new | Y_j.y_new], j over the history
+__global__ void __launch_bounds__(DOT_THREADS)
+k_hist_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Dp, int m,
+            const float *__restrict__ gpool, const void *__restrict__ Spool,
+            const void *__restrict__ Ypool, int hist_bf16, double *__restrict__ dots)
+{
+    const int b = list[blockIdx.y];
+    const SlotDev &S = sd[b];
+    const int nh = S.nhist;
+    const float *g = gpool + (int64_t)(2 * b + S.gcur) * Dp;
+    const bool has_new = S.ring_new >= 0;
+    const int64_t ybase = ((int64_t)b * m + (has_new ? S.ring_new : 0)) * Dp;
+    float aSg[MAXHIST], aYg[MAXHIST], aSy[MAXHIST], aYy[MAXHIST];
+#pragma unroll
+    for (int j = 0; j < MAXHIST; ++j) aSg[j] = aYg[j] = aSy[j] = aYy[j] = 0.f;
+    for (int64_t e = 4 * ((int64_t)blockIdx.x * DOT_THREADS + threadIdx.x); e < Dp;
+         e += 4 * (int64_t)gridDim.x * DOT_THREADS) {
+        const float4 gv = *reinterpret_cast<const float4 *>(g + e);
+        const float4 yn = has_new ? load_hist4(Ypool, ybase + e, hist_bf16)
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < MAXHIST; ++j) {
+            if (j < nh) {
+                const int64_t off = ((int64_t)b * m + S.ring[j]) * Dp + e;
+                const float4 sv = load_hist4(Spool, off, hist_bf16);
+                const float4 yv = load_hist4(Ypool, off, hist_bf16);
+                aSg[j] += dot4(sv, gv);
+                aYg[j] += dot4(yv, gv);
+                aSy[j] += dot4(sv, yn);
+                aYy[j] += dot4(yv, yn);
+            }
+        }
+    }
+    double v[4 * MAXHIST];
+    int idx[4 * MAXHIST];
+#pragma unroll
+    for (int j = 0; j < MAXHIST; ++j) {
+        v[j] = aSg[j];
+        v[MAXHIST + j] = aYg[j];
+        v[2 * MAXHIST + j] = aSy[j];
+        v[3 * MAXHIST + j] = aYy[j];
+    }
+#pragma unroll
+    for (int k = 0; k < 4 * MAXHIST; ++k) idx[k] = k;
+    block_sum_atomic<4 * MAXHIST>(v, dots + (int64_t)b * 4 * MAXHIST, idx);
+}
+
+// d = coef_g g + sum_j (coefS_j s_j + coefY_j y_j), J_rr block zero;
+// reductions g.d, d.d and x.d split into the J and h parts.
+__global__ void __launch_bounds__(DOT_THREADS)
+k_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t L,
+            int64_t Dp, int m, const float *__restrict__ gpool, const void *__restrict__ Spool,
+            const void *__restrict__ Ypool, int hist_bf16, const float *__restrict__ wa,
+            float *__restrict__ d, double *__restrict__ acc)
+{
+    const int b = list[blockIdx.y];
+    const SlotDev &S = sd[b];
+    const int nh = S.nhist;
+    const float *g = gpool + (int64_t)(2 * b + S.gcur) * Dp;
+    const float cg = (float)S.coef_g;
+    float cS[MAXHIST], cY[MAXHIST];
+#pragma unroll
+    for (int j = 0; j < MAXHIST; ++j) {
+        cS[j] = j < nh ? (float)S.coefS[j] : 0.f;
+        cY[j] = j < nh ? (float)S.coefY[j] : 0.f;
+    }
+    const int64_t hoff = QQ * L;
+    const int64_t rlo = (int64_t)S.locus * QQ, rhi = rlo + QQ;
+    float gd = 0.f, ddJ = 0.f, ddH = 0.f, xdJ = 0.f, xdH = 0.f;
+    for (int64_t e = 4 * ((int64_t)blockIdx.x * DOT_THREADS + threadIdx.x); e < Dp;
+         e += 4 * (int64_t)gridDim.x * DOT_THREADS) {
+        const float4 gv = *reinterpret_cast<const float4 *>(g + e);
+        float4 dv = make_float4(cg * gv.x, cg * gv.y, cg * gv.z, cg * gv.w);
+#pragma unroll
+        for (int j = 0; j < MAXHIST; ++j) {
+            if (j < nh) {
+                const int64_t off = ((int64_t)b * m + S.ring[j]) * Dp + e;
+                const float4 sv = load_hist4(Spool, off, hist_bf16);
+                const float4 yv = load_hist4(Ypool, off, hist_bf16);
+                dv.x += cS[j] * sv.x + cY[j] * yv.x;
+                dv.y += cS[j] * sv.y + cY[j] * yv.y;
+                dv.z += cS[j] * sv.z + cY[j] * yv.z;
+                dv.w += cS[j] * sv.w + cY[j] * yv.w;
+            }
+        }
+        if (e >= rlo && e < rhi) dv = make_float4(0.f, 0.f, 0.f, 0.f);
+        *reinterpret_cast<float4 *>(d + (int64_t)b * Dp + e) = dv;
+        const float4 xv = *reinterpret_cast<const float4 *>(wa + (int64_t)b * Dp + e);
+        gd += dot4(gv, dv);
+        if (e < hoff) {
+            ddJ += dot4(dv, dv);
+            xdJ += dot4(xv, dv);
+        } else {
+            ddH += dot4(dv, dv);
+            xdH += dot4(xv, dv);
+        }
+    }
+    double v[5] = {gd, ddJ, ddH, xdJ, xdH};
+    const int idx[5] = {ACC_GD, ACC_DDJ, ACC_DDH, ACC_XDJ, ACC_XDH};
+    block_sum_atomic<5>(v, acc + (int64_t)b * NACC, idx);
+}
+
+// S[r][n] = || gauge(M) ||_F without GAP, M = J_rn (transposed for n < r):
+// SuperDCA/include/plmDCA.hpp:378-393, plmDCA_utility.hpp:57-83,
+// Matrix_math.hpp:166-213.  G[i][j] = ((M[i][j] - rowmean(M)[j]) -
+// colmean(M)[i]) + mean(rowmean(M)), evaluated in FP64 like the reference.
+__global__ void k_score(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list,
+                        int64_t L, int64_t Dp, const float *__restrict__ wa, int gap,
+                        float *__restrict__ rows)
+{
+    const int k = blockIdx.y;
+    const int b = list[k];
+    const int64_t r = sd[b].locus;
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= L) return;
+    float *row = rows + (int64_t)k * L;
+    if (n == r) {
+        row[n] = __int_as_float(0x7fc00000);
+        return;
+    }
+    const float4 *jp = reinterpret_cast<const float4 *>(wa + (int64_t)b * Dp + n * QQ);
+    double J[4][4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const float4 v = jp[s];
+        const double t[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            if (n < r) J[a][s] = t[a];
+            else J[s][a] = t[a];
+        }
+    }
+    double rm[4], cm[4], gm = 0.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        double t = 0.0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) t = t + J[i][j];
+        rm[i] = t / 4.0;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        double t = 0.0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) t = t + J[i][j];
+        cm[j] = t / 4.0;
+    }
+    {
+        double t = 0.0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) t += rm[i];
+        gm = t / 4.0;
+    }
+    double sum = 0.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        if (i == gap) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (j == gap) continue;
+            const double gij = ((J[i][j] - rm[j]) - cm[i]) + gm;
+            sum += gij * gij;
+        }
+    }
+    row[n] = (float)sqrt(sum);
+}
+
+unsigned dgrid(int64_t Dp, int threads)
+{
+    const int64_t need = (Dp / 4 + threads - 1) / threads;
+    return (unsigned)(need < 256 ? need : 256);
+}
+
+} // namespace
+
+void launch_trial(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                  const double *lbase, const float *u, const uint8_t *rstate, const double *w,
+                  float *R, double *acc, cudaStream_t st)
+{
+    if (n <= 0) return;
+    int gx = (int)((P.N + TRIAL_THREADS - 1) / TRIAL_THREADS);
+    if (gx > 32) gx = 32;
+    dim3 grid((unsigned)gx, (unsigned)n);
+    k_trial<<<grid, TRIAL_THREADS, 0, st>>>(sd, list, (int)P.N, P.Nx, lbase,
+                                            reinterpret_cast<const float4 *>(u), rstate, w,
+                                            reinterpret_cast<float4 *>(R), acc);
+}
+
+void launch_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float *wa,
+                   const float *d, void *Spool, int hist_bf16, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 grid(dgrid(P.Dp, 256), (unsigned)n);
+    k_accept<<<grid, 256, 0, st>>>(sd, list, P.Dp, P.ring, wa, d, Spool, hist_bf16);
+}
+
+void launch_lbase_update(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                         double *lbase, const float *u, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 grid((unsigned)((P.N + 255) / 256), (unsigned)n);
+    k_lbase_update<<<grid, 256, 0, st>>>(sd, list, (int)P.N, P.Nx, lbase,
+                                         reinterpret_cast<const float4 *>(u));
+}
+
+void launch_hpart(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                  const float *wa, float *gpool, void *Ypool, const void *Spool, int hist_bf16,
+                  double *acc, cudaStream_t st)
+{
+    if (n <= 0) return;
+    k_hpart<<<n, 32, 0, st>>>(sd, list, P.L, P.Dp, P.ring, P.lambda_h, wa, gpool, Ypool, Spool,
+                              hist_bf16, acc);
+}
+
+void launch_hist_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                      const float *gpool, const void *Spool, const void *Ypool, int hist_bf16,
+                      double *dots, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 grid(dgrid(P.Dp, DOT_THREADS), (unsigned)n);
+    k_hist_dots<<<grid, DOT_THREADS, 0, st>>>(sd, list, P.Dp, P.ring, gpool, Spool, Ypool, hist_bf16,
+                                              dots);
+}
+
+void launch_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                      const float *gpool, const void *Spool, const void *Ypool, int hist_bf16,
+                      const float *wa, float *d, double *acc, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 grid(dgrid(P.Dp, DOT_THREADS), (unsigned)n);
+    k_direction<<<grid, DOT_THREADS, 0, st>>>(sd, list, P.L, P.Dp, P.ring, gpool, Spool, Ypool,
+                                              hist_bf16, wa, d, acc);
+}
+
+void launch_score(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                  const float *wa, int gap, float *rows, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 grid((unsigned)((P.L + 127) / 128), (unsigned)n);
+    k_score<<<grid, 128, 0, st>>>(sd, list, P.L, P.Dp, wa, gap, rows);
+}
+
+} // namespace sdca

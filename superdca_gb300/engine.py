@@ -1,0 +1,154 @@
+"""Host-side mirror of SuperDCA's solve boundary over the engine's C ABI.
+
+SuperDCA runs its per-locus solve as
+    run_plmDCA<double, triallelic_state_t>(alignments, loci_list)
+(SuperDCA/include/plmDCA.hpp:436-437), configured through plmDCA_options
+(--lambda-h, --lambda-J, --gradient-threshold; SuperDCA/src/plmDCA_options.cpp)
+and writing its results to files.  `Engine` takes the same inputs (encoded
+alignment, weights, loci list, option values) and returns the per-locus score
+rows and statistics; `run_plmDCA` adds the symmetrised coupling lines that
+SuperDCA writes (plmDCA.hpp:667-693).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import EngineError
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+@dataclass
+class SolveResult:
+    scores: np.ndarray       # n_loci x L float32, NaN on the diagonal
+    f: np.ndarray            # objective per locus
+    gnorm: np.ndarray        # gradient max-norm per locus
+    iterations: np.ndarray
+    nfeval: np.ndarray       # evaluations counted as SuperDCA counts them
+    contractions: np.ndarray
+    status: np.ndarray
+    x: np.ndarray | None = None  # solutions, reference layout
+
+
+class Engine:
+    """One alignment resident on one GPU; solves batches of target loci."""
+
+    def __init__(self, n_seqs: int, n_loci: int, *, lambda_h: float = -1.0,
+                 lambda_J: float = -1.0, gradient_threshold: float = 1e-3,
+                 max_iterations: int = 2000, history: int = 10, batch: int = 64,
+                 form: int = _lib.FORM_GATHER, history_bf16: bool = False, gap_state: int = 3,
+                 device: int = 0, stream: int | None = None):
+        self.lib = _lib.load()
+        cfg = _lib.Config()
+        self.lib.sdca_config_default(C.byref(cfg))
+        cfg.n_seqs, cfg.n_loci = int(n_seqs), int(n_loci)
+        cfg.lambda_h, cfg.lambda_J = float(lambda_h), float(lambda_J)
+        cfg.gradient_threshold = float(gradient_threshold)
+        cfg.max_iterations, cfg.history, cfg.batch = int(max_iterations), int(history), int(batch)
+        cfg.form = int(form)
+        cfg.flags = _lib.FLAG_HISTORY_BF16 if history_bf16 else 0
+        cfg.gap_state, cfg.device = int(gap_state), int(device)
+        cfg.stream = stream
+        self.cfg = cfg
+        h = C.c_void_p()
+        rc = self.lib.sdca_create(C.byref(cfg), C.byref(h))
+        if rc != 0:
+            raise EngineError(rc, self.lib.sdca_last_error(None).decode())
+        self.h = h
+        self.N, self.L = int(n_seqs), int(n_loci)
+        self.D = 16 * self.L + 4
+
+    def _check(self, rc):
+        if rc != 0:
+            raise EngineError(rc, self.lib.sdca_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sdca_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_alignment(self, states: np.ndarray, weights: np.ndarray):
+        self._states = np.ascontiguousarray(states, dtype=np.uint8)
+        self._weights = np.ascontiguousarray(weights, dtype=np.float64)
+        assert self._states.shape == (self.N, self.L) and self._weights.shape == (self.N,)
+        self._check(self.lib.sdca_set_alignment(self.h, _ptr(self._states), _ptr(self._weights)))
+
+    def lambdas(self):
+        lh, lJ, be = C.c_double(), C.c_double(), C.c_double()
+        self._check(self.lib.sdca_get_lambdas(self.h, C.byref(lh), C.byref(lJ), C.byref(be)))
+        return lh.value, lJ.value, be.value
+
+    def solve(self, loci, x_init=None, want_x=False, want_scores=True) -> SolveResult:
+        loci = np.ascontiguousarray(loci, dtype=np.uint32)
+        n = len(loci)
+        scores = np.zeros((n, self.L), dtype=np.float32) if want_scores else None
+        stats = (_lib.LocusStat * max(n, 1))()
+        xo = np.zeros((n, self.D), dtype=np.float64) if want_x else None
+        xi = None if x_init is None else np.ascontiguousarray(x_init, dtype=np.float64)
+        self._check(self.lib.sdca_solve_ex(self.h, _ptr(loci), n, _ptr(xi), _ptr(xo), _ptr(scores),
+                                           C.cast(stats, C.c_void_p)))
+        st = stats[:n]
+        return SolveResult(
+            scores=scores,
+            f=np.array([s.f for s in st]), gnorm=np.array([s.gnorm for s in st]),
+            iterations=np.array([s.iterations for s in st]),
+            nfeval=np.array([s.nfeval for s in st]),
+            contractions=np.array([s.contractions for s in st]),
+            status=np.array([s.status for s in st]), x=xo)
+
+    def eval(self, r: int, x: np.ndarray, grad: bool = True):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        f = C.c_double()
+        g = np.zeros(self.D) if grad else None
+        self._check(self.lib.sdca_eval(self.h, int(r), _ptr(x), C.byref(f), _ptr(g)))
+        return (f.value, g) if grad else f.value
+
+    def profile(self) -> dict:
+        p = _lib.Profile()
+        self._check(self.lib.sdca_get_profile(self.h, C.byref(p)))
+        return dict(solve_ms=p.solve_ms,
+                    kernel_ms={k: p.kernel_ms[i] for i, k in enumerate(_lib.KERNEL_CLASSES)},
+                    kernel_launches={k: p.kernel_launches[i] for i, k in enumerate(_lib.KERNEL_CLASSES)},
+                    kernel_units={k: p.kernel_units[i] for i, k in enumerate(_lib.KERNEL_CLASSES)},
+                    gpu_launches=p.gpu_launches, iterations=p.iterations, contractions=p.contractions,
+                    h2d_bytes=p.h2d_bytes, d2h_bytes=p.d2h_bytes)
+
+
+def coupling_lines(scores: np.ndarray, loci, translation=None, base: int = 1):
+    """The lines SuperDCA writes for mean-of-norms scoring
+    (SuperDCA/include/plmDCA.hpp:667-693): for each r in the loci list and each
+    n before it, ((float)(S[r][n] + S[n][r])) * 0.5 with 1-based original
+    column indices."""
+    loci = [int(v) for v in loci]
+    pos = {r: k for k, r in enumerate(loci)}
+    tr = (lambda v: v) if translation is None else (lambda v: int(translation[v]))
+    out = []
+    for k, r in enumerate(loci):
+        for n in loci[:k]:
+            a = np.float32(scores[k, n])
+            b = np.float32(scores[pos[n], r])
+            out.append((float(np.float32(a + b)) * 0.5, tr(r) + base, tr(n) + base))
+    return out
+
+
+def format_coupling_lines(lines) -> str:
+    """Text as SuperDCA streams it: std::fixed, precision 8, space separated."""
+    return "".join(f"{v:.8f} {r} {n}\n" for v, r, n in lines)
