@@ -285,7 +285,7 @@ def engine_arm(args):
         t1 = time.time()
         for s in range(args.steps):
             E.set_alignment(hst, w)
-            E.solve(loci_for(args.warmup + args.steps + s), want_scores=True)
+            E.solve(loci_for(args.warmup + s), want_scores=True)
         barrier()
         t_e2e = time.time() - t1
         if world > 1:

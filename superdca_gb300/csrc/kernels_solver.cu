@@ -312,10 +312,12 @@ __global__ void k_score(const SlotDev *__restrict__ sd, const int32_t *__restric
     row[n] = (float)sqrt(sum);
 }
 
-unsigned dgrid(int64_t Dp, int threads)
+// blocks per slot for the D-length passes: at most `cap`, so that every
+// thread streams many float4 before the per-block reduction
+unsigned dgrid(int64_t Dp, int threads, int64_t cap = 256)
 {
     const int64_t need = (Dp / 4 + threads - 1) / threads;
-    return (unsigned)(need < 256 ? need : 256);
+    return (unsigned)(need < cap ? need : cap);
 }
 
 } // namespace
@@ -364,7 +366,7 @@ void launch_hist_dots(const Problem &P, const SlotDev *sd, const int32_t *list, 
                       double *dots, cudaStream_t st)
 {
     if (n <= 0) return;
-    dim3 grid(dgrid(P.Dp, DOT_THREADS), (unsigned)n);
+    dim3 grid(dgrid(P.Dp, DOT_THREADS, 48), (unsigned)n);
     k_hist_dots<<<grid, DOT_THREADS, 0, st>>>(sd, list, P.Dp, P.ring, gpool, Spool, Ypool, hist_bf16,
                                               dots);
 }
