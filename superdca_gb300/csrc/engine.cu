@@ -111,6 +111,13 @@ struct sdca_handle {
     int *flag_h = nullptr;
     int hist_bf16 = 0;
 
+    // tensor-core form
+    int form = SDCA_FORM_GATHER;
+    TcPlan *tc = nullptr;
+    __half *Dhi = nullptr, *Dlo = nullptr, *Rhi = nullptr, *Rlo = nullptr;
+    int *tc_err = nullptr;
+    float r_scale = 1.0f;
+
     std::vector<SlotHost> slots;
 
     // profiling
@@ -334,19 +341,40 @@ int fetch_acc(sdca_handle *h)
 {
     CK(cudaMemcpyAsync(h->acc_h, h->acc, sizeof(double) * NACC * h->P.Bmax, cudaMemcpyDeviceToHost,
                        h->stream));
+    if (h->tc_err) CK(cudaMemcpyAsync(h->flag_h + 1, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    if (h->tc_err && h->flag_h[1])
+        return fail(h, SDCA_E_CUDA, "tensor-core pipeline wait timed out (kernel abandoned its tile)");
     return SDCA_OK;
+}
+
+// power of two that brings max|v| into (2^13, 2^14] for the fp16 hi/lo split
+double pow2_scale(double vmax)
+{
+    if (!(vmax > 0.0) || !std::isfinite(vmax)) return 1.0;
+    const int e = (int)std::floor(std::log2(16384.0 / vmax));
+    return std::ldexp(1.0, std::max(-120, std::min(120, e)));
 }
 
 double acc_get(sdca_handle *h, int b, int k) { return h->acc_h[(int64_t)b * NACC + k]; }
 
-// forward contraction u = X . v_J (+ v_h): into `u` (float) or `lbase` (double)
+// forward contraction u = X . v_J (+ v_h): into `u` (float) or `lbase` (double).
+// The tensor-core form serves the per-iteration direction; logits at a
+// stored point (start, final refresh) always use the FP32 gather.
 int run_forward(sdca_handle *h, const std::vector<int32_t> &lst, const float *vecs, bool to_lbase)
 {
     if (lst.empty()) return SDCA_OK;
-    int rc = upload_list(h, lst);
+    const bool use_tc = h->form == SDCA_FORM_TC && !to_lbase;
+    int rc = use_tc ? upload_slots(h, lst) : upload_list(h, lst);
     if (rc) return rc;
-    {
+    if (use_tc) {
+        const int splits = tc_fwd_splits(h->P, (int)lst.size());
+        Timed t(h, SDCA_K_FORWARD, 3, (int64_t)lst.size());
+        CK(tc_launch_fwd(h->tc, h->P, h->sd, h->list, (int)lst.size(), vecs, h->Dhi, h->Dlo, h->partial,
+                         splits, h->tc_err, h->stream));
+        launch_reduce_partial(h->P, h->list, (int)lst.size(), h->partial, vecs, 1, h->u, nullptr,
+                              h->stream, splits);
+    } else {
         Timed t(h, SDCA_K_FORWARD, 2, (int64_t)lst.size());
         launch_fwd_gather(h->P, h->X, h->list, (int)lst.size(), vecs, h->partial, h->stream);
         launch_reduce_partial(h->P, h->list, (int)lst.size(), h->partial, vecs, 1,
@@ -588,7 +616,15 @@ int phase_step(sdca_handle *h)
     }
     rc = zero_acc(h);
     if (rc) return rc;
-    {
+    if (h->form == SDCA_FORM_TC) {
+        Timed t(h, SDCA_K_BACKWARD, 4, (int64_t)all.size());
+        CK(tc_launch_bwd(h->tc, P, h->sd, h->list, (int)all.size(), h->R, h->r_scale, h->Rhi, h->Rlo,
+                         h->gpool, h->tc_err, h->stream));
+        launch_grad_finalize(P, h->sd, h->list, (int)all.size(), h->wa, h->gpool, h->Ypool, h->Spool,
+                             h->hist_bf16, h->acc, h->stream);
+        launch_hpart(P, h->sd, h->list, (int)all.size(), h->wa, h->gpool, h->Ypool, h->Spool,
+                     h->hist_bf16, h->acc, h->stream);
+    } else {
         Timed t(h, SDCA_K_BACKWARD, 2, (int64_t)all.size());
         launch_bwd_gather(P, h->XT, h->sd, h->list, (int)all.size(), h->R, h->wa, h->gpool, h->Ypool,
                           h->Spool, h->hist_bf16, h->acc, h->stream);
@@ -752,6 +788,8 @@ int phase_step(sdca_handle *h)
         S.ddH = acc_get(h, b, ACC_DDH);
         S.xdJ = acc_get(h, b, ACC_XDJ);
         S.xdH = acc_get(h, b, ACC_XDH);
+        h->sd_h[b].tc_scale = pow2_scale(acc_get(h, b, ACC_DMAX));
+        h->sd_h[b].tc_inv_scale = 1.0 / h->sd_h[b].tc_scale;
         const double releps = 1e-4 * std::max(1.0, std::sqrt(S.x2J + S.x2H));
         if (!S.hist.empty() && !(S.gd <= -1e-4 * releps)) restart.push_back(b);
     }
@@ -773,6 +811,8 @@ int phase_step(sdca_handle *h)
             S.ddH = acc_get(h, b, ACC_DDH);
             S.xdJ = acc_get(h, b, ACC_XDJ);
             S.xdH = acc_get(h, b, ACC_XDH);
+            h->sd_h[b].tc_scale = pow2_scale(acc_get(h, b, ACC_DMAX));
+            h->sd_h[b].tc_inv_scale = 1.0 / h->sd_h[b].tc_scale;
         }
     }
     rc = run_forward(h, cont, h->d, false);
@@ -840,8 +880,8 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
         return fail(nullptr, SDCA_E_ARG, "history must be in 1..10");
     if (cfg->batch < 1 || cfg->batch > 4096) return fail(nullptr, SDCA_E_ARG, "batch must be in 1..4096");
     if (cfg->gap_state < -1 || cfg->gap_state >= Q) return fail(nullptr, SDCA_E_ARG, "gap_state out of range");
-    if (cfg->form != SDCA_FORM_GATHER)
-        return fail(nullptr, SDCA_E_UNSUPPORTED, "contraction form not available in this build");
+    if (cfg->form != SDCA_FORM_GATHER && cfg->form != SDCA_FORM_TC)
+        return fail(nullptr, SDCA_E_UNSUPPORTED, "unknown contraction form");
     if (!(cfg->gradient_threshold >= 0.0) || cfg->max_iterations < 0)
         return fail(nullptr, SDCA_E_ARG, "invalid stopping criteria");
     int ndev = 0;
@@ -880,8 +920,10 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
         want = std::max<int64_t>(1, want);
         P.LC = round_up((P.L + want - 1) / want, 32);
         P.LC = std::max<int64_t>(P.LC, 512);
-        P.C = (P.L + P.LC - 1) / P.LC;
+        P.Cg = (P.L + P.LC - 1) / P.LC;
+        P.C = std::max<int64_t>(P.Cg, cfg->form == SDCA_FORM_TC ? 24 : 1);
     }
+    h->form = cfg->form;
     h->slots.resize(P.Bmax);
     int rc = SDCA_OK;
     const size_t B = P.Bmax;
@@ -899,7 +941,12 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
         (rc = dalloc(h, reinterpret_cast<uint8_t **>(&h->Ypool), B * P.ring * P.Dp * hsz)) ||
         (rc = halloc(h, &h->sd_h, B)) || (rc = halloc(h, &h->list_h, B)) ||
         (rc = halloc(h, &h->acc_h, B * NACC)) || (rc = halloc(h, &h->dots_h, B * 4 * MAXHIST)) ||
-        (rc = halloc(h, &h->rows_h, B * P.L)) || (rc = halloc(h, &h->flag_h, 4))) {
+        (rc = halloc(h, &h->rows_h, B * P.L)) || (rc = halloc(h, &h->flag_h, 4)) ||
+        (h->form == SDCA_FORM_TC &&
+         ((rc = dalloc(h, &h->Dhi, 4 * B * (size_t)round_up(4 * P.L, 64))) ||
+          (rc = dalloc(h, &h->Dlo, 4 * B * (size_t)round_up(4 * P.L, 64))) ||
+          (rc = dalloc(h, &h->Rhi, 4 * B * (size_t)P.Nx)) || (rc = dalloc(h, &h->Rlo, 4 * B * (size_t)P.Nx)) ||
+          (rc = dalloc(h, &h->tc_err, 4))))) {
         std::string msg = h->err;
         free_all(h);
         if (h->own_stream) cudaStreamDestroy(h->stream);
@@ -911,6 +958,23 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
         if (h->own_stream) cudaStreamDestroy(h->stream);
         delete h;
         return fail(nullptr, SDCA_E_CUDA, "initialisation failed");
+    }
+    if (h->form == SDCA_FORM_TC) {
+        int major = 0, minor = 0;
+        cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, cfg->device);
+        cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, cfg->device);
+        std::string why;
+        if (major != 10 || minor != 3) why = "the tensor-core form needs an sm_103 (GB300) device";
+        else if (tc_configure() != cudaSuccess) why = "could not reserve the tensor-core kernel's shared memory";
+        else if (!(h->tc = tc_plan_create(P, h->X, h->XT, h->Dhi, h->Dlo, h->Rhi, h->Rlo, round_up(4 * P.L, 64))))
+            why = "TMA tensor-map encoding failed";
+        if (!why.empty()) {
+            cudaGetLastError();
+            free_all(h);
+            if (h->own_stream) cudaStreamDestroy(h->stream);
+            delete h;
+            return fail(nullptr, SDCA_E_UNSUPPORTED, why);
+        }
     }
     *out = h;
     return SDCA_OK;
@@ -945,6 +1009,11 @@ int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weig
     for (int64_t i = 0; i < P.N; ++i) beff += weights[i];
     const double autol = (beff > 500.0) ? 0.1 : 1.0 - ((1.0 - 0.1) * beff / 500.0);
     P.b_eff = beff;
+    {
+        double wmax = 0.0;
+        for (int64_t i = 0; i < P.N; ++i) wmax = std::max(wmax, weights[i]);
+        h->r_scale = (float)pow2_scale(wmax);
+    }
     P.lambda_J = (h->cfg.lambda_J < 0.0) ? autol * beff / 2.0 : h->cfg.lambda_J * beff;
     P.lambda_h = (h->cfg.lambda_h < 0.0) ? autol * beff : h->cfg.lambda_h * beff;
     h->has_alignment = true;
@@ -1095,6 +1164,7 @@ int sdca_destroy(sdca_handle *h)
     cudaSetDevice(h->cfg.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (auto e : h->ev_pool) cudaEventDestroy(e);
+    if (h->tc) tc_plan_destroy(h->tc);
     free_all(h);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     delete h;

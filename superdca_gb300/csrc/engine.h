@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/superdca_gb300.h"
@@ -41,6 +42,7 @@ enum Acc {
     ACC_XDJ,        // x_J . d_J                                    (direction)
     ACC_XDH,        // x_h . d_h                                    (direction)
     ACC_GMAX,       // max |g| (bits of a non-negative double, atomicMax) (gradient)
+    ACC_DMAX,       // max |d| (bits of a non-negative double, atomicMax) (direction)
     NACC = 20
 };
 
@@ -58,6 +60,8 @@ struct SlotDev {
     double coefS[MAXHIST];
     double coefY[MAXHIST];
     double rs[Q];           // R sums at the accepted point (h gradient)
+    double tc_scale;        // power of two applied to d before the fp16 hi/lo split
+    double tc_inv_scale;
 };
 
 enum SlotFlags {
@@ -77,7 +81,9 @@ struct SlotList {
 };
 
 struct Problem {
-    int64_t N = 0, L = 0, Lx = 0, Nx = 0, Dp = 0, LC = 0, C = 0;
+    int64_t N = 0, L = 0, Lx = 0, Nx = 0, Dp = 0, LC = 0;
+    int64_t Cg = 0;  // locus chunks of the gather forward
+    int64_t C = 0;   // partial-sum slices allocated (>= Cg and >= tensor-core K splits)
     int m = 10;
     int ring = 11;   // history positions per slot: m + 1 (one spare for the pending pair)
     int Bmax = 0;
@@ -89,7 +95,10 @@ void launch_fwd_gather(const Problem &P, const uint8_t *X, const int32_t *list, 
                        const float *vecs, float *partial, cudaStream_t st);
 void launch_reduce_partial(const Problem &P, const int32_t *list, int n, const float *partial,
                            const float *vecs, int add_h, float *out_f, double *out_d,
-                           cudaStream_t st);
+                           cudaStream_t st, int C = 0);
+void launch_grad_finalize(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                          const float *wa, float *gpool, void *Ypool, const void *Spool, int hist_bf16,
+                          double *acc, cudaStream_t st);
 void launch_bwd_gather(const Problem &P, const uint8_t *XT, const SlotDev *sd,
                        const int32_t *list, int n, const float *R, const float *wa,
                        float *gpool, void *Ypool, const void *Spool, int hist_bf16,
@@ -112,5 +121,19 @@ void launch_direction(const Problem &P, const SlotDev *sd, const int32_t *list, 
                       const float *wa, float *d, double *acc, cudaStream_t st);
 void launch_score(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
                   const float *wa, int gap, float *rows, cudaStream_t st);
+
+// tensor-core form (kernels_tc.cu)
+struct TcPlan;
+TcPlan *tc_plan_create(const Problem &P, const uint8_t *X, const uint8_t *XT, __half *Dhi, __half *Dlo,
+                       __half *Rhi, __half *Rlo, int64_t Kp);
+void tc_plan_destroy(TcPlan *p);
+int tc_fwd_splits(const Problem &P, int nlist);
+cudaError_t tc_configure();
+cudaError_t tc_launch_fwd(const TcPlan *pl, const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                          const float *vecs, __half *Dhi, __half *Dlo, float *partial, int splits, int *err,
+                          cudaStream_t st);
+cudaError_t tc_launch_bwd(const TcPlan *pl, const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                          const float *R, float r_scale, __half *Rhi, __half *Rlo, float *gpool, int *err,
+                          cudaStream_t st);
 
 } // namespace sdca

@@ -88,4 +88,47 @@ __device__ __forceinline__ float dot4(float4 a, float4 b)
     return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
 }
 
+struct GradRed {
+    float gmax = 0.f, g2 = 0.f, x2 = 0.f, sy = 0.f, yy = 0.f;
+};
+
+// Gradient of the 16 J entries of locus n for one slot: g = c + 2 lambda_J x
+// (c the contraction X^T R), zero for the J_rr block; writes g to the new
+// gradient buffer and, with a history push, y = g - g_old to the ring.
+// SuperDCA: plmDCA_objective.hpp:153-190 (scatter) and 192-244 (L2 part).
+template <typename SlotT>
+__device__ __forceinline__ void grad_locus(const SlotT &S, int b, int64_t n, const float (&c)[16],
+                                           const float *__restrict__ wa, float *__restrict__ gpool,
+                                           void *__restrict__ Ypool, const void *__restrict__ Spool,
+                                           int hist_bf16, int ring, int64_t Dp, float l2, GradRed &red)
+{
+    const float *x = wa + (int64_t)b * Dp + n * 16;
+    float *gn = gpool + (int64_t)(2 * b + 1 - S.gcur) * Dp + n * 16;
+    const float *go = gpool + (int64_t)(2 * b + S.gcur) * Dp + n * 16;
+    const bool zero = (n == S.locus);
+    const bool push = (S.flags & 2) && S.ring_new >= 0;
+    const int64_t hoff = ((int64_t)b * ring + (push ? S.ring_new : 0)) * Dp + n * 16;
+#pragma unroll
+    for (int k4 = 0; k4 < 4; ++k4) {
+        const float4 xv = reinterpret_cast<const float4 *>(x)[k4];
+        float4 gv;
+        gv.x = zero ? 0.f : c[4 * k4 + 0] + l2 * xv.x;
+        gv.y = zero ? 0.f : c[4 * k4 + 1] + l2 * xv.y;
+        gv.z = zero ? 0.f : c[4 * k4 + 2] + l2 * xv.z;
+        gv.w = zero ? 0.f : c[4 * k4 + 3] + l2 * xv.w;
+        reinterpret_cast<float4 *>(gn)[k4] = gv;
+        red.gmax = fmaxf(red.gmax, fmaxf(fmaxf(fabsf(gv.x), fabsf(gv.y)), fmaxf(fabsf(gv.z), fabsf(gv.w))));
+        red.g2 += dot4(gv, gv);
+        red.x2 += dot4(xv, xv);
+        if (push) {
+            const float4 ov = reinterpret_cast<const float4 *>(go)[k4];
+            float4 yv = make_float4(gv.x - ov.x, gv.y - ov.y, gv.z - ov.z, gv.w - ov.w);
+            yv = store_hist4(Ypool, hoff + 4 * k4, yv, hist_bf16);
+            const float4 sv = load_hist4(Spool, hoff + 4 * k4, hist_bf16);
+            red.sy += dot4(sv, yv);
+            red.yy += dot4(yv, yv);
+        }
+    }
+}
+
 } // namespace sdca

@@ -174,43 +174,43 @@ k_bwd_gather(const uint8_t *__restrict__ XT, int64_t Nx, int N, int L,
     for (int g = 0; g < BWD_G; ++g) {
         if (slot[g] < 0) continue;  // uniform across the block
         const int b = slot[g];
-        const SlotDev &S = sd[b];
-        float gmax = 0.f, g2 = 0.f, x2 = 0.f, sy = 0.f, yy = 0.f;
-        if (n < L) {
-            const float *x = wa + (int64_t)b * Dp + (int64_t)n * QQ;
-            float *gn = gpool + (int64_t)(2 * b + 1 - S.gcur) * Dp + (int64_t)n * QQ;
-            const float *go = gpool + (int64_t)(2 * b + S.gcur) * Dp + (int64_t)n * QQ;
-            const bool zero = (n == S.locus);
-            const bool push = (S.flags & SLOT_F_PUSH) && S.ring_new >= 0;
-            const int64_t hoff = ((int64_t)b * m + (push ? S.ring_new : 0)) * Dp + (int64_t)n * QQ;
-#pragma unroll
-            for (int k4 = 0; k4 < 4; ++k4) {
-                const float4 xv = reinterpret_cast<const float4 *>(x)[k4];
-                float4 gv;
-                gv.x = zero ? 0.f : a[g][4 * k4 + 0] + l2 * xv.x;
-                gv.y = zero ? 0.f : a[g][4 * k4 + 1] + l2 * xv.y;
-                gv.z = zero ? 0.f : a[g][4 * k4 + 2] + l2 * xv.z;
-                gv.w = zero ? 0.f : a[g][4 * k4 + 3] + l2 * xv.w;
-                reinterpret_cast<float4 *>(gn)[k4] = gv;
-                gmax = fmaxf(gmax, fmaxf(fmaxf(fabsf(gv.x), fabsf(gv.y)), fmaxf(fabsf(gv.z), fabsf(gv.w))));
-                g2 += dot4(gv, gv);
-                x2 += dot4(xv, xv);
-                if (push) {
-                    const float4 ov = reinterpret_cast<const float4 *>(go)[k4];
-                    float4 yv = make_float4(gv.x - ov.x, gv.y - ov.y, gv.z - ov.z, gv.w - ov.w);
-                    yv = store_hist4(Ypool, hoff + 4 * k4, yv, hist_bf16);
-                    const float4 sv = load_hist4(Spool, hoff + 4 * k4, hist_bf16);
-                    sy += dot4(sv, yv);
-                    yy += dot4(yv, yv);
-                }
-            }
-        }
-        double v[4] = {g2, x2, sy, yy};
+        GradRed red;
+        if (n < L) grad_locus(sd[b], b, n, a[g], wa, gpool, Ypool, Spool, hist_bf16, m, Dp, l2, red);
+        double v[4] = {red.g2, red.x2, red.sy, red.yy};
         const int idx[4] = {ACC_G2, ACC_X2J, ACC_SY, ACC_YY};
         block_sum_atomic<4>(v, acc + (int64_t)b * NACC, idx);
-        const float wm = warp_max(gmax);
+        const float wm = warp_max(red.gmax);
         if ((threadIdx.x & 31) == 0 && wm > 0.f) atomic_max_nonneg(acc + (int64_t)b * NACC + ACC_GMAX, (double)wm);
     }
+}
+
+// The tensor-core backward leaves X^T R (scaled back) in the new-gradient
+// buffer; this adds the L2 part and does the same bookkeeping.
+__global__ void __launch_bounds__(BWD_THREADS)
+k_grad_finalize(int L, const SlotDev *__restrict__ sd, const int32_t *__restrict__ list,
+                const float *__restrict__ wa, float *__restrict__ gpool, void *__restrict__ Ypool,
+                const void *__restrict__ Spool, int hist_bf16, int m, int64_t Dp, double lambda_J,
+                double *__restrict__ acc)
+{
+    const int b = list[blockIdx.y];
+    const SlotDev &S = sd[b];
+    const float l2 = (float)(2.0 * lambda_J);
+    GradRed red;
+    for (int64_t n = (int64_t)blockIdx.x * BWD_THREADS + threadIdx.x; n < L; n += (int64_t)gridDim.x * BWD_THREADS) {
+        const float4 *gr = reinterpret_cast<const float4 *>(gpool + (int64_t)(2 * b + 1 - S.gcur) * Dp + n * QQ);
+        float c[16];
+#pragma unroll
+        for (int k4 = 0; k4 < 4; ++k4) {
+            const float4 v = gr[k4];
+            c[4 * k4] = v.x; c[4 * k4 + 1] = v.y; c[4 * k4 + 2] = v.z; c[4 * k4 + 3] = v.w;
+        }
+        grad_locus(S, b, n, c, wa, gpool, Ypool, Spool, hist_bf16, m, Dp, l2, red);
+    }
+    double v[4] = {red.g2, red.x2, red.sy, red.yy};
+    const int idx[4] = {ACC_G2, ACC_X2J, ACC_SY, ACC_YY};
+    block_sum_atomic<4>(v, acc + (int64_t)b * NACC, idx);
+    const float wm = warp_max(red.gmax);
+    if ((threadIdx.x & 31) == 0 && wm > 0.f) atomic_max_nonneg(acc + (int64_t)b * NACC + ACC_GMAX, (double)wm);
 }
 
 } // namespace
@@ -220,20 +220,31 @@ void launch_fwd_gather(const Problem &P, const uint8_t *X, const int32_t *list, 
 {
     if (n <= 0) return;
     dim3 grid((unsigned)((P.N + FWD_THREADS - 1) / FWD_THREADS), (unsigned)((n + FWD_G - 1) / FWD_G),
-              (unsigned)P.C);
+              (unsigned)P.Cg);
     k_fwd_gather<<<grid, FWD_THREADS, 0, st>>>(X, P.Lx, (int)P.N, (int)P.L, P.LC, list, n, vecs, P.Dp,
                                                reinterpret_cast<float4 *>(partial), P.Bmax, P.Nx);
 }
 
 void launch_reduce_partial(const Problem &P, const int32_t *list, int n, const float *partial,
                            const float *vecs, int add_h, float *out_f, double *out_d,
-                           cudaStream_t st)
+                           cudaStream_t st, int C)
 {
     if (n <= 0) return;
     dim3 grid((unsigned)((P.N + 255) / 256), (unsigned)n);
-    k_reduce_partial<<<grid, 256, 0, st>>>(reinterpret_cast<const float4 *>(partial), (int)P.C,
+    k_reduce_partial<<<grid, 256, 0, st>>>(reinterpret_cast<const float4 *>(partial), C > 0 ? C : (int)P.Cg,
                                            P.Bmax, P.Nx, (int)P.N, list, vecs, P.Dp, QQ * P.L, add_h,
                                            reinterpret_cast<float4 *>(out_f), out_d);
+}
+
+void launch_grad_finalize(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                          const float *wa, float *gpool, void *Ypool, const void *Spool, int hist_bf16,
+                          double *acc, cudaStream_t st)
+{
+    if (n <= 0) return;
+    const int64_t need = (P.L + BWD_THREADS - 1) / BWD_THREADS;
+    dim3 grid((unsigned)(need < 512 ? need : 512), (unsigned)n);
+    k_grad_finalize<<<grid, BWD_THREADS, 0, st>>>((int)P.L, sd, list, wa, gpool, Ypool, Spool, hist_bf16,
+                                                   P.ring, P.Dp, P.lambda_J, acc);
 }
 
 void launch_bwd_gather(const Problem &P, const uint8_t *XT, const SlotDev *sd,

@@ -213,7 +213,7 @@ k_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
     }
     const int64_t hoff = QQ * L;
     const int64_t rlo = (int64_t)S.locus * QQ, rhi = rlo + QQ;
-    float gd = 0.f, ddJ = 0.f, ddH = 0.f, xdJ = 0.f, xdH = 0.f;
+    float gd = 0.f, ddJ = 0.f, ddH = 0.f, xdJ = 0.f, xdH = 0.f, dmax = 0.f;
     for (int64_t e = 4 * ((int64_t)blockIdx.x * DOT_THREADS + threadIdx.x); e < Dp;
          e += 4 * (int64_t)gridDim.x * DOT_THREADS) {
         const float4 gv = *reinterpret_cast<const float4 *>(g + e);
@@ -234,6 +234,7 @@ k_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
         *reinterpret_cast<float4 *>(d + (int64_t)b * Dp + e) = dv;
         const float4 xv = *reinterpret_cast<const float4 *>(wa + (int64_t)b * Dp + e);
         gd += dot4(gv, dv);
+        dmax = fmaxf(dmax, fmaxf(fmaxf(fabsf(dv.x), fabsf(dv.y)), fmaxf(fabsf(dv.z), fabsf(dv.w))));
         if (e < hoff) {
             ddJ += dot4(dv, dv);
             xdJ += dot4(xv, dv);
@@ -245,6 +246,8 @@ k_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
     double v[5] = {gd, ddJ, ddH, xdJ, xdH};
     const int idx[5] = {ACC_GD, ACC_DDJ, ACC_DDH, ACC_XDJ, ACC_XDH};
     block_sum_atomic<5>(v, acc + (int64_t)b * NACC, idx);
+    const float wm = warp_max(dmax);
+    if ((threadIdx.x & 31) == 0 && wm > 0.f) atomic_max_nonneg(acc + (int64_t)b * NACC + ACC_DMAX, (double)wm);
 }
 
 // S[r][n] = || gauge(M) ||_F without GAP, M = J_rn (transposed for n < r):

@@ -1,0 +1,572 @@
+// kernels_tc.cu -- the tensor-core contraction form (tcgen05, sm_103a).
+//
+// Both contractions of an L-BFGS iteration are one-hot GEMMs, C = A . B^T with
+// A the one-hot expansion of the alignment and B the per-slot operand:
+//
+//   forward   u[i][p*4+a]      = sum_{k=n*4+s} [X_in == s] * D_p[a][k]   (A: N x 4L)
+//   backward  G[n*4+s][p*4+a]  = sum_i [X_in == s] * R_p[a][i]           (A: 4L x N)
+//
+// which are SuperDCA's gather (plmDCA_objective.hpp:86-121) and gradient
+// scatter (plmDCA_objective.hpp:153-190) for a batch of target loci.
+//
+// Data path per CTA (128 x 128 output tile, K in steps of 64):
+//   * warp 0, one thread: TMA loads of the u8 state tile (2 KB) and of the
+//     fp16 hi and lo tiles of B (128 B swizzle), completing on full_raw[s];
+//   * warps 2-5: expand the u8 tile to the fp16 one-hot A tile directly in the
+//     128-byte-swizzled K-major layout the MMA reads (the one-hot matrix never
+//     exists in HBM: 1 byte per locus is read instead of 8), fence to the async
+//     proxy, arrive on full_a[s];
+//   * warp 1, one thread: tcgen05.mma kind::f16 (M128 N128 K16, FP32
+//     accumulator in TMEM), A x B_hi then A x B_lo, tcgen05.commit frees the
+//     stage;
+//   * warps 2-5 again: tcgen05.ld the accumulator and store it, scaled back
+//     by the per-slot power of two.
+// B is split as hi + lo fp16 halves of (value * 2^e) so that the product keeps
+// about 22 significant bits; the one-hot A is exact in fp16.
+//
+// Every mbarrier wait is bounded: on timeout the kernel records an error code
+// in *err and skips the remaining work instead of spinning.
+#include <cuda.h>
+#include <cuda_fp16.h>
+
+#include "engine.h"
+#include "kernels_common.cuh"
+
+namespace sdca {
+namespace tc {
+
+constexpr int BM = 128, BN = 128, BK = 64, STAGES = 4;
+constexpr int A_BYTES = BM * BK * 2;
+constexpr int B_BYTES = BN * BK * 2;
+constexpr int RAW_BYTES = 2048;
+constexpr int STAGE_BYTES = A_BYTES + 2 * B_BYTES + RAW_BYTES;  // 51200, a multiple of 1024
+constexpr int THREADS = 192;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+constexpr uint32_t TMEM_COLS = 128;
+constexpr long long WAIT_LIMIT = 1ll << 26;  // polls before a wait gives up
+
+enum { MODE_FWD = 0, MODE_BWD = 1 };
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    for (long long i = 0; i < WAIT_LIMIT; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *tm, int x, int y,
+                                            uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+// tcgen05 shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row
+// groups 1024 bytes apart (SBO), descriptor version 1.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFF);          // start address
+    d |= (uint64_t)(0) << 16;                        // LBO (unused for swizzled K-major)
+    d |= (uint64_t)((1024 >> 4) & 0x3FFF) << 32;     // SBO
+    d |= (uint64_t)1 << 46;                          // version
+    d |= (uint64_t)2 << 61;                          // SWIZZLE_128B
+    return d;
+}
+
+// instruction descriptor, kind::f16: A = B = F16, D = F32, K-major, M = 128, N = 128
+constexpr uint32_t IDESC = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                        uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+          "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// 16-byte chunk c of row r of a 128-byte-swizzled tile
+__device__ __forceinline__ uint32_t sw128(uint32_t base, int r, int c)
+{
+    return base + (uint32_t)r * 128u + ((uint32_t)(c ^ (r & 7)) << 4);
+}
+
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint4 v)
+{
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z),
+                 "r"(v.w)
+                 : "memory");
+}
+
+// fp16 1.0 in lane s of four 16-bit lanes
+__device__ __forceinline__ uint64_t onehot4(uint32_t s)
+{
+    return (uint64_t)0x3C00u << (16u * (s & 3u));
+}
+
+// forward: raw = 128 rows x 16 loci (u8); A row r = sequence, K = locus*4+state
+__device__ __forceinline__ void expand_fwd(const uint8_t *raw, uint32_t a_base, int t)
+{
+    const uint4 w = *reinterpret_cast<const uint4 *>(raw + t * 16);
+    const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const uint32_t wd = words[c >> 1];
+        const uint32_t s0 = (wd >> (16 * (c & 1))) & 0xFF, s1 = (wd >> (16 * (c & 1) + 8)) & 0xFF;
+        const uint64_t lo = onehot4(s0), hi = onehot4(s1);
+        st_shared_v4(sw128(a_base, t, c),
+                     make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32)));
+    }
+}
+
+// four bytes -> four fp16 lanes holding 1.0 where the byte equals s
+__device__ __forceinline__ uint2 eq_halves(uint32_t bytes, uint32_t s4)
+{
+    const uint32_t m = __vcmpeq4(bytes, s4);  // 0xFF per equal byte
+    const uint32_t a = __byte_perm(m, 0u, 0x1404) & 0x3C003C00u;
+    const uint32_t b = __byte_perm(m, 0u, 0x3424) & 0x3C003C00u;
+    return make_uint2(a, b);
+}
+
+// backward: raw = 32 loci x 64 sequences (u8); A row r = locus*4+state, K = sequence
+__device__ __forceinline__ void expand_bwd(const uint8_t *raw, uint32_t a_base, int t)
+{
+    const int nl = t >> 2;
+    const uint32_t s4 = (uint32_t)(t & 3) * 0x01010101u;
+    const uint4 *rp = reinterpret_cast<const uint4 *>(raw + nl * 64);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const uint4 w = rp[q];
+        const uint2 e0 = eq_halves(w.x, s4), e1 = eq_halves(w.y, s4);
+        const uint2 e2 = eq_halves(w.z, s4), e3 = eq_halves(w.w, s4);
+        st_shared_v4(sw128(a_base, t, 2 * q), make_uint4(e0.x, e0.y, e1.x, e1.y));
+        st_shared_v4(sw128(a_base, t, 2 * q + 1), make_uint4(e2.x, e2.y, e3.x, e3.y));
+    }
+}
+
+struct GemmArgs {
+    int mode;
+    int kt_begin_stride;  // k-tiles per split
+    int kt_total;
+    int m_rows;           // valid output rows (N for forward, 4L for backward)
+    int nlist;
+    const int32_t *list;  // list position -> slot
+    const SlotDev *sd;
+    float inv_scale_fwd;  // unused when per-slot scales are read from sd
+    // forward output: partial[split][slot][Nx] float4
+    float4 *partial;
+    int Bmax;
+    int64_t Nx;
+    // backward output: raw gradient into the slot's new-gradient buffer
+    float *gpool;
+    int64_t Dp;
+    float inv_scale_bwd;
+    int *err;
+};
+
+__global__ void __launch_bounds__(THREADS, 1)
+k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtensorMap tmBhi,
+       const __grid_constant__ CUtensorMap tmBlo, const GemmArgs args)
+{
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t sbase0 = smem_u32(smem_raw);
+    const uint32_t sbase = (sbase0 + 1023u) & ~1023u;
+    uint8_t *const sgen = smem_raw + (sbase - sbase0);
+    const uint32_t bars = sbase + STAGES * STAGE_BYTES;
+    // barrier layout: full_raw[STAGES], full_a[STAGES], empty[STAGES], tmem_full, tmem addr
+    auto full_raw = [&](int s) { return bars + 8u * s; };
+    auto full_a = [&](int s) { return bars + 8u * (STAGES + s); };
+    auto empty = [&](int s) { return bars + 8u * (2 * STAGES + s); };
+    const uint32_t tmem_full = bars + 8u * (3 * STAGES);
+    const uint32_t tmem_slot = bars + 8u * (3 * STAGES + 1);
+    uint32_t *tmem_slot_gen = reinterpret_cast<uint32_t *>(sgen + STAGES * STAGE_BYTES + 8 * (3 * STAGES + 1));
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m_tile = blockIdx.x, n_tile = blockIdx.y, split = blockIdx.z;
+    const int kt0 = split * args.kt_begin_stride;
+    const int kt1 = min(args.kt_total, kt0 + args.kt_begin_stride);
+    const int nkt = max(0, kt1 - kt0);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(full_raw(s), 1);
+            mbar_init(full_a(s), 128);
+            mbar_init(empty(s), 1);
+        }
+        mbar_init(tmem_full, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tmem_slot),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem_base = *tmem_slot_gen;
+    bool failed = false;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int j = 0; j < nkt; ++j) {
+                const int s = j % STAGES;
+                const uint32_t ph = (uint32_t)((j / STAGES) & 1);
+                if (!mbar_wait(empty(s), ph ^ 1u)) { failed = true; break; }
+                const uint32_t st = sbase + (uint32_t)s * STAGE_BYTES;
+                mbar_expect_tx(full_raw(s), RAW_BYTES + 2 * B_BYTES);
+                const int kt = kt0 + j;
+                if (args.mode == MODE_FWD)
+                    tma_load_2d(st + A_BYTES + 2 * B_BYTES, &tmRaw, kt * 16, m_tile * BM, full_raw(s));
+                else
+                    tma_load_2d(st + A_BYTES + 2 * B_BYTES, &tmRaw, kt * BK, m_tile * 32, full_raw(s));
+                tma_load_2d(st + A_BYTES, &tmBhi, kt * BK, n_tile * BN, full_raw(s));
+                tma_load_2d(st + A_BYTES + B_BYTES, &tmBlo, kt * BK, n_tile * BN, full_raw(s));
+            }
+            // loads still in flight land before the block retires
+            for (int j = max(0, nkt - STAGES); j < nkt; ++j)
+                if (!mbar_wait(full_raw(j % STAGES), (uint32_t)((j / STAGES) & 1))) failed = true;
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            for (int j = 0; j < nkt; ++j) {
+                const int s = j % STAGES;
+                const uint32_t ph = (uint32_t)((j / STAGES) & 1);
+                if (!mbar_wait(full_a(s), ph)) { failed = true; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t st = sbase + (uint32_t)s * STAGE_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < BK / 16; ++kk) {
+                    const uint64_t ad = smem_desc_sw128(st + kk * 32);
+                    const uint64_t bh = smem_desc_sw128(st + A_BYTES + kk * 32);
+                    const uint64_t bl = smem_desc_sw128(st + A_BYTES + B_BYTES + kk * 32);
+                    mma_f16(tmem_base, ad, bh, (j > 0 || kk > 0) ? 1u : 0u);
+                    mma_f16(tmem_base, ad, bl, 1u);
+                }
+                mma_commit(empty(s));
+            }
+            // the accumulator is complete (or abandoned) once every issued MMA retired
+            mma_commit(tmem_full);
+        }
+    } else {
+        const int t = threadIdx.x - 64;  // 0..127
+        for (int j = 0; j < nkt; ++j) {
+            const int s = j % STAGES;
+            const uint32_t ph = (uint32_t)((j / STAGES) & 1);
+            if (!mbar_wait(full_raw(s), ph)) { failed = true; break; }
+            const uint8_t *raw = sgen + s * STAGE_BYTES + A_BYTES + 2 * B_BYTES;
+            const uint32_t a_base = sbase + (uint32_t)s * STAGE_BYTES;
+            if (args.mode == MODE_FWD) expand_fwd(raw, a_base, t);
+            else expand_bwd(raw, a_base, t);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(full_a(s));
+        }
+        // epilogue
+        const bool ok = nkt > 0 && mbar_wait(tmem_full, 0u);
+        if (!ok && nkt > 0) failed = true;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int q = warp & 3;  // TMEM lane quadrant of this warp
+        const int r = q * 32 + lane;
+        const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+        for (int cj = 0; cj < BN / 32; ++cj) {
+            float v[32];
+            if (ok) tmem_ld32(tbase + (uint32_t)(cj * 32), v);
+            if (!ok) continue;
+            const int row = m_tile * BM + r;
+#pragma unroll
+            for (int tt = 0; tt < 8; ++tt) {
+                const int P = (n_tile * BN + cj * 32) / 4 + tt;
+                if (P >= args.nlist) continue;
+                const int b = args.list[P];
+                if (args.mode == MODE_FWD) {
+                    if (row < args.Nx) {
+                        const float sc = (float)args.sd[b].tc_inv_scale;
+                        args.partial[((int64_t)split * args.Bmax + b) * args.Nx + row] =
+                            make_float4(v[4 * tt] * sc, v[4 * tt + 1] * sc, v[4 * tt + 2] * sc, v[4 * tt + 3] * sc);
+                    }
+                } else if (row < args.m_rows) {
+                    const float sc = args.inv_scale_bwd;
+                    const int gb = args.sd[b].gcur;
+                    float *gn = args.gpool + (int64_t)(2 * b + 1 - gb) * args.Dp + (int64_t)(row >> 2) * QQ +
+                                (row & 3) * Q;
+                    *reinterpret_cast<float4 *>(gn) =
+                        make_float4(v[4 * tt] * sc, v[4 * tt + 1] * sc, v[4 * tt + 2] * sc, v[4 * tt + 3] * sc);
+                }
+            }
+        }
+    }
+    if (failed) atomicExch(args.err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
+                     : "memory");
+    }
+}
+
+// d (engine layout [n][s][a]) -> B rows p*4+a, columns n*4+s, fp16 hi and lo of d*2^e
+__global__ void k_split_dir(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t L,
+                            int64_t Dp, int64_t Kp, const float *__restrict__ vecs, __half *__restrict__ hi,
+                            __half *__restrict__ lo)
+{
+    const int P = blockIdx.y;
+    const int b = list[P];
+    const float sc = (float)sd[b].tc_scale;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < 4 * L; k += (int64_t)gridDim.x * blockDim.x) {
+        const float4 v = *reinterpret_cast<const float4 *>(vecs + (int64_t)b * Dp + k * 4);
+        const float vv[4] = {v.x * sc, v.y * sc, v.z * sc, v.w * sc};
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const __half h = __float2half_rn(vv[a]);
+            const __half l = __float2half_rn(vv[a] - __half2float(h));
+            const int64_t o = ((int64_t)P * 4 + a) * Kp + k;
+            hi[o] = h;
+            lo[o] = l;
+        }
+    }
+}
+
+// R (float4 per sequence) -> B rows p*4+a, columns i, fp16 hi and lo of R*2^e
+__global__ void k_split_R(const int32_t *__restrict__ list, int64_t Nx, const float4 *__restrict__ R, float sc,
+                          __half *__restrict__ hi, __half *__restrict__ lo)
+{
+    const int P = blockIdx.y;
+    const int b = list[P];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Nx; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 v = R[(int64_t)b * Nx + i];
+        const float vv[4] = {v.x * sc, v.y * sc, v.z * sc, v.w * sc};
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const __half h = __float2half_rn(vv[a]);
+            const __half l = __float2half_rn(vv[a] - __half2float(h));
+            const int64_t o = ((int64_t)P * 4 + a) * Nx + i;
+            hi[o] = h;
+            lo[o] = l;
+        }
+    }
+}
+
+} // namespace tc
+
+// ---------------------------------------------------------------------------
+// host side
+
+namespace {
+
+using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                              const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeFn encode_fn()
+{
+    static EncodeFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeFn>(p);
+    }
+    return fn;
+}
+
+bool make_map(CUtensorMap *m, CUtensorMapDataType dt, void *base, uint64_t cols, uint64_t rows,
+              uint64_t row_bytes, uint32_t box_cols, uint32_t box_rows, CUtensorMapSwizzle sw)
+{
+    EncodeFn fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {row_bytes};
+    const cuuint32_t box[2] = {box_cols, box_rows};
+    const cuuint32_t es[2] = {1, 1};
+    return fn(m, dt, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+} // namespace
+
+struct TcPlan {
+    CUtensorMap mX, mXT, mDhi, mDlo, mRhi, mRlo;
+    int64_t Kp = 0;
+    int fwd_splits = 1;
+};
+
+int tc_smem_bytes() { return tc::SMEM_BYTES; }
+
+TcPlan *tc_plan_create(const Problem &P, const uint8_t *X, const uint8_t *XT, __half *Dhi, __half *Dlo,
+                       __half *Rhi, __half *Rlo, int64_t Kp)
+{
+    TcPlan *p = new TcPlan();
+    p->Kp = Kp;
+    bool ok = true;
+    ok &= make_map(&p->mX, CU_TENSOR_MAP_DATA_TYPE_UINT8, const_cast<uint8_t *>(X), (uint64_t)P.Lx,
+                   (uint64_t)P.N, (uint64_t)P.Lx, 16, 128, CU_TENSOR_MAP_SWIZZLE_NONE);
+    ok &= make_map(&p->mXT, CU_TENSOR_MAP_DATA_TYPE_UINT8, const_cast<uint8_t *>(XT), (uint64_t)P.Nx,
+                   (uint64_t)P.L, (uint64_t)P.Nx, 64, 32, CU_TENSOR_MAP_SWIZZLE_NONE);
+    ok &= make_map(&p->mDhi, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Dhi, (uint64_t)Kp, (uint64_t)4 * P.Bmax,
+                   (uint64_t)Kp * 2, 64, 128, CU_TENSOR_MAP_SWIZZLE_128B);
+    ok &= make_map(&p->mDlo, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Dlo, (uint64_t)Kp, (uint64_t)4 * P.Bmax,
+                   (uint64_t)Kp * 2, 64, 128, CU_TENSOR_MAP_SWIZZLE_128B);
+    ok &= make_map(&p->mRhi, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Rhi, (uint64_t)P.Nx, (uint64_t)4 * P.Bmax,
+                   (uint64_t)P.Nx * 2, 64, 128, CU_TENSOR_MAP_SWIZZLE_128B);
+    ok &= make_map(&p->mRlo, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Rlo, (uint64_t)P.Nx, (uint64_t)4 * P.Bmax,
+                   (uint64_t)P.Nx * 2, 64, 128, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (!ok) {
+        delete p;
+        return nullptr;
+    }
+    return p;
+}
+
+void tc_plan_destroy(TcPlan *p) { delete p; }
+
+int tc_fwd_splits(const Problem &P, int nlist)
+{
+    // split K so that the CTAs fill whole waves of 152 SMs (one CTA per SM)
+    const int mt = (int)((P.Nx + tc::BM - 1) / tc::BM);
+    const int nt = (4 * nlist + tc::BN - 1) / tc::BN;
+    const int kt = (int)((4 * P.L + tc::BK - 1) / tc::BK);
+    int best = 1;
+    double best_t = 1e30;
+    for (int s = 1; s <= (int)P.C; ++s) {
+        const double waves = std::ceil((double)mt * nt * s / 152.0);
+        const double t = waves * std::ceil((double)kt / s) + 8.0 * waves;
+        if (t < best_t) {
+            best_t = t;
+            best = s;
+        }
+    }
+    // no empty split: every launched split owns at least one k-tile
+    const int stride = (kt + best - 1) / best;
+    return (kt + stride - 1) / stride;
+}
+
+cudaError_t tc_launch_fwd(const TcPlan *pl, const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                          const float *vecs, __half *Dhi, __half *Dlo, float *partial, int splits, int *err,
+                          cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    {
+        dim3 g((unsigned)std::min<int64_t>((4 * P.L + 255) / 256, 1024), (unsigned)n);
+        tc::k_split_dir<<<g, 256, 0, st>>>(sd, list, P.L, P.Dp, pl->Kp, vecs, Dhi, Dlo);
+    }
+    tc::GemmArgs a{};
+    a.mode = tc::MODE_FWD;
+    a.kt_total = (int)((4 * P.L + tc::BK - 1) / tc::BK);
+    a.kt_begin_stride = (a.kt_total + splits - 1) / splits;
+    a.m_rows = (int)P.N;
+    a.nlist = n;
+    a.list = list;
+    a.sd = sd;
+    a.partial = reinterpret_cast<float4 *>(partial);
+    a.Bmax = P.Bmax;
+    a.Nx = P.Nx;
+    a.err = err;
+    dim3 grid((unsigned)((P.Nx + tc::BM - 1) / tc::BM), (unsigned)((4 * n + tc::BN - 1) / tc::BN), (unsigned)splits);
+    tc::k_gemm<<<grid, tc::THREADS, tc::SMEM_BYTES, st>>>(pl->mX, pl->mDhi, pl->mDlo, a);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_launch_bwd(const TcPlan *pl, const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                          const float *R, float r_scale, __half *Rhi, __half *Rlo, float *gpool, int *err,
+                          cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    {
+        dim3 g((unsigned)std::min<int64_t>((P.Nx + 255) / 256, 64), (unsigned)n);
+        tc::k_split_R<<<g, 256, 0, st>>>(list, P.Nx, reinterpret_cast<const float4 *>(R), r_scale, Rhi, Rlo);
+    }
+    tc::GemmArgs a{};
+    a.mode = tc::MODE_BWD;
+    a.kt_total = (int)(P.Nx / tc::BK);
+    a.kt_begin_stride = a.kt_total;
+    a.m_rows = (int)(4 * P.L);
+    a.nlist = n;
+    a.list = list;
+    a.sd = sd;
+    a.gpool = gpool;
+    a.Dp = P.Dp;
+    a.inv_scale_bwd = 1.0f / r_scale;
+    a.Nx = P.Nx;
+    a.err = err;
+    dim3 grid((unsigned)((4 * P.L + tc::BM - 1) / tc::BM), (unsigned)((4 * n + tc::BN - 1) / tc::BN), 1);
+    tc::k_gemm<<<grid, tc::THREADS, tc::SMEM_BYTES, st>>>(pl->mXT, pl->mRhi, pl->mRlo, a);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_configure()
+{
+    return cudaFuncSetAttribute(tc::k_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+}
+
+} // namespace sdca
