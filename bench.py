@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--loci-per-step", type=int, default=0, help="default: batch")
-    ap.add_argument("--form", default="gather", choices=["gather", "tc"])
+    ap.add_argument("--form", default="tc", choices=["gather", "tc"])
     ap.add_argument("--history-bf16", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -250,12 +250,14 @@ def engine_arm(args):
     dev_ms = 0.0
     nfe, iters, contr, statuses = [], [], [], []
     clocks = Clocks(local)
+    walls = []
     barrier()
     clocks.start()
     t0 = time.time()
     for s in range(args.steps):
         res = E.solve(loci_for(args.warmup + s), want_scores=True)
         p = E.profile()
+        walls.append(time.time() - t0 - sum(walls))
         dev_ms += p["solve_ms"]
         launches += p["gpu_launches"]
         for k in keys:
@@ -283,9 +285,15 @@ def engine_arm(args):
         hst = pinned.numpy()
         barrier()
         t1 = time.time()
+        t_up = t_sol = 0.0
         for s in range(args.steps):
+            ta = time.time()
             E.set_alignment(hst, w)
+            tb = time.time()
             E.solve(loci_for(args.warmup + s), want_scores=True)
+            tc_ = time.time()
+            t_up += tb - ta
+            t_sol += tc_ - tb
         barrier()
         t_e2e = time.time() - t1
         if world > 1:
@@ -293,7 +301,8 @@ def engine_arm(args):
             torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
             t_e2e = float(tt.item())
         e2e = dict(value=round(args.steps * per_step * world / t_e2e, 4), unit="loci/s",
-                   h2d_bytes_per_step=int(N * L + 8 * N), d2h_bytes_per_step=int(per_step * L * 4 + per_step * 32))
+                   h2d_bytes_per_step=int(N * L + 8 * N), d2h_bytes_per_step=int(per_step * L * 4 + per_step * 32),
+                   upload_s_per_step=round(t_up / args.steps, 4), solve_s_per_step=round(t_sol / args.steps, 4))
 
     Dp = ((16 * L + 4 + 63) // 64) * 64
     rf, dom = roofline(tot, N, L, Dp, 10, 2 if args.history_bf16 else 4)
@@ -303,7 +312,8 @@ def engine_arm(args):
         "metric": "loci/s at N=3000,L=94k (per-locus plmDCA solve, gradient threshold 1e-3)",
         "value": round(value, 4), "unit": "loci/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(t_dev * 1e3 / args.steps, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp16x2->fp32 (tensor cores), fp64 reductions" if args.form == "tc" else "fp32",
         "data": "synthetic (seeded coalescent-tree alignment)",
         "config": {"workload": f"{args.workload} seed {args.seed}", "N": int(N), "L": int(L),
                    "batch": B, "loci_per_step": per_step, "form": args.form,
@@ -316,7 +326,7 @@ def engine_arm(args):
         "solver": {"median_nfeval": float(np.median(nfe)), "median_iterations": float(np.median(iters)),
                    "median_contractions": float(np.median(contr)),
                    "status_counts": {str(k): statuses.count(k) for k in sorted(set(statuses))},
-                   "wall_s": round(wall, 2)},
+                   "wall_s": round(wall, 2), "wall_s_per_step": [round(v, 3) for v in walls]},
     }
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1

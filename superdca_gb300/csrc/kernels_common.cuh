@@ -21,6 +21,39 @@ __device__ __forceinline__ float warp_max(float v)
     return v;
 }
 
+__device__ __forceinline__ float warp_sum_f(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum K per-thread values over the block; thread 0 adds them to dst[idx[k]].
+// Warp sums run in FP32 (each thread's value is itself an FP32 partial over
+// a stretch of one vector), the cross-warp sum in FP64.
+// Requires blockDim.x a multiple of 32 and <= 1024.
+template <int K>
+__device__ __forceinline__ void block_sum_atomic_f(float (&v)[K], double *dst, const int *idx)
+{
+    __shared__ double redf[32][K];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = warp_sum_f(v[k]);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) redf[wid][k] = (double)v[k];
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        for (int k = 0; k < K; ++k) {
+            double t = lane < nw ? redf[lane][k] : 0.0;
+            t = warp_sum(t);
+            if (lane == 0 && t != 0.0) atomicAdd(dst + idx[k], t);
+        }
+    }
+    __syncthreads();
+}
+
 // Sum K per-thread values over the block; thread 0 adds them to dst[0..K-1].
 // Requires blockDim.x a multiple of 32 and <= 1024.
 template <int K>

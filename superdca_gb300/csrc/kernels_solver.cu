@@ -8,6 +8,8 @@
 // exactly SuperDCA's objective along the search line (plmDCA_objective.hpp:
 // 126-151 for the pseudo-likelihood part; the L2 part is a quadratic in stp
 // that the host evaluates from x.d and d.d).
+#include <algorithm>
+
 #include "engine.h"
 #include "kernels_common.cuh"
 
@@ -178,7 +180,7 @@ k_hist_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
             }
         }
     }
-    double v[4 * MAXHIST];
+    float v[4 * MAXHIST];
     int idx[4 * MAXHIST];
 #pragma unroll
     for (int j = 0; j < MAXHIST; ++j) {
@@ -189,7 +191,7 @@ k_hist_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
     }
 #pragma unroll
     for (int k = 0; k < 4 * MAXHIST; ++k) idx[k] = k;
-    block_sum_atomic<4 * MAXHIST>(v, dots + (int64_t)b * 4 * MAXHIST, idx);
+    block_sum_atomic_f<4 * MAXHIST>(v, dots + (int64_t)b * 4 * MAXHIST, idx);
 }
 
 // d = coef_g g + sum_j (coefS_j s_j + coefY_j y_j), J_rr block zero;
@@ -369,7 +371,10 @@ void launch_hist_dots(const Problem &P, const SlotDev *sd, const int32_t *list, 
                       double *dots, cudaStream_t st)
 {
     if (n <= 0) return;
-    dim3 grid(dgrid(P.Dp, DOT_THREADS, 48), (unsigned)n);
+    // enough blocks for about two waves in total, each thread streaming
+    // hundreds of float4 before the block reduction
+    const int64_t per_slot = std::max<int64_t>(4, std::min<int64_t>(64, (4 * 152 + n - 1) / n));
+    dim3 grid(dgrid(P.Dp, DOT_THREADS, per_slot), (unsigned)n);
     k_hist_dots<<<grid, DOT_THREADS, 0, st>>>(sd, list, P.Dp, P.ring, gpool, Spool, Ypool, hist_bf16,
                                               dots);
 }
@@ -379,7 +384,8 @@ void launch_direction(const Problem &P, const SlotDev *sd, const int32_t *list, 
                       const float *wa, float *d, double *acc, cudaStream_t st)
 {
     if (n <= 0) return;
-    dim3 grid(dgrid(P.Dp, DOT_THREADS), (unsigned)n);
+    const int64_t per_slot = std::max<int64_t>(4, std::min<int64_t>(256, (8 * 152 + n - 1) / n));
+    dim3 grid(dgrid(P.Dp, DOT_THREADS, per_slot), (unsigned)n);
     k_direction<<<grid, DOT_THREADS, 0, st>>>(sd, list, P.L, P.Dp, P.ring, gpool, Spool, Ypool,
                                               hist_bf16, wa, d, acc);
 }

@@ -90,3 +90,21 @@ def test_tc_tree_workload_subset(engine_lib, oracle_mod):
     _, ost = P.solve(loci, threads=4, gtol=1e-3)
     np.testing.assert_allclose(res.f, [s["f"] for s in ost], rtol=1e-6)
     E.close()
+
+
+def test_tc_bf16_history(engine_lib, oracle_mod):
+    """L-BFGS (s, y) pairs stored in BF16: the direction is still a descent
+    direction built from consistent dot products; the optimum is unchanged."""
+    from superdca_gb300 import synthetic
+
+    O = oracle_mod
+    st, _, _ = synthetic.workload("independent-200x500", seed=3)
+    w = O.weights(st, 0.9)
+    loci = np.arange(0, 500, 10)
+    E = make_engine(st, w, batch=32, history_bf16=True)
+    res = E.solve(loci, want_x=True)
+    assert np.all(res.status == 0), res.status
+    P = fp64_check(O, st, w, E, loci, res)
+    _, ost = P.solve(loci, threads=8, gtol=1e-3)
+    np.testing.assert_allclose(res.f, [s["f"] for s in ost], rtol=1e-6)
+    E.close()
