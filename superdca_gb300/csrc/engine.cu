@@ -104,7 +104,9 @@ struct sdca_handle {
     int32_t *list = nullptr;
     int *flag = nullptr;
     // pinned host mirrors
-    SlotDev *sd_h = nullptr;
+    SlotDev *sd_h = nullptr;       // host-side slot parameters (edited freely)
+    uint8_t *stage = nullptr;      // pinned staging arena for host->device copies: a
+    size_t stage_cap = 0, stage_off = 0;  // region is reused only after a stream sync
     int32_t *list_h = nullptr;
     double *acc_h = nullptr, *dots_h = nullptr;
     float *rows_h = nullptr;
@@ -244,6 +246,8 @@ void free_all(sdca_handle *h)
     if (h->dots_h) cudaFreeHost(h->dots_h);
     if (h->rows_h) cudaFreeHost(h->rows_h);
     if (h->flag_h) cudaFreeHost(h->flag_h);
+    if (h->stage) cudaFreeHost(h->stage);
+    h->stage = nullptr;
     h->sd_h = nullptr; h->list_h = nullptr; h->acc_h = nullptr; h->dots_h = nullptr;
     h->rows_h = nullptr; h->flag_h = nullptr;
     h->X = h->XT = h->rstate = nullptr;
@@ -301,13 +305,35 @@ void engine_to_ref(const Problem &P, const float *v, double *out)
     for (int a = 0; a < Q; ++a) out[QQ * P.L + a] = v[QQ * P.L + a];
 }
 
+// Synchronise the stream; every staged host region is free afterwards.
+int stream_sync(sdca_handle *h)
+{
+    CK(cudaStreamSynchronize(h->stream));
+    h->stage_off = 0;
+    return SDCA_OK;
+}
+
+// Copy `bytes` from src to device dst through a staging region that no copy
+// still queued on the stream reads.
+int staged_h2d(sdca_handle *h, void *dst, const void *src, size_t bytes)
+{
+    const size_t need = (bytes + 255) & ~(size_t)255;
+    if (need > h->stage_cap) return fail(h, SDCA_E_ARG, "staging arena too small");
+    if (h->stage_off + need > h->stage_cap) {
+        int rc = stream_sync(h);
+        if (rc) return rc;
+    }
+    uint8_t *p = h->stage + h->stage_off;
+    h->stage_off += need;
+    std::memcpy(p, src, bytes);
+    CK(cudaMemcpyAsync(dst, p, bytes, cudaMemcpyHostToDevice, h->stream));
+    return SDCA_OK;
+}
+
 int upload_list(sdca_handle *h, const std::vector<int32_t> &lst)
 {
     if (lst.empty()) return SDCA_OK;
-    std::memcpy(h->list_h, lst.data(), sizeof(int32_t) * lst.size());
-    CK(cudaMemcpyAsync(h->list, h->list_h, sizeof(int32_t) * lst.size(), cudaMemcpyHostToDevice,
-                       h->stream));
-    return SDCA_OK;
+    return staged_h2d(h, h->list, lst.data(), sizeof(int32_t) * lst.size());
 }
 
 // copy the host slot parameters of `lst` into the device mirror
@@ -326,8 +352,8 @@ int upload_slots(sdca_handle *h, const std::vector<int32_t> &lst)
         for (int a = 0; a < Q; ++a) D.rs[a] = S.rs[a];
     }
     // the mirror is small; copy it whole
-    CK(cudaMemcpyAsync(h->sd, h->sd_h, sizeof(SlotDev) * h->P.Bmax, cudaMemcpyHostToDevice,
-                       h->stream));
+    int rc = staged_h2d(h, h->sd, h->sd_h, sizeof(SlotDev) * h->P.Bmax);
+    if (rc) return rc;
     return upload_list(h, lst);
 }
 
@@ -342,7 +368,8 @@ int fetch_acc(sdca_handle *h)
     CK(cudaMemcpyAsync(h->acc_h, h->acc, sizeof(double) * NACC * h->P.Bmax, cudaMemcpyDeviceToHost,
                        h->stream));
     if (h->tc_err) CK(cudaMemcpyAsync(h->flag_h + 1, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
+    int rc = stream_sync(h);
+    if (rc) return rc;
     if (h->tc_err && h->flag_h[1])
         return fail(h, SDCA_E_CUDA, "tensor-core pipeline wait timed out (kernel abandoned its tile)");
     return SDCA_OK;
@@ -439,7 +466,7 @@ int refill(sdca_handle *h, Queue &Qu)
         if (rc) return rc;
         if (x0) {
             // the copy reads the staging buffer: finish it before the next slot reuses it
-            CK(cudaStreamSynchronize(h->stream));
+            { const int r_ = stream_sync(h); if (r_) return r_; }
             warm.push_back(b);
         }
     }
@@ -473,12 +500,12 @@ int retire(sdca_handle *h, Queue &Qu, const std::vector<int32_t> &done)
         if (Qu.x_out) {
             CK(cudaMemcpyAsync(xe.data(), h->wa + (int64_t)b * P.Dp, sizeof(float) * P.Dp,
                                cudaMemcpyDeviceToHost, h->stream));
-            CK(cudaStreamSynchronize(h->stream));
+            { const int r_ = stream_sync(h); if (r_) return r_; }
             engine_to_ref(P, xe.data(), Qu.x_out + S.k * (QQ * P.L + Q));
             h->prof.d2h_bytes += (int64_t)sizeof(float) * P.Dp;
         }
     }
-    CK(cudaStreamSynchronize(h->stream));
+    { const int r_ = stream_sync(h); if (r_) return r_; }
     for (size_t j = 0; j < done.size(); ++j) {
         const int b = done[j];
         SlotHost &S = h->slots[b];
@@ -715,7 +742,7 @@ int phase_step(sdca_handle *h)
         CKL();
         CK(cudaMemcpyAsync(h->dots_h, h->dots, sizeof(double) * 4 * MAXHIST * P.Bmax,
                            cudaMemcpyDeviceToHost, h->stream));
-        CK(cudaStreamSynchronize(h->stream));
+        { const int r_ = stream_sync(h); if (r_) return r_; }
     }
     for (int b : cont) {
         SlotHost &S = h->slots[b];
@@ -764,8 +791,9 @@ int phase_step(sdca_handle *h)
             D.nhist = (int)S.hist.size();
             for (int j = 0; j < D.nhist; ++j) D.ring[j] = S.hist[j];
         }
-        CK(cudaMemcpyAsync(h->sd, h->sd_h, sizeof(SlotDev) * P.Bmax, cudaMemcpyHostToDevice, h->stream));
-        int r2 = upload_list(h, lst);
+        int r2 = staged_h2d(h, h->sd, h->sd_h, sizeof(SlotDev) * P.Bmax);
+        if (r2) return r2;
+        r2 = upload_list(h, lst);
         if (r2) return r2;
         r2 = zero_acc(h);
         if (r2) return r2;
@@ -942,6 +970,7 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
         (rc = halloc(h, &h->sd_h, B)) || (rc = halloc(h, &h->list_h, B)) ||
         (rc = halloc(h, &h->acc_h, B * NACC)) || (rc = halloc(h, &h->dots_h, B * 4 * MAXHIST)) ||
         (rc = halloc(h, &h->rows_h, B * P.L)) || (rc = halloc(h, &h->flag_h, 4)) ||
+        (rc = halloc(h, &h->stage, (h->stage_cap = 64 * (((sizeof(SlotDev) + 4) * B + 1024 + 255) & ~(size_t)255)))) ||
         (h->form == SDCA_FORM_TC &&
          ((rc = dalloc(h, &h->Dhi, 4 * B * (size_t)round_up(4 * P.L, 64))) ||
           (rc = dalloc(h, &h->Dlo, 4 * B * (size_t)round_up(4 * P.L, 64))) ||
@@ -999,7 +1028,7 @@ int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weig
     }
     CKL();
     CK(cudaMemcpyAsync(h->flag_h, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
+    { const int r_ = stream_sync(h); if (r_) return r_; }
     if (h->flag_h[0]) {
         h->has_alignment = false;
         return fail(h, SDCA_E_ARG, "state codes must be in 0..q-1");
@@ -1067,7 +1096,7 @@ int sdca_solve_ex(sdca_handle *h, const uint32_t *loci, size_t n_loci, const dou
         if (rc) return rc;
     }
     CK(cudaEventRecord(t1, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
+    { const int r_ = stream_sync(h); if (r_) return r_; }
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, t0, t1));
     h->prof.solve_ms = ms;
@@ -1127,7 +1156,7 @@ int sdca_eval(sdca_handle *h, uint32_t r, const double *x, double *f, double *g)
         std::vector<float> ge(P.Dp);
         CK(cudaMemcpyAsync(ge.data(), h->gpool + (int64_t)(2 * b + 1 - S.gcur) * P.Dp,
                            sizeof(float) * P.Dp, cudaMemcpyDeviceToHost, h->stream));
-        CK(cudaStreamSynchronize(h->stream));
+        { const int r_ = stream_sync(h); if (r_) return r_; }
         engine_to_ref(P, ge.data(), g);
     }
     S.phase = PH_EMPTY;

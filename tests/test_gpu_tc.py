@@ -70,7 +70,8 @@ def test_tc_matches_gather_small_workload(engine_lib, oracle_mod):
     fp64_check(O, st, w, E, loci, res)
     G = Engine(N, L, batch=64)
     G.set_alignment(st, w)
-    ref = G.solve(loci)
+    ref = G.solve(loci, want_x=True)
+    fp64_check(O, st, w, G, loci, ref)
     np.testing.assert_allclose(res.f, ref.f, rtol=1e-6)
     np.testing.assert_allclose(res.scores, ref.scores, atol=1e-4, equal_nan=True)
     E.close(); G.close()
