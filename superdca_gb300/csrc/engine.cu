@@ -99,7 +99,7 @@ struct sdca_handle {
     float *wa = nullptr, *d = nullptr, *gpool = nullptr, *u = nullptr, *R = nullptr;
     float *partial = nullptr, *rows = nullptr;
     void *Spool = nullptr, *Ypool = nullptr;
-    double *lbase = nullptr, *acc = nullptr, *dots = nullptr;
+    double *lbase = nullptr, *acc = nullptr, *dots = nullptr, *partial64 = nullptr;
     SlotDev *sd = nullptr;
     int32_t *list = nullptr;
     int *flag = nullptr;
@@ -401,11 +401,13 @@ int run_forward(sdca_handle *h, const std::vector<int32_t> &lst, const float *ve
                          splits, h->tc_err, h->stream));
         launch_reduce_partial(h->P, h->list, (int)lst.size(), h->partial, vecs, 1, h->u, nullptr,
                               h->stream, splits);
+    } else if (to_lbase) {
+        Timed t(h, SDCA_K_FORWARD, 2, (int64_t)lst.size());
+        launch_fwd_exact(h->P, h->X, h->list, (int)lst.size(), vecs, h->partial64, h->lbase, h->stream);
     } else {
         Timed t(h, SDCA_K_FORWARD, 2, (int64_t)lst.size());
         launch_fwd_gather(h->P, h->X, h->list, (int)lst.size(), vecs, h->partial, h->stream);
-        launch_reduce_partial(h->P, h->list, (int)lst.size(), h->partial, vecs, 1,
-                              to_lbase ? nullptr : h->u, to_lbase ? h->lbase : nullptr, h->stream);
+        launch_reduce_partial(h->P, h->list, (int)lst.size(), h->partial, vecs, 1, h->u, nullptr, h->stream);
     }
     CKL();
     for (int b : lst) h->slots[b].contractions++;
@@ -962,6 +964,7 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
         (rc = dalloc(h, &h->gpool, 2 * B * P.Dp)) || (rc = dalloc(h, &h->u, B * P.Nx * 4)) ||
         (rc = dalloc(h, &h->R, B * P.Nx * 4)) || (rc = dalloc(h, &h->lbase, B * P.Nx * 4)) ||
         (rc = dalloc(h, &h->partial, (size_t)P.C * B * P.Nx * 4)) ||
+        (rc = dalloc(h, &h->partial64, (size_t)P.Cg * B * P.Nx * 4)) ||
         (rc = dalloc(h, &h->rows, B * P.L)) || (rc = dalloc(h, &h->acc, B * NACC)) ||
         (rc = dalloc(h, &h->dots, B * 4 * MAXHIST)) || (rc = dalloc(h, &h->sd, B)) ||
         (rc = dalloc(h, &h->list, B)) || (rc = dalloc(h, &h->flag, 4)) ||

@@ -96,6 +96,8 @@ void launch_fwd_gather(const Problem &P, const uint8_t *X, const int32_t *list, 
 void launch_reduce_partial(const Problem &P, const int32_t *list, int n, const float *partial,
                            const float *vecs, int add_h, float *out_f, double *out_d,
                            cudaStream_t st, int C = 0);
+void launch_fwd_exact(const Problem &P, const uint8_t *X, const int32_t *list, int n, const float *vecs,
+                      double *partial64, double *lbase, cudaStream_t st);
 void launch_grad_finalize(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
                           const float *wa, float *gpool, void *Ypool, const void *Spool, int hist_bf16,
                           double *acc, cudaStream_t st);

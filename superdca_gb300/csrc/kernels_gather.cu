@@ -81,6 +81,108 @@ k_fwd_gather(const uint8_t *__restrict__ X, int64_t Lx, int N, int L, int64_t LC
     }
 }
 
+// Logits at a stored point, for the start of a locus and for the objective a
+// converged locus reports.  The sequences of an alignment share most of their
+// states, so rounding errors of long FP32 locus sums are correlated across
+// sequences and add up over the N terms of the objective; here FP32 sums run
+// over 64-locus stretches only and the stretches accumulate in FP64.
+constexpr int EX_G = 4;
+
+__global__ void __launch_bounds__(FWD_THREADS)
+k_fwd_gather_exact(const uint8_t *__restrict__ X, int64_t Lx, int N, int L, int64_t LC,
+                   const int32_t *__restrict__ list, int nlist, const float *__restrict__ vecs,
+                   int64_t Dp, double4 *__restrict__ partial, int Bmax, int64_t Nx)
+{
+    __shared__ float4 sJ[EX_G][FWD_SUB][Q];
+    const int i = blockIdx.x * FWD_THREADS + threadIdx.x;
+    const int c = blockIdx.z;
+    const int64_t n_begin = (int64_t)c * LC;
+    const int64_t n_end = min((int64_t)L, n_begin + LC);
+    int slot[EX_G];
+#pragma unroll
+    for (int g = 0; g < EX_G; ++g) {
+        const int k = blockIdx.y * EX_G + g;
+        slot[g] = k < nlist ? list[k] : -1;
+    }
+    float4 acc[EX_G];
+    double a64[EX_G][4];
+#pragma unroll
+    for (int g = 0; g < EX_G; ++g) {
+        acc[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+        a64[g][0] = a64[g][1] = a64[g][2] = a64[g][3] = 0.0;
+    }
+    int sub = 0;
+    for (int64_t n0 = n_begin; n0 < n_end; n0 += FWD_SUB, ++sub) {
+        for (int k = threadIdx.x; k < EX_G * FWD_SUB * Q; k += FWD_THREADS) {
+            const int g = k / (FWD_SUB * Q), rem = k % (FWD_SUB * Q);
+            const int nl = rem / Q, s = rem % Q;
+            const int64_t n = n0 + nl;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (slot[g] >= 0 && n < n_end)
+                v = reinterpret_cast<const float4 *>(vecs + (int64_t)slot[g] * Dp)[n * Q + s];
+            sJ[g][nl][s] = v;
+        }
+        __syncthreads();
+        if (i < N) {
+            const uint4 *xp = reinterpret_cast<const uint4 *>(X + (int64_t)i * Lx + n0);
+            const uint4 w0 = xp[0], w1 = xp[1];
+            const uint32_t words[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+            for (int wd = 0; wd < 8; ++wd) {
+#pragma unroll
+                for (int bt = 0; bt < 4; ++bt) {
+                    const int nl = wd * 4 + bt;
+                    const int s = (words[wd] >> (8 * bt)) & 0x3;
+#pragma unroll
+                    for (int g = 0; g < EX_G; ++g) {
+                        const float4 j = sJ[g][nl][s];
+                        acc[g].x += j.x;
+                        acc[g].y += j.y;
+                        acc[g].z += j.z;
+                        acc[g].w += j.w;
+                    }
+                }
+            }
+            if (sub & 1) {
+#pragma unroll
+                for (int g = 0; g < EX_G; ++g) {
+                    a64[g][0] += acc[g].x; a64[g][1] += acc[g].y;
+                    a64[g][2] += acc[g].z; a64[g][3] += acc[g].w;
+                    acc[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (i < N) {
+#pragma unroll
+        for (int g = 0; g < EX_G; ++g)
+            if (slot[g] >= 0)
+                partial[((int64_t)c * Bmax + slot[g]) * Nx + i] =
+                    make_double4(a64[g][0] + acc[g].x, a64[g][1] + acc[g].y, a64[g][2] + acc[g].z,
+                                 a64[g][3] + acc[g].w);
+    }
+}
+
+__global__ void k_reduce_partial64(const double4 *__restrict__ partial, int C, int Bmax, int64_t Nx,
+                                   int N, const int32_t *__restrict__ list,
+                                   const float *__restrict__ vecs, int64_t Dp, int64_t hoff,
+                                   double *__restrict__ out_d)
+{
+    const int b = list[blockIdx.y];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const float *h = vecs + (int64_t)b * Dp + hoff;
+    double s0 = h[0], s1 = h[1], s2 = h[2], s3 = h[3];
+    for (int c = 0; c < C; ++c) {
+        const double4 p = partial[((int64_t)c * Bmax + b) * Nx + i];
+        s0 += p.x; s1 += p.y; s2 += p.z; s3 += p.w;
+    }
+    const int64_t o = (int64_t)b * Nx + i;
+    out_d[o * 4 + 0] = s0; out_d[o * 4 + 1] = s1;
+    out_d[o * 4 + 2] = s2; out_d[o * 4 + 3] = s3;
+}
+
 __global__ void k_reduce_partial(const float4 *__restrict__ partial, int C, int Bmax, int64_t Nx,
                                  int N, const int32_t *__restrict__ list,
                                  const float *__restrict__ vecs, int64_t Dp, int64_t hoff,
@@ -223,6 +325,19 @@ void launch_fwd_gather(const Problem &P, const uint8_t *X, const int32_t *list, 
               (unsigned)P.Cg);
     k_fwd_gather<<<grid, FWD_THREADS, 0, st>>>(X, P.Lx, (int)P.N, (int)P.L, P.LC, list, n, vecs, P.Dp,
                                                reinterpret_cast<float4 *>(partial), P.Bmax, P.Nx);
+}
+
+void launch_fwd_exact(const Problem &P, const uint8_t *X, const int32_t *list, int n, const float *vecs,
+                      double *partial64, double *lbase, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 grid((unsigned)((P.N + FWD_THREADS - 1) / FWD_THREADS), (unsigned)((n + EX_G - 1) / EX_G),
+              (unsigned)P.Cg);
+    k_fwd_gather_exact<<<grid, FWD_THREADS, 0, st>>>(X, P.Lx, (int)P.N, (int)P.L, P.LC, list, n, vecs, P.Dp,
+                                                     reinterpret_cast<double4 *>(partial64), P.Bmax, P.Nx);
+    dim3 g2((unsigned)((P.N + 255) / 256), (unsigned)n);
+    k_reduce_partial64<<<g2, 256, 0, st>>>(reinterpret_cast<const double4 *>(partial64), (int)P.Cg, P.Bmax,
+                                           P.Nx, (int)P.N, list, vecs, P.Dp, QQ * P.L, lbase);
 }
 
 void launch_reduce_partial(const Problem &P, const int32_t *list, int n, const float *partial,

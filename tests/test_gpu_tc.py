@@ -19,11 +19,16 @@ def make_engine(states, weights, **kw):
 
 
 def fp64_check(O, states, weights, E, loci, res, rel=1e-6):
+    """Reported objective == FP64 oracle objective at the returned parameters;
+    returns the FP64 values."""
     lh, lJ, _ = E.lambdas()
     P = O.Problem(states, weights, lh, lJ)
+    f64s = []
     for k, r in enumerate(loci):
         f64 = P.objective(int(r), res.x[k], grad=False)
         assert res.f[k] == pytest.approx(f64, rel=rel), (r, res.f[k], f64)
+        f64s.append(f64)
+    P.f64 = np.array(f64s)
     return P
 
 
@@ -67,11 +72,14 @@ def test_tc_matches_gather_small_workload(engine_lib, oracle_mod):
     E = make_engine(st, w, batch=64)
     res = E.solve(loci, want_x=True)
     assert np.all(res.status == 0), res.status
-    fp64_check(O, st, w, E, loci, res)
+    a = fp64_check(O, st, w, E, loci, res, rel=1e-7).f64
     G = Engine(N, L, batch=64)
     G.set_alignment(st, w)
     ref = G.solve(loci, want_x=True)
-    fp64_check(O, st, w, G, loci, ref)
+    b = fp64_check(O, st, w, G, loci, ref, rel=1e-7).f64
+    # both forms stop at max|g| < 1e-3 of a strictly convex objective: the
+    # FP64 objectives at their two solutions agree far inside the bar
+    np.testing.assert_allclose(a, b, rtol=1e-6)
     np.testing.assert_allclose(res.f, ref.f, rtol=1e-6)
     np.testing.assert_allclose(res.scores, ref.scores, atol=1e-4, equal_nan=True)
     E.close(); G.close()
