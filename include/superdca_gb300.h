@@ -155,6 +155,29 @@ int sdca_destroy(sdca_handle *h);
 
 int sdca_abi_version(void);
 
+/* Largest alignment sdca_eval_noalloc accepts: its scratch is a fixed array. */
+#define SDCA_NOALLOC_MAX_SEQS 65536
+#define SDCA_NOALLOC_MAX_LOCI 262144
+
+/* One objective + gradient evaluation that allocates nothing (no counterpart
+ * in SuperDCA; same value as sdca_eval).  For callers that cannot call
+ * cudaMalloc -- code running while a CUDA graph is captured, or host programs
+ * whose own allocator owns all device memory.  Every pointer is a DEVICE
+ * pointer the caller allocated: states (n_seqs x n_loci codes 0..3), weights
+ * (n_seqs), x and g (16 n_loci + 4 doubles, SuperDCA's parameter layout) and
+ * f (one double).  lambda_h and lambda_J are absolute strengths (as
+ * sdca_get_lambdas reports them).  Work is queued on `stream` (a cudaStream_t
+ * or NULL) of the current device and is complete when that stream is.
+ * Intermediate values live in one fixed __device__ array of the library
+ * (about 2.1 MB, held by every GPU that loads the library until exit), so
+ * n_seqs <= SDCA_NOALLOC_MAX_SEQS and n_loci <= SDCA_NOALLOC_MAX_LOCI, else
+ * SDCA_E_ARG before any work is queued.  All calls share that array: calls
+ * whose work overlaps on the GPU race.  The first call on a device looks up
+ * the array's address on that device; make it before any stream capture. */
+int sdca_eval_noalloc(const uint8_t *states, int64_t n_seqs, int64_t n_loci,
+                      const double *weights, double lambda_h, double lambda_J, uint32_t r,
+                      const double *x, double *f, double *g, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

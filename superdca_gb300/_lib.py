@@ -30,7 +30,7 @@ KERNEL_CLASSES = ["forward", "backward", "linesearch", "history", "direction", "
 # every entry point include/superdca_gb300.h declares
 EXPORTS = ["sdca_abi_version", "sdca_config_default", "sdca_create", "sdca_set_alignment",
            "sdca_compute_weights", "sdca_get_lambdas", "sdca_solve", "sdca_solve_ex", "sdca_eval",
-           "sdca_get_profile", "sdca_last_error", "sdca_destroy"]
+           "sdca_get_profile", "sdca_last_error", "sdca_destroy", "sdca_eval_noalloc"]
 
 
 class Config(C.Structure):
@@ -79,6 +79,7 @@ def load(path: str = LIB_PATH):
     L.sdca_last_error.restype = C.c_char_p
     L.sdca_last_error.argtypes = [vp]
     L.sdca_destroy.argtypes = [vp]
+    L.sdca_eval_noalloc.argtypes = [vp, i64, i64, vp, dp, dp, C.c_uint32, vp, vp, vp, vp]
     L.sdca_internal_lbfgs_coeffs.argtypes = [C.c_int, vp, vp, vp, vp, dp, C.POINTER(dp), vp, vp]
     for name in EXPORTS + ["sdca_internal_lbfgs_coeffs"]:
         if name not in ("sdca_abi_version", "sdca_last_error"):
