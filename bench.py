@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--cache-dir", default="", help="keep the generated alignment here between runs")
     return ap.parse_args()
 
 
@@ -141,7 +142,15 @@ def measured_peaks():
 def load_workload(args):
     from superdca_gb300 import synthetic
 
+    path = None
+    if args.cache_dir:
+        os.makedirs(args.cache_dir, exist_ok=True)
+        path = os.path.join(args.cache_dir, f"{args.workload}-seed{args.seed}.npy")
+        if os.path.exists(path):
+            return np.load(path)
     st, cols, _ = synthetic.workload(args.workload, seed=args.seed)
+    if path:
+        np.save(path, st)
     return st
 
 

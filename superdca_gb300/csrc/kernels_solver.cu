@@ -146,8 +146,12 @@ __global__ void k_hpart(const SlotDev *__restrict__ sd, const int32_t *__restric
 }
 
 constexpr int DOT_THREADS = 256;
+constexpr int DOT_U = 4;  // float4 groups per thread per tile: 16 KB runs per stream per block
 
-// dots[b] = [S_j.g | Y_j.g | S_j.y_new | Y_j.y_new], j over the history
+// dots[b] = [S_j.g | Y_j.g | S_j.y_new | Y_j.y_new], j over the history.
+// Blocks walk tiles of DOT_THREADS x DOT_U float4 groups; within a tile g and
+// y_new stay in registers while the history vectors stream through one at a
+// time, so every stream is read in long contiguous runs.
 __global__ void __launch_bounds__(DOT_THREADS)
 k_hist_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Dp, int m,
             const float *__restrict__ gpool, const void *__restrict__ Spool,
@@ -156,27 +160,41 @@ k_hist_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
     const int b = list[blockIdx.y];
     const SlotDev &S = sd[b];
     const int nh = S.nhist;
-    const float *g = gpool + (int64_t)(2 * b + S.gcur) * Dp;
+    const float4 *g4 = reinterpret_cast<const float4 *>(gpool + (int64_t)(2 * b + S.gcur) * Dp);
     const bool has_new = S.ring_new >= 0;
     const int64_t ybase = ((int64_t)b * m + (has_new ? S.ring_new : 0)) * Dp;
+    const int64_t nv4 = Dp / 4, tile = (int64_t)DOT_THREADS * DOT_U;
     float aSg[MAXHIST], aYg[MAXHIST], aSy[MAXHIST], aYy[MAXHIST];
 #pragma unroll
     for (int j = 0; j < MAXHIST; ++j) aSg[j] = aYg[j] = aSy[j] = aYy[j] = 0.f;
-    for (int64_t e = 4 * ((int64_t)blockIdx.x * DOT_THREADS + threadIdx.x); e < Dp;
-         e += 4 * (int64_t)gridDim.x * DOT_THREADS) {
-        const float4 gv = *reinterpret_cast<const float4 *>(g + e);
-        const float4 yn = has_new ? load_hist4(Ypool, ybase + e, hist_bf16)
-                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t tb = (int64_t)blockIdx.x * tile; tb < nv4; tb += (int64_t)gridDim.x * tile) {
+        float4 gv[DOT_U], yn[DOT_U];
+#pragma unroll
+        for (int u = 0; u < DOT_U; ++u) {
+            const int64_t v = tb + u * DOT_THREADS + threadIdx.x;
+            const bool ok = v < nv4;
+            gv[u] = ok ? g4[v] : make_float4(0.f, 0.f, 0.f, 0.f);
+            yn[u] = (ok && has_new) ? load_hist4(Ypool, ybase + 4 * v, hist_bf16) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
 #pragma unroll
         for (int j = 0; j < MAXHIST; ++j) {
             if (j < nh) {
-                const int64_t off = ((int64_t)b * m + S.ring[j]) * Dp + e;
-                const float4 sv = load_hist4(Spool, off, hist_bf16);
-                const float4 yv = load_hist4(Ypool, off, hist_bf16);
-                aSg[j] += dot4(sv, gv);
-                aYg[j] += dot4(yv, gv);
-                aSy[j] += dot4(sv, yn);
-                aYy[j] += dot4(yv, yn);
+                const int64_t base = ((int64_t)b * m + S.ring[j]) * Dp;
+                float4 sv[DOT_U], yv[DOT_U];
+#pragma unroll
+                for (int u = 0; u < DOT_U; ++u) {
+                    const int64_t v = tb + u * DOT_THREADS + threadIdx.x;
+                    const bool ok = v < nv4;
+                    sv[u] = ok ? load_hist4(Spool, base + 4 * v, hist_bf16) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    yv[u] = ok ? load_hist4(Ypool, base + 4 * v, hist_bf16) : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < DOT_U; ++u) {
+                    aSg[j] += dot4(sv[u], gv[u]);
+                    aYg[j] += dot4(yv[u], gv[u]);
+                    aSy[j] += dot4(sv[u], yn[u]);
+                    aYy[j] += dot4(yv[u], yn[u]);
+                }
             }
         }
     }
@@ -195,7 +213,9 @@ k_hist_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
 }
 
 // d = coef_g g + sum_j (coefS_j s_j + coefY_j y_j), J_rr block zero;
-// reductions g.d, d.d and x.d split into the J and h parts.
+// reductions g.d, d.d and x.d split into the J and h parts, and max|d|.
+// Same tiling as k_hist_dots: d and g of a tile stay in registers while the
+// history streams through.
 __global__ void __launch_bounds__(DOT_THREADS)
 k_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t L,
             int64_t Dp, int m, const float *__restrict__ gpool, const void *__restrict__ Spool,
@@ -205,49 +225,65 @@ k_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
     const int b = list[blockIdx.y];
     const SlotDev &S = sd[b];
     const int nh = S.nhist;
-    const float *g = gpool + (int64_t)(2 * b + S.gcur) * Dp;
+    const float4 *g4 = reinterpret_cast<const float4 *>(gpool + (int64_t)(2 * b + S.gcur) * Dp);
+    const float4 *x4 = reinterpret_cast<const float4 *>(wa + (int64_t)b * Dp);
+    float4 *d4 = reinterpret_cast<float4 *>(d + (int64_t)b * Dp);
     const float cg = (float)S.coef_g;
-    float cS[MAXHIST], cY[MAXHIST];
-#pragma unroll
-    for (int j = 0; j < MAXHIST; ++j) {
-        cS[j] = j < nh ? (float)S.coefS[j] : 0.f;
-        cY[j] = j < nh ? (float)S.coefY[j] : 0.f;
-    }
-    const int64_t hoff = QQ * L;
-    const int64_t rlo = (int64_t)S.locus * QQ, rhi = rlo + QQ;
+    const int64_t hoff4 = QQ * L / 4;
+    const int64_t rlo4 = (int64_t)S.locus * QQ / 4, rhi4 = rlo4 + QQ / 4;
+    const int64_t nv4 = Dp / 4, tile = (int64_t)DOT_THREADS * DOT_U;
     float gd = 0.f, ddJ = 0.f, ddH = 0.f, xdJ = 0.f, xdH = 0.f, dmax = 0.f;
-    for (int64_t e = 4 * ((int64_t)blockIdx.x * DOT_THREADS + threadIdx.x); e < Dp;
-         e += 4 * (int64_t)gridDim.x * DOT_THREADS) {
-        const float4 gv = *reinterpret_cast<const float4 *>(g + e);
-        float4 dv = make_float4(cg * gv.x, cg * gv.y, cg * gv.z, cg * gv.w);
+    for (int64_t tb = (int64_t)blockIdx.x * tile; tb < nv4; tb += (int64_t)gridDim.x * tile) {
+        float4 gv[DOT_U], dv[DOT_U];
+#pragma unroll
+        for (int u = 0; u < DOT_U; ++u) {
+            const int64_t v = tb + u * DOT_THREADS + threadIdx.x;
+            gv[u] = v < nv4 ? g4[v] : make_float4(0.f, 0.f, 0.f, 0.f);
+            dv[u] = make_float4(cg * gv[u].x, cg * gv[u].y, cg * gv[u].z, cg * gv[u].w);
+        }
 #pragma unroll
         for (int j = 0; j < MAXHIST; ++j) {
             if (j < nh) {
-                const int64_t off = ((int64_t)b * m + S.ring[j]) * Dp + e;
-                const float4 sv = load_hist4(Spool, off, hist_bf16);
-                const float4 yv = load_hist4(Ypool, off, hist_bf16);
-                dv.x += cS[j] * sv.x + cY[j] * yv.x;
-                dv.y += cS[j] * sv.y + cY[j] * yv.y;
-                dv.z += cS[j] * sv.z + cY[j] * yv.z;
-                dv.w += cS[j] * sv.w + cY[j] * yv.w;
+                const int64_t base = ((int64_t)b * m + S.ring[j]) * Dp;
+                const float cs = (float)S.coefS[j], cy = (float)S.coefY[j];
+                float4 sv[DOT_U], yv[DOT_U];
+#pragma unroll
+                for (int u = 0; u < DOT_U; ++u) {
+                    const int64_t v = tb + u * DOT_THREADS + threadIdx.x;
+                    const bool ok = v < nv4;
+                    sv[u] = ok ? load_hist4(Spool, base + 4 * v, hist_bf16) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    yv[u] = ok ? load_hist4(Ypool, base + 4 * v, hist_bf16) : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < DOT_U; ++u) {
+                    dv[u].x += cs * sv[u].x + cy * yv[u].x;
+                    dv[u].y += cs * sv[u].y + cy * yv[u].y;
+                    dv[u].z += cs * sv[u].z + cy * yv[u].z;
+                    dv[u].w += cs * sv[u].w + cy * yv[u].w;
+                }
             }
         }
-        if (e >= rlo && e < rhi) dv = make_float4(0.f, 0.f, 0.f, 0.f);
-        *reinterpret_cast<float4 *>(d + (int64_t)b * Dp + e) = dv;
-        const float4 xv = *reinterpret_cast<const float4 *>(wa + (int64_t)b * Dp + e);
-        gd += dot4(gv, dv);
-        dmax = fmaxf(dmax, fmaxf(fmaxf(fabsf(dv.x), fabsf(dv.y)), fmaxf(fabsf(dv.z), fabsf(dv.w))));
-        if (e < hoff) {
-            ddJ += dot4(dv, dv);
-            xdJ += dot4(xv, dv);
-        } else {
-            ddH += dot4(dv, dv);
-            xdH += dot4(xv, dv);
+#pragma unroll
+        for (int u = 0; u < DOT_U; ++u) {
+            const int64_t v = tb + u * DOT_THREADS + threadIdx.x;
+            if (v >= nv4) continue;
+            if (v >= rlo4 && v < rhi4) dv[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            d4[v] = dv[u];
+            const float4 xv = x4[v];
+            gd += dot4(gv[u], dv[u]);
+            dmax = fmaxf(dmax, fmaxf(fmaxf(fabsf(dv[u].x), fabsf(dv[u].y)), fmaxf(fabsf(dv[u].z), fabsf(dv[u].w))));
+            if (v < hoff4) {
+                ddJ += dot4(dv[u], dv[u]);
+                xdJ += dot4(xv, dv[u]);
+            } else {
+                ddH += dot4(dv[u], dv[u]);
+                xdH += dot4(xv, dv[u]);
+            }
         }
     }
-    double v[5] = {gd, ddJ, ddH, xdJ, xdH};
+    float v[5] = {gd, ddJ, ddH, xdJ, xdH};
     const int idx[5] = {ACC_GD, ACC_DDJ, ACC_DDH, ACC_XDJ, ACC_XDH};
-    block_sum_atomic<5>(v, acc + (int64_t)b * NACC, idx);
+    block_sum_atomic_f<5>(v, acc + (int64_t)b * NACC, idx);
     const float wm = warp_max(dmax);
     if ((threadIdx.x & 31) == 0 && wm > 0.f) atomic_max_nonneg(acc + (int64_t)b * NACC + ACC_DMAX, (double)wm);
 }
@@ -374,7 +410,7 @@ void launch_hist_dots(const Problem &P, const SlotDev *sd, const int32_t *list, 
     // enough blocks for about two waves in total, each thread streaming
     // hundreds of float4 before the block reduction
     const int64_t per_slot = std::max<int64_t>(4, std::min<int64_t>(64, (4 * 152 + n - 1) / n));
-    dim3 grid(dgrid(P.Dp, DOT_THREADS, per_slot), (unsigned)n);
+    dim3 grid(dgrid(P.Dp, DOT_THREADS * DOT_U, per_slot), (unsigned)n);
     k_hist_dots<<<grid, DOT_THREADS, 0, st>>>(sd, list, P.Dp, P.ring, gpool, Spool, Ypool, hist_bf16,
                                               dots);
 }
@@ -384,8 +420,8 @@ void launch_direction(const Problem &P, const SlotDev *sd, const int32_t *list, 
                       const float *wa, float *d, double *acc, cudaStream_t st)
 {
     if (n <= 0) return;
-    const int64_t per_slot = std::max<int64_t>(4, std::min<int64_t>(256, (8 * 152 + n - 1) / n));
-    dim3 grid(dgrid(P.Dp, DOT_THREADS, per_slot), (unsigned)n);
+    const int64_t per_slot = std::max<int64_t>(4, std::min<int64_t>(128, (4 * 152 + n - 1) / n));
+    dim3 grid(dgrid(P.Dp, DOT_THREADS * DOT_U, per_slot), (unsigned)n);
     k_direction<<<grid, DOT_THREADS, 0, st>>>(sd, list, P.L, P.Dp, P.ring, gpool, Spool, Ypool,
                                               hist_bf16, wa, d, acc);
 }
