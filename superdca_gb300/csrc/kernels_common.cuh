@@ -90,11 +90,10 @@ __device__ __forceinline__ void atomic_max_nonneg(double *addr, double v)
 __device__ __forceinline__ float4 load_hist4(const void *base, int64_t off, int bf16)
 {
     if (bf16) {
-        const __nv_bfloat162 *p = reinterpret_cast<const __nv_bfloat162 *>(
-            reinterpret_cast<const __nv_bfloat16 *>(base) + off);
-        const float2 a = __bfloat1622float2(p[0]);
-        const float2 b = __bfloat1622float2(p[1]);
-        return make_float4(a.x, a.y, b.x, b.y);
+        // one 8-byte load for four values (off is a multiple of 4)
+        const uint2 raw = *reinterpret_cast<const uint2 *>(reinterpret_cast<const __nv_bfloat16 *>(base) + off);
+        return make_float4(__uint_as_float(raw.x << 16), __uint_as_float(raw.x & 0xFFFF0000u),
+                           __uint_as_float(raw.y << 16), __uint_as_float(raw.y & 0xFFFF0000u));
     }
     return *reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(base) + off);
 }
@@ -103,12 +102,12 @@ __device__ __forceinline__ float4 load_hist4(const void *base, int64_t off, int 
 __device__ __forceinline__ float4 store_hist4(void *base, int64_t off, float4 v, int bf16)
 {
     if (bf16) {
-        __nv_bfloat162 *p = reinterpret_cast<__nv_bfloat162 *>(
-            reinterpret_cast<__nv_bfloat16 *>(base) + off);
         const __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y);
         const __nv_bfloat162 b = __floats2bfloat162_rn(v.z, v.w);
-        p[0] = a;
-        p[1] = b;
+        uint2 raw;
+        raw.x = *reinterpret_cast<const uint32_t *>(&a);
+        raw.y = *reinterpret_cast<const uint32_t *>(&b);
+        *reinterpret_cast<uint2 *>(reinterpret_cast<__nv_bfloat16 *>(base) + off) = raw;
         const float2 fa = __bfloat1622float2(a), fb = __bfloat1622float2(b);
         return make_float4(fa.x, fa.y, fb.x, fb.y);
     }

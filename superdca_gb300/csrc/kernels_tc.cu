@@ -16,9 +16,9 @@
 //     128-byte-swizzled K-major layout the MMA reads (the one-hot matrix never
 //     exists in HBM: 1 byte per locus is read instead of 8), fence to the async
 //     proxy, arrive on full_a[s];
-//   * warp 1, one thread: tcgen05.mma kind::f16 (M128 N128 K16, FP32
-//     accumulator in TMEM), A x B_hi then A x B_lo, tcgen05.commit frees the
-//     stage;
+//   * warp 1, one thread: tcgen05.mma kind::f16 (M128 N256 K16, FP32
+//     accumulators in TMEM): the B tile stacks B_hi on B_lo, so one MMA forms
+//     A x B_hi and A x B_lo side by side; tcgen05.commit frees the stage;
 //   * warps 2-5 again: tcgen05.ld the accumulator and store it, scaled back
 //     by the per-slot power of two.
 // B is split as hi + lo fp16 halves of (value * 2^e) so that the product keeps
@@ -42,7 +42,7 @@ constexpr int RAW_BYTES = 2048;
 constexpr int STAGE_BYTES = A_BYTES + 2 * B_BYTES + RAW_BYTES;  // 51200, a multiple of 1024
 constexpr int THREADS = 192;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-constexpr uint32_t TMEM_COLS = 128;
+constexpr uint32_t TMEM_COLS = 256;  // hi products in columns 0..127, lo products in 128..255
 constexpr long long WAIT_LIMIT = 1ll << 26;  // polls before a wait gives up
 
 enum { MODE_FWD = 0, MODE_BWD = 1 };
@@ -112,8 +112,10 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr)
     return d;
 }
 
-// instruction descriptor, kind::f16: A = B = F16, D = F32, K-major, M = 128, N = 128
-constexpr uint32_t IDESC = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(BN >> 3) << 17) |
+// instruction descriptor, kind::f16: A = B = F16, D = F32, K-major, M = 128,
+// N = 256: the B tile stacks the hi rows (0..127) on the lo rows (128..255),
+// so one MMA forms both products into adjacent accumulator column ranges.
+constexpr uint32_t IDESC = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)((2 * BN) >> 3) << 17) |
                            ((uint32_t)(BM >> 4) << 24);
 
 __device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
@@ -305,10 +307,8 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
 #pragma unroll
                 for (int kk = 0; kk < BK / 16; ++kk) {
                     const uint64_t ad = smem_desc_sw128(st + kk * 32);
-                    const uint64_t bh = smem_desc_sw128(st + A_BYTES + kk * 32);
-                    const uint64_t bl = smem_desc_sw128(st + A_BYTES + B_BYTES + kk * 32);
-                    mma_f16(tmem_base, ad, bh, (j > 0 || kk > 0) ? 1u : 0u);
-                    mma_f16(tmem_base, ad, bl, 1u);
+                    const uint64_t bd = smem_desc_sw128(st + A_BYTES + kk * 32);  // 256 rows: hi then lo
+                    mma_f16(tmem_base, ad, bd, (j > 0 || kk > 0) ? 1u : 0u);
                 }
                 mma_commit(empty(s));
             }
@@ -337,8 +337,13 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
         const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
         for (int cj = 0; cj < BN / 32; ++cj) {
-            float v[32];
-            if (ok) tmem_ld32(tbase + (uint32_t)(cj * 32), v);
+            float v[32], vl[32];
+            if (ok) {
+                tmem_ld32(tbase + (uint32_t)(cj * 32), v);
+                tmem_ld32(tbase + (uint32_t)(BN + cj * 32), vl);
+#pragma unroll
+                for (int k = 0; k < 32; ++k) v[k] += vl[k];
+            }
             if (!ok) continue;
             const int row = m_tile * BM + r;
 #pragma unroll
