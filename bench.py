@@ -333,6 +333,7 @@ def engine_arm(args):
         "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": rf,
         "kernel_ms": {k: round(v, 2) for k, v in tot["kernel_ms"].items()},
         "solver": {"median_nfeval": float(np.median(nfe)), "median_iterations": float(np.median(iters)),
+                   "p90_iterations": float(np.percentile(iters, 90)), "max_iterations": int(np.max(iters)),
                    "median_contractions": float(np.median(contr)),
                    "status_counts": {str(k): statuses.count(k) for k in sorted(set(statuses))},
                    "wall_s": round(wall, 2), "wall_s_per_step": [round(v, 3) for v in walls]},

@@ -29,21 +29,33 @@
 #include <cuda.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+
 #include "engine.h"
 #include "kernels_common.cuh"
 
 namespace sdca {
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 4;
-constexpr int A_BYTES = BM * BK * 2;
-constexpr int B_BYTES = BN * BK * 2;
-constexpr int RAW_BYTES = 2048;
-constexpr int STAGE_BYTES = A_BYTES + 2 * B_BYTES + RAW_BYTES;  // 51200, a multiple of 1024
+constexpr int BM = 128, BN = 128, BK = 64;
+constexpr int A_BYTES = BM * BK * 2;   // one 128-row one-hot subtile
+constexpr int B_BYTES = BN * BK * 2;   // one fp16 half (hi or lo) of the slot operand
+constexpr int RAW_BYTES = 2048;        // u8 states behind one subtile
 constexpr int THREADS = 192;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-constexpr uint32_t TMEM_COLS = 256;  // hi products in columns 0..127, lo products in 128..255
 constexpr long long WAIT_LIMIT = 1ll << 26;  // polls before a wait gives up
+
+// A CTA owns MSUB consecutive 128-row subtiles and reuses each staged B tile
+// for all of them: the slot operand is the traffic that the L2 has to carry,
+// once per CTA per k-step.  TMEM holds one 128-column accumulator per subtile.
+template <int MSUB, int STG> struct Cfg {
+    static constexpr int STAGE_BYTES = MSUB * A_BYTES + 2 * B_BYTES + MSUB * RAW_BYTES;
+    static constexpr int SMEM_BYTES = STG * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+    static constexpr uint32_t TMEM_COLS = MSUB * BN;
+    static_assert(STAGE_BYTES % 1024 == 0, "stage must keep 1024-byte alignment");
+    static_assert(MSUB * BN <= 512, "TMEM holds 512 columns");
+};
 
 enum { MODE_FWD = 0, MODE_BWD = 1 };
 
@@ -112,10 +124,8 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr)
     return d;
 }
 
-// instruction descriptor, kind::f16: A = B = F16, D = F32, K-major, M = 128,
-// N = 256: the B tile stacks the hi rows (0..127) on the lo rows (128..255),
-// so one MMA forms both products into adjacent accumulator column ranges.
-constexpr uint32_t IDESC = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)((2 * BN) >> 3) << 17) |
+// instruction descriptor, kind::f16: A = B = F16, D = F32, K-major, M = 128, N = 128
+constexpr uint32_t IDESC = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(BN >> 3) << 17) |
                            ((uint32_t)(BM >> 4) << 24);
 
 __device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
@@ -232,31 +242,37 @@ struct GemmArgs {
     int *err;
 };
 
+template <int MSUB, int STG>
 __global__ void __launch_bounds__(THREADS, 1)
 k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtensorMap tmBhi,
        const __grid_constant__ CUtensorMap tmBlo, const GemmArgs args)
 {
+    using C = Cfg<MSUB, STG>;
+    constexpr int SB = C::STAGE_BYTES;
     extern __shared__ uint8_t smem_raw[];
     const uint32_t sbase0 = smem_u32(smem_raw);
     const uint32_t sbase = (sbase0 + 1023u) & ~1023u;
     uint8_t *const sgen = smem_raw + (sbase - sbase0);
-    const uint32_t bars = sbase + STAGES * STAGE_BYTES;
-    // barrier layout: full_raw[STAGES], full_a[STAGES], empty[STAGES], tmem_full, tmem addr
+    const uint32_t bars = sbase + STG * SB;
+    // stage layout: [A subtiles | B hi | B lo | raw u8 tiles]
+    auto a_off = [](int ms) { return (uint32_t)(ms * A_BYTES); };
+    constexpr uint32_t BHI = MSUB * A_BYTES, BLO = BHI + B_BYTES, RAW = BLO + B_BYTES;
+    // barrier layout: full_raw[STG], full_a[STG], empty[STG], tmem_full, tmem addr
     auto full_raw = [&](int s) { return bars + 8u * s; };
-    auto full_a = [&](int s) { return bars + 8u * (STAGES + s); };
-    auto empty = [&](int s) { return bars + 8u * (2 * STAGES + s); };
-    const uint32_t tmem_full = bars + 8u * (3 * STAGES);
-    const uint32_t tmem_slot = bars + 8u * (3 * STAGES + 1);
-    uint32_t *tmem_slot_gen = reinterpret_cast<uint32_t *>(sgen + STAGES * STAGE_BYTES + 8 * (3 * STAGES + 1));
+    auto full_a = [&](int s) { return bars + 8u * (STG + s); };
+    auto empty = [&](int s) { return bars + 8u * (2 * STG + s); };
+    const uint32_t tmem_full = bars + 8u * (3 * STG);
+    const uint32_t tmem_slot = bars + 8u * (3 * STG + 1);
+    uint32_t *tmem_slot_gen = reinterpret_cast<uint32_t *>(sgen + STG * SB + 8 * (3 * STG + 1));
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m_tile = blockIdx.x, n_tile = blockIdx.y, split = blockIdx.z;
+    const int m_group = blockIdx.x, n_tile = blockIdx.y, split = blockIdx.z;
     const int kt0 = split * args.kt_begin_stride;
     const int kt1 = min(args.kt_total, kt0 + args.kt_begin_stride);
     const int nkt = max(0, kt1 - kt0);
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) {
+        for (int s = 0; s < STG; ++s) {
             mbar_init(full_raw(s), 1);
             mbar_init(full_a(s), 128);
             mbar_init(empty(s), 1);
@@ -266,7 +282,7 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tmem_slot),
-                     "r"(TMEM_COLS)
+                     "r"(C::TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -279,52 +295,65 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
     if (warp == 0) {
         if (lane == 0) {
             for (int j = 0; j < nkt; ++j) {
-                const int s = j % STAGES;
-                const uint32_t ph = (uint32_t)((j / STAGES) & 1);
+                const int s = j % STG;
+                const uint32_t ph = (uint32_t)((j / STG) & 1);
                 if (!mbar_wait(empty(s), ph ^ 1u)) { failed = true; break; }
-                const uint32_t st = sbase + (uint32_t)s * STAGE_BYTES;
-                mbar_expect_tx(full_raw(s), RAW_BYTES + 2 * B_BYTES);
+                const uint32_t st = sbase + (uint32_t)s * SB;
+                mbar_expect_tx(full_raw(s), MSUB * RAW_BYTES + 2 * B_BYTES);
                 const int kt = kt0 + j;
-                if (args.mode == MODE_FWD)
-                    tma_load_2d(st + A_BYTES + 2 * B_BYTES, &tmRaw, kt * 16, m_tile * BM, full_raw(s));
-                else
-                    tma_load_2d(st + A_BYTES + 2 * B_BYTES, &tmRaw, kt * BK, m_tile * 32, full_raw(s));
-                tma_load_2d(st + A_BYTES, &tmBhi, kt * BK, n_tile * BN, full_raw(s));
-                tma_load_2d(st + A_BYTES + B_BYTES, &tmBlo, kt * BK, n_tile * BN, full_raw(s));
+#pragma unroll
+                for (int ms = 0; ms < MSUB; ++ms) {
+                    const int mt = m_group * MSUB + ms;
+                    if (args.mode == MODE_FWD)
+                        tma_load_2d(st + RAW + ms * RAW_BYTES, &tmRaw, kt * 16, mt * BM, full_raw(s));
+                    else
+                        tma_load_2d(st + RAW + ms * RAW_BYTES, &tmRaw, kt * BK, mt * 32, full_raw(s));
+                }
+                tma_load_2d(st + BHI, &tmBhi, kt * BK, n_tile * BN, full_raw(s));
+                tma_load_2d(st + BLO, &tmBlo, kt * BK, n_tile * BN, full_raw(s));
             }
             // loads still in flight land before the block retires
-            for (int j = max(0, nkt - STAGES); j < nkt; ++j)
-                if (!mbar_wait(full_raw(j % STAGES), (uint32_t)((j / STAGES) & 1))) failed = true;
+            for (int j = max(0, nkt - STG); j < nkt; ++j)
+                if (!mbar_wait(full_raw(j % STG), (uint32_t)((j / STG) & 1))) failed = true;
         }
     } else if (warp == 1) {
         if (lane == 0) {
             for (int j = 0; j < nkt; ++j) {
-                const int s = j % STAGES;
-                const uint32_t ph = (uint32_t)((j / STAGES) & 1);
+                const int s = j % STG;
+                const uint32_t ph = (uint32_t)((j / STG) & 1);
                 if (!mbar_wait(full_a(s), ph)) { failed = true; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t st = sbase + (uint32_t)s * STAGE_BYTES;
+                const uint32_t st = sbase + (uint32_t)s * SB;
 #pragma unroll
                 for (int kk = 0; kk < BK / 16; ++kk) {
-                    const uint64_t ad = smem_desc_sw128(st + kk * 32);
-                    const uint64_t bd = smem_desc_sw128(st + A_BYTES + kk * 32);  // 256 rows: hi then lo
-                    mma_f16(tmem_base, ad, bd, (j > 0 || kk > 0) ? 1u : 0u);
+                    const uint64_t bh = smem_desc_sw128(st + BHI + kk * 32);
+                    const uint64_t bl = smem_desc_sw128(st + BLO + kk * 32);
+#pragma unroll
+                    for (int ms = 0; ms < MSUB; ++ms) {
+                        const uint64_t ad = smem_desc_sw128(st + a_off(ms) + kk * 32);
+                        const uint32_t td = tmem_base + (uint32_t)(ms * BN);
+                        mma_f16(td, ad, bh, (j > 0 || kk > 0) ? 1u : 0u);
+                        mma_f16(td, ad, bl, 1u);
+                    }
                 }
                 mma_commit(empty(s));
             }
-            // the accumulator is complete (or abandoned) once every issued MMA retired
+            // the accumulators are complete (or abandoned) once every issued MMA retired
             mma_commit(tmem_full);
         }
     } else {
         const int t = threadIdx.x - 64;  // 0..127
         for (int j = 0; j < nkt; ++j) {
-            const int s = j % STAGES;
-            const uint32_t ph = (uint32_t)((j / STAGES) & 1);
+            const int s = j % STG;
+            const uint32_t ph = (uint32_t)((j / STG) & 1);
             if (!mbar_wait(full_raw(s), ph)) { failed = true; break; }
-            const uint8_t *raw = sgen + s * STAGE_BYTES + A_BYTES + 2 * B_BYTES;
-            const uint32_t a_base = sbase + (uint32_t)s * STAGE_BYTES;
-            if (args.mode == MODE_FWD) expand_fwd(raw, a_base, t);
-            else expand_bwd(raw, a_base, t);
+            const uint32_t st = sbase + (uint32_t)s * SB;
+#pragma unroll
+            for (int ms = 0; ms < MSUB; ++ms) {
+                const uint8_t *raw = sgen + s * SB + RAW + ms * RAW_BYTES;
+                if (args.mode == MODE_FWD) expand_fwd(raw, st + a_off(ms), t);
+                else expand_bwd(raw, st + a_off(ms), t);
+            }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(full_a(s));
         }
@@ -334,36 +363,35 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const int q = warp & 3;  // TMEM lane quadrant of this warp
         const int r = q * 32 + lane;
-        const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
-        for (int cj = 0; cj < BN / 32; ++cj) {
-            float v[32], vl[32];
-            if (ok) {
-                tmem_ld32(tbase + (uint32_t)(cj * 32), v);
-                tmem_ld32(tbase + (uint32_t)(BN + cj * 32), vl);
+        for (int ms = 0; ms < MSUB; ++ms) {
+            const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(ms * BN);
+            const int row = (m_group * MSUB + ms) * BM + r;
+#pragma unroll 1
+            for (int cj = 0; cj < BN / 32; ++cj) {
+                float v[32];
+                if (ok) tmem_ld32(tbase + (uint32_t)(cj * 32), v);
+                if (!ok) continue;
 #pragma unroll
-                for (int k = 0; k < 32; ++k) v[k] += vl[k];
-            }
-            if (!ok) continue;
-            const int row = m_tile * BM + r;
-#pragma unroll
-            for (int tt = 0; tt < 8; ++tt) {
-                const int P = (n_tile * BN + cj * 32) / 4 + tt;
-                if (P >= args.nlist) continue;
-                const int b = args.list[P];
-                if (args.mode == MODE_FWD) {
-                    if (row < args.Nx) {
-                        const float sc = (float)args.sd[b].tc_inv_scale;
-                        args.partial[((int64_t)split * args.Bmax + b) * args.Nx + row] =
-                            make_float4(v[4 * tt] * sc, v[4 * tt + 1] * sc, v[4 * tt + 2] * sc, v[4 * tt + 3] * sc);
+                for (int tt = 0; tt < 8; ++tt) {
+                    const int P = (n_tile * BN + cj * 32) / 4 + tt;
+                    if (P >= args.nlist) continue;
+                    const int b = args.list[P];
+                    if (args.mode == MODE_FWD) {
+                        if (row < args.Nx) {
+                            const float sc = (float)args.sd[b].tc_inv_scale;
+                            args.partial[((int64_t)split * args.Bmax + b) * args.Nx + row] =
+                                make_float4(v[4 * tt] * sc, v[4 * tt + 1] * sc, v[4 * tt + 2] * sc,
+                                            v[4 * tt + 3] * sc);
+                        }
+                    } else if (row < args.m_rows) {
+                        const float sc = args.inv_scale_bwd;
+                        const int gb = args.sd[b].gcur;
+                        float *gn = args.gpool + (int64_t)(2 * b + 1 - gb) * args.Dp + (int64_t)(row >> 2) * QQ +
+                                    (row & 3) * Q;
+                        *reinterpret_cast<float4 *>(gn) = make_float4(v[4 * tt] * sc, v[4 * tt + 1] * sc,
+                                                                      v[4 * tt + 2] * sc, v[4 * tt + 3] * sc);
                     }
-                } else if (row < args.m_rows) {
-                    const float sc = args.inv_scale_bwd;
-                    const int gb = args.sd[b].gcur;
-                    float *gn = args.gpool + (int64_t)(2 * b + 1 - gb) * args.Dp + (int64_t)(row >> 2) * QQ +
-                                (row & 3) * Q;
-                    *reinterpret_cast<float4 *>(gn) =
-                        make_float4(v[4 * tt] * sc, v[4 * tt + 1] * sc, v[4 * tt + 2] * sc, v[4 * tt + 3] * sc);
                 }
             }
         }
@@ -373,7 +401,7 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
     __syncthreads();
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(C::TMEM_COLS)
                      : "memory");
     }
 }
@@ -466,7 +494,62 @@ struct TcPlan {
     int fwd_splits = 1;
 };
 
-int tc_smem_bytes() { return tc::SMEM_BYTES; }
+namespace {
+
+// Subtiles per CTA (MSUB) and pipeline depth: {4, 2} keeps four 128-row
+// accumulators (all 512 TMEM columns) and two 104 KB stages; {2, 3} and
+// {1, 4} trade L2 reuse of the slot operand for deeper pipelines.
+// SDCA_TC_MSUB (1, 2 or 4) overrides the choice for tuning runs.
+int msub_choice()
+{
+    static int v = 0;
+    if (!v) {
+        const char *e = std::getenv("SDCA_TC_MSUB");
+        v = (e && (e[0] == '1' || e[0] == '2')) ? e[0] - '0' : 4;
+    }
+    return v;
+}
+
+template <int MSUB, int STG>
+void launch_gemm(dim3 grid, const CUtensorMap &a, const CUtensorMap &bh, const CUtensorMap &bl,
+                 const tc::GemmArgs &args, cudaStream_t st)
+{
+    tc::k_gemm<MSUB, STG><<<grid, tc::THREADS, tc::Cfg<MSUB, STG>::SMEM_BYTES, st>>>(a, bh, bl, args);
+}
+
+void launch_gemm_any(int msub, int m_tiles, int n_tiles, int splits, const CUtensorMap &a, const CUtensorMap &bh,
+                     const CUtensorMap &bl, const tc::GemmArgs &args, cudaStream_t st)
+{
+    const dim3 grid((unsigned)((m_tiles + msub - 1) / msub), (unsigned)n_tiles, (unsigned)splits);
+    if (msub == 4) launch_gemm<4, 2>(grid, a, bh, bl, args, st);
+    else if (msub == 2) launch_gemm<2, 3>(grid, a, bh, bl, args, st);
+    else launch_gemm<1, 4>(grid, a, bh, bl, args, st);
+}
+
+} // namespace
+
+int tc_fwd_splits(const Problem &P, int nlist)
+{
+    // split K so that the CTAs fill whole waves of 152 SMs (one CTA per SM)
+    const int msub = msub_choice();
+    const int mt = (int)((P.Nx + tc::BM - 1) / tc::BM);
+    const int mg = (mt + msub - 1) / msub;
+    const int nt = (4 * nlist + tc::BN - 1) / tc::BN;
+    const int kt = (int)((4 * P.L + tc::BK - 1) / tc::BK);
+    int best = 1;
+    double best_t = 1e30;
+    for (int s = 1; s <= (int)P.C; ++s) {
+        const double waves = std::ceil((double)mg * nt * s / 152.0);
+        const double t = waves * std::ceil((double)kt / s) + 8.0 * waves;
+        if (t < best_t) {
+            best_t = t;
+            best = s;
+        }
+    }
+    // no empty split: every launched split owns at least one k-tile
+    const int stride = (kt + best - 1) / best;
+    return (kt + stride - 1) / stride;
+}
 
 TcPlan *tc_plan_create(const Problem &P, const uint8_t *X, const uint8_t *XT, __half *Dhi, __half *Dlo,
                        __half *Rhi, __half *Rlo, int64_t Kp)
@@ -495,27 +578,6 @@ TcPlan *tc_plan_create(const Problem &P, const uint8_t *X, const uint8_t *XT, __
 
 void tc_plan_destroy(TcPlan *p) { delete p; }
 
-int tc_fwd_splits(const Problem &P, int nlist)
-{
-    // split K so that the CTAs fill whole waves of 152 SMs (one CTA per SM)
-    const int mt = (int)((P.Nx + tc::BM - 1) / tc::BM);
-    const int nt = (4 * nlist + tc::BN - 1) / tc::BN;
-    const int kt = (int)((4 * P.L + tc::BK - 1) / tc::BK);
-    int best = 1;
-    double best_t = 1e30;
-    for (int s = 1; s <= (int)P.C; ++s) {
-        const double waves = std::ceil((double)mt * nt * s / 152.0);
-        const double t = waves * std::ceil((double)kt / s) + 8.0 * waves;
-        if (t < best_t) {
-            best_t = t;
-            best = s;
-        }
-    }
-    // no empty split: every launched split owns at least one k-tile
-    const int stride = (kt + best - 1) / best;
-    return (kt + stride - 1) / stride;
-}
-
 cudaError_t tc_launch_fwd(const TcPlan *pl, const Problem &P, const SlotDev *sd, const int32_t *list, int n,
                           const float *vecs, __half *Dhi, __half *Dlo, float *partial, int splits, int *err,
                           cudaStream_t st)
@@ -537,8 +599,8 @@ cudaError_t tc_launch_fwd(const TcPlan *pl, const Problem &P, const SlotDev *sd,
     a.Bmax = P.Bmax;
     a.Nx = P.Nx;
     a.err = err;
-    dim3 grid((unsigned)((P.Nx + tc::BM - 1) / tc::BM), (unsigned)((4 * n + tc::BN - 1) / tc::BN), (unsigned)splits);
-    tc::k_gemm<<<grid, tc::THREADS, tc::SMEM_BYTES, st>>>(pl->mX, pl->mDhi, pl->mDlo, a);
+    launch_gemm_any(msub_choice(), (int)((P.Nx + tc::BM - 1) / tc::BM), (4 * n + tc::BN - 1) / tc::BN, splits,
+                    pl->mX, pl->mDhi, pl->mDlo, a, st);
     return cudaGetLastError();
 }
 
@@ -564,14 +626,22 @@ cudaError_t tc_launch_bwd(const TcPlan *pl, const Problem &P, const SlotDev *sd,
     a.inv_scale_bwd = 1.0f / r_scale;
     a.Nx = P.Nx;
     a.err = err;
-    dim3 grid((unsigned)((4 * P.L + tc::BM - 1) / tc::BM), (unsigned)((4 * n + tc::BN - 1) / tc::BN), 1);
-    tc::k_gemm<<<grid, tc::THREADS, tc::SMEM_BYTES, st>>>(pl->mXT, pl->mRhi, pl->mRlo, a);
+    launch_gemm_any(msub_choice(), (int)((4 * P.L + tc::BM - 1) / tc::BM), (4 * n + tc::BN - 1) / tc::BN, 1,
+                    pl->mXT, pl->mRhi, pl->mRlo, a, st);
     return cudaGetLastError();
 }
 
 cudaError_t tc_configure()
 {
-    return cudaFuncSetAttribute(tc::k_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+    cudaError_t e = cudaFuncSetAttribute(tc::k_gemm<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tc::Cfg<4, 2>::SMEM_BYTES);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(tc::k_gemm<2, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc::Cfg<2, 3>::SMEM_BYTES);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(tc::k_gemm<1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc::Cfg<1, 4>::SMEM_BYTES);
+    return e;
 }
 
 } // namespace sdca
