@@ -72,6 +72,10 @@ typedef struct {
     int32_t contractions;      /* forward + backward contraction passes run */
     int32_t status;            /* 0 gradient tolerance, 1 iteration limit,
                                   2 relative-epsilon stop, -1 non-finite */
+    int32_t restarts;          /* steepest-descent restarts (non-descent direction) */
+    int32_t skipped_pairs;     /* history pairs not stored (s.y <= 0) */
+    int32_t weak_searches;     /* line searches that ended without the Wolfe conditions */
+    int32_t max_trials;        /* most trial steps any line search took */
 } sdca_locus_stat;
 
 typedef struct {

@@ -43,7 +43,9 @@ class Config(C.Structure):
 
 class LocusStat(C.Structure):
     _fields_ = [("f", C.c_double), ("gnorm", C.c_double), ("iterations", C.c_int32),
-                ("nfeval", C.c_int32), ("contractions", C.c_int32), ("status", C.c_int32)]
+                ("nfeval", C.c_int32), ("contractions", C.c_int32), ("status", C.c_int32),
+                ("restarts", C.c_int32), ("skipped_pairs", C.c_int32), ("weak_searches", C.c_int32),
+                ("max_trials", C.c_int32)]
 
 
 class Profile(C.Structure):

@@ -71,6 +71,9 @@ struct SlotHost {
     int gcur = 0;
     double rs[Q] = {0, 0, 0, 0};
     double f_final = 0;
+    int restarts = 0, skipped = 0, weak = 0, max_trials = 0;
+    bool force_restart = false;
+    bool stalled = false;    // steepest descent itself was not downhill: stop
     MoreThuente ls;
 };
 
@@ -400,14 +403,15 @@ int run_forward(sdca_handle *h, const std::vector<int32_t> &lst, const float *ve
         CK(tc_launch_fwd(h->tc, h->P, h->sd, h->list, (int)lst.size(), vecs, h->Dhi, h->Dlo, h->partial,
                          splits, h->tc_err, h->stream));
         launch_reduce_partial(h->P, h->list, (int)lst.size(), h->partial, vecs, 1, h->u, nullptr,
-                              h->stream, splits);
+                              h->stream, splits, h->R, h->acc);
     } else if (to_lbase) {
         Timed t(h, SDCA_K_FORWARD, 2, (int64_t)lst.size());
         launch_fwd_exact(h->P, h->X, h->list, (int)lst.size(), vecs, h->partial64, h->lbase, h->stream);
     } else {
         Timed t(h, SDCA_K_FORWARD, 2, (int64_t)lst.size());
         launch_fwd_gather(h->P, h->X, h->list, (int)lst.size(), vecs, h->partial, h->stream);
-        launch_reduce_partial(h->P, h->list, (int)lst.size(), h->partial, vecs, 1, h->u, nullptr, h->stream);
+        launch_reduce_partial(h->P, h->list, (int)lst.size(), h->partial, vecs, 1, h->u, nullptr, h->stream, 0,
+                              h->R, h->acc);
     }
     CKL();
     for (int b : lst) h->slots[b].contractions++;
@@ -520,6 +524,10 @@ int retire(sdca_handle *h, Queue &Qu, const std::vector<int32_t> &done)
             st.nfeval = (int32_t)S.nfeval;
             st.contractions = (int32_t)S.contractions;
             st.status = S.status;
+            st.restarts = S.restarts;
+            st.skipped_pairs = S.skipped;
+            st.weak_searches = S.weak;
+            st.max_trials = S.max_trials;
         }
         h->prof.iterations += S.iterations;
         h->prof.contractions += S.contractions;
@@ -591,6 +599,8 @@ int phase_trials(sdca_handle *h, Queue &Qu)
                     S.stp = stp_eval;  // the accepted point is the last trial
                     S.f = f;
                     S.phase = PH_READY_STEP;
+                    if (S.ls.info != 1) S.weak++;
+                    S.max_trials = std::max(S.max_trials, S.trials);
                 } else {
                     S.stp = S.ls.stp;
                 }
@@ -691,12 +701,16 @@ int phase_step(sdca_handle *h)
                 S.iter++;
             } else {
                 S.ring_new = -1;  // pair not usable: keep the history as it is
+                S.skipped++;
             }
             if (S.iterations > h->cfg.max_iterations) {
                 S.status = 1;
                 stop = true;
             } else if (S.gmax < h->cfg.gradient_threshold) {
                 S.status = 0;
+                stop = true;
+            } else if (S.stalled) {
+                S.status = 2;  // no downhill step left at working precision
                 stop = true;
             }
         }
@@ -821,7 +835,8 @@ int phase_step(sdca_handle *h)
         h->sd_h[b].tc_scale = pow2_scale(acc_get(h, b, ACC_DMAX));
         h->sd_h[b].tc_inv_scale = 1.0 / h->sd_h[b].tc_scale;
         const double releps = 1e-4 * std::max(1.0, std::sqrt(S.x2J + S.x2H));
-        if (!S.hist.empty() && !(S.gd <= -1e-4 * releps)) restart.push_back(b);
+        if (!S.hist.empty() && (S.force_restart || !(S.gd <= -1e-4 * releps))) restart.push_back(b);
+        S.force_restart = false;
     }
     std::vector<char> restarted(P.Bmax, 0);
     if (!restart.empty()) {
@@ -829,6 +844,7 @@ int phase_step(sdca_handle *h)
         for (int b : restart) {
             h->slots[b].hist.clear();
             h->slots[b].iter = 0;
+            h->slots[b].restarts++;
             h->sd_h[b].coef_g = -1.0;
             restarted[b] = 1;
         }
@@ -845,7 +861,11 @@ int phase_step(sdca_handle *h)
             h->sd_h[b].tc_inv_scale = 1.0 / h->sd_h[b].tc_scale;
         }
     }
+    rc = zero_acc(h);
+    if (rc) return rc;
     rc = run_forward(h, cont, h->d, false);
+    if (rc) return rc;
+    rc = fetch_acc(h);
     if (rc) return rc;
     for (int b : cont) {
         SlotHost &S = h->slots[b];
@@ -853,12 +873,19 @@ int phase_step(sdca_handle *h)
         S.trials = 0;
         S.use_u = true;
         S.push = false;
-        if (S.ls.start(S.f, S.gd, alpha_init) == MoreThuente::NEED_EVAL) {
+        // slope of the search line at 0 from the numbers the trials use
+        const double dg0 = acc_get(h, b, ACC_DG0) + dl2_along(P, S, 0.0);
+        if (S.ls.start(S.f, dg0, alpha_init) == MoreThuente::NEED_EVAL) {
             S.stp = S.ls.stp;
             S.phase = PH_LS;
         } else {
-            S.stp = alpha_init;
+            // not downhill along this line: stay, and restart from steepest
+            // descent at the next iteration
+            S.stp = 0.0;
             S.phase = PH_FINAL_EVAL;
+            if (S.hist.empty()) S.stalled = true;
+            else S.force_restart = true;
+            S.weak++;
         }
     }
     return SDCA_OK;

@@ -43,6 +43,7 @@ enum Acc {
     ACC_XDH,        // x_h . d_h                                    (direction)
     ACC_GMAX,       // max |g| (bits of a non-negative double, atomicMax) (gradient)
     ACC_DMAX,       // max |d| (bits of a non-negative double, atomicMax) (direction)
+    ACC_DG0,        // sum_i R_i . u_i at the current point: slope of the search line at 0 (forward)
     NACC = 20
 };
 
@@ -95,7 +96,7 @@ void launch_fwd_gather(const Problem &P, const uint8_t *X, const int32_t *list, 
                        const float *vecs, float *partial, cudaStream_t st);
 void launch_reduce_partial(const Problem &P, const int32_t *list, int n, const float *partial,
                            const float *vecs, int add_h, float *out_f, double *out_d,
-                           cudaStream_t st, int C = 0);
+                           cudaStream_t st, int C = 0, const float *R = nullptr, double *acc = nullptr);
 void launch_fwd_exact(const Problem &P, const uint8_t *X, const int32_t *list, int n, const float *vecs,
                       double *partial64, double *lbase, cudaStream_t st);
 void launch_grad_finalize(const Problem &P, const SlotDev *sd, const int32_t *list, int n,

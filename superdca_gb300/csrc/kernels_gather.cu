@@ -183,13 +183,41 @@ __global__ void k_reduce_partial64(const double4 *__restrict__ partial, int C, i
     out_d[o * 4 + 2] = s2; out_d[o * 4 + 3] = s3;
 }
 
+// Sums the partial slices into u (float) or logits (double).  With R given,
+// also reduces sum_i R_i . u_i per slot into acc[ACC_DG0]: the slope at
+// step 0 of the line the next search walks, from the same numbers the
+// trial steps will use.
 __global__ void k_reduce_partial(const float4 *__restrict__ partial, int C, int Bmax, int64_t Nx,
                                  int N, const int32_t *__restrict__ list,
                                  const float *__restrict__ vecs, int64_t Dp, int64_t hoff,
-                                 int add_h, float4 *__restrict__ out_f, double *__restrict__ out_d)
+                                 int add_h, float4 *__restrict__ out_f, double *__restrict__ out_d,
+                                 const float4 *__restrict__ R, double *__restrict__ acc)
 {
     const int b = list[blockIdx.y];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (R) {
+        // every thread of the block takes part in the reduction
+        double ru = 0.0;
+        if (i < N) {
+            double t[4] = {0, 0, 0, 0};
+            if (add_h) {
+                const float *h = vecs + (int64_t)b * Dp + hoff;
+                t[0] = h[0]; t[1] = h[1]; t[2] = h[2]; t[3] = h[3];
+            }
+            for (int c = 0; c < C; ++c) {
+                const float4 p = partial[((int64_t)c * Bmax + b) * Nx + i];
+                t[0] += p.x; t[1] += p.y; t[2] += p.z; t[3] += p.w;
+            }
+            const float4 uf = make_float4((float)t[0], (float)t[1], (float)t[2], (float)t[3]);
+            out_f[(int64_t)b * Nx + i] = uf;
+            const float4 r = R[(int64_t)b * Nx + i];
+            ru = (double)r.x * uf.x + (double)r.y * uf.y + (double)r.z * uf.z + (double)r.w * uf.w;
+        }
+        double v[1] = {ru};
+        const int idx[1] = {ACC_DG0};
+        block_sum_atomic<1>(v, acc + (int64_t)b * NACC, idx);
+        return;
+    }
     if (i >= N) return;
     double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
     if (add_h) {
@@ -342,13 +370,14 @@ void launch_fwd_exact(const Problem &P, const uint8_t *X, const int32_t *list, i
 
 void launch_reduce_partial(const Problem &P, const int32_t *list, int n, const float *partial,
                            const float *vecs, int add_h, float *out_f, double *out_d,
-                           cudaStream_t st, int C)
+                           cudaStream_t st, int C, const float *R, double *acc)
 {
     if (n <= 0) return;
     dim3 grid((unsigned)((P.N + 255) / 256), (unsigned)n);
     k_reduce_partial<<<grid, 256, 0, st>>>(reinterpret_cast<const float4 *>(partial), C > 0 ? C : (int)P.Cg,
                                            P.Bmax, P.Nx, (int)P.N, list, vecs, P.Dp, QQ * P.L, add_h,
-                                           reinterpret_cast<float4 *>(out_f), out_d);
+                                           reinterpret_cast<float4 *>(out_f), out_d,
+                                           reinterpret_cast<const float4 *>(R), acc);
 }
 
 void launch_grad_finalize(const Problem &P, const SlotDev *sd, const int32_t *list, int n,

@@ -34,6 +34,10 @@ class SolveResult:
     contractions: np.ndarray
     status: np.ndarray
     x: np.ndarray | None = None  # solutions, reference layout
+    restarts: np.ndarray | None = None
+    skipped_pairs: np.ndarray | None = None
+    weak_searches: np.ndarray | None = None
+    max_trials: np.ndarray | None = None
 
 
 class Engine:
@@ -112,7 +116,11 @@ class Engine:
             iterations=np.array([s.iterations for s in st]),
             nfeval=np.array([s.nfeval for s in st]),
             contractions=np.array([s.contractions for s in st]),
-            status=np.array([s.status for s in st]), x=xo)
+            status=np.array([s.status for s in st]), x=xo,
+            restarts=np.array([s.restarts for s in st]),
+            skipped_pairs=np.array([s.skipped_pairs for s in st]),
+            weak_searches=np.array([s.weak_searches for s in st]),
+            max_trials=np.array([s.max_trials for s in st]))
 
     def eval(self, r: int, x: np.ndarray, grad: bool = True):
         x = np.ascontiguousarray(x, dtype=np.float64)
