@@ -46,6 +46,8 @@ enum Phase {
     PH_READY_INIT,  // start point evaluated, waiting for the gradient pass
     PH_READY_STEP,  // step accepted, waiting for the gradient pass
     PH_FINALIZE,    // converged: logits refreshed, needs the final evaluation
+    PH_REFRESH,     // logits recomputed from the stored parameters: needs the evaluation there
+    PH_READY_REFRESH,  // re-evaluated, waiting for the gradient pass (history kept)
 };
 
 struct SlotHost {
@@ -71,9 +73,10 @@ struct SlotHost {
     int gcur = 0;
     double rs[Q] = {0, 0, 0, 0};
     double f_final = 0;
-    int restarts = 0, skipped = 0, weak = 0, max_trials = 0;
+    int restarts = 0, skipped = 0, weak = 0, max_trials = 0, refreshes = 0;
     bool force_restart = false;
     bool stalled = false;    // steepest descent itself was not downhill: stop
+    int last_refresh = 0;    // iteration of the last logit refresh
     MoreThuente ls;
 };
 
@@ -122,6 +125,11 @@ struct sdca_handle {
     __half *Dhi = nullptr, *Dlo = nullptr, *Rhi = nullptr, *Rlo = nullptr;
     int *tc_err = nullptr;
     float r_scale = 1.0f;
+    // logit refresh policy: when max|g| first falls
+    // below refresh_factor x threshold, and again every refresh_every
+    // iterations while it stays there
+    double refresh_factor = 8.0;
+    int refresh_every = 30;
 
     std::vector<SlotHost> slots;
 
@@ -556,7 +564,8 @@ int phase_trials(sdca_handle *h, Queue &Qu)
         std::vector<int32_t> lst;
         for (int b = 0; b < P.Bmax; ++b) {
             const int ph = h->slots[b].phase;
-            if (ph == PH_INIT || ph == PH_LS || ph == PH_FINAL_EVAL || ph == PH_FINALIZE) lst.push_back(b);
+            if (ph == PH_INIT || ph == PH_LS || ph == PH_FINAL_EVAL || ph == PH_FINALIZE || ph == PH_REFRESH)
+                lst.push_back(b);
         }
         if (lst.empty()) return SDCA_OK;
         int rc = upload_slots(h, lst);
@@ -579,6 +588,9 @@ int phase_trials(sdca_handle *h, Queue &Qu)
             if (S.phase == PH_INIT) {
                 S.f = fdata;  // the L2 part is added once |x|^2 is known
                 S.phase = PH_READY_INIT;
+            } else if (S.phase == PH_REFRESH) {
+                S.f = fdata;
+                S.phase = PH_READY_REFRESH;
             } else if (S.phase == PH_FINALIZE) {
                 S.f_final = fdata + P.lambda_J * S.x2J + P.lambda_h * S.x2H;
                 done.push_back(b);
@@ -631,7 +643,7 @@ int phase_step(sdca_handle *h)
             int pos = 0;
             while (std::find(S.hist.begin(), S.hist.end(), pos) != S.hist.end()) ++pos;
             S.ring_new = pos;
-        } else if (S.phase == PH_READY_INIT) {
+        } else if (S.phase == PH_READY_INIT || S.phase == PH_READY_REFRESH) {
             all.push_back(b);
             S.push = false;
             S.ring_new = -1;
@@ -690,6 +702,13 @@ int phase_step(sdca_handle *h)
         if (S.phase == PH_READY_INIT) {
             S.f += P.lambda_J * S.x2J + P.lambda_h * S.x2H;
             S.nfeval = 1;
+        } else if (S.phase == PH_READY_REFRESH) {
+            // same point, logits recomputed exactly: a fresh gradient, no new pair
+            S.f += P.lambda_J * S.x2J + P.lambda_h * S.x2H;
+            if (S.gmax < h->cfg.gradient_threshold) {
+                S.status = 0;
+                stop = true;
+            }
         } else {
             S.iterations++;
             S.nfeval += 2 + S.trials;
@@ -727,6 +746,37 @@ int phase_step(sdca_handle *h)
         }
         if (stop) fin.push_back(b);
         else cont.push_back(b);
+    }
+
+    // Slots approaching the threshold get their logits recomputed from the
+    // stored parameters: the running logits lbase += stp u carry the rounding
+    // of every forward contraction, and near the threshold that drift is
+    // larger than the gradient left to remove.
+    {
+        std::vector<int32_t> keep, refresh;
+        for (int b : cont) {
+            SlotHost &S = h->slots[b];
+            const bool near = S.gmax < h->refresh_factor * h->cfg.gradient_threshold;
+            if (S.phase == PH_READY_STEP && near &&
+                S.iterations - S.last_refresh >= h->refresh_every) {
+                refresh.push_back(b);
+                S.last_refresh = S.iterations;
+            } else {
+                keep.push_back(b);
+            }
+        }
+        if (!refresh.empty()) {
+            rc = run_forward(h, refresh, h->wa, true);
+            if (rc) return rc;
+            for (int b : refresh) {
+                SlotHost &S = h->slots[b];
+                S.phase = PH_REFRESH;
+                S.stp = 0.0;
+                S.use_u = false;
+                S.refreshes++;
+            }
+            cont.swap(keep);
+        }
     }
 
     // converged slots: refresh their logits from the stored parameters
