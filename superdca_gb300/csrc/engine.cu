@@ -712,8 +712,10 @@ int phase_step(sdca_handle *h)
         } else {
             S.iterations++;
             S.nfeval += 2 + S.trials;
-            const double sy = acc_get(h, b, ACC_SY), yy = acc_get(h, b, ACC_YY);
-            if (sy > 0.0 && yy > 0.0 && std::isfinite(sy) && std::isfinite(yy)) {
+            const double sy = acc_get(h, b, ACC_SY), yy = acc_get(h, b, ACC_YY), ss = acc_get(h, b, ACC_SS);
+            // keep a pair only if it carries curvature above the rounding of
+            // the FP32 gradients: cos(s, y) > 1e-3
+            if (sy > 1e-3 * std::sqrt(ss * yy) && yy > 0.0 && std::isfinite(sy) && std::isfinite(yy)) {
                 if ((int)S.hist.size() == m) S.hist.pop_front();
                 S.hist.push_back(S.ring_new);
                 S.gamma = sy / yy;

@@ -44,6 +44,7 @@ enum Acc {
     ACC_GMAX,       // max |g| (bits of a non-negative double, atomicMax) (gradient)
     ACC_DMAX,       // max |d| (bits of a non-negative double, atomicMax) (direction)
     ACC_DG0,        // sum_i R_i . u_i at the current point: slope of the search line at 0 (forward)
+    ACC_SS,         // s_k . s_k                                    (gradient)
     NACC = 20
 };
 

@@ -121,7 +121,7 @@ __device__ __forceinline__ float dot4(float4 a, float4 b)
 }
 
 struct GradRed {
-    float gmax = 0.f, g2 = 0.f, x2 = 0.f, sy = 0.f, yy = 0.f;
+    float gmax = 0.f, g2 = 0.f, x2 = 0.f, sy = 0.f, yy = 0.f, ss = 0.f;
 };
 
 // Gradient of the 16 J entries of locus n for one slot: g = c + 2 lambda_J x
@@ -159,6 +159,7 @@ __device__ __forceinline__ void grad_locus(const SlotT &S, int b, int64_t n, con
             const float4 sv = load_hist4(Spool, hoff + 4 * k4, hist_bf16);
             red.sy += dot4(sv, yv);
             red.yy += dot4(yv, yv);
+            red.ss += dot4(sv, sv);
         }
     }
 }

@@ -306,9 +306,9 @@ k_bwd_gather(const uint8_t *__restrict__ XT, int64_t Nx, int N, int L,
         const int b = slot[g];
         GradRed red;
         if (n < L) grad_locus(sd[b], b, n, a[g], wa, gpool, Ypool, Spool, hist_bf16, m, Dp, l2, red);
-        double v[4] = {red.g2, red.x2, red.sy, red.yy};
-        const int idx[4] = {ACC_G2, ACC_X2J, ACC_SY, ACC_YY};
-        block_sum_atomic<4>(v, acc + (int64_t)b * NACC, idx);
+        double v[5] = {red.g2, red.x2, red.sy, red.yy, red.ss};
+        const int idx[5] = {ACC_G2, ACC_X2J, ACC_SY, ACC_YY, ACC_SS};
+        block_sum_atomic<5>(v, acc + (int64_t)b * NACC, idx);
         const float wm = warp_max(red.gmax);
         if ((threadIdx.x & 31) == 0 && wm > 0.f) atomic_max_nonneg(acc + (int64_t)b * NACC + ACC_GMAX, (double)wm);
     }
@@ -336,9 +336,9 @@ k_grad_finalize(int L, const SlotDev *__restrict__ sd, const int32_t *__restrict
         }
         grad_locus(S, b, n, c, wa, gpool, Ypool, Spool, hist_bf16, m, Dp, l2, red);
     }
-    double v[4] = {red.g2, red.x2, red.sy, red.yy};
-    const int idx[4] = {ACC_G2, ACC_X2J, ACC_SY, ACC_YY};
-    block_sum_atomic<4>(v, acc + (int64_t)b * NACC, idx);
+    double v[5] = {red.g2, red.x2, red.sy, red.yy, red.ss};
+    const int idx[5] = {ACC_G2, ACC_X2J, ACC_SY, ACC_YY, ACC_SS};
+    block_sum_atomic<5>(v, acc + (int64_t)b * NACC, idx);
     const float wm = warp_max(red.gmax);
     if ((threadIdx.x & 31) == 0 && wm > 0.f) atomic_max_nonneg(acc + (int64_t)b * NACC + ACC_GMAX, (double)wm);
 }

@@ -116,7 +116,7 @@ __global__ void k_hpart(const SlotDev *__restrict__ sd, const int32_t *__restric
     float *gn = gpool + (int64_t)(2 * b + 1 - S.gcur) * Dp + hoff;
     const float *go = gpool + (int64_t)(2 * b + S.gcur) * Dp + hoff;
     const bool push = (S.flags & SLOT_F_PUSH) && S.ring_new >= 0;
-    double g2 = 0, x2 = 0, sy = 0, yy = 0, gmax = 0;
+    double g2 = 0, x2 = 0, sy = 0, yy = 0, ss = 0, gmax = 0;
     float4 gv, yv;
     float *gp = &gv.x, *yp = &yv.x;
     for (int a = 0; a < 4; ++a) {
@@ -134,6 +134,7 @@ __global__ void k_hpart(const SlotDev *__restrict__ sd, const int32_t *__restric
         const float4 sv = load_hist4(Spool, off, hist_bf16);
         sy = (double)dot4(sv, yv);
         yy = (double)dot4(yv, yv);
+        ss = (double)dot4(sv, sv);
     }
     double *A = acc + (int64_t)b * NACC;
     atomicAdd(A + ACC_G2, g2);
@@ -141,6 +142,7 @@ __global__ void k_hpart(const SlotDev *__restrict__ sd, const int32_t *__restric
     if (push) {
         atomicAdd(A + ACC_SY, sy);
         atomicAdd(A + ACC_YY, yy);
+        atomicAdd(A + ACC_SS, ss);
     }
     if (gmax > 0) atomic_max_nonneg(A + ACC_GMAX, gmax);
 }
