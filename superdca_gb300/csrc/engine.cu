@@ -20,6 +20,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -77,6 +78,10 @@ struct SlotHost {
     bool force_restart = false;
     bool stalled = false;    // steepest descent itself was not downhill: stop
     int last_refresh = 0;    // iteration of the last logit refresh
+    int since_refresh = 0;   // accepted steps since the logits were last recomputed
+    double xmax = 0.0;       // bound on max|x| (sets the fp16 scale of a refresh)
+    double dmax = 0.0;       // max|d| of the current direction
+    double f_fresh = 0.0;    // pseudo-likelihood part of f at recomputed logits
     MoreThuente ls;
 };
 
@@ -130,6 +135,7 @@ struct sdca_handle {
     // iterations while it stays there
     double refresh_factor = 8.0;
     int refresh_every = 30;
+    int tc_refresh_every = 10;  // tensor-core form: recompute logits every this many accepted steps
 
     std::vector<SlotHost> slots;
 
@@ -397,15 +403,25 @@ double pow2_scale(double vmax)
 double acc_get(sdca_handle *h, int b, int k) { return h->acc_h[(int64_t)b * NACC + k]; }
 
 // forward contraction u = X . v_J (+ v_h): into `u` (float) or `lbase` (double).
-// The tensor-core form serves the per-iteration direction; logits at a
-// stored point (start, final refresh) always use the FP32 gather.
-int run_forward(sdca_handle *h, const std::vector<int32_t> &lst, const float *vecs, bool to_lbase)
+// The tensor-core form serves the per-iteration direction (and, with
+// tc_lbase, the periodic recomputation of a slot's logits at its accepted
+// point); logits that a locus starts from or reports use the gather with
+// FP64 accumulation.
+int run_forward(sdca_handle *h, const std::vector<int32_t> &lst, const float *vecs, bool to_lbase,
+                bool tc_lbase = false)
 {
     if (lst.empty()) return SDCA_OK;
-    const bool use_tc = h->form == SDCA_FORM_TC && !to_lbase;
+    const bool use_tc = h->form == SDCA_FORM_TC && (!to_lbase || tc_lbase);
     int rc = use_tc ? upload_slots(h, lst) : upload_list(h, lst);
     if (rc) return rc;
-    if (use_tc) {
+    if (use_tc && to_lbase) {
+        const int splits = tc_fwd_splits(h->P, (int)lst.size());
+        Timed t(h, SDCA_K_FORWARD, 3, (int64_t)lst.size());
+        CK(tc_launch_fwd(h->tc, h->P, h->sd, h->list, (int)lst.size(), vecs, h->Dhi, h->Dlo, h->partial,
+                         splits, h->tc_err, h->stream));
+        launch_reduce_partial(h->P, h->list, (int)lst.size(), h->partial, vecs, 1, nullptr, h->lbase,
+                              h->stream, splits);
+    } else if (use_tc) {
         const int splits = tc_fwd_splits(h->P, (int)lst.size());
         Timed t(h, SDCA_K_FORWARD, 3, (int64_t)lst.size());
         CK(tc_launch_fwd(h->tc, h->P, h->sd, h->list, (int)lst.size(), vecs, h->Dhi, h->Dlo, h->partial,
@@ -437,8 +453,10 @@ int slot_begin(sdca_handle *h, int b, int64_t k, int32_t locus, const float *x0_
     S.gcur = 0;
     const Problem &P = h->P;
     float *wab = h->wa + (int64_t)b * P.Dp;
-    if (x0_engine)
+    if (x0_engine) {
         CK(cudaMemcpyAsync(wab, x0_engine, sizeof(float) * P.Dp, cudaMemcpyHostToDevice, h->stream));
+        for (int64_t e = 0; e < P.Dp; ++e) S.xmax = std::max(S.xmax, (double)std::fabs(x0_engine[e]));
+    }
     else
         CK(cudaMemsetAsync(wab, 0, sizeof(float) * P.Dp, h->stream));
     CK(cudaMemsetAsync(h->d + (int64_t)b * P.Dp, 0, sizeof(float) * P.Dp, h->stream));
@@ -652,19 +670,74 @@ int phase_step(sdca_handle *h)
     if (all.empty()) return SDCA_OK;
     int rc = upload_slots(h, all);
     if (rc) return rc;
+    // The running logits lbase += stp u carry the rounding of every forward
+    // contraction, and the sequences share that rounding; every
+    // refresh_every accepted steps a slot's logits are recomputed at its
+    // accepted point instead (tensor-core form: one extra forward).
+    std::vector<int32_t> fresh, drift;
+    for (int b : steps) {
+        SlotHost &S = h->slots[b];
+        S.xmax += S.stp * S.dmax;
+        if (h->form == SDCA_FORM_TC && ++S.since_refresh >= h->tc_refresh_every) {
+            S.since_refresh = 0;
+            fresh.push_back(b);
+        } else {
+            drift.push_back(b);
+        }
+    }
     if (!steps.empty()) {
         rc = upload_slots(h, steps);
         if (rc) return rc;
         {
-            Timed t(h, SDCA_K_ACCEPT, 2, (int64_t)steps.size());
+            Timed t(h, SDCA_K_ACCEPT, 1, (int64_t)steps.size());
             launch_accept(P, h->sd, h->list, (int)steps.size(), h->wa, h->d, h->Spool, h->hist_bf16,
                           h->stream);
-            launch_lbase_update(P, h->sd, h->list, (int)steps.size(), h->lbase, h->u, h->stream);
         }
         CKL();
+        if (!drift.empty()) {
+            rc = upload_list(h, drift);
+            if (rc) return rc;
+            Timed t(h, SDCA_K_ACCEPT, 1, (int64_t)drift.size());
+            launch_lbase_update(P, h->sd, h->list, (int)drift.size(), h->lbase, h->u, h->stream);
+        }
+        CKL();
+        if (!fresh.empty()) {
+            for (int b : fresh) {
+                h->sd_h[b].tc_scale = pow2_scale(h->slots[b].xmax);
+                h->sd_h[b].tc_inv_scale = 1.0 / h->sd_h[b].tc_scale;
+            }
+            rc = run_forward(h, fresh, h->wa, true, true);
+            if (rc) return rc;
+            // node beliefs and objective at the recomputed logits
+            for (int b : fresh) {
+                h->slots[b].stp = 0.0;
+                h->slots[b].use_u = false;
+            }
+            rc = upload_slots(h, fresh);
+            if (rc) return rc;
+            rc = zero_acc(h);
+            if (rc) return rc;
+            {
+                Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)fresh.size());
+                launch_trial(P, h->sd, h->list, (int)fresh.size(), h->lbase, h->u, h->rstate, h->w, h->R,
+                             h->acc, h->stream);
+            }
+            CKL();
+            rc = fetch_acc(h);
+            if (rc) return rc;
+            for (int b : fresh) {
+                SlotHost &S = h->slots[b];
+                S.f_fresh = acc_get(h, b, ACC_F);
+                for (int a = 0; a < Q; ++a) S.rs[a] = acc_get(h, b, ACC_RS0 + a);
+            }
+            rc = upload_slots(h, all);
+            if (rc) return rc;
+        }
         rc = upload_list(h, all);
         if (rc) return rc;
     }
+    std::vector<char> was_fresh(P.Bmax, 0);
+    for (int b : fresh) was_fresh[b] = 1;
     rc = zero_acc(h);
     if (rc) return rc;
     if (h->form == SDCA_FORM_TC) {
@@ -724,6 +797,7 @@ int phase_step(sdca_handle *h)
                 S.ring_new = -1;  // pair not usable: keep the history as it is
                 S.skipped++;
             }
+            if (was_fresh[b]) S.f = S.f_fresh + P.lambda_J * S.x2J + P.lambda_h * S.x2H;
             if (S.iterations > h->cfg.max_iterations) {
                 S.status = 1;
                 stop = true;
@@ -759,7 +833,7 @@ int phase_step(sdca_handle *h)
         for (int b : cont) {
             SlotHost &S = h->slots[b];
             const bool near = S.gmax < h->refresh_factor * h->cfg.gradient_threshold;
-            if (S.phase == PH_READY_STEP && near &&
+            if (h->form != SDCA_FORM_TC && S.phase == PH_READY_STEP && near &&
                 S.iterations - S.last_refresh >= h->refresh_every) {
                 refresh.push_back(b);
                 S.last_refresh = S.iterations;
@@ -884,7 +958,8 @@ int phase_step(sdca_handle *h)
         S.ddH = acc_get(h, b, ACC_DDH);
         S.xdJ = acc_get(h, b, ACC_XDJ);
         S.xdH = acc_get(h, b, ACC_XDH);
-        h->sd_h[b].tc_scale = pow2_scale(acc_get(h, b, ACC_DMAX));
+        S.dmax = acc_get(h, b, ACC_DMAX);
+        h->sd_h[b].tc_scale = pow2_scale(S.dmax);
         h->sd_h[b].tc_inv_scale = 1.0 / h->sd_h[b].tc_scale;
         const double releps = 1e-4 * std::max(1.0, std::sqrt(S.x2J + S.x2H));
         if (!S.hist.empty() && (S.force_restart || !(S.gd <= -1e-4 * releps))) restart.push_back(b);
@@ -909,7 +984,8 @@ int phase_step(sdca_handle *h)
             S.ddH = acc_get(h, b, ACC_DDH);
             S.xdJ = acc_get(h, b, ACC_XDJ);
             S.xdH = acc_get(h, b, ACC_XDH);
-            h->sd_h[b].tc_scale = pow2_scale(acc_get(h, b, ACC_DMAX));
+            S.dmax = acc_get(h, b, ACC_DMAX);
+            h->sd_h[b].tc_scale = pow2_scale(S.dmax);
             h->sd_h[b].tc_inv_scale = 1.0 / h->sd_h[b].tc_scale;
         }
     }
@@ -1033,6 +1109,9 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
         P.C = std::max<int64_t>(P.Cg, cfg->form == SDCA_FORM_TC ? 24 : 1);
     }
     h->form = cfg->form;
+    if (const char *e = std::getenv("SDCA_REFRESH_EVERY")) h->refresh_every = std::max(1, std::atoi(e));
+    if (const char *e = std::getenv("SDCA_REFRESH_FACTOR")) h->refresh_factor = std::atof(e);
+    if (const char *e = std::getenv("SDCA_TC_REFRESH_EVERY")) h->tc_refresh_every = std::max(1, std::atoi(e));
     h->slots.resize(P.Bmax);
     int rc = SDCA_OK;
     const size_t B = P.Bmax;
