@@ -135,7 +135,7 @@ struct sdca_handle {
     // iterations while it stays there
     double refresh_factor = 8.0;
     int refresh_every = 30;
-    int tc_refresh_every = 10;  // tensor-core form: recompute logits every this many accepted steps
+    int tc_refresh_every = 5;   // tensor-core form: recompute logits every this many accepted steps
 
     std::vector<SlotHost> slots;
 
