@@ -18,7 +18,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsuperdca_gb300.so")
 
-SOURCES = ["engine.cu", "kernels_gather.cu", "kernels_solver.cu", "kernels_tc.cu", "noalloc.cu"]
+SOURCES = ["engine.cu", "kernels_gather.cu", "kernels_solver.cu", "kernels_tc.cu", "kernels_weights.cu",
+           "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr",
          "-I" + os.path.join(ROOT, "include")]

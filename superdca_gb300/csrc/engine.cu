@@ -1327,9 +1327,62 @@ int sdca_eval(sdca_handle *h, uint32_t r, const double *x, double *f, double *g)
 int sdca_compute_weights(sdca_handle *h, const uint8_t *states, const double *mult,
                          double threshold, double *weights_out)
 {
-    (void)states; (void)mult; (void)threshold; (void)weights_out;
     if (!h) return SDCA_E_ARG;
-    return fail(h, SDCA_E_UNSUPPORTED, "sequence reweighting on the GPU is not in this build");
+    if (!states || !weights_out) return fail(h, SDCA_E_ARG, "states and weights_out are required");
+    const Problem &P = h->P;
+    if (mult)
+        for (int64_t i = 0; i < P.N; ++i)
+            if (!(mult[i] >= 0.0) || !std::isfinite(mult[i]))
+                return fail(h, SDCA_E_ARG, "multiplicities must be finite and non-negative");
+    CK(cudaSetDevice(h->cfg.device));
+    // the states go through the alignment buffer: a following
+    // sdca_set_alignment overwrites it anyway
+    h->has_alignment = false;
+    const int64_t W = (P.L + 31) / 32;
+    uint64_t *packed = nullptr;
+    double *d = nullptr;
+    unsigned long long *nonid = nullptr;
+    auto release = [&]() {
+        if (packed) cudaFree(packed);
+        if (d) cudaFree(d);
+    };
+    if (cudaMalloc(&packed, sizeof(uint64_t) * P.N * W) != cudaSuccess ||
+        cudaMalloc(&d, sizeof(double) * (2 * P.N + 1)) != cudaSuccess) {
+        cudaGetLastError();
+        release();
+        return fail(h, SDCA_E_NOMEM, "device allocation for reweighting failed");
+    }
+    double *nbr = d, *dmult = d + P.N;
+    nonid = reinterpret_cast<unsigned long long *>(d + 2 * P.N);
+    int rc = SDCA_OK;
+    do {
+        if (cudaMemcpy2DAsync(h->X, P.Lx, states, P.L, P.L, P.N, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+            cudaMemsetAsync(d, 0, sizeof(double) * (2 * P.N + 1), h->stream) != cudaSuccess ||
+            (mult && cudaMemcpyAsync(dmult, mult, sizeof(double) * P.N, cudaMemcpyHostToDevice, h->stream) !=
+                         cudaSuccess)) {
+            rc = fail(h, SDCA_E_CUDA, "reweighting upload failed");
+            break;
+        }
+        launch_weights(h->X, P.Lx, (int)P.N, (int)P.L, packed, threshold, mult ? dmult : nullptr, nbr, nonid,
+                       h->stream);
+        if (cudaGetLastError() != cudaSuccess) {
+            rc = fail(h, SDCA_E_CUDA, "reweighting kernel launch failed");
+            break;
+        }
+        std::vector<double> hn(P.N);
+        if (cudaMemcpyAsync(hn.data(), nbr, sizeof(double) * P.N, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+            cudaStreamSynchronize(h->stream) != cudaSuccess) {
+            rc = fail(h, SDCA_E_CUDA, "reweighting failed");
+            break;
+        }
+        // w_i = mult_i / (mult_i + sum of neighbour multiplicities)
+        for (int64_t i = 0; i < P.N; ++i) {
+            const double mi = mult ? mult[i] : 1.0;
+            weights_out[i] = mi / (mi + hn[i]);
+        }
+    } while (0);
+    release();
+    return rc;
 }
 
 int sdca_get_profile(const sdca_handle *h, sdca_profile *out)

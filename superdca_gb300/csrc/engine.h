@@ -126,6 +126,10 @@ void launch_direction(const Problem &P, const SlotDev *sd, const int32_t *list, 
 void launch_score(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
                   const float *wa, int gap, float *rows, cudaStream_t st);
 
+// sequence reweighting (kernels_weights.cu)
+void launch_weights(const uint8_t *X, int64_t ld, int N, int L, uint64_t *packed, double threshold,
+                    const double *mult, double *nbr, unsigned long long *nonidentical, cudaStream_t st);
+
 // tensor-core form (kernels_tc.cu)
 struct TcPlan;
 TcPlan *tc_plan_create(const Problem &P, const uint8_t *X, const uint8_t *XT, __half *Dhi, __half *Dlo,

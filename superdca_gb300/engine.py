@@ -95,6 +95,17 @@ class Engine:
         assert self._states.shape == (self.N, self.L) and self._weights.shape == (self.N,)
         self._check(self.lib.sdca_set_alignment(self.h, _ptr(self._states), _ptr(self._weights)))
 
+    def compute_weights(self, states: np.ndarray, threshold: float = 0.9, mult=None) -> np.ndarray:
+        """SuperDCA's sequence weights computed on the GPU (calculate_weights,
+        SuperDCA/include/plmDCA_optimizer_parameters.hpp:39-98).  Leaves the
+        handle without an alignment: call set_alignment afterwards."""
+        st = np.ascontiguousarray(states, dtype=np.uint8)
+        assert st.shape == (self.N, self.L)
+        m = None if mult is None else np.ascontiguousarray(mult, dtype=np.float64)
+        w = np.zeros(self.N, dtype=np.float64)
+        self._check(self.lib.sdca_compute_weights(self.h, _ptr(st), _ptr(m), float(threshold), _ptr(w)))
+        return w
+
     def lambdas(self):
         lh, lJ, be = C.c_double(), C.c_double(), C.c_double()
         self._check(self.lib.sdca_get_lambdas(self.h, C.byref(lh), C.byref(lJ), C.byref(be)))

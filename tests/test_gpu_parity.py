@@ -190,3 +190,32 @@ def test_tree_workload_subset(engine_lib, oracle_mod):
     _, ost = P.solve(loci, threads=4, gtol=1e-3)
     np.testing.assert_allclose(res.f, [s["f"] for s in ost], rtol=1e-6)
     E.close()
+
+
+def test_gpu_weights_match_reference_rule(engine_lib, oracle_mod, golden_obj):
+    """Sequence reweighting on the GPU equals the oracle (itself bit-exact with
+    SuperDCA's calculate_weights on the golden fixtures) exactly."""
+    from superdca_gb300 import Engine
+
+    O = oracle_mod
+    # golden fixtures: weights produced by SuperDCA's own calculate_weights
+    for name, d in golden_obj.items():
+        st = d["states"]
+        E = Engine(*st.shape)
+        w = E.compute_weights(st, float(d["threshold"]))
+        np.testing.assert_array_equal(w, d["weights"], err_msg=name)
+        E.close()
+    rng = np.random.default_rng(41)
+    for N, L, thr in [(300, 777, 0.9), (129, 64, 0.8), (65, 33, 1.0), (1000, 5000, 0.95)]:
+        st = rng.integers(0, 4, size=(N, L)).astype(np.uint8)
+        base = st[0].copy()
+        for i in range(1, N, 3):  # clusters of near-identical sequences
+            st[i] = base
+            flip = rng.random(L) < 0.05
+            st[i, flip] = rng.integers(0, 4, size=flip.sum())
+        mult = rng.integers(1, 4, size=N).astype(np.float64)
+        E = Engine(N, L)
+        for m in (None, mult):
+            w = E.compute_weights(st, thr, mult=m)
+            np.testing.assert_array_equal(w, O.weights(st, thr, mult=m), err_msg=f"{N}x{L} thr {thr}")
+        E.close()
