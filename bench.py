@@ -313,6 +313,17 @@ def engine_arm(args):
                    h2d_bytes_per_step=int(N * L + 8 * N), d2h_bytes_per_step=int(per_step * L * 4 + per_step * 32),
                    upload_s_per_step=round(t_up / args.steps, 4), solve_s_per_step=round(t_sol / args.steps, 4))
 
+    # sequence reweighting on the GPU at this size (outside the solve metric)
+    rw = None
+    if rank == 0:
+        torch.cuda.synchronize(local)
+        t_rw = time.time()
+        w_gpu = E.compute_weights(st, 0.9)
+        t_rw = time.time() - t_rw
+        E.set_alignment(st, w)
+        rw = {"seconds": round(t_rw, 4), "pairs": int(N * (N - 1) // 2),
+              "pair_loci_per_s": float(N * (N - 1) / 2 * L / t_rw), "b_eff": round(float(w_gpu.sum()), 3)}
+
     Dp = ((16 * L + 4 + 63) // 64) * 64
     rf, dom = roofline(tot, N, L, Dp, 10, 2 if args.history_bf16 else 4)
     if rf is not None:
@@ -330,7 +341,7 @@ def engine_arm(args):
                    "weights": "unit (--no-reweighting)", "gradient_threshold": 1e-3,
                    "l2": "inputs larger than L2 (282 MB alignment, per-slot solver state)",
                    "parallelism": f"loci sharded over {world} rank(s)"},
-        "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": rf,
+        "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": rf, "reweighting": rw,
         "kernel_ms": {k: round(v, 2) for k, v in tot["kernel_ms"].items()},
         "solver": {"median_nfeval": float(np.median(nfe)), "median_iterations": float(np.median(iters)),
                    "p90_iterations": float(np.percentile(iters, 90)), "max_iterations": int(np.max(iters)),
