@@ -17,6 +17,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsuperdca_gb300.so")
+CLI = os.path.join(HERE, "superdca-gb300")
+CLI_SOURCES = [os.path.join(HERE, "cli", "superdca_gb300_cli.cpp")]
 
 SOURCES = ["engine.cu", "kernels_gather.cu", "kernels_solver.cu", "kernels_tc.cu", "kernels_weights.cu",
            "noalloc.cu"]
@@ -52,9 +54,23 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
     if out.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{out.stdout}{out.stderr}")
     os.replace(tmp, LIB)
+    build_cli()
     if verbose:
-        print("built", LIB)
+        print("built", LIB, "and", CLI)
     return LIB
+
+
+def build_cli() -> str:
+    """The command-line front end: host C++ linked against the engine library."""
+    cxx = shutil.which("g++") or "g++"
+    tmp = CLI + ".tmp"
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"), *CLI_SOURCES,
+           "-L" + HERE, "-lsuperdca_gb300", "-Wl,-rpath,$ORIGIN", "-pthread", "-o", tmp]
+    out = subprocess.run(cmd, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError(f"CLI build failed:\n{' '.join(cmd)}\n{out.stdout}{out.stderr}")
+    os.replace(tmp, CLI)
+    return CLI
 
 
 if __name__ == "__main__":

@@ -1,0 +1,611 @@
+// superdca-gb300: SuperDCA's command line on the GB300 engine.
+//
+// The flow follows SuperDCA's main (SuperDCA/src/SuperDCA.cpp:232-408) and
+// run_plmDCA (SuperDCA/include/plmDCA.hpp:436-697):
+//   read the FASTA alignment -> (filter list | MAF/gap filter) -> sample list
+//   -> 4-state (triallelic) envelope -> loci list -> weights (GPU, or 1.0
+//   with --no-reweighting) -> per-locus solves (GPU) -> symmetrised coupling
+//   lines "%.8f r n" in <id>.SuperDCA_couplings.1-based.all.
+// Option spellings and defaults are those of SuperDCA/src/SuperDCA_options.cpp:
+// 155-190 and SuperDCA/src/plmDCA_options.cpp:131-150; the alignment options
+// that apegrunt defines (absent from the reference tree) use the spellings of
+// the reference README.  GPU options are prefixed --gpu-.
+//
+// The alignment rules (symbols, allele ranking, MAF and gap frequency, the
+// three-allele envelope) are the ones of superdca_gb300/alignment.py, which
+// the tests hold this program to.
+#include <algorithm>
+#include <cctype>
+#include <charconv>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <sys/stat.h>
+#include <thread>
+#include <vector>
+
+#include "superdca_gb300.h"
+
+namespace {
+
+const char *USAGE =
+    "superdca-gb300 [options] alignmentfile\n"
+    "\n"
+    "General:\n"
+    "  -h [ --help ]                      Print this help message.\n"
+    "  -v [ --verbose ]                   Be verbose.\n"
+    "  --alignmentfile arg                The input alignment filename (FASTA).\n"
+    "  --filterlistfile arg               The loci filter list input filename.\n"
+    "  --output-filtered-alignment        Write filtered alignment to file.\n"
+    "  --output-filterlist-alignment      Output alignment after filterlist selection.\n"
+    "  --samplelistfile arg               The sample filter list input filename.\n"
+    "  --output-samplelist-alignment      Output alignment after samplelist selection.\n"
+    "  --locilistfile arg                 Analysable loci list filename.\n"
+    "  -t [ --threads ] arg (=-1)         Host threads for output formatting (-1 = all).\n"
+    "Alignment:\n"
+    "  --maf-threshold arg (=0.01)        Minimum minor allele frequency of a kept locus.\n"
+    "  --gap-threshold arg (=0.15)        Maximum gap frequency of a kept locus.\n"
+    "  --no-filter-alignment              Keep every locus that fits the 4-state envelope.\n"
+    "  --begin-locus arg (=0)             First analysed locus when no loci list is given.\n"
+    "  --end-locus arg (=-1)              Last analysed locus (-1 = the last one).\n"
+    "  --input-indexing-base arg (=1)     Index base of list files.\n"
+    "  --output-indexing-base arg (=1)    Index base of written loci indices.\n"
+    "  --no-reweighting                   Do not reweight samples.\n"
+    "  --reweighting-threshold arg (=0.9) Fraction of identical positions required for two\n"
+    "                                     sequences to be considered identical.\n"
+    "  --output-weights                   Write sample weights to file.\n"
+    "plmDCA:\n"
+    "  --gradient-threshold arg (=0.001)  L-BFGS gradient threshold stopping criterion.\n"
+    "  --lambda-h arg (=-1)               h regularization factor (< 0: automatic).\n"
+    "  --lambda-J arg (=-1)               J regularization factor (< 0: automatic).\n"
+    "  --no-dca                           Don't run DCA.\n"
+    "  --no-coupling-output               Don't write coupling scores to file.\n"
+    "GPU:\n"
+    "  --gpu-device arg (=0)              CUDA device.\n"
+    "  --gpu-form arg (=tc)               Contraction form: tc (tensor cores) or plain.\n"
+    "  --gpu-batch arg (=64)              Loci solved together.\n"
+    "  --gpu-history arg (=fp32)          L-BFGS history storage: fp32 or bf16.\n"
+    "  --gpu-chunk arg (=4096)            Loci per solve call (bounds host memory).\n";
+
+struct Options {
+    std::vector<std::string> alignment_files;
+    std::string filterlist, samplelist, locilist;
+    bool verbose = false, out_filtered = false, out_filterlist = false, out_samplelist = false;
+    int threads = -1;
+    double maf = 0.01, gap = 0.15;
+    bool no_filter = false;
+    long begin_locus = 0, end_locus = -1;
+    int in_base = 1, out_base = 1;
+    bool no_reweighting = false, output_weights = false;
+    double reweighting_threshold = 0.9;
+    bool norm_of_mean = false;
+    double gradient_threshold = 1e-3, lambda_h = -1.0, lambda_J = -1.0;
+    bool no_dca = false, no_coupling_output = false;
+    int device = 0, batch = 64, form = SDCA_FORM_TC;
+    bool history_bf16 = false;
+    long chunk = 4096;
+};
+
+[[noreturn]] void fail(const std::string &msg)
+{
+    std::cerr << "superdca-gb300 error: " << msg << "\n";
+    std::exit(EXIT_FAILURE);
+}
+
+template <typename T> T parse_number(const std::string &opt, const std::string &v)
+{
+    T out{};
+    const char *b = v.data(), *e = v.data() + v.size();
+    std::from_chars_result r;
+    if constexpr (std::is_floating_point_v<T>) {
+        char *end = nullptr;
+        out = (T)std::strtod(v.c_str(), &end);
+        if (v.empty() || end != v.c_str() + v.size()) fail("invalid value '" + v + "' for " + opt);
+        return out;
+    } else {
+        r = std::from_chars(b, e, out);
+        if (r.ec != std::errc() || r.ptr != e) fail("invalid value '" + v + "' for " + opt);
+        return out;
+    }
+}
+
+// Boost.Program_options style: --name value, --name=value, -x value, positionals.
+Options parse_options(int argc, char **argv)
+{
+    Options o;
+    struct Flag { const char *name; bool *dst; };
+    const Flag flags[] = {
+        {"verbose", &o.verbose}, {"output-filtered-alignment", &o.out_filtered},
+        {"output-filterlist-alignment", &o.out_filterlist},
+        {"output-samplelist-alignment", &o.out_samplelist}, {"no-filter-alignment", &o.no_filter},
+        {"no-reweighting", &o.no_reweighting}, {"output-weights", &o.output_weights},
+        {"norm-of-mean-scoring", &o.norm_of_mean}, {"no-dca", &o.no_dca},
+        {"no-coupling-output", &o.no_coupling_output},
+    };
+    for (int i = 1; i < argc; ++i) {
+        std::string a = argv[i];
+        if (a == "-h" || a == "--help") {
+            std::cout << USAGE;
+            std::exit(EXIT_SUCCESS);
+        }
+        if (a == "-v") a = "--verbose";
+        if (a == "-t") a = "--threads";
+        if (a.size() < 2 || a[0] != '-' || a == "-") {
+            o.alignment_files.push_back(a);
+            continue;
+        }
+        if (a.rfind("--", 0) != 0) fail("unrecognised option '" + a + "'");
+        std::string name = a.substr(2), value;
+        bool has_value = false;
+        const size_t eq = name.find('=');
+        if (eq != std::string::npos) {
+            value = name.substr(eq + 1);
+            name = name.substr(0, eq);
+            has_value = true;
+        }
+        bool matched = false;
+        for (const Flag &f : flags)
+            if (name == f.name) {
+                if (has_value) fail("option '--" + name + "' takes no value");
+                *f.dst = true;
+                matched = true;
+            }
+        if (matched) continue;
+        if (!has_value) {
+            if (i + 1 >= argc) fail("option '--" + name + "' requires an argument");
+            value = argv[++i];
+        }
+        const std::string opt = "--" + name;
+        if (name == "alignmentfile") o.alignment_files.push_back(value);
+        else if (name == "filterlistfile") o.filterlist = value;
+        else if (name == "samplelistfile") o.samplelist = value;
+        else if (name == "locilistfile") o.locilist = value;
+        else if (name == "threads") o.threads = parse_number<int>(opt, value);
+        else if (name == "maf-threshold") o.maf = parse_number<double>(opt, value);
+        else if (name == "gap-threshold") o.gap = parse_number<double>(opt, value);
+        else if (name == "begin-locus") o.begin_locus = parse_number<long>(opt, value);
+        else if (name == "end-locus") o.end_locus = parse_number<long>(opt, value);
+        else if (name == "input-indexing-base") o.in_base = parse_number<int>(opt, value);
+        else if (name == "output-indexing-base") o.out_base = parse_number<int>(opt, value);
+        else if (name == "reweighting-threshold") o.reweighting_threshold = parse_number<double>(opt, value);
+        else if (name == "gradient-threshold") o.gradient_threshold = parse_number<double>(opt, value);
+        else if (name == "lambda-h") o.lambda_h = parse_number<double>(opt, value);
+        else if (name == "lambda-J") o.lambda_J = parse_number<double>(opt, value);
+        else if (name == "gpu-device") o.device = parse_number<int>(opt, value);
+        else if (name == "gpu-batch") o.batch = parse_number<int>(opt, value);
+        else if (name == "gpu-chunk") o.chunk = parse_number<long>(opt, value);
+        else if (name == "gpu-form") {
+            if (value == "tc") o.form = SDCA_FORM_TC;
+            else if (value == "plain") o.form = SDCA_FORM_GATHER;
+            else fail("--gpu-form must be tc or plain");
+        } else if (name == "gpu-history") {
+            if (value == "fp32") o.history_bf16 = false;
+            else if (value == "bf16") o.history_bf16 = true;
+            else fail("--gpu-history must be fp32 or bf16");
+        } else fail("unrecognised option '" + opt + "'");
+    }
+    if (o.alignment_files.empty()) fail("no input alignment (see --help)");
+    if (o.alignment_files.size() > 2) fail("at most two alignment files");
+    if (o.gradient_threshold <= 0) fail("--gradient-threshold must be positive");
+    if (o.chunk < 1) fail("--gpu-chunk must be positive");
+    return o;
+}
+
+// ---------------------------------------------------------------- alignment
+
+struct Alignment {
+    std::string id;                 // output file stem
+    std::vector<std::string> names; // sequence headers
+    int64_t N = 0, L = 0;
+    std::vector<uint8_t> nuc;       // N x L codes A0 C1 G2 T3 gap4
+    std::vector<int64_t> translation;  // column -> original column index
+};
+
+std::string stem(const std::string &path)
+{
+    std::string base = path.substr(path.find_last_of('/') == std::string::npos ? 0 : path.find_last_of('/') + 1);
+    const size_t dot = base.find_last_of('.');
+    return (dot == std::string::npos || dot == 0) ? base : base.substr(0, dot);
+}
+
+uint8_t nucleotide_code(unsigned char c)
+{
+    switch (c) {
+    case 'A': case 'a': return 0;
+    case 'C': case 'c': return 1;
+    case 'G': case 'g': return 2;
+    case 'T': case 't': return 3;
+    default: return 4;   // '-', 'N' and every other symbol count as gap
+    }
+}
+
+Alignment read_fasta(const std::string &path)
+{
+    std::ifstream in(path, std::ios::binary);
+    if (!in) fail("cannot open alignment file \"" + path + "\"");
+    Alignment a;
+    a.id = stem(path);
+    std::vector<std::string> seqs;
+    std::string line;
+    while (std::getline(in, line)) {
+        if (!line.empty() && line.back() == '\r') line.pop_back();
+        if (line.empty()) continue;
+        if (line[0] == '>') {
+            a.names.push_back(line.substr(1));
+            seqs.emplace_back();
+        } else if (line[0] == ';') {
+            continue;
+        } else {
+            if (seqs.empty()) fail("\"" + path + "\" is not FASTA: sequence data before the first header");
+            for (char c : line)
+                if (!std::isspace((unsigned char)c)) seqs.back().push_back(c);
+        }
+    }
+    if (seqs.empty()) fail("no sequences in \"" + path + "\"");
+    a.N = (int64_t)seqs.size();
+    a.L = (int64_t)seqs[0].size();
+    for (size_t i = 0; i < seqs.size(); ++i)
+        if ((int64_t)seqs[i].size() != a.L)
+            fail("sequence " + std::to_string(i + 1) + " of \"" + path + "\" has length " +
+                 std::to_string(seqs[i].size()) + ", expected " + std::to_string(a.L));
+    a.nuc.resize((size_t)(a.N * a.L));
+    for (int64_t i = 0; i < a.N; ++i)
+        for (int64_t n = 0; n < a.L; ++n) a.nuc[i * a.L + n] = nucleotide_code((unsigned char)seqs[i][n]);
+    a.translation.resize(a.L);
+    for (int64_t n = 0; n < a.L; ++n) a.translation[n] = n;
+    return a;
+}
+
+Alignment select_columns(const Alignment &a, const std::vector<int64_t> &cols)
+{
+    Alignment b;
+    b.id = a.id;
+    b.names = a.names;
+    b.N = a.N;
+    b.L = (int64_t)cols.size();
+    b.nuc.resize((size_t)(b.N * b.L));
+    for (int64_t i = 0; i < a.N; ++i)
+        for (int64_t k = 0; k < b.L; ++k) b.nuc[i * b.L + k] = a.nuc[i * a.L + cols[k]];
+    b.translation.resize(b.L);
+    for (int64_t k = 0; k < b.L; ++k) b.translation[k] = a.translation[cols[k]];
+    return b;
+}
+
+Alignment select_rows(const Alignment &a, const std::vector<int64_t> &rows, const std::string &id)
+{
+    Alignment b;
+    b.id = id;
+    b.N = (int64_t)rows.size();
+    b.L = a.L;
+    b.translation = a.translation;
+    b.nuc.resize((size_t)(b.N * b.L));
+    for (int64_t k = 0; k < b.N; ++k) {
+        b.names.push_back(a.names[rows[k]]);
+        std::memcpy(&b.nuc[k * b.L], &a.nuc[rows[k] * a.L], (size_t)a.L);
+    }
+    return b;
+}
+
+// Per-column allele counts and the rank of each nucleotide (by count, ties
+// A<C<G<T); gaps are not alleles.
+struct ColumnStats {
+    int64_t count[5];
+    int rank[4];
+    int alleles;
+};
+
+std::vector<ColumnStats> column_stats(const Alignment &a)
+{
+    std::vector<ColumnStats> cs((size_t)a.L);
+    for (auto &c : cs) std::memset(&c, 0, sizeof c);
+    for (int64_t i = 0; i < a.N; ++i) {
+        const uint8_t *row = &a.nuc[i * a.L];
+        for (int64_t n = 0; n < a.L; ++n) ++cs[n].count[row[n]];
+    }
+    for (auto &c : cs) {
+        int order[4] = {0, 1, 2, 3};
+        std::stable_sort(order, order + 4, [&](int x, int y) { return c.count[x] > c.count[y]; });
+        for (int k = 0; k < 4; ++k) c.rank[order[k]] = k;
+        c.alleles = 0;
+        for (int k = 0; k < 4; ++k) c.alleles += c.count[k] > 0;
+    }
+    return cs;
+}
+
+// MAF / gap filter: more than one allele, MAF >= maf, gap frequency <= gap.
+std::vector<int64_t> filter_columns(const Alignment &a, double maf, double gap)
+{
+    const auto cs = column_stats(a);
+    std::vector<int64_t> keep;
+    for (int64_t n = 0; n < a.L; ++n) {
+        const ColumnStats &c = cs[n];
+        int64_t sorted[4] = {c.count[0], c.count[1], c.count[2], c.count[3]};
+        std::sort(sorted, sorted + 4, [](int64_t x, int64_t y) { return x > y; });
+        const int64_t nongap = a.N - c.count[4];
+        const double f_minor = nongap > 0 ? (double)sorted[1] / (double)nongap : 0.0;
+        const double f_gap = (double)c.count[4] / (double)a.N;
+        if (c.alleles > 1 && f_minor >= maf && f_gap <= gap) keep.push_back(n);
+    }
+    return keep;
+}
+
+// The 4-state envelope: a locus with four alleles is dropped; the others are
+// coded by allele rank (0, 1, 2) with gap = 3.
+std::vector<uint8_t> four_state(const Alignment &a, std::vector<int64_t> &kept)
+{
+    const auto cs = column_stats(a);
+    kept.clear();
+    for (int64_t n = 0; n < a.L; ++n)
+        if (cs[n].alleles <= 3) kept.push_back(n);
+    const int64_t Lk = (int64_t)kept.size();
+    std::vector<uint8_t> lut((size_t)Lk * 5);
+    for (int64_t k = 0; k < Lk; ++k) {
+        for (int v = 0; v < 4; ++v) lut[k * 5 + v] = (uint8_t)std::min(cs[kept[k]].rank[v], 3);
+        lut[k * 5 + 4] = 3;
+    }
+    std::vector<uint8_t> st((size_t)(a.N * Lk));
+    for (int64_t i = 0; i < a.N; ++i)
+        for (int64_t k = 0; k < Lk; ++k) st[i * Lk + k] = lut[k * 5 + a.nuc[i * a.L + kept[k]]];
+    return st;
+}
+
+// List files: integers separated by whitespace or commas, '#' starts a comment.
+std::vector<int64_t> read_index_list(const std::string &path, int base)
+{
+    std::ifstream in(path);
+    if (!in) fail("cannot open list file \"" + path + "\"");
+    std::vector<int64_t> out;
+    std::string line;
+    while (std::getline(in, line)) {
+        const size_t hash = line.find('#');
+        if (hash != std::string::npos) line.resize(hash);
+        for (char &c : line)
+            if (c == ',') c = ' ';
+        std::istringstream ls(line);
+        std::string tok;
+        while (ls >> tok) {
+            const int64_t v = parse_number<int64_t>("list file \"" + path + "\"", tok) - base;
+            if (v < 0) fail("index " + tok + " in \"" + path + "\" is below the index base");
+            out.push_back(v);
+        }
+    }
+    return out;
+}
+
+// SuperDCA's get_unique_ofstream (SuperDCA/include/SuperDCA_commons.h:66-81):
+// name, name.1, name.2, ... whichever does not exist yet.
+std::string unique_name(const std::string &name)
+{
+    for (int index = 0;; ++index) {
+        const std::string p = index == 0 ? name : name + "." + std::to_string(index);
+        struct stat sb;
+        if (stat(p.c_str(), &sb) != 0) return p;
+    }
+}
+
+void write_fasta(const Alignment &a, const Options &o, const char *what)
+{
+    static const char sym[5] = {'A', 'C', 'G', 'T', '-'};
+    const std::string path = unique_name(a.id + ".fasta");
+    if (o.verbose) std::cout << "superdca-gb300: write " << what << " alignment to file " << path << "\n";
+    std::ofstream out(path, std::ios::binary);
+    std::string row((size_t)a.L, ' ');
+    for (int64_t i = 0; i < a.N; ++i) {
+        for (int64_t n = 0; n < a.L; ++n) row[n] = sym[a.nuc[i * a.L + n]];
+        out << '>' << a.names[i] << '\n' << row << '\n';
+    }
+    if (!out) fail("failed to write \"" + path + "\"");
+}
+
+void write_loci(const Alignment &a, const Options &o)
+{
+    const std::string path = unique_name(a.id + ".loci");
+    if (o.verbose) std::cout << "superdca-gb300: write original loci indices to file " << path << "\n";
+    std::ofstream out(path, std::ios::binary);
+    for (int64_t n = 0; n < a.L; ++n) out << a.translation[n] + o.out_base << '\n';
+    if (!out) fail("failed to write \"" + path + "\"");
+}
+
+// ---------------------------------------------------------------- engine
+
+struct Handle {
+    sdca_handle *h = nullptr;
+    ~Handle() { if (h) sdca_destroy(h); }
+};
+
+void check(int rc, sdca_handle *h, const char *what)
+{
+    if (rc != SDCA_OK) fail(std::string(what) + ": " + sdca_last_error(h));
+}
+
+// Coupling lines of mean-of-norms scoring (plmDCA.hpp:667-693): for r over
+// the loci list and n over the entries before r,
+// (double)(float)(S[r][n] + S[n][r]) * 0.5 with std::fixed precision 8.
+void write_couplings(const std::string &path, const std::vector<float> &S, const std::vector<uint32_t> &loci,
+                     const std::vector<int64_t> &translation, int base, int threads)
+{
+    std::FILE *f = std::fopen(path.c_str(), "wb");
+    if (!f) fail("cannot open \"" + path + "\" for writing");
+    const size_t n = loci.size();
+    const int T = std::max(1, threads);
+    const size_t window = 64;  // rows formatted per thread per round
+    std::vector<std::string> buf((size_t)T);
+    for (size_t k0 = 0; k0 < n; k0 += window * T) {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < T; ++t) {
+            pool.emplace_back([&, t] {
+                std::string &out = buf[t];
+                out.clear();
+                char tmp[64];
+                const size_t lo = k0 + (size_t)t * window, hi = std::min(n, lo + window);
+                for (size_t k = lo; k < hi; ++k) {
+                    const int64_t r_index = translation[loci[k]] + base;
+                    char rbuf[24];
+                    const auto rr = std::to_chars(rbuf, rbuf + sizeof rbuf, r_index);
+                    for (size_t j = 0; j < k; ++j) {
+                        const float sum = S[k * n + j] + S[j * n + k];
+                        const double v = (double)sum * 0.5;
+                        char *p = std::to_chars(tmp, tmp + sizeof tmp, v, std::chars_format::fixed, 8).ptr;
+                        *p++ = ' ';
+                        out.append(tmp, p);
+                        out.append(rbuf, rr.ptr);
+                        out.push_back(' ');
+                        p = std::to_chars(tmp, tmp + sizeof tmp, translation[loci[j]] + base).ptr;
+                        *p++ = '\n';
+                        out.append(tmp, p);
+                    }
+                }
+            });
+        }
+        for (auto &th : pool) th.join();
+        for (int t = 0; t < T; ++t)
+            if (!buf[t].empty() && std::fwrite(buf[t].data(), 1, buf[t].size(), f) != buf[t].size())
+                fail("failed to write \"" + path + "\"");
+    }
+    if (std::fclose(f) != 0) fail("failed to write \"" + path + "\"");
+}
+
+} // namespace
+
+int main(int argc, char **argv)
+{
+    const Options o = parse_options(argc, argv);
+    if (o.alignment_files.size() > 1)
+        fail("the two-alignment scan mode is not supported by this build");
+    if (o.norm_of_mean)
+        fail("--norm-of-mean-scoring is not supported by this build");
+    const int threads = o.threads > 0 ? o.threads : (int)std::max(1u, std::thread::hardware_concurrency());
+
+    if (o.verbose) std::cout << "superdca-gb300: read alignment \"" << o.alignment_files[0] << "\"\n";
+    Alignment a = read_fasta(o.alignment_files[0]);
+    if (o.verbose) std::cout << "superdca-gb300: " << a.N << " sequences, " << a.L << " loci\n";
+
+    if (!o.filterlist.empty()) {
+        std::vector<int64_t> cols = read_index_list(o.filterlist, o.in_base);
+        for (int64_t c : cols)
+            if (c >= a.L) fail("filter list index " + std::to_string(c + o.in_base) + " is beyond the alignment");
+        std::sort(cols.begin(), cols.end());
+        cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+        a = select_columns(a, cols);
+        if (o.out_filterlist) write_fasta(a, o, "filterlist-selected");
+    } else {
+        if (!o.no_filter) a = select_columns(a, filter_columns(a, o.maf, o.gap));
+        if (o.out_filtered) {
+            write_fasta(a, o, "filtered");
+            write_loci(a, o);
+        }
+    }
+    if (!o.samplelist.empty()) {
+        std::vector<int64_t> rows = read_index_list(o.samplelist, o.in_base);
+        for (int64_t r : rows)
+            if (r >= a.N) fail("sample list index " + std::to_string(r + o.in_base) + " is beyond the alignment");
+        a = select_rows(a, rows, stem(o.samplelist));
+        if (o.out_samplelist) write_fasta(a, o, "samplelist-selected");
+    }
+
+    std::vector<int64_t> kept;
+    const std::vector<uint8_t> states = four_state(a, kept);
+    std::vector<int64_t> translation(kept.size());
+    for (size_t k = 0; k < kept.size(); ++k) translation[k] = a.translation[kept[k]];
+    const int64_t N = a.N, L = (int64_t)kept.size();
+    if (o.verbose) std::cout << "superdca-gb300: 4-state alignment has " << N << " sequences and " << L << " loci\n";
+
+    std::vector<uint32_t> loci;
+    if (!o.locilist.empty()) {
+        for (int64_t v : read_index_list(o.locilist, o.in_base)) {
+            if (v >= L) fail("loci list index " + std::to_string(v + o.in_base) + " is beyond the alignment");
+            loci.push_back((uint32_t)v);
+        }
+    } else {
+        const int64_t end = o.end_locus < 0 ? L : std::min<int64_t>(L, o.end_locus + 1);
+        for (int64_t n = o.begin_locus; n < end; ++n) loci.push_back((uint32_t)n);
+    }
+    if (L == 0) {
+        std::cerr << "superdca-gb300: there are no loci to analyze (need at least 2)\n";
+        return EXIT_FAILURE;
+    }
+    if (loci.size() < 2) {
+        std::cerr << "superdca-gb300: there are not enough loci for plmDCA analysis (found " << loci.size()
+                  << " loci that qualify, but need at least 2)\n";
+        return EXIT_FAILURE;
+    }
+
+    const bool need_gpu = !o.no_reweighting || !o.no_dca;
+    Handle H;
+    if (need_gpu) {
+        sdca_config cfg;
+        sdca_config_default(&cfg);
+        cfg.n_seqs = N;
+        cfg.n_loci = L;
+        cfg.lambda_h = o.lambda_h;
+        cfg.lambda_J = o.lambda_J;
+        cfg.gradient_threshold = o.gradient_threshold;
+        cfg.batch = o.batch;
+        cfg.form = o.form;
+        cfg.flags = o.history_bf16 ? SDCA_FLAG_HISTORY_BF16 : 0;
+        cfg.device = o.device;
+        check(sdca_create(&cfg, &H.h), nullptr, "engine set-up failed");
+    }
+
+    std::vector<double> weights((size_t)N, 1.0);
+    if (!o.no_reweighting) {
+        if (o.verbose) std::cout << "superdca-gb300: calculate sequence weights\n";
+        check(sdca_compute_weights(H.h, states.data(), nullptr, o.reweighting_threshold, weights.data()), H.h,
+              "reweighting failed");
+    }
+    if (o.output_weights) {
+        // std::scientific, precision 8 (plmDCA.hpp:547-556)
+        const std::string path = unique_name(a.id + ".weights");
+        std::FILE *f = std::fopen(path.c_str(), "wb");
+        if (!f) fail("cannot open \"" + path + "\" for writing");
+        for (double w : weights) std::fprintf(f, "%.8e\n", w);
+        if (std::fclose(f) != 0) fail("failed to write \"" + path + "\"");
+    }
+    if (o.no_dca) {
+        if (o.verbose) std::cout << "superdca-gb300: exit on users request without performing DCA\n";
+        return EXIT_SUCCESS;
+    }
+
+    check(sdca_set_alignment(H.h, states.data(), weights.data()), H.h, "alignment upload failed");
+    if (o.verbose) {
+        double lh, lJ, beff;
+        sdca_get_lambdas(H.h, &lh, &lJ, &beff);
+        std::cout << "superdca-gb300: B_eff = " << beff << ", lambda_h = " << lh << ", lambda_J = " << lJ << "\n";
+    }
+
+    // Solve the loci list in chunks; keep the scores of the listed columns.
+    const size_t n = loci.size();
+    std::vector<float> S(n * n);
+    std::vector<float> rows;
+    std::vector<sdca_locus_stat> stats;
+    size_t not_converged = 0;
+    for (size_t k0 = 0; k0 < n; k0 += (size_t)o.chunk) {
+        const size_t m = std::min(n - k0, (size_t)o.chunk);
+        rows.resize(m * (size_t)L);
+        stats.resize(m);
+        check(sdca_solve(H.h, loci.data() + k0, m, rows.data(), stats.data()), H.h, "solve failed");
+        for (size_t k = 0; k < m; ++k) {
+            for (size_t j = 0; j < n; ++j) S[(k0 + k) * n + j] = rows[k * (size_t)L + loci[j]];
+            not_converged += stats[k].status != 0;
+        }
+        if (o.verbose)
+            std::cout << "superdca-gb300: solved " << k0 + m << " of " << n << " loci\n" << std::flush;
+    }
+    if (not_converged)
+        std::cerr << "superdca-gb300: " << not_converged << " loci stopped before the gradient threshold\n";
+
+    if (!o.no_coupling_output) {
+        const std::string path =
+            unique_name(a.id + ".SuperDCA_couplings." + std::to_string(o.out_base) + "-based.all");
+        if (o.verbose) std::cout << "superdca-gb300: writing coupling values to file \"" << path << "\"\n";
+        write_couplings(path, S, loci, translation, o.out_base, threads);
+    }
+    return EXIT_SUCCESS;
+}

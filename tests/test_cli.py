@@ -1,0 +1,161 @@
+"""The superdca-gb300 command line: SuperDCA's flow from FASTA to coupling file.
+
+CPU tests hold the C++ parser, filter and 4-state encoding to the rules of
+superdca_gb300/alignment.py and check the side outputs (.fasta, .loci,
+.weights) and the file-name uniquifier of SuperDCA_commons.h:66-81.  The GPU
+test runs the whole program and compares the coupling file with the oracle's
+solves of the same encoded alignment."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from superdca_gb300 import alignment as A
+from superdca_gb300 import synthetic
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(ROOT, "superdca_gb300", "superdca-gb300")
+
+
+@pytest.fixture(scope="module")
+def cli():
+    from superdca_gb300 import build
+    if not os.path.exists(os.path.join(ROOT, "superdca_gb300", "libsuperdca_gb300.so")):
+        pytest.skip("engine library not built")
+    build.build_cli()
+    return CLI
+
+
+def run(cli, args, cwd):
+    return subprocess.run([cli, *args], cwd=cwd, capture_output=True, text=True, timeout=600)
+
+
+def messy_alignment(seed=0, N=60, L=400):
+    """Nucleotides with every case the rules distinguish: gaps as '-' and 'N',
+    lower case, monomorphic, rare-allele, gappy and four-allele columns."""
+    rng = np.random.default_rng(seed)
+    nuc = rng.integers(0, 4, size=(N, L)).astype(np.uint8)
+    nuc[:, 0:20] = nuc[0, 0:20]                                  # monomorphic
+    nuc[:, 20:40] = 0
+    nuc[0, 20:40] = 2                                            # MAF 1/60 above 0.01
+    nuc[:, 40:60] = rng.integers(0, 2, size=(N, 20))
+    blk = nuc[:, 40:60]
+    blk[rng.random((N, 20)) < 0.3] = 4                            # gappy
+    nuc[:, 60:80] = rng.integers(0, 3, size=(N, 20))              # three alleles
+    nuc[rng.random((N, L)) < 0.02] = 4
+    return nuc
+
+
+def write_messy_fasta(path, nuc, seed=0):
+    rng = np.random.default_rng(seed + 1)
+    with open(path, "w") as f:
+        for i, row in enumerate(nuc):
+            s = "".join("ACGT-"[v] for v in row)
+            s = "".join(c.lower() if rng.random() < 0.1 else c for c in s)
+            s = "".join("N" if (c == "-" and rng.random() < 0.5) else c for c in s)
+            f.write(f">sample_{i} some description\n")
+            for k in range(0, len(s), 70):                       # wrapped lines
+                f.write(s[k:k + 70] + "\n")
+
+
+def test_cli_help_and_option_errors(cli, tmp_path):
+    r = run(cli, ["--help"], tmp_path)
+    assert r.returncode == 0 and "--gradient-threshold" in r.stdout and "--no-reweighting" in r.stdout
+    r = run(cli, ["--no-such-flag", "x.fasta"], tmp_path)
+    assert r.returncode == 1 and "unrecognised option" in r.stderr
+    r = run(cli, [], tmp_path)
+    assert r.returncode == 1 and "no input alignment" in r.stderr
+    r = run(cli, ["--gradient-threshold", "abc", "x.fasta"], tmp_path)
+    assert r.returncode == 1 and "invalid value" in r.stderr
+    r = run(cli, ["missing.fasta"], tmp_path)
+    assert r.returncode == 1 and "cannot open" in r.stderr
+    (tmp_path / "bad.fasta").write_text(">a\nACGT\n>b\nACG\n")
+    r = run(cli, ["bad.fasta"], tmp_path)
+    assert r.returncode == 1 and "has length 3, expected 4" in r.stderr
+    r = run(cli, ["a.fasta", "b.fasta"], tmp_path)
+    assert r.returncode == 1 and "scan mode" in r.stderr
+
+
+def test_cli_filter_encode_and_side_outputs(cli, tmp_path):
+    nuc = messy_alignment()
+    write_messy_fasta(tmp_path / "aln.fasta", nuc)
+    names, seqs = A.read_fasta(str(tmp_path / "aln.fasta"))
+    parsed = A.nucleotide_codes(seqs)
+    assert np.array_equal(parsed, nuc)
+
+    args = ["--no-reweighting", "--no-dca", "--output-filtered-alignment", "--output-weights",
+            "aln.fasta"]
+    r = run(cli, args, tmp_path)
+    assert r.returncode == 0, r.stderr
+    # the filtered alignment is written next to the input: aln.fasta exists, so .1
+    cols = A.filter_columns(nuc)
+    got_loci = np.loadtxt(tmp_path / "aln.loci", dtype=np.int64, ndmin=1)
+    assert np.array_equal(got_loci, cols + 1)
+    fn, fs = A.read_fasta(str(tmp_path / "aln.fasta.1"))
+    assert fn == names
+    assert np.array_equal(A.nucleotide_codes(fs), nuc[:, cols])
+    w = (tmp_path / "aln.weights").read_text().splitlines()
+    assert w == ["1.00000000e+00"] * nuc.shape[0]
+
+    # a second run finds every name taken and appends .1 / .2
+    r = run(cli, args, tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert (tmp_path / "aln.loci.1").exists() and (tmp_path / "aln.weights.1").exists()
+    assert (tmp_path / "aln.fasta.2").exists()
+
+    # thresholds and --no-filter-alignment
+    r = run(cli, ["--no-reweighting", "--no-dca", "--output-filtered-alignment", "--maf-threshold", "0.2",
+                  "--gap-threshold=0.05", "--output-indexing-base", "0", "aln.fasta"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    got = np.loadtxt(tmp_path / "aln.loci.2", dtype=np.int64, ndmin=1)
+    assert np.array_equal(got, A.filter_columns(nuc, 0.2, 0.05))
+
+
+def test_cli_filter_and_sample_lists(cli, tmp_path):
+    nuc = messy_alignment(seed=3)
+    write_messy_fasta(tmp_path / "aln.fasta", nuc, seed=3)
+    sel_cols = [5, 61, 62, 300, 301, 399, 61]          # 1-based, with a duplicate
+    (tmp_path / "keep.txt").write_text("# loci\n" + ", ".join(str(c) for c in sel_cols) + "\n")
+    (tmp_path / "samples.txt").write_text("1 3 5\n7\n60\n")
+    r = run(cli, ["--no-reweighting", "--no-dca", "--filterlistfile", "keep.txt", "--output-filterlist-alignment",
+                  "--samplelistfile", "samples.txt", "--output-samplelist-alignment", "aln.fasta"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    cols = sorted(set(c - 1 for c in sel_cols))
+    _, fs = A.read_fasta(str(tmp_path / "aln.fasta.1"))
+    assert np.array_equal(A.nucleotide_codes(fs), nuc[:, cols])
+    rows = [0, 2, 4, 6, 59]
+    _, ss = A.read_fasta(str(tmp_path / "samples.fasta"))
+    assert np.array_equal(A.nucleotide_codes(ss), nuc[np.ix_(rows, cols)])
+    (tmp_path / "bad.txt").write_text("0\n")
+    r = run(cli, ["--no-reweighting", "--no-dca", "--filterlistfile", "bad.txt", "aln.fasta"], tmp_path)
+    assert r.returncode == 1 and "below the index base" in r.stderr
+
+
+@pytest.mark.gpu
+def test_gpu_cli_couplings_match_oracle(cli, tmp_path, oracle_mod):
+    """Full run: GPU reweighting, GPU solves of every locus, coupling file.
+    Lines, their order and indices exactly; values within 1e-4."""
+    O = oracle_mod
+    nuc, _ = synthetic.independent(N=200, L=500, seed=7)
+    A.write_fasta(str(tmp_path / "ind.fasta"), nuc, width=60)
+    r = run(cli, ["-v", "--output-weights", "--gpu-batch", "32", "ind.fasta"], tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    states, cols = A.encode(nuc)
+    w_ref = O.weights(states, 0.9)
+    w_got = np.loadtxt(tmp_path / "ind.weights")
+    np.testing.assert_allclose(w_got, w_ref, rtol=1e-8, atol=0)
+    lh, lJ = O.lambdas(w_ref)[:2]
+    P = O.Problem(states, w_ref, lh, lJ)
+    L = states.shape[1]
+    loci = np.arange(L)
+    scores, st = P.solve(loci, threads=os.cpu_count() or 1)
+    from superdca_gb300.engine import coupling_lines
+    want = coupling_lines(scores, loci, translation=cols, base=1)
+    got = (tmp_path / "ind.SuperDCA_couplings.1-based.all").read_text().splitlines()
+    assert len(got) == len(want) == L * (L - 1) // 2
+    vals = np.array([float(g.split()[0]) for g in got])
+    idx = [tuple(int(t) for t in g.split()[1:]) for g in got]
+    assert idx == [(rr, nn) for _, rr, nn in want]
+    assert all(len(g.split()[0].split(".")[1]) == 8 for g in got[:100])
+    np.testing.assert_allclose(vals, [v for v, _, _ in want], rtol=0, atol=1e-4)
