@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--loci-per-step", type=int, default=0, help="default: batch")
     ap.add_argument("--form", default="tc", choices=["gather", "tc"])
     ap.add_argument("--history-bf16", action="store_true")
+    ap.add_argument("--warm-start", default=os.path.join(ROOT, "superdca_gb300", "warmstart_tree-3000x94000.npy"),
+                    help="learned warm-start parameter blob ('none': zero start)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
@@ -240,6 +242,10 @@ def engine_arm(args):
     form = FORM_TC if args.form == "tc" else FORM_GATHER
     E = Engine(N, L, batch=B, device=local, form=form, history_bf16=args.history_bf16)
     E.set_alignment(st, w)
+    ws = None if args.warm_start in ("", "none") else args.warm_start
+    if ws:
+        from superdca_gb300 import warmstart
+        E.set_warm_start(warmstart.load(ws))
 
     def loci_for(step):
         base = (step * world + rank) * per_step
@@ -338,6 +344,7 @@ def engine_arm(args):
         "config": {"workload": f"{args.workload} seed {args.seed}", "N": int(N), "L": int(L),
                    "batch": B, "loci_per_step": per_step, "form": args.form,
                    "history": "bf16" if args.history_bf16 else "fp32",
+                   "warm_start": os.path.basename(ws) if ws else None,
                    "weights": "unit (--no-reweighting)", "gradient_threshold": 1e-3,
                    "l2": "inputs larger than L2 (282 MB alignment, per-slot solver state)",
                    "parallelism": f"loci sharded over {world} rank(s)"},

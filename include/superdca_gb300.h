@@ -159,6 +159,45 @@ int sdca_destroy(sdca_handle *h);
 
 int sdca_abi_version(void);
 
+/* ---- Learned warm start.  No counterpart in the reference: SuperDCA starts
+ * every locus from zero (SuperDCA/include/plmDCA.hpp:298).  A per-pair MLP
+ * (40 -> 128 -> 128 -> 16, ReLU) maps the statistics of each pair (r, n) to
+ * an initial block J_rn (and optionally h fitted with J fixed).  The optimum is
+ * unchanged (the objective is strictly convex); only the start moves.
+ * The parameter blob holds sdca_mlp_blob_size() floats:
+ *   [0] version (1), [1] neighbours k (1..8), [2] smoothing eps,
+ *   [3] 1: fit h by Newton's method with J fixed, 0: start from h = 0,
+ *   [4, 44) input mean, [44, 84) input scale, W1 (128 x 40), b1 (128),
+ *   W2 (128 x 128), b2 (128), W3 (16 x 128), b3 (16), output scale (16).
+ * Pair statistics per (r, n), in this order: joint[s][a] (16), residual-
+ * weighted joint[s][a] (16), f_n[s] (4), f_r[a] (4), with s the state at n
+ * and a the state at r, all divided by B_eff; the residuals come from each
+ * sequence's k nearest neighbours in Hamming distance.  The start block is
+ * output[s][a] * scale[s*4+a] * B_eff / (2 lambda_J). */
+
+/* Enable the warm start with this blob for later sdca_solve* calls whose
+ * x_init is NULL; params = NULL disables it. */
+int sdca_set_warm_start(sdca_handle *h, const float *params, size_t n_params);
+
+/* Pair statistics of target loci (for training): out holds n_loci x n_sel x
+ * 40 floats for pairs (loci[k], sel[k*n_sel + j]), or n_loci x L x 40 when
+ * sel is NULL. */
+int sdca_ws_features(sdca_handle *h, int k, float eps, const uint32_t *loci, size_t n_loci,
+                     const uint32_t *sel, size_t n_sel, float *out);
+
+/* The network on the GPU (current device), host buffers: X is M x 40 raw
+ * pair statistics, T is M x 16 targets in output units (before the output
+ * scale).  Loss = mean over rows of the squared error summed over the 16
+ * outputs.  sdca_mlp_grad: loss and its gradient (blob layout, zero outside
+ * W1..b3).  sdca_mlp_train: Adam over shuffled minibatches, params updated in
+ * place, mean minibatch loss per epoch into losses (may be NULL). */
+int sdca_mlp_blob_size(void);
+int sdca_mlp_grad(const float *params, const float *X, const float *T, int64_t M, double *loss, float *grad);
+int sdca_mlp_predict(const float *params, const float *X, int64_t M, float *out);
+int sdca_mlp_train(float *params, const float *X, const float *T, int64_t M, int epochs, int batch, float lr,
+                   uint64_t seed, double *losses);
+const char *sdca_mlp_last_error(void);
+
 /* Largest alignment sdca_eval_noalloc accepts: its scratch is a fixed array. */
 #define SDCA_NOALLOC_MAX_SEQS 65536
 #define SDCA_NOALLOC_MAX_LOCI 262144

@@ -30,7 +30,9 @@ KERNEL_CLASSES = ["forward", "backward", "linesearch", "history", "direction", "
 # every entry point include/superdca_gb300.h declares
 EXPORTS = ["sdca_abi_version", "sdca_config_default", "sdca_create", "sdca_set_alignment",
            "sdca_compute_weights", "sdca_get_lambdas", "sdca_solve", "sdca_solve_ex", "sdca_eval",
-           "sdca_get_profile", "sdca_last_error", "sdca_destroy", "sdca_eval_noalloc"]
+           "sdca_get_profile", "sdca_last_error", "sdca_destroy", "sdca_eval_noalloc",
+           "sdca_set_warm_start", "sdca_ws_features", "sdca_mlp_blob_size", "sdca_mlp_grad",
+           "sdca_mlp_predict", "sdca_mlp_train", "sdca_mlp_last_error"]
 
 
 class Config(C.Structure):
@@ -82,9 +84,17 @@ def load(path: str = LIB_PATH):
     L.sdca_last_error.argtypes = [vp]
     L.sdca_destroy.argtypes = [vp]
     L.sdca_eval_noalloc.argtypes = [vp, i64, i64, vp, dp, dp, C.c_uint32, vp, vp, vp, vp]
+    L.sdca_set_warm_start.argtypes = [vp, vp, C.c_size_t]
+    L.sdca_ws_features.argtypes = [vp, C.c_int, C.c_float, vp, C.c_size_t, vp, C.c_size_t, vp]
+    L.sdca_mlp_blob_size.argtypes = []
+    L.sdca_mlp_grad.argtypes = [vp, vp, vp, i64, C.POINTER(dp), vp]
+    L.sdca_mlp_predict.argtypes = [vp, vp, i64, vp]
+    L.sdca_mlp_train.argtypes = [vp, vp, vp, i64, C.c_int, C.c_int, C.c_float, C.c_uint64, vp]
+    L.sdca_mlp_last_error.restype = C.c_char_p
+    L.sdca_mlp_last_error.argtypes = []
     L.sdca_internal_lbfgs_coeffs.argtypes = [C.c_int, vp, vp, vp, vp, dp, C.POINTER(dp), vp, vp]
     for name in EXPORTS + ["sdca_internal_lbfgs_coeffs"]:
-        if name not in ("sdca_abi_version", "sdca_last_error"):
+        if name not in ("sdca_abi_version", "sdca_last_error", "sdca_mlp_last_error"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L

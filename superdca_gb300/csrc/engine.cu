@@ -137,6 +137,19 @@ struct sdca_handle {
     int refresh_every = 30;
     int tc_refresh_every = 5;   // tensor-core form: recompute logits every this many accepted steps
 
+    // learned warm start (warmstart.cu, mlp.cu)
+    float *ws_params = nullptr;
+    bool ws_on = false;
+    int ws_k = 0;
+    float ws_eps = 0.f;
+    bool ws_hfit = false;          // fit h to the predicted J (blob flag) or start from h = 0
+    int32_t *knn = nullptr;
+    int knn_k = 0;                 // k of the nearest-neighbour table held (0: none)
+    float *ws_R = nullptr, *ws_feats = nullptr, *ws_out = nullptr;
+    float *ws_xn = nullptr, *ws_h1 = nullptr, *ws_h2 = nullptr;
+    int32_t *ws_idx = nullptr;     // [0, WS_G): slots, [WS_G, 2 WS_G): loci
+    double *ws_xmax = nullptr;
+
     std::vector<SlotHost> slots;
 
     // profiling
@@ -471,6 +484,167 @@ int slot_begin(sdca_handle *h, int b, int64_t k, int32_t locus, const float *x0_
     return SDCA_OK;
 }
 
+// ---- learned warm start
+
+constexpr int WS_G = 32;              // loci whose start points are prepared together
+constexpr int64_t WS_ROWS = 65536;    // network rows per inference pass
+
+int ws_buffers(sdca_handle *h)
+{
+    if (h->ws_feats) return SDCA_OK;
+    const Problem &P = h->P;
+    const size_t rows = (size_t)std::min<int64_t>(WS_ROWS, WS_G * P.L);
+    int rc;
+    if ((rc = dalloc(h, &h->ws_R, (size_t)WS_G * P.Nx * 8))) return rc;   // [g][Nx][8], or R2 [g][Nx][4]
+    if ((rc = dalloc(h, &h->ws_out, (size_t)WS_G * P.L * MLP_OUT))) return rc;
+    if ((rc = dalloc(h, &h->ws_xn, rows * MLP_IN))) return rc;
+    if ((rc = dalloc(h, &h->ws_h1, rows * MLP_H))) return rc;
+    if ((rc = dalloc(h, &h->ws_h2, rows * MLP_H))) return rc;
+    if ((rc = dalloc(h, &h->ws_idx, 2 * WS_G))) return rc;
+    if ((rc = dalloc(h, &h->ws_xmax, WS_G))) return rc;
+    return dalloc(h, &h->ws_feats, (size_t)WS_G * P.L * MLP_IN);
+}
+
+// each sequence's k nearest neighbours in Hamming distance (kept until the
+// alignment changes)
+int ws_knn(sdca_handle *h, int k)
+{
+    if (h->knn_k == k) return SDCA_OK;
+    const Problem &P = h->P;
+    if (P.N > 32768) return fail(h, SDCA_E_UNSUPPORTED, "the warm start supports at most 32768 sequences");
+    int rc;
+    if (!h->knn && (rc = dalloc(h, &h->knn, (size_t)P.N * WS_MAX_K))) return rc;
+    const int64_t W = (P.L + 31) / 32;
+    uint64_t *packed = nullptr;
+    int32_t *dist = nullptr;
+    if (cudaMalloc(&packed, sizeof(uint64_t) * P.N * W) != cudaSuccess ||
+        cudaMalloc(&dist, sizeof(int32_t) * P.N * P.N) != cudaSuccess) {
+        cudaGetLastError();
+        if (packed) cudaFree(packed);
+        return fail(h, SDCA_E_NOMEM, "device allocation for the neighbour table failed");
+    }
+    launch_distances(h->X, P.Lx, (int)P.N, (int)P.L, packed, dist, h->stream);
+    launch_knn(dist, (int)P.N, k, h->knn, h->stream);
+    const cudaError_t e1 = cudaGetLastError();
+    const cudaError_t e2 = cudaStreamSynchronize(h->stream);
+    cudaFree(packed);
+    cudaFree(dist);
+    if (e1 != cudaSuccess || e2 != cudaSuccess)
+        return fail(h, SDCA_E_CUDA, std::string("neighbour table: ") + cudaGetErrorString(e1 ? e1 : e2));
+    h->knn_k = k;
+    return SDCA_OK;
+}
+
+// pair statistics of up to WS_G loci into ws_feats ([g][n][MLP_IN])
+int ws_features(sdca_handle *h, const std::vector<int32_t> &loci, int k, float eps)
+{
+    const Problem &P = h->P;
+    const int G = (int)loci.size();
+    int rc = ws_buffers(h);
+    if (rc) return rc;
+    if ((rc = ws_knn(h, k))) return rc;
+    CK(cudaMemcpyAsync(h->ws_idx + WS_G, loci.data(), sizeof(int32_t) * G, cudaMemcpyHostToDevice, h->stream));
+    Timed t(h, SDCA_K_OTHER, 2, G);
+    launch_ws_residual(h->XT, P.Nx, (int)P.N, h->ws_idx + WS_G, G, h->w, h->knn, k, eps, h->ws_R, h->stream);
+    launch_ws_pairs(h->XT, P.Nx, (int)P.N, (int)P.L, G, h->ws_R, P.b_eff, h->ws_feats, h->stream);
+    CKL();
+    return SDCA_OK;
+}
+
+// the same statistics for slots that are about to start, by two tensor-core
+// backward contractions X^T R through the slots' own R rows and gradient
+// buffers (both free until the slot's first evaluation)
+int ws_features_tc(sdca_handle *h, const std::vector<int32_t> &grp, int k, float eps)
+{
+    const Problem &P = h->P;
+    const int G = (int)grp.size();
+    int rc = ws_buffers(h);
+    if (rc) return rc;
+    if ((rc = ws_knn(h, k))) return rc;
+    // ws_idx: slots then loci, as ws_begin expects them
+    std::vector<int32_t> loci(G);
+    for (int g = 0; g < G; ++g) loci[g] = h->slots[grp[g]].locus;
+    CK(cudaMemcpyAsync(h->ws_idx, grp.data(), sizeof(int32_t) * G, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->ws_idx + WS_G, loci.data(), sizeof(int32_t) * G, cudaMemcpyHostToDevice, h->stream));
+    {
+        Timed t(h, SDCA_K_OTHER, 1, G);
+        launch_ws_residual_split(h->XT, P.Nx, (int)P.N, h->ws_idx + WS_G, h->ws_idx, G, h->w, h->knn, k, eps, h->R,
+                                 h->ws_R, h->stream);
+    }
+    CKL();
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int b : grp) h->slots[b].gcur = pass;   // pass 0 fills buffer 2b+1, pass 1 buffer 2b
+        if ((rc = upload_slots(h, grp))) return rc;
+        if (pass == 1) {
+            Timed t(h, SDCA_K_OTHER, 1, G);
+            launch_ws_copy_r(P.Nx, h->ws_idx, G, h->ws_R, h->R, h->stream);
+        }
+        Timed t(h, SDCA_K_OTHER, 2, G);
+        CK(tc_launch_bwd(h->tc, P, h->sd, h->list, G, h->R, h->r_scale, h->Rhi, h->Rlo, h->gpool, h->tc_err,
+                         h->stream));
+    }
+    for (int b : grp) h->slots[b].gcur = 0;
+    {
+        Timed t(h, SDCA_K_OTHER, 1, G);
+        launch_ws_assemble((int)P.L, P.Dp, h->ws_idx, G, h->gpool, P.b_eff, h->ws_feats, h->stream);
+    }
+    CKL();
+    return SDCA_OK;
+}
+
+// start points of slots `bs` from the network: J blocks with h = 0, or h
+// fitted with J fixed when the blob asks for it
+int ws_begin(sdca_handle *h, const std::vector<int32_t> &bs)
+{
+    const Problem &P = h->P;
+    for (size_t g0 = 0; g0 < bs.size(); g0 += WS_G) {
+        const int G = (int)std::min<size_t>(WS_G, bs.size() - g0);
+        std::vector<int32_t> grp(bs.begin() + g0, bs.begin() + g0 + G), loci(G);
+        for (int g = 0; g < G; ++g) loci[g] = h->slots[grp[g]].locus;
+        int rc = h->form == SDCA_FORM_TC ? ws_features_tc(h, grp, h->ws_k, h->ws_eps)
+                                         : ws_features(h, loci, h->ws_k, h->ws_eps);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(h->ws_idx, grp.data(), sizeof(int32_t) * G, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemsetAsync(h->ws_xmax, 0, sizeof(double) * WS_G, h->stream));
+        {
+            const int64_t M = (int64_t)G * P.L, rows = std::min<int64_t>(WS_ROWS, WS_G * P.L);
+            Timed t(h, SDCA_K_OTHER, (int)(4 * ((M + rows - 1) / rows) + 1), G);
+            for (int64_t r0 = 0; r0 < M; r0 += rows)
+                mlp_infer(h->ws_params, h->ws_feats + r0 * MLP_IN, std::min(rows, M - r0), h->ws_xn, h->ws_h1,
+                          h->ws_h2, h->ws_out + r0 * MLP_OUT, h->stream);
+            launch_ws_scatter((int)P.L, P.Dp, h->ws_idx, h->ws_idx + WS_G, G, h->ws_out, h->ws_params,
+                              P.b_eff / (2.0 * P.lambda_J), h->wa, h->ws_xmax, h->stream);
+        }
+        CKL();
+        std::vector<double> xm(G);
+        auto fetch_xmax = [&]() -> int {
+            CK(cudaMemcpyAsync(xm.data(), h->ws_xmax, sizeof(double) * G, cudaMemcpyDeviceToHost, h->stream));
+            const int r_ = stream_sync(h);
+            if (r_) return r_;
+            for (int g = 0; g < G; ++g) {
+                const int b = grp[g];
+                h->slots[b].xmax = xm[g];
+                h->sd_h[b].tc_scale = pow2_scale(xm[g]);
+                h->sd_h[b].tc_inv_scale = 1.0 / h->sd_h[b].tc_scale;
+            }
+            return SDCA_OK;
+        };
+        if ((rc = fetch_xmax())) return rc;
+        // logits at the start point: the tensor-core form uses its own forward
+        // (as for its periodic logit refresh), the plain form the FP64-accumulated gather
+        if ((rc = run_forward(h, grp, h->wa, true, h->form == SDCA_FORM_TC))) return rc;
+        if (h->ws_hfit) {
+            {
+                Timed t(h, SDCA_K_OTHER, 1, G);
+                launch_ws_hfit(P, h->ws_idx, h->rstate, h->w, G, h->wa, h->lbase, h->ws_xmax, h->stream);
+            }
+            CKL();
+            if ((rc = fetch_xmax())) return rc;
+        }
+    }
+    return SDCA_OK;
+}
+
 // the per-solve queue
 struct Queue {
     const uint32_t *loci = nullptr;
@@ -484,7 +658,7 @@ struct Queue {
 
 int refill(sdca_handle *h, Queue &Qu)
 {
-    std::vector<int32_t> warm;
+    std::vector<int32_t> warm, learned;
     for (int b = 0; b < h->P.Bmax && Qu.next < Qu.n; ++b) {
         if (h->slots[b].phase != PH_EMPTY) continue;
         const int64_t k = (int64_t)Qu.next++;
@@ -500,9 +674,15 @@ int refill(sdca_handle *h, Queue &Qu)
             // the copy reads the staging buffer: finish it before the next slot reuses it
             { const int r_ = stream_sync(h); if (r_) return r_; }
             warm.push_back(b);
+        } else if (h->ws_on) {
+            learned.push_back(b);
         }
     }
-    if (!warm.empty()) return run_forward(h, warm, h->wa, true);
+    if (!warm.empty()) {
+        const int rc = run_forward(h, warm, h->wa, true);
+        if (rc) return rc;
+    }
+    if (!learned.empty()) return ws_begin(h, learned);
     return SDCA_OK;
 }
 
@@ -1173,6 +1353,7 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
 int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weights)
 {
     if (!h) return SDCA_E_ARG;
+    h->knn_k = 0;
     if (!states || !weights) return fail(h, SDCA_E_ARG, "states and weights are required");
     Problem &P = h->P;
     for (int64_t i = 0; i < P.N; ++i)
@@ -1338,6 +1519,7 @@ int sdca_compute_weights(sdca_handle *h, const uint8_t *states, const double *mu
     // the states go through the alignment buffer: a following
     // sdca_set_alignment overwrites it anyway
     h->has_alignment = false;
+    h->knn_k = 0;
     const int64_t W = (P.L + 31) / 32;
     uint64_t *packed = nullptr;
     double *d = nullptr;
@@ -1383,6 +1565,74 @@ int sdca_compute_weights(sdca_handle *h, const uint8_t *states, const double *mu
     } while (0);
     release();
     return rc;
+}
+
+int sdca_set_warm_start(sdca_handle *h, const float *params, size_t n_params)
+{
+    if (!h) return SDCA_E_ARG;
+    if (!params) {
+        h->ws_on = false;
+        return SDCA_OK;
+    }
+    if (n_params != (size_t)MLP_BLOB_SIZE)
+        return fail(h, SDCA_E_ARG, "warm-start parameters: expected " + std::to_string(MLP_BLOB_SIZE) + " floats");
+    if (params[MLP_VERSION] != (float)MLP_BLOB_VERSION)
+        return fail(h, SDCA_E_ARG, "warm-start parameters: unknown version");
+    const float kf = params[MLP_KNN], eps = params[MLP_EPS];
+    if (!(kf >= 1.f && kf <= (float)WS_MAX_K && kf == std::floor(kf)) || !(eps >= 0.f) || !std::isfinite(eps))
+        return fail(h, SDCA_E_ARG, "warm-start parameters: neighbours must be 1..8 and eps >= 0");
+    for (size_t i = 0; i < n_params; ++i)
+        if (!std::isfinite(params[i])) return fail(h, SDCA_E_ARG, "warm-start parameters must be finite");
+    CK(cudaSetDevice(h->cfg.device));
+    int rc;
+    if (!h->ws_params && (rc = dalloc(h, &h->ws_params, MLP_BLOB_SIZE))) return rc;
+    CK(cudaMemcpyAsync(h->ws_params, params, sizeof(float) * MLP_BLOB_SIZE, cudaMemcpyHostToDevice, h->stream));
+    if ((rc = stream_sync(h))) return rc;
+    h->ws_k = (int)kf;
+    h->ws_eps = eps;
+    h->ws_hfit = params[MLP_HFIT] != 0.f;
+    h->ws_on = true;
+    return SDCA_OK;
+}
+
+int sdca_ws_features(sdca_handle *h, int k, float eps, const uint32_t *loci, size_t n_loci, const uint32_t *sel,
+                     size_t n_sel, float *out)
+{
+    if (!h) return SDCA_E_ARG;
+    if (!h->has_alignment) return fail(h, SDCA_E_STATE, "sdca_set_alignment must come first");
+    if (!loci || !out) return fail(h, SDCA_E_ARG, "loci and out are required");
+    if (k < 1 || k > WS_MAX_K || !(eps >= 0.f)) return fail(h, SDCA_E_ARG, "k must be 1..8 and eps >= 0");
+    const Problem &P = h->P;
+    for (size_t i = 0; i < n_loci; ++i)
+        if (loci[i] >= (uint32_t)P.L) return fail(h, SDCA_E_ARG, "locus index out of range");
+    if (sel)
+        for (size_t i = 0; i < n_loci * n_sel; ++i)
+            if (sel[i] >= (uint32_t)P.L) return fail(h, SDCA_E_ARG, "pair index out of range");
+    CK(cudaSetDevice(h->cfg.device));
+    std::vector<float> buf;
+    for (size_t g0 = 0; g0 < n_loci; g0 += WS_G) {
+        const int G = (int)std::min<size_t>(WS_G, n_loci - g0);
+        std::vector<int32_t> grp(G);
+        for (int g = 0; g < G; ++g) grp[g] = (int32_t)loci[g0 + g];
+        int rc = ws_features(h, grp, k, eps);
+        if (rc) return rc;
+        const size_t per = (size_t)P.L * MLP_IN;
+        if (!sel) {
+            CK(cudaMemcpyAsync(out + g0 * per, h->ws_feats, sizeof(float) * per * G, cudaMemcpyDeviceToHost,
+                               h->stream));
+            if ((rc = stream_sync(h))) return rc;
+            continue;
+        }
+        buf.resize(per * G);
+        CK(cudaMemcpyAsync(buf.data(), h->ws_feats, sizeof(float) * per * G, cudaMemcpyDeviceToHost, h->stream));
+        if ((rc = stream_sync(h))) return rc;
+        for (int g = 0; g < G; ++g)
+            for (size_t j = 0; j < n_sel; ++j)
+                std::memcpy(out + ((g0 + g) * n_sel + j) * MLP_IN,
+                            buf.data() + ((size_t)g * P.L + sel[(g0 + g) * n_sel + j]) * MLP_IN,
+                            sizeof(float) * MLP_IN);
+    }
+    return SDCA_OK;
 }
 
 int sdca_get_profile(const sdca_handle *h, sdca_profile *out)

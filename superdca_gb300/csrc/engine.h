@@ -25,6 +25,25 @@ constexpr int Q = 4;
 constexpr int QQ = Q * Q;
 constexpr int MAXHIST = 10;      // upper bound on the L-BFGS history length m
 
+// Learned warm start: per-pair MLP MLP_IN -> MLP_H -> MLP_H -> MLP_OUT (ReLU).
+// Parameter blob (floats): version, neighbours k, smoothing eps, h-fit flag,
+// input mean and scale, W1 b1 W2 b2 W3 b3 (trained), output scale.
+constexpr int MLP_IN = 40, MLP_H = 128, MLP_OUT = 16;
+constexpr int MLP_BLOB_VERSION = 1;
+constexpr int MLP_VERSION = 0, MLP_KNN = 1, MLP_EPS = 2, MLP_HFIT = 3;
+constexpr int MLP_IN_MEAN = 4;
+constexpr int MLP_IN_SCALE = MLP_IN_MEAN + MLP_IN;
+constexpr int MLP_W1 = MLP_IN_SCALE + MLP_IN;
+constexpr int MLP_B1 = MLP_W1 + MLP_H * MLP_IN;
+constexpr int MLP_W2 = MLP_B1 + MLP_H;
+constexpr int MLP_B2 = MLP_W2 + MLP_H * MLP_H;
+constexpr int MLP_W3 = MLP_B2 + MLP_H;
+constexpr int MLP_B3 = MLP_W3 + MLP_OUT * MLP_H;
+constexpr int MLP_TRAIN_END = MLP_B3 + MLP_OUT;
+constexpr int MLP_OUT_SCALE = MLP_TRAIN_END;
+constexpr int MLP_BLOB_SIZE = MLP_OUT_SCALE + MLP_OUT;
+constexpr int WS_MAX_K = 8;       // nearest neighbours per sequence, at most
+
 // per-slot accumulators (doubles), zeroed by the host before each use
 enum Acc {
     ACC_F = 0,      // sum_i w_i (lse_i - l_i[s_i(r)])             (trial)
@@ -127,6 +146,26 @@ void launch_score(const Problem &P, const SlotDev *sd, const int32_t *list, int 
                   const float *wa, int gap, float *rows, cudaStream_t st);
 
 // sequence reweighting (kernels_weights.cu)
+// warm start (mlp.cu, warmstart.cu)
+void mlp_infer(const float *p_dev, const float *X, int64_t M, float *Xn, float *h1, float *h2, float *out,
+               cudaStream_t st);
+void launch_distances(const uint8_t *X, int64_t ld, int N, int L, uint64_t *packed, int32_t *dist,
+                      cudaStream_t st);
+void launch_knn(const int32_t *dist, int N, int k, int32_t *knn, cudaStream_t st);
+void launch_ws_residual(const uint8_t *XT, int64_t Nx, int N, const int32_t *loci, int G, const double *w,
+                        const int32_t *knn, int k, float eps, float *Rws, cudaStream_t st);
+void launch_ws_residual_split(const uint8_t *XT, int64_t Nx, int N, const int32_t *loci, const int32_t *slots, int G,
+                              const double *w, const int32_t *knn, int k, float eps, float *R, float *R2,
+                              cudaStream_t st);
+void launch_ws_copy_r(int64_t Nx, const int32_t *slots, int G, const float *R2, float *R, cudaStream_t st);
+void launch_ws_assemble(int L, int64_t Dp, const int32_t *slots, int G, const float *gpool, double b_eff,
+                        float *feats, cudaStream_t st);
+void launch_ws_pairs(const uint8_t *XT, int64_t Nx, int N, int L, int G, const float *Rws, double b_eff,
+                     float *feats, cudaStream_t st);
+void launch_ws_scatter(int L, int64_t Dp, const int32_t *slots, const int32_t *loci, int G, const float *out,
+                       const float *p_dev, double out_mult, float *wa, double *xmax, cudaStream_t st);
+void launch_ws_hfit(const Problem &P, const int32_t *slots, const uint8_t *rstate, const double *w, int G,
+                    float *wa, double *lbase, double *xmax, cudaStream_t st);
 void launch_weights(const uint8_t *X, int64_t ld, int N, int L, uint64_t *packed, double threshold,
                     const double *mult, double *nbr, unsigned long long *nonidentical, cudaStream_t st);
 

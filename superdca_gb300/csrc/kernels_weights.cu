@@ -41,10 +41,12 @@ __global__ void k_pack2(const uint8_t *__restrict__ X, int64_t ld, int N, int L,
     packed[t] = v;
 }
 
+// DIST: write every pair's distance (both orders) instead of the neighbour sums
+template <bool DIST>
 __global__ void __launch_bounds__(256)
 k_pair_neighbours(const uint64_t *__restrict__ packed, int N, int L, int64_t W, double threshold,
                   const double *__restrict__ mult, double *__restrict__ nbr,
-                  unsigned long long *__restrict__ nonidentical)
+                  unsigned long long *__restrict__ nonidentical, int32_t *__restrict__ dist)
 {
     // lower-triangle tile index -> (ti, tj) with tj <= ti
     const int64_t tid = blockIdx.x;
@@ -91,6 +93,21 @@ k_pair_neighbours(const uint64_t *__restrict__ packed, int N, int L, int64_t W, 
         }
         __syncthreads();
     }
+    if (DIST) {
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int i = i0 + ty + 16 * a;
+            if (i >= N) continue;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int j = j0 + tx + 16 * b;
+                if (j > i) continue;
+                dist[(int64_t)i * N + j] = d[a][b];
+                dist[(int64_t)j * N + i] = d[a][b];
+            }
+        }
+        return;
+    }
     unsigned long long nonid = 0;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
@@ -122,7 +139,19 @@ void launch_weights(const uint8_t *X, int64_t ld, int N, int L, uint64_t *packed
     k_pack2<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(X, ld, N, L, W, packed);
     const int64_t nt = (N + WT - 1) / WT;
     const int64_t tiles = nt * (nt + 1) / 2;
-    k_pair_neighbours<<<(unsigned)tiles, 256, 0, st>>>(packed, N, L, W, threshold, mult, nbr, nonidentical);
+    k_pair_neighbours<false><<<(unsigned)tiles, 256, 0, st>>>(packed, N, L, W, threshold, mult, nbr, nonidentical,
+                                                              nullptr);
+}
+
+// the full N x N matrix of differing-locus counts (diagonal 0)
+void launch_distances(const uint8_t *X, int64_t ld, int N, int L, uint64_t *packed, int32_t *dist, cudaStream_t st)
+{
+    const int64_t W = (L + 31) / 32;
+    const int64_t total = (int64_t)N * W;
+    k_pack2<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(X, ld, N, L, W, packed);
+    const int64_t nt = (N + WT - 1) / WT;
+    const int64_t tiles = nt * (nt + 1) / 2;
+    k_pair_neighbours<true><<<(unsigned)tiles, 256, 0, st>>>(packed, N, L, W, 0.0, nullptr, nullptr, nullptr, dist);
 }
 
 } // namespace sdca

@@ -133,6 +133,32 @@ class Engine:
             weak_searches=np.array([s.weak_searches for s in st]),
             max_trials=np.array([s.max_trials for s in st]))
 
+    def set_warm_start(self, blob):
+        """Start later solves (without x_init) from the learned warm start
+        given by a parameter blob (superdca_gb300.warmstart); None disables."""
+        if blob is None:
+            self._ws_blob = None
+            self._check(self.lib.sdca_set_warm_start(self.h, None, 0))
+            return
+        self._ws_blob = np.ascontiguousarray(blob, dtype=np.float32)
+        self._check(self.lib.sdca_set_warm_start(self.h, _ptr(self._ws_blob), self._ws_blob.size))
+
+    def ws_features(self, loci, k: int, eps: float, sel=None) -> np.ndarray:
+        """Pair statistics of the warm start for target loci: n x L x 40, or
+        n x P x 40 for the pairs sel (n x P locus indices)."""
+        loci = np.ascontiguousarray(loci, dtype=np.uint32)
+        n = len(loci)
+        if sel is None:
+            out = np.zeros((n, self.L, 40), dtype=np.float32)
+            self._check(self.lib.sdca_ws_features(self.h, int(k), float(eps), _ptr(loci), n, None, 0, _ptr(out)))
+            return out
+        sel = np.ascontiguousarray(sel, dtype=np.uint32)
+        assert sel.shape[0] == n
+        out = np.zeros((n, sel.shape[1], 40), dtype=np.float32)
+        self._check(self.lib.sdca_ws_features(self.h, int(k), float(eps), _ptr(loci), n, _ptr(sel), sel.shape[1],
+                                              _ptr(out)))
+        return out
+
     def eval(self, r: int, x: np.ndarray, grad: bool = True):
         x = np.ascontiguousarray(x, dtype=np.float64)
         f = C.c_double()

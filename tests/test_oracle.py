@@ -133,3 +133,27 @@ def test_oracle_against_live_reference(oracle_mod):
             assert f1 == f2
             np.testing.assert_allclose(g1, g2, atol=1e-12)
             np.testing.assert_array_equal(R.score_row(r, x), O.score_row(x, L, r))
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    """The FP64 restatement of the warm-start network (oracle/mlp_oracle.py),
+    which the GPU gradients are checked against, against central differences."""
+    from oracle import mlp_oracle as M
+    rng = np.random.default_rng(3)
+    p = np.zeros(M.SIZE)
+    p[0], p[1], p[2] = 1, 3, 0.5
+    p[M.IN_MEAN:M.IN_MEAN + M.N_IN] = rng.normal(size=M.N_IN) * 0.1
+    p[M.IN_SCALE:M.IN_SCALE + M.N_IN] = rng.uniform(0.5, 2.0, M.N_IN)
+    p[M.W1:M.TRAIN_END] = rng.normal(size=M.TRAIN_END - M.W1) * 0.2
+    X = rng.normal(size=(20, M.N_IN))
+    T = rng.normal(size=(20, M.N_OUT))
+    f0, g = M.loss_and_grad(p, X, T)
+    idx = np.concatenate([rng.choice(np.arange(M.W1, M.TRAIN_END), 60, replace=False),
+                          [M.B1, M.B2 + 5, M.B3 + 15, M.W3]])
+    h = 1e-6
+    for i in idx:
+        q = p.copy(); q[i] += h
+        fp = M.loss_and_grad(q, X, T)[0]
+        q[i] -= 2 * h
+        fm = M.loss_and_grad(q, X, T)[0]
+        assert abs((fp - fm) / (2 * h) - g[i]) <= 1e-6 * max(1.0, abs(g[i])), i
