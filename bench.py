@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--loci-per-step", type=int, default=0, help="default: batch")
-    ap.add_argument("--form", default="tc", choices=["gather", "tc"])
+    ap.add_argument("--form", default="tc", choices=["gather", "tc", "dual"])
     ap.add_argument("--history-bf16", action="store_true")
     ap.add_argument("--warm-start", default=os.path.join(ROOT, "superdca_gb300", "warmstart_tree-3000x94000.npy"),
                     help="learned warm-start parameter blob ('none': zero start)")
@@ -232,17 +232,17 @@ def engine_arm(args):
 
         torch.cuda.set_device(local)
         tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from superdca_gb300 import Engine, FORM_GATHER, FORM_TC
+    from superdca_gb300 import Engine, FORM_DUAL, FORM_GATHER, FORM_TC
 
     st = load_workload(args)
     N, L = st.shape
     w = np.ones(N)
     B = args.batch
     per_step = args.loci_per_step or B
-    form = FORM_TC if args.form == "tc" else FORM_GATHER
+    form = {"tc": FORM_TC, "gather": FORM_GATHER, "dual": FORM_DUAL}[args.form]
     E = Engine(N, L, batch=B, device=local, form=form, history_bf16=args.history_bf16)
     E.set_alignment(st, w)
-    ws = None if args.warm_start in ("", "none") else args.warm_start
+    ws = None if args.warm_start in ("", "none") or args.form == "dual" else args.warm_start
     if ws:
         from superdca_gb300 import warmstart
         E.set_warm_start(warmstart.load(ws))

@@ -40,7 +40,10 @@ extern "C" {
 
 /* contraction forms (sdca_config.form) */
 #define SDCA_FORM_GATHER 0    /* plain form: FP32 gather/scatter on CUDA cores */
-#define SDCA_FORM_TC 1        /* tcgen05 one-hot GEMMs, BF16 hi+lo, FP32 accumulate */
+#define SDCA_FORM_TC 1        /* tcgen05 one-hot GEMMs, fp16 hi+lo, FP32 accumulate */
+#define SDCA_FORM_DUAL 2      /* the same L-BFGS iteration kept in the span of the sequences:
+                                 N x 4 coefficients, one exact integer product with the
+                                 N x N agreement matrix per iteration; zero start only */
 
 /* sdca_config.flags */
 #define SDCA_FLAG_HISTORY_BF16 0x1 /* keep L-BFGS (s, y) history in BF16 */

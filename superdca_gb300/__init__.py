@@ -5,5 +5,5 @@ include/superdca_gb300.h; this package is its Python host binding plus the
 alignment encoding and the seeded synthetic workloads used by the tests and
 the benchmark.
 """
-from ._lib import EngineError, FORM_GATHER, FORM_TC  # noqa: F401
+from ._lib import EngineError, FORM_DUAL, FORM_GATHER, FORM_TC  # noqa: F401
 from .engine import Engine, SolveResult, coupling_lines, format_coupling_lines  # noqa: F401

@@ -21,6 +21,7 @@ SDCA_E_UNSUPPORTED = -6
 
 FORM_GATHER = 0
 FORM_TC = 1
+FORM_DUAL = 2
 FLAG_HISTORY_BF16 = 0x1
 
 K_FORWARD, K_BACKWARD, K_LINESEARCH, K_HISTORY, K_DIRECTION, K_ACCEPT, K_SCORE, K_OTHER = range(8)

@@ -82,6 +82,14 @@ struct SlotHost {
     double xmax = 0.0;       // bound on max|x| (sets the fp16 scale of a refresh)
     double dmax = 0.0;       // max|d| of the current direction
     double f_fresh = 0.0;    // pseudo-likelihood part of f at recomputed logits
+    // dual form: h parts of x, d, the two gradients and the history pairs
+    // (their J parts live on the device as coefficient pairs)
+    double eta_x[Q] = {0, 0, 0, 0}, eta_d[Q] = {0, 0, 0, 0};
+    double eta_g[2][Q] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+    double eta_s[MAXHIST + 1][Q] = {}, eta_y[MAXHIST + 1][Q] = {};
+    double chk_ratio = 0.0;  // max|g| / ||g|| at the last exact max-norm check (0: none yet)
+    int last_check = -1000;  // iteration of that check
+    double amax_g = 0.0, amax_x = 0.0;  // max |a| of the gradient and of x
     MoreThuente ls;
 };
 
@@ -136,6 +144,13 @@ struct sdca_handle {
     double refresh_factor = 8.0;
     int refresh_every = 30;
     int tc_refresh_every = 5;   // tensor-core form: recompute logits every this many accepted steps
+
+    // dual form (kernels_dual.cu)
+    double *dv = nullptr, *u64 = nullptr, *KR = nullptr, *amax = nullptr, *J64 = nullptr;
+    int32_t *rq = nullptr, *Kmat = nullptr;
+    long long *csum = nullptr;
+    float *Rchk = nullptr;
+    double qscale = 1.0;
 
     // learned warm start (warmstart.cu, mlp.cu)
     float *ws_params = nullptr;
@@ -477,6 +492,11 @@ int slot_begin(sdca_handle *h, int b, int64_t k, int32_t locus, const float *x0_
                        cudaMemcpyDeviceToDevice, h->stream));
     if (!x0_engine)
         CK(cudaMemsetAsync(h->lbase + (int64_t)b * P.Nx * 4, 0, sizeof(double) * P.Nx * 4, h->stream));
+    if (h->form == SDCA_FORM_DUAL) {
+        const size_t NV = DV_S + 2 * (size_t)P.ring;
+        CK(cudaMemsetAsync(h->dv + (size_t)b * NV * 2 * P.Nx * 4, 0, sizeof(double) * NV * 2 * P.Nx * 4, h->stream));
+        CK(cudaMemsetAsync(h->u64 + (size_t)b * P.Nx * 4, 0, sizeof(double) * P.Nx * 4, h->stream));
+    }
     S.stp = 0.0;
     S.use_u = false;
     S.push = false;
@@ -663,6 +683,8 @@ int refill(sdca_handle *h, Queue &Qu)
         if (h->slots[b].phase != PH_EMPTY) continue;
         const int64_t k = (int64_t)Qu.next++;
         const float *x0 = nullptr;
+        if (Qu.x_init && h->form == SDCA_FORM_DUAL)
+            return fail(h, SDCA_E_UNSUPPORTED, "the dual form starts every locus from zero (no x_init)");
         if (Qu.x_init) {
             const double *xr = Qu.x_init + k * (QQ * h->P.L + Q);
             ref_to_engine(h->P, Qu.loci[k], xr, Qu.xbuf.data());
@@ -674,7 +696,7 @@ int refill(sdca_handle *h, Queue &Qu)
             // the copy reads the staging buffer: finish it before the next slot reuses it
             { const int r_ = stream_sync(h); if (r_) return r_; }
             warm.push_back(b);
-        } else if (h->ws_on) {
+        } else if (h->ws_on && h->form != SDCA_FORM_DUAL) {
             learned.push_back(b);
         }
     }
@@ -772,8 +794,12 @@ int phase_trials(sdca_handle *h, Queue &Qu)
         if (rc) return rc;
         {
             Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)lst.size());
-            launch_trial(P, h->sd, h->list, (int)lst.size(), h->lbase, h->u, h->rstate, h->w, h->R,
-                         h->acc, h->stream);
+            if (h->form == SDCA_FORM_DUAL)
+                launch_trial64(P, h->sd, h->list, (int)lst.size(), h->lbase, h->u64, h->rstate, h->w, h->R,
+                               h->acc, h->stream);
+            else
+                launch_trial(P, h->sd, h->list, (int)lst.size(), h->lbase, h->u, h->rstate, h->w, h->R,
+                             h->acc, h->stream);
         }
         CKL();
         rc = fetch_acc(h);
@@ -1199,6 +1225,351 @@ int phase_step(sdca_handle *h)
     return SDCA_OK;
 }
 
+// ---- dual form, phase B: accept, gradient through K rho, tests (the
+// max-norm test exactly, on the tensor cores, when the norm says it may
+// pass), history dots, direction.  The host logic is phase_step's; the
+// h parts of all vectors (eta) are kept here.
+
+double dot4h(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3]; }
+
+int phase_step_dual(sdca_handle *h)
+{
+    const Problem &P = h->P;
+    const int m = P.m;
+    const double gtol = h->cfg.gradient_threshold;
+    std::vector<int32_t> all, steps;
+    for (int b = 0; b < P.Bmax; ++b) {
+        SlotHost &S = h->slots[b];
+        if (S.phase == PH_READY_STEP) {
+            steps.push_back(b);
+            all.push_back(b);
+            S.push = true;
+            int pos = 0;
+            while (std::find(S.hist.begin(), S.hist.end(), pos) != S.hist.end()) ++pos;
+            S.ring_new = pos;
+        } else if (S.phase == PH_READY_INIT) {
+            all.push_back(b);
+            S.push = false;
+            S.ring_new = -1;
+        }
+    }
+    if (all.empty()) return SDCA_OK;
+    int rc;
+    if (!steps.empty()) {
+        if ((rc = upload_slots(h, steps))) return rc;
+        {
+            Timed t(h, SDCA_K_ACCEPT, 1, (int64_t)steps.size());
+            launch_dual_accept(P, h->sd, h->list, (int)steps.size(), h->dv, h->u64, h->lbase, h->stream);
+        }
+        CKL();
+        for (int b : steps) {
+            SlotHost &S = h->slots[b];
+            for (int a = 0; a < Q; ++a) {
+                const double xn = S.eta_x[a] + S.stp * S.eta_d[a];
+                if (S.ring_new >= 0) S.eta_s[S.ring_new][a] = xn - S.eta_x[a];
+                S.eta_x[a] = xn;
+            }
+        }
+    }
+    // gradient at the accepted points
+    if ((rc = upload_slots(h, all))) return rc;
+    CK(cudaMemsetAsync(h->csum, 0, sizeof(long long) * 16 * P.Bmax, h->stream));
+    CK(cudaMemsetAsync(h->amax, 0, sizeof(double) * 2 * P.Bmax, h->stream));
+    if ((rc = zero_acc(h))) return rc;
+    {
+        Timed t(h, SDCA_K_BACKWARD, 3, (int64_t)all.size());
+        launch_dual_gradient(P, h->sd, h->list, (int)all.size(), h->R, h->rstate, h->Kmat, h->qscale, h->rq, h->csum,
+                             h->KR, h->dv, h->acc, h->amax, h->stream);
+    }
+    CKL();
+    std::vector<double> amax(2 * P.Bmax);
+    CK(cudaMemcpyAsync(amax.data(), h->amax, sizeof(double) * 2 * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
+    if ((rc = fetch_acc(h))) return rc;
+
+    std::vector<int32_t> cont, fin, chk;
+    std::vector<char> stop(P.Bmax, 0), releps_stop(P.Bmax, 0);
+    for (int b : all) {
+        SlotHost &S = h->slots[b];
+        S.contractions++;
+        const int gn = 1 - S.gcur;
+        double eg[Q];
+        for (int a = 0; a < Q; ++a) eg[a] = S.rs[a] + 2.0 * P.lambda_h * S.eta_x[a];
+        const bool pushed = S.push && S.ring_new >= 0;
+        if (pushed)
+            for (int a = 0; a < Q; ++a) S.eta_y[S.ring_new][a] = eg[a] - S.eta_g[S.gcur][a];
+        for (int a = 0; a < Q; ++a) S.eta_g[gn][a] = eg[a];
+        S.gcur = gn;
+        S.g2 = acc_get(h, b, ACC_G2) + dot4h(eg, eg);
+        S.x2J = acc_get(h, b, ACC_X2J);
+        S.x2H = dot4h(S.eta_x, S.eta_x);
+        S.amax_g = amax[2 * b];
+        S.amax_x = amax[2 * b + 1];
+        const double gnorm = std::sqrt(std::max(S.g2, 0.0));
+        S.gmax = S.chk_ratio > 0.0 ? S.chk_ratio * gnorm : gnorm;   // estimate until checked
+        bool st = false;
+        if (S.phase == PH_READY_INIT) {
+            S.f += P.lambda_J * S.x2J + P.lambda_h * S.x2H;
+            S.nfeval = 1;
+        } else {
+            S.iterations++;
+            S.nfeval += 2 + S.trials;
+            const double *es = S.eta_s[S.ring_new >= 0 ? S.ring_new : 0];
+            const double *ey = S.eta_y[S.ring_new >= 0 ? S.ring_new : 0];
+            const double sy = acc_get(h, b, ACC_SY) + (pushed ? dot4h(es, ey) : 0.0);
+            const double yy = acc_get(h, b, ACC_YY) + (pushed ? dot4h(ey, ey) : 0.0);
+            const double ss = acc_get(h, b, ACC_SS) + (pushed ? dot4h(es, es) : 0.0);
+            if (pushed && sy > 1e-3 * std::sqrt(ss * yy) && yy > 0.0 && std::isfinite(sy) && std::isfinite(yy)) {
+                if ((int)S.hist.size() == m) S.hist.pop_front();
+                S.hist.push_back(S.ring_new);
+                S.gamma = sy / yy;
+                S.iter++;
+            } else {
+                S.ring_new = -1;
+                S.skipped++;
+            }
+            if (S.iterations > h->cfg.max_iterations) {
+                S.status = 1;
+                st = true;
+            } else if (S.stalled) {
+                S.status = 2;
+                st = true;
+            }
+        }
+        if (!std::isfinite(S.f) || !std::isfinite(S.g2)) {
+            S.status = -1;
+            st = true;
+        }
+        if (st) {
+            stop[b] = 1;
+            continue;
+        }
+        // the relative-norm stop, decided after the max-norm test as in the
+        // other forms (status 0 when both hold)
+        const double releps = 1e-4 * std::max(1.0, std::sqrt(S.x2J + S.x2H));
+        releps_stop[b] = gnorm < releps;
+        // the max-norm test needs J = Phi^T a_g: run it when the last check's
+        // ratio max|g| / ||g|| predicts a pass, and every 10 iterations
+        const bool due = S.iterations - S.last_check >= 10;
+        const bool near = S.chk_ratio > 0.0 && S.chk_ratio * gnorm < 1.5 * gtol;
+        if (due || near || gnorm < gtol || releps_stop[b]) chk.push_back(b);
+        else if (releps_stop[b]) {
+            S.status = 2;
+            stop[b] = 1;
+        }
+    }
+    if (!chk.empty()) {
+        double sc = 0.0;
+        for (int b : chk) sc = std::max(sc, h->slots[b].amax_g);
+        if ((rc = upload_slots(h, chk))) return rc;
+        if ((rc = zero_acc(h))) return rc;
+        {
+            Timed t(h, SDCA_K_BACKWARD, 5, (int64_t)chk.size());
+            launch_dual_to_r(P, h->sd, h->list, (int)chk.size(), 0, h->dv, h->Rchk, h->stream);
+            CK(tc_launch_bwd(h->tc, P, h->sd, h->list, (int)chk.size(), h->Rchk, (float)pow2_scale(sc), h->Rhi,
+                             h->Rlo, h->gpool, h->tc_err, h->stream));
+            launch_dual_gmax(P, h->sd, h->list, (int)chk.size(), h->gpool, h->acc, h->stream);
+        }
+        CKL();
+        if ((rc = fetch_acc(h))) return rc;
+        for (int b : chk) {
+            SlotHost &S = h->slots[b];
+            const double *eg = S.eta_g[S.gcur];
+            double gm = acc_get(h, b, ACC_GMAX);
+            for (int a = 0; a < Q; ++a) gm = std::max(gm, std::fabs(eg[a]));
+            const double gnorm = std::sqrt(std::max(S.g2, 0.0));
+            S.gmax = gm;
+            S.chk_ratio = gnorm > 0.0 ? gm / gnorm : 0.0;
+            S.last_check = S.iterations;
+            if (gm < gtol) {
+                S.status = 0;
+                stop[b] = 1;
+            } else if (releps_stop[b]) {
+                S.status = 2;
+                stop[b] = 1;
+            }
+        }
+    }
+    for (int b : all) (stop[b] ? fin : cont).push_back(b);
+
+    // Stopped slots: x in the engine layout (J = Phi^T a_x, J_rr = 0,
+    // h = eta_x), then the final evaluation.  J is formed exactly: the
+    // logits K a_x are O(1) while sum_j |K_ij a_j| is hundreds, so a rounding
+    // of a in the last bits of single precision would move the gradient at
+    // the reported x by far more than the threshold.
+    if (!fin.empty()) {
+        for (int b : fin) {
+            const double am = h->slots[b].amax_x;
+            h->sd_h[b].tc_scale = am > 0.0 ? std::ldexp(1.0, 32) / am : 1.0;
+            for (int a = 0; a < Q; ++a) h->sd_h[b].eta[a] = h->slots[b].eta_x[a];
+        }
+        if ((rc = upload_slots(h, fin))) return rc;
+        {
+            Timed t(h, SDCA_K_OTHER, 3 * 4 + 1, (int64_t)fin.size());
+            for (int d = 0; d < 3; ++d) {
+                launch_dual_digits(P, h->sd, h->list, (int)fin.size(), d, h->dv, h->Rchk, h->stream);
+                CK(tc_launch_bwd(h->tc, P, h->sd, h->list, (int)fin.size(), h->Rchk, 1.0f, h->Rhi, h->Rlo, h->gpool,
+                                 h->tc_err, h->stream));
+                launch_dual_digit_acc(P, h->sd, h->list, (int)fin.size(), d, h->gpool, h->J64, h->stream);
+            }
+            launch_dual_to_wa(P, h->sd, h->list, (int)fin.size(), h->J64, h->wa, h->stream);
+        }
+        CKL();
+        for (int b : fin) {
+            SlotHost &S = h->slots[b];
+            S.phase = PH_FINALIZE;
+            S.stp = 0.0;
+            S.use_u = false;
+        }
+    }
+    if (cont.empty()) return SDCA_OK;
+
+    std::vector<int32_t> withh;
+    for (int b : cont)
+        if (!h->slots[b].hist.empty()) withh.push_back(b);
+    if (!withh.empty()) {
+        if ((rc = upload_slots(h, withh))) return rc;
+        CK(cudaMemsetAsync(h->dots, 0, sizeof(double) * 4 * MAXHIST * P.Bmax, h->stream));
+        {
+            Timed t(h, SDCA_K_HISTORY, 1, (int64_t)withh.size());
+            launch_dual_dots(P, h->sd, h->list, (int)withh.size(), h->dv, h->dots, h->stream);
+        }
+        CKL();
+        CK(cudaMemcpyAsync(h->dots_h, h->dots, sizeof(double) * 4 * MAXHIST * P.Bmax, cudaMemcpyDeviceToHost,
+                           h->stream));
+        { const int r_ = stream_sync(h); if (r_) return r_; }
+    }
+    for (int b : cont) {
+        SlotHost &S = h->slots[b];
+        SlotDev &D = h->sd_h[b];
+        const int k = (int)S.hist.size();
+        const double *eg = S.eta_g[S.gcur];
+        D.coef_g = -1.0;
+        if (k > 0) {
+            double *dt = h->dots_h + (int64_t)b * 4 * MAXHIST;
+            for (int j = 0; j < k; ++j) {
+                const int pj = S.hist[j];
+                dt[j] += dot4h(S.eta_s[pj], eg);
+                dt[MAXHIST + j] += dot4h(S.eta_y[pj], eg);
+                if (S.ring_new >= 0) {
+                    dt[2 * MAXHIST + j] += dot4h(S.eta_s[pj], S.eta_y[S.ring_new]);
+                    dt[3 * MAXHIST + j] += dot4h(S.eta_y[pj], S.eta_y[S.ring_new]);
+                }
+            }
+            if (S.ring_new >= 0) {
+                const int pn = S.ring_new;
+                for (int j = 0; j < k; ++j) {
+                    const int pj = S.hist[j];
+                    S.SY[pj][pn] = dt[2 * MAXHIST + j];
+                    S.YY[pj][pn] = dt[3 * MAXHIST + j];
+                    S.YY[pn][pj] = dt[3 * MAXHIST + j];
+                }
+            }
+            double Rm[MAXHIST * MAXHIST], YYm[MAXHIST * MAXHIST], sg[MAXHIST], yg[MAXHIST];
+            for (int a = 0; a < k; ++a) {
+                sg[a] = dt[a];
+                yg[a] = dt[MAXHIST + a];
+                for (int c = 0; c < k; ++c) {
+                    Rm[a * k + c] = (a <= c) ? S.SY[S.hist[a]][S.hist[c]] : 0.0;
+                    YYm[a * k + c] = S.YY[S.hist[a]][S.hist[c]];
+                }
+            }
+            double cg, cS[MAXHIST], cY[MAXHIST];
+            if (lbfgs_compact_coeffs(k, Rm, YYm, sg, yg, S.gamma, &cg, cS, cY)) {
+                D.coef_g = cg;
+                for (int a = 0; a < k; ++a) {
+                    D.coefS[a] = cS[a];
+                    D.coefY[a] = cY[a];
+                }
+            } else {
+                S.hist.clear();
+                S.iter = 0;
+            }
+        }
+    }
+    auto set_eta_d = [&](int b) {
+        SlotHost &S = h->slots[b];
+        SlotDev &D = h->sd_h[b];
+        const double *eg = S.eta_g[S.gcur];
+        for (int a = 0; a < Q; ++a) {
+            double v = D.coef_g * eg[a];
+            for (size_t j = 0; j < S.hist.size(); ++j)
+                v += D.coefS[j] * S.eta_s[S.hist[j]][a] + D.coefY[j] * S.eta_y[S.hist[j]][a];
+            S.eta_d[a] = v;
+            D.eta[a] = v;
+        }
+    };
+    std::vector<double> dg0(P.Bmax, 0.0);
+    auto run_direction = [&](const std::vector<int32_t> &lst) -> int {
+        for (int b : lst) {
+            SlotHost &S = h->slots[b];
+            SlotDev &D = h->sd_h[b];
+            D.nhist = (int)S.hist.size();
+            for (int j = 0; j < D.nhist; ++j) D.ring[j] = S.hist[j];
+            D.gcur = S.gcur;
+            set_eta_d(b);
+        }
+        int r2 = staged_h2d(h, h->sd, h->sd_h, sizeof(SlotDev) * P.Bmax);
+        if (r2) return r2;
+        if ((r2 = upload_list(h, lst))) return r2;
+        if ((r2 = zero_acc(h))) return r2;
+        {
+            Timed t(h, SDCA_K_DIRECTION, 1, (int64_t)lst.size());
+            launch_dual_direction(P, h->sd, h->list, (int)lst.size(), h->dv, h->R, h->u64, h->acc, h->stream);
+        }
+        CKL();
+        if ((r2 = fetch_acc(h))) return r2;
+        for (int b : lst) {
+            SlotHost &S = h->slots[b];
+            const double *eg = S.eta_g[S.gcur];
+            S.gd = acc_get(h, b, ACC_GD) + dot4h(eg, S.eta_d);
+            S.ddJ = acc_get(h, b, ACC_DDJ);
+            S.ddH = dot4h(S.eta_d, S.eta_d);
+            S.xdJ = acc_get(h, b, ACC_XDJ);
+            S.xdH = dot4h(S.eta_x, S.eta_d);
+            dg0[b] = acc_get(h, b, ACC_DG0);
+        }
+        return SDCA_OK;
+    };
+    if ((rc = run_direction(cont))) return rc;
+    std::vector<int32_t> restart;
+    for (int b : cont) {
+        SlotHost &S = h->slots[b];
+        const double releps = 1e-4 * std::max(1.0, std::sqrt(S.x2J + S.x2H));
+        if (!S.hist.empty() && (S.force_restart || !(S.gd <= -1e-4 * releps))) restart.push_back(b);
+        S.force_restart = false;
+    }
+    std::vector<char> restarted(P.Bmax, 0);
+    if (!restart.empty()) {
+        for (int b : restart) {
+            h->slots[b].hist.clear();
+            h->slots[b].iter = 0;
+            h->slots[b].restarts++;
+            h->sd_h[b].coef_g = -1.0;
+            restarted[b] = 1;
+        }
+        if ((rc = run_direction(restart))) return rc;
+    }
+    for (int b : cont) {
+        SlotHost &S = h->slots[b];
+        const double alpha_init = restarted[b] ? 1.0 : 1.0 / std::sqrt(S.g2);
+        S.trials = 0;
+        S.use_u = true;
+        S.push = false;
+        const double d0 = dg0[b] + dl2_along(P, S, 0.0);
+        if (S.ls.start(S.f, d0, alpha_init) == MoreThuente::NEED_EVAL) {
+            S.stp = S.ls.stp;
+            S.phase = PH_LS;
+        } else {
+            S.stp = 0.0;
+            S.phase = PH_FINAL_EVAL;
+            if (S.hist.empty()) S.stalled = true;
+            else S.force_restart = true;
+            S.weak++;
+        }
+    }
+    return SDCA_OK;
+}
+
 int check_ready(sdca_handle *h)
 {
     if (!h) return SDCA_E_ARG;
@@ -1245,8 +1616,10 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
         return fail(nullptr, SDCA_E_ARG, "history must be in 1..10");
     if (cfg->batch < 1 || cfg->batch > 4096) return fail(nullptr, SDCA_E_ARG, "batch must be in 1..4096");
     if (cfg->gap_state < -1 || cfg->gap_state >= Q) return fail(nullptr, SDCA_E_ARG, "gap_state out of range");
-    if (cfg->form != SDCA_FORM_GATHER && cfg->form != SDCA_FORM_TC)
+    if (cfg->form != SDCA_FORM_GATHER && cfg->form != SDCA_FORM_TC && cfg->form != SDCA_FORM_DUAL)
         return fail(nullptr, SDCA_E_UNSUPPORTED, "unknown contraction form");
+    if (cfg->form == SDCA_FORM_DUAL && cfg->n_seqs > 16383)
+        return fail(nullptr, SDCA_E_UNSUPPORTED, "the dual form supports at most 16383 sequences");
     if (!(cfg->gradient_threshold >= 0.0) || cfg->max_iterations < 0)
         return fail(nullptr, SDCA_E_ARG, "invalid stopping criteria");
     int ndev = 0;
@@ -1286,7 +1659,7 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
         P.LC = round_up((P.L + want - 1) / want, 32);
         P.LC = std::max<int64_t>(P.LC, 512);
         P.Cg = (P.L + P.LC - 1) / P.LC;
-        P.C = std::max<int64_t>(P.Cg, cfg->form == SDCA_FORM_TC ? 24 : 1);
+        P.C = std::max<int64_t>(P.Cg, cfg->form != SDCA_FORM_GATHER ? 24 : 1);
     }
     h->form = cfg->form;
     if (const char *e = std::getenv("SDCA_REFRESH_EVERY")) h->refresh_every = std::max(1, std::atoi(e));
@@ -1296,6 +1669,11 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
     int rc = SDCA_OK;
     const size_t B = P.Bmax;
     const size_t hsz = h->hist_bf16 ? 2 : 4;
+    const bool dual = h->form == SDCA_FORM_DUAL;
+    const bool tcres = h->form != SDCA_FORM_GATHER;   // the dual form uses the tensor-core backward too
+    // the dual form keeps its history as N x 4 coefficient pairs, not as D-vectors
+    const size_t hist_bytes = dual ? 256 : B * P.ring * P.Dp * hsz;
+    const size_t NV = DV_S + 2 * (size_t)P.ring;
     if ((rc = dalloc(h, &h->X, (size_t)P.N * P.Lx)) || (rc = dalloc(h, &h->XT, (size_t)P.L * P.Nx)) ||
         (rc = dalloc(h, &h->w, (size_t)P.Nx)) || (rc = dalloc(h, &h->rstate, B * P.Nx)) ||
         (rc = dalloc(h, &h->wa, B * P.Dp)) || (rc = dalloc(h, &h->d, B * P.Dp)) ||
@@ -1306,13 +1684,18 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
         (rc = dalloc(h, &h->rows, B * P.L)) || (rc = dalloc(h, &h->acc, B * NACC)) ||
         (rc = dalloc(h, &h->dots, B * 4 * MAXHIST)) || (rc = dalloc(h, &h->sd, B)) ||
         (rc = dalloc(h, &h->list, B)) || (rc = dalloc(h, &h->flag, 4)) ||
-        (rc = dalloc(h, reinterpret_cast<uint8_t **>(&h->Spool), B * P.ring * P.Dp * hsz)) ||
-        (rc = dalloc(h, reinterpret_cast<uint8_t **>(&h->Ypool), B * P.ring * P.Dp * hsz)) ||
+        (rc = dalloc(h, reinterpret_cast<uint8_t **>(&h->Spool), hist_bytes)) ||
+        (rc = dalloc(h, reinterpret_cast<uint8_t **>(&h->Ypool), hist_bytes)) ||
         (rc = halloc(h, &h->sd_h, B)) || (rc = halloc(h, &h->list_h, B)) ||
         (rc = halloc(h, &h->acc_h, B * NACC)) || (rc = halloc(h, &h->dots_h, B * 4 * MAXHIST)) ||
         (rc = halloc(h, &h->rows_h, B * P.L)) || (rc = halloc(h, &h->flag_h, 4)) ||
         (rc = halloc(h, &h->stage, (h->stage_cap = 64 * (((sizeof(SlotDev) + 4) * B + 1024 + 255) & ~(size_t)255)))) ||
-        (h->form == SDCA_FORM_TC &&
+        (dual && ((rc = dalloc(h, &h->dv, B * NV * 2 * P.Nx * 4)) || (rc = dalloc(h, &h->u64, B * P.Nx * 4)) ||
+                  (rc = dalloc(h, &h->KR, B * P.Nx * 4)) || (rc = dalloc(h, &h->amax, 2 * B)) ||
+                  (rc = dalloc(h, &h->rq, B * P.Nx * 4)) || (rc = dalloc(h, &h->csum, 16 * B)) ||
+                  (rc = dalloc(h, &h->Rchk, B * P.Nx * 4)) || (rc = dalloc(h, &h->J64, B * P.Dp)) ||
+                  (rc = dalloc(h, &h->Kmat, (size_t)P.Nx * P.Nx)))) ||
+        (tcres &&
          ((rc = dalloc(h, &h->Dhi, 4 * B * (size_t)round_up(4 * P.L, 64))) ||
           (rc = dalloc(h, &h->Dlo, 4 * B * (size_t)round_up(4 * P.L, 64))) ||
           (rc = dalloc(h, &h->Rhi, 4 * B * (size_t)P.Nx)) || (rc = dalloc(h, &h->Rlo, 4 * B * (size_t)P.Nx)) ||
@@ -1329,12 +1712,12 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
         delete h;
         return fail(nullptr, SDCA_E_CUDA, "initialisation failed");
     }
-    if (h->form == SDCA_FORM_TC) {
+    if (tcres) {
         int major = 0, minor = 0;
         cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, cfg->device);
         cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, cfg->device);
         std::string why;
-        if (major != 10 || minor != 3) why = "the tensor-core form needs an sm_103 (GB300) device";
+        if (major != 10 || minor != 3) why = "the tensor-core and dual forms need an sm_103 (GB300) device";
         else if (tc_configure() != cudaSuccess) why = "could not reserve the tensor-core kernel's shared memory";
         else if (!(h->tc = tc_plan_create(P, h->X, h->XT, h->Dhi, h->Dlo, h->Rhi, h->Rlo, round_up(4 * P.L, 64))))
             why = "TMA tensor-map encoding failed";
@@ -1387,6 +1770,34 @@ int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weig
     }
     P.lambda_J = (h->cfg.lambda_J < 0.0) ? autol * beff / 2.0 : h->cfg.lambda_J * beff;
     P.lambda_h = (h->cfg.lambda_h < 0.0) ? autol * beff : h->cfg.lambda_h * beff;
+    if (h->form == SDCA_FORM_DUAL) {
+        // K_ij = loci where sequences i and j agree; rho is rounded to QB
+        // fractional bits of w_max so that |sum_j K_ij rho_q| < 2^62
+        const int64_t W = (P.L + 31) / 32;
+        uint64_t *packed = nullptr;
+        int32_t *dist = nullptr;
+        if (cudaMalloc(&packed, sizeof(uint64_t) * P.N * W) != cudaSuccess ||
+            cudaMalloc(&dist, sizeof(int32_t) * P.N * P.N) != cudaSuccess) {
+            cudaGetLastError();
+            if (packed) cudaFree(packed);
+            h->has_alignment = false;
+            return fail(h, SDCA_E_NOMEM, "device allocation for the agreement matrix failed");
+        }
+        launch_distances(h->X, P.Lx, (int)P.N, (int)P.L, packed, dist, h->stream);
+        launch_dual_kmat(dist, (int)P.N, P.Nx, (int)P.L, h->Kmat, h->stream);
+        const cudaError_t e1 = cudaGetLastError();
+        const cudaError_t e2 = cudaStreamSynchronize(h->stream);
+        cudaFree(packed);
+        cudaFree(dist);
+        if (e1 != cudaSuccess || e2 != cudaSuccess) {
+            h->has_alignment = false;
+            return fail(h, SDCA_E_CUDA, std::string("agreement matrix: ") + cudaGetErrorString(e1 ? e1 : e2));
+        }
+        double wmax = 0.0;
+        for (int64_t i = 0; i < P.N; ++i) wmax = std::max(wmax, weights[i]);
+        const int qb = std::min(30, 62 - (int)std::ceil(std::log2((double)P.N * (double)P.L + 1.0)));
+        h->qscale = wmax > 0.0 ? std::ldexp(1.0, qb) / wmax : 1.0;
+    }
     h->has_alignment = true;
     h->prof.h2d_bytes = (int64_t)P.N * P.L + (int64_t)sizeof(double) * P.N;
     return SDCA_OK;
@@ -1434,7 +1845,7 @@ int sdca_solve_ex(sdca_handle *h, const uint32_t *loci, size_t n_loci, const dou
         if (!any) break;
         rc = phase_trials(h, Qu);
         if (rc) return rc;
-        rc = phase_step(h);
+        rc = h->form == SDCA_FORM_DUAL ? phase_step_dual(h) : phase_step(h);
         if (rc) return rc;
     }
     CK(cudaEventRecord(t1, h->stream));
@@ -1574,6 +1985,8 @@ int sdca_set_warm_start(sdca_handle *h, const float *params, size_t n_params)
         h->ws_on = false;
         return SDCA_OK;
     }
+    if (h->form == SDCA_FORM_DUAL)
+        return fail(h, SDCA_E_UNSUPPORTED, "the dual form starts every locus from zero (no warm start)");
     if (n_params != (size_t)MLP_BLOB_SIZE)
         return fail(h, SDCA_E_ARG, "warm-start parameters: expected " + std::to_string(MLP_BLOB_SIZE) + " floats");
     if (params[MLP_VERSION] != (float)MLP_BLOB_VERSION)

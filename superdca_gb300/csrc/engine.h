@@ -83,7 +83,12 @@ struct SlotDev {
     double rs[Q];           // R sums at the accepted point (h gradient)
     double tc_scale;        // power of two applied to d before the fp16 hi/lo split
     double tc_inv_scale;
+    double eta[Q];          // dual form: h part of the direction (trial logits) or of x (final layout)
 };
+
+// dual form: per slot, vectors (a, k = K a) of N x 4 doubles each:
+// x, d, two gradients, then the s ring and the y ring (P.ring positions each)
+constexpr int DV_X = 0, DV_D = 1, DV_G = 2, DV_S = 4;
 
 enum SlotFlags {
     SLOT_F_USE_U = 1,       // trial logits use lbase + stp u (else lbase)
@@ -146,6 +151,32 @@ void launch_score(const Problem &P, const SlotDev *sd, const int32_t *list, int 
                   const float *wa, int gap, float *rows, cudaStream_t st);
 
 // sequence reweighting (kernels_weights.cu)
+void launch_trial64(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                    const double *lbase, const double *u, const uint8_t *rstate, const double *w,
+                    float *R, double *acc, cudaStream_t st);
+
+// dual form (kernels_dual.cu)
+void launch_dual_kmat(const int32_t *dist, int N, int64_t Nx, int L, int32_t *K, cudaStream_t st);
+void launch_dual_gradient(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *R,
+                          const uint8_t *rstate, const int32_t *K, double qscale, int32_t *rq, long long *csum,
+                          double *KR, double *dv, double *acc, double *amax, cudaStream_t st);
+void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *dv,
+                      double *dots, cudaStream_t st);
+void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
+                           const float *R, double *u, double *acc, cudaStream_t st);
+void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
+                        const double *u, double *lbase, cudaStream_t st);
+void launch_dual_to_r(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int which,
+                      const double *dv, float *R, cudaStream_t st);
+void launch_dual_gmax(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *gpool,
+                      double *acc, cudaStream_t st);
+void launch_dual_digits(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d, const double *dv,
+                        float *R, cudaStream_t st);
+void launch_dual_digit_acc(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d,
+                           const float *gpool, double *J64, cudaStream_t st);
+void launch_dual_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *J64,
+                       float *wa, cudaStream_t st);
+
 // warm start (mlp.cu, warmstart.cu)
 void mlp_infer(const float *p_dev, const float *X, int64_t M, float *Xn, float *h1, float *h2, float *out,
                cudaStream_t st);

@@ -14,6 +14,12 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
+__device__ __forceinline__ double warp_max_d(double v)
+{
+    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+    return v;
+}
+
 __device__ __forceinline__ float warp_max(float v)
 {
 #pragma unroll

@@ -1,0 +1,482 @@
+// kernels_dual.cu -- the per-locus solve in the span of the sequences.
+//
+// For target locus r let phi_i be sequence i's one-hot features over the
+// loci n != r (4 per locus).  The logits are l_i = h + J^T phi_i, and from
+// x = 0 every L-BFGS vector of SuperDCA's solve (gradient, direction, steps,
+// gradient differences) has the form v = (Phi^T a_v, eta_v) with a_v an
+// N x 4 coefficient matrix and eta_v a 4-vector: the J gradient is
+// Phi^T rho + 2 lambda_J J with rho_i = w_i (p_i - onehot(s_i(r))), and the
+// iteration only forms linear combinations.  With K = Phi Phi^T
+// (K_ij = number of loci n != r where s_i(n) = s_j(n)) a vector's logit
+// image is K a_v + eta_v and inner products are a_v . K a_w + eta_v . eta_w.
+// So the same iteration runs on N x 4 coefficients; a vector is kept as the
+// pair (a, k = K a) in FP64 and its eta on the host.
+//
+// The one product per iteration, K rho, is exact: rho is rounded to integers
+// rho_q = round(rho * 2^QB / w_max) (the rounded value is the one used, so
+// the pair (a, K a) stays consistent), K is an integer matrix, and the sums
+// are taken in 64-bit integers; QB keeps them below 2^62.  K = K_all minus
+// the agreement at r itself, a class sum per state of r.
+#include <cstdint>
+
+#include "engine.h"
+#include "kernels_common.cuh"
+
+namespace sdca {
+namespace {
+
+__global__ void k_dual_kmat(const int32_t *__restrict__ dist, int N, int64_t Nx, int L, int32_t *__restrict__ K)
+{
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < Nx * Nx; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / Nx, j = t % Nx;
+        K[t] = (i < N && j < N) ? L - dist[i * N + j] : 0;
+    }
+}
+
+// rho_q = round(R * qscale); class sums csum[b][a][c] = sum over i with s_i(r) = a
+__global__ void __launch_bounds__(256)
+k_dual_quant(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int N, int64_t Nx,
+             const float4 *__restrict__ R, const uint8_t *__restrict__ rstate, double qscale, int4 *__restrict__ rq,
+             unsigned long long *__restrict__ csum)
+{
+    const int b = list[blockIdx.y];
+    __shared__ unsigned long long red[16];
+    if (threadIdx.x < 16) red[threadIdx.x] = 0ull;
+    __syncthreads();
+    long long cs[4][4] = {};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Nx; i += (int64_t)gridDim.x * blockDim.x) {
+        int4 q = make_int4(0, 0, 0, 0);
+        if (i < N) {
+            const float4 v = R[(int64_t)b * Nx + i];
+            q = make_int4((int)llrint((double)v.x * qscale), (int)llrint((double)v.y * qscale),
+                          (int)llrint((double)v.z * qscale), (int)llrint((double)v.w * qscale));
+            const int y = rstate[(int64_t)b * Nx + i] & 3;
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                if (a != y) continue;
+                cs[a][0] += q.x; cs[a][1] += q.y; cs[a][2] += q.z; cs[a][3] += q.w;
+            }
+        }
+        rq[(int64_t)b * Nx + i] = q;
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            long long v = cs[a][c];
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if ((threadIdx.x & 31) == 0 && v != 0) atomicAdd(&red[a * 4 + c], (unsigned long long)v);
+        }
+    __syncthreads();
+    if (threadIdx.x < 16 && red[threadIdx.x] != 0ull) atomicAdd(csum + (int64_t)b * 16 + threadIdx.x, red[threadIdx.x]);
+}
+
+constexpr int KP_M = 64;   // rows (sequences i) per CTA
+constexpr int KP_S = 16;   // slots per CTA (64 columns: 16 slots x 4 states)
+constexpr int KP_J = 16;   // sequences j per shared-memory stage
+
+// KR[b][i][c] = (sum_j K_ij rho_q[b][j][c] - csum[b][s_i(r)][c]) / qscale
+__global__ void __launch_bounds__(256)
+k_dual_kprod(const int32_t *__restrict__ K, int64_t Nx, int N, const int32_t *__restrict__ list, int nlist,
+             const int4 *__restrict__ rq, const long long *__restrict__ csum, const uint8_t *__restrict__ rstate,
+             double inv_qscale, double *__restrict__ KR)
+{
+    __shared__ __align__(16) int32_t sK[KP_J][KP_M];
+    __shared__ __align__(16) int32_t sR[KP_J][KP_S * 4];
+    const int t = threadIdx.x;
+    const int ty = t >> 4, tx = t & 15;
+    const int64_t i0 = (int64_t)blockIdx.x * KP_M;
+    const int s0 = blockIdx.y * KP_S;
+    const int my_slot = (s0 + tx < nlist) ? list[s0 + tx] : -1;
+    const int ld_jj = t >> 4, ld_part = t & 15;
+    const int ld_slot = my_slot;  // the loader of sR row ld_jj, slot column ld_part = tx
+    long long acc[4][4] = {};
+    for (int64_t j0 = 0; j0 < Nx; j0 += KP_J) {
+        *reinterpret_cast<int4 *>(&sK[ld_jj][ld_part * 4]) =
+            *reinterpret_cast<const int4 *>(K + (j0 + ld_jj) * Nx + i0 + ld_part * 4);
+        int4 rv = make_int4(0, 0, 0, 0);
+        if (ld_slot >= 0) rv = rq[(int64_t)ld_slot * Nx + j0 + ld_jj];
+        *reinterpret_cast<int4 *>(&sR[ld_jj][ld_part * 4]) = rv;
+        __syncthreads();
+#pragma unroll
+        for (int jj = 0; jj < KP_J; ++jj) {
+            const int4 kv = *reinterpret_cast<const int4 *>(&sK[jj][ty * 4]);
+            const int4 r4 = *reinterpret_cast<const int4 *>(&sR[jj][tx * 4]);
+            const int k[4] = {kv.x, kv.y, kv.z, kv.w};
+            const int r[4] = {r4.x, r4.y, r4.z, r4.w};
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) acc[a][c] += (long long)k[a] * (long long)r[c];
+        }
+        __syncthreads();
+    }
+    if (my_slot < 0) return;
+    const int b = my_slot;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int64_t i = i0 + ty * 4 + a;
+        double *o = KR + ((int64_t)b * Nx + i) * 4;
+        if (i >= N) {
+            o[0] = o[1] = o[2] = o[3] = 0.0;
+            continue;
+        }
+        const int y = rstate[(int64_t)b * Nx + i] & 3;
+        const long long *cs = csum + (int64_t)b * 16 + y * 4;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) o[c] = (double)(acc[a][c] - cs[c]) * inv_qscale;
+    }
+}
+
+__device__ __forceinline__ int64_t dvo(int64_t b, int v, int part, int NV, int64_t Nx)
+{
+    return (((b * NV + v) * 2 + part) * Nx) * 4;
+}
+
+// new gradient (a, k) = (rho_q / qscale + 2 lambda_J a_x, K rho + 2 lambda_J k_x),
+// y = g_new - g_old into the history when the slot pushes a pair;
+// J-part sums: g.g, x.x, s.y, y.y, s.s; max |a_g| and max |a_x|
+__global__ void __launch_bounds__(256)
+k_dual_grad(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
+            double lambda_J, const int32_t *__restrict__ rq, double inv_qscale, const double *__restrict__ KR,
+            double *__restrict__ dv, double *__restrict__ acc, double *__restrict__ amax)
+{
+    const int b = list[blockIdx.y];
+    const SlotDev &S = sd[b];
+    const bool push = (S.flags & SLOT_F_PUSH) && S.ring_new >= 0;
+    const double l2 = 2.0 * lambda_J;
+    const double *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = dv + dvo(b, DV_X, 1, NV, Nx);
+    const double *ago = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kgo = dv + dvo(b, DV_G + S.gcur, 1, NV, Nx);
+    double *agn = dv + dvo(b, DV_G + 1 - S.gcur, 0, NV, Nx), *kgn = dv + dvo(b, DV_G + 1 - S.gcur, 1, NV, Nx);
+    const int ps = push ? S.ring_new : 0;
+    const double *as = dv + dvo(b, DV_S + ps, 0, NV, Nx), *ks = dv + dvo(b, DV_S + ps, 1, NV, Nx);
+    double *ay = dv + dvo(b, DV_S + ring + ps, 0, NV, Nx), *ky = dv + dvo(b, DV_S + ring + ps, 1, NV, Nx);
+    double g2 = 0, x2 = 0, sy = 0, yy = 0, ss = 0, mg = 0, mx = 0;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
+        const double a_x = ax[e], k_x = kx[e];
+        const double a_g = (double)rq[(int64_t)b * Nx * 4 + e] * inv_qscale + l2 * a_x;
+        const double k_g = KR[(int64_t)b * Nx * 4 + e] + l2 * k_x;
+        g2 += a_g * k_g;
+        x2 += a_x * k_x;
+        mg = fmax(mg, fabs(a_g));
+        mx = fmax(mx, fabs(a_x));
+        if (push) {
+            const double a_y = a_g - ago[e], k_y = k_g - kgo[e];
+            ay[e] = a_y;
+            ky[e] = k_y;
+            const double a_s = as[e], k_s = ks[e];
+            sy += a_s * k_y;
+            yy += a_y * k_y;
+            ss += a_s * k_s;
+        }
+        agn[e] = a_g;
+        kgn[e] = k_g;
+    }
+    double v[5] = {g2, x2, sy, yy, ss};
+    const int idx[5] = {ACC_G2, ACC_X2J, ACC_SY, ACC_YY, ACC_SS};
+    block_sum_atomic<5>(v, acc + (int64_t)b * NACC, idx);
+    mg = warp_max_d(mg);
+    mx = warp_max_d(mx);
+    if ((threadIdx.x & 31) == 0) {
+        if (mg > 0.0) atomic_max_nonneg(amax + 2 * b, mg);
+        if (mx > 0.0) atomic_max_nonneg(amax + 2 * b + 1, mx);
+    }
+}
+
+// J-part dots of the history with the gradient and with the newest y:
+// dots[b][j] = a_sj . k_g, [MAXHIST + j] = a_yj . k_g,
+// [2 MAXHIST + j] = a_sj . k_ynew, [3 MAXHIST + j] = a_yj . k_ynew
+__global__ void __launch_bounds__(256)
+k_dual_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
+            const double *__restrict__ dv, double *__restrict__ dots)
+{
+    const int b = list[blockIdx.y];
+    const SlotDev &S = sd[b];
+    const int k = S.nhist;
+    const bool ynew = S.ring_new >= 0;
+    const double *kg = dv + dvo(b, DV_G + S.gcur, 1, NV, Nx);
+    const double *kyn = dv + dvo(b, DV_S + ring + (ynew ? S.ring_new : 0), 1, NV, Nx);
+    double s[4 * MAXHIST];
+#pragma unroll
+    for (int q = 0; q < 4 * MAXHIST; ++q) s[q] = 0.0;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
+        const double g = kg[e], yn = ynew ? kyn[e] : 0.0;
+#pragma unroll
+        for (int j = 0; j < MAXHIST; ++j) {
+            if (j >= k) break;
+            const double as = dv[dvo(b, DV_S + S.ring[j], 0, NV, Nx) + e];
+            const double ay = dv[dvo(b, DV_S + ring + S.ring[j], 0, NV, Nx) + e];
+            s[j] += as * g;
+            s[MAXHIST + j] += ay * g;
+            s[2 * MAXHIST + j] += as * yn;
+            s[3 * MAXHIST + j] += ay * yn;
+        }
+    }
+    __shared__ double red[4 * MAXHIST];
+    if (threadIdx.x < 4 * MAXHIST) red[threadIdx.x] = 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4 * MAXHIST; ++q) {
+        if ((q % MAXHIST) >= k) continue;
+        const double v = warp_sum(s[q]);
+        if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(&red[q], v);
+    }
+    __syncthreads();
+    if (threadIdx.x < 4 * MAXHIST && red[threadIdx.x] != 0.0)
+        atomicAdd(dots + (int64_t)b * 4 * MAXHIST + threadIdx.x, red[threadIdx.x]);
+}
+
+// d = coef_g g + sum_j coefS_j s_j + coefY_j y_j (a and k parts); trial
+// logits direction u = k_d + eta_d; sums g.d, d.d, x.d (J parts) and the
+// slope of the search line at 0 from the trial's own numbers, sum_i R_i . u_i
+__global__ void __launch_bounds__(256)
+k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int N, int NV,
+                 int ring, double *__restrict__ dv, const float4 *__restrict__ R, double *__restrict__ u,
+                 double *__restrict__ acc)
+{
+    const int b = list[blockIdx.y];
+    const SlotDev &S = sd[b];
+    const int k = S.nhist;
+    const double *ag = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kg = dv + dvo(b, DV_G + S.gcur, 1, NV, Nx);
+    const double *ax = dv + dvo(b, DV_X, 0, NV, Nx);
+    double *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = dv + dvo(b, DV_D, 1, NV, Nx);
+    double gd = 0, dd = 0, xd = 0, dg0 = 0;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
+        double a = S.coef_g * ag[e], kk = S.coef_g * kg[e];
+#pragma unroll
+        for (int j = 0; j < MAXHIST; ++j) {
+            if (j >= k) break;
+            const int64_t os = dvo(b, DV_S + S.ring[j], 0, NV, Nx), oy = dvo(b, DV_S + ring + S.ring[j], 0, NV, Nx);
+            const int64_t part = Nx * 4;
+            a += S.coefS[j] * dv[os + e] + S.coefY[j] * dv[oy + e];
+            kk += S.coefS[j] * dv[os + part + e] + S.coefY[j] * dv[oy + part + e];
+        }
+        ad[e] = a;
+        kd[e] = kk;
+        gd += ag[e] * kk;
+        dd += a * kk;
+        xd += ax[e] * kk;
+        const int c = (int)(e & 3);
+        const double uu = kk + S.eta[c];
+        u[(int64_t)b * Nx * 4 + e] = uu;
+        if (e / 4 < N) {
+            const float4 r = R[(int64_t)b * Nx + e / 4];
+            const float rc = c == 0 ? r.x : c == 1 ? r.y : c == 2 ? r.z : r.w;
+            dg0 += (double)rc * uu;
+        }
+    }
+    double v[4] = {gd, dd, xd, dg0};
+    const int idx[4] = {ACC_GD, ACC_DDJ, ACC_XDJ, ACC_DG0};
+    block_sum_atomic<4>(v, acc + (int64_t)b * NACC, idx);
+}
+
+// x += stp d (a and k parts), s = x_new - x_old into the history on a push,
+// logits lbase += stp u
+__global__ void __launch_bounds__(256)
+k_dual_accept(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int NV,
+              double *__restrict__ dv, const double *__restrict__ u, double *__restrict__ lbase)
+{
+    const int b = list[blockIdx.y];
+    const SlotDev &S = sd[b];
+    const double stp = S.stp;
+    const bool push = (S.flags & SLOT_F_PUSH) && S.ring_new >= 0;
+    double *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = dv + dvo(b, DV_X, 1, NV, Nx);
+    const double *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = dv + dvo(b, DV_D, 1, NV, Nx);
+    double *as = dv + dvo(b, DV_S + (push ? S.ring_new : 0), 0, NV, Nx);
+    double *ks = dv + dvo(b, DV_S + (push ? S.ring_new : 0), 1, NV, Nx);
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
+        const double a0 = ax[e], k0 = kx[e];
+        const double a1 = a0 + stp * ad[e], k1 = k0 + stp * kd[e];
+        ax[e] = a1;
+        kx[e] = k1;
+        if (push) {
+            as[e] = a1 - a0;
+            ks[e] = k1 - k0;
+        }
+        lbase[(int64_t)b * Nx * 4 + e] += stp * u[(int64_t)b * Nx * 4 + e];
+    }
+}
+
+// FP32 copy of a vector's a part (the current gradient, or x) as the R rows
+// of a tensor-core backward contraction, scaled by `scale`
+__global__ void k_dual_to_r(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int N,
+                            int NV, int which, const double *__restrict__ dv, float4 *__restrict__ R)
+{
+    const int b = list[blockIdx.y];
+    const int v = which == 0 ? DV_G + sd[b].gcur : DV_X;
+    const double *a = dv + dvo(b, v, 0, NV, Nx);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Nx; i += (int64_t)gridDim.x * blockDim.x) {
+        float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i < N) r = make_float4((float)a[4 * i], (float)a[4 * i + 1], (float)a[4 * i + 2], (float)a[4 * i + 3]);
+        R[(int64_t)b * Nx + i] = r;
+    }
+}
+
+// Digit d (0: high) of a_x rounded to 32 bits of the slot's scale (the
+// slot's tc_scale field): A = round(a qa), A = D0 2^22 + D1 2^11 + D2 with
+// |D| <= 2^10.  Digits are exact in fp16 and their sums over fewer than
+// 2^14 sequences are exact in FP32, so X^T D is exact on the tensor cores.
+__global__ void k_dual_digits(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int N,
+                              int NV, int d, const double *__restrict__ dv, float4 *__restrict__ R)
+{
+    const int b = list[blockIdx.y];
+    const double qa = sd[b].tc_scale;
+    const double *a = dv + dvo(b, DV_X, 0, NV, Nx);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Nx; i += (int64_t)gridDim.x * blockDim.x) {
+        float v[4] = {0.f, 0.f, 0.f, 0.f};
+        if (i < N) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const long long A = llrint(a[4 * i + c] * qa);
+                const long long d0 = (A + (1ll << 21)) >> 22;          // round(A / 2^22)
+                const long long r0 = A - (d0 << 22);
+                const long long d1 = (r0 + (1ll << 10)) >> 11;         // round(r0 / 2^11)
+                const long long d2 = r0 - (d1 << 11);
+                v[c] = (float)(d == 0 ? d0 : d == 1 ? d1 : d2);
+            }
+        }
+        R[(int64_t)b * Nx + i] = make_float4(v[0], v[1], v[2], v[3]);
+    }
+}
+
+// J64 (=, or +=) weight * (X^T D) from the tensor-core backward output
+__global__ void k_dual_digit_acc(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Dp,
+                                 int d, const float *__restrict__ gpool, double *__restrict__ J64)
+{
+    const int b = list[blockIdx.y];
+    const SlotDev &S = sd[b];
+    const float *g = gpool + (int64_t)(2 * b + 1 - S.gcur) * Dp;
+    const double wgt = ldexp(1.0, d == 0 ? 22 : d == 1 ? 11 : 0) / S.tc_scale;
+    double *o = J64 + (int64_t)b * Dp;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Dp; e += (int64_t)gridDim.x * blockDim.x)
+        o[e] = (d == 0 ? 0.0 : o[e]) + (double)g[e] * wgt;
+}
+
+// max |Phi^T a| over the J blocks n != r, from the tensor-core backward output
+__global__ void k_dual_gmax(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int L, int64_t Dp,
+                            const float *__restrict__ gpool, double *__restrict__ acc)
+{
+    const int b = list[blockIdx.y];
+    const SlotDev &S = sd[b];
+    const float *g = gpool + (int64_t)(2 * b + 1 - S.gcur) * Dp;
+    float m = 0.f;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < (int64_t)QQ * L;
+         e += (int64_t)gridDim.x * blockDim.x)
+        if (e / QQ != S.locus) m = fmaxf(m, fabsf(g[e]));
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0 && m > 0.f) atomic_max_nonneg(acc + (int64_t)b * NACC + ACC_GMAX, (double)m);
+}
+
+// x in the engine layout from the combined digits: J blocks (J_rr = 0),
+// h = eta (the slot's eta field), padding 0
+__global__ void k_dual_to_wa(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int L, int64_t Dp,
+                             const double *__restrict__ J64, float *__restrict__ wa)
+{
+    const int b = list[blockIdx.y];
+    const SlotDev &S = sd[b];
+    const double *g = J64 + (int64_t)b * Dp;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Dp; e += (int64_t)gridDim.x * blockDim.x) {
+        float v = 0.f;
+        if (e < (int64_t)QQ * L) v = (e / QQ == S.locus) ? 0.f : (float)g[e];
+        else if (e < (int64_t)QQ * L + Q) v = (float)S.eta[e - (int64_t)QQ * L];
+        wa[(int64_t)b * Dp + e] = v;
+    }
+}
+
+unsigned grid_for(int64_t elems, int per_block_elems, int cap)
+{
+    const int64_t g = (elems + per_block_elems - 1) / per_block_elems;
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(g, cap));
+}
+
+} // namespace
+
+void launch_dual_kmat(const int32_t *dist, int N, int64_t Nx, int L, int32_t *K, cudaStream_t st)
+{
+    k_dual_kmat<<<grid_for(Nx * Nx, 256 * 8, 4096), 256, 0, st>>>(dist, N, Nx, L, K);
+}
+
+void launch_dual_gradient(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *R,
+                          const uint8_t *rstate, const int32_t *K, double qscale, int32_t *rq, long long *csum,
+                          double *KR, double *dv, double *acc, double *amax, cudaStream_t st)
+{
+    if (n <= 0) return;
+    const int NV = DV_S + 2 * P.ring;
+    dim3 gq(grid_for(P.Nx, 256 * 4, 64), n);
+    k_dual_quant<<<gq, 256, 0, st>>>(sd, list, (int)P.N, P.Nx, reinterpret_cast<const float4 *>(R), rstate, qscale,
+                                     reinterpret_cast<int4 *>(rq), reinterpret_cast<unsigned long long *>(csum));
+    dim3 gk((unsigned)(P.Nx / KP_M), (unsigned)((n + KP_S - 1) / KP_S));
+    k_dual_kprod<<<gk, 256, 0, st>>>(K, P.Nx, (int)P.N, list, n, reinterpret_cast<const int4 *>(rq), csum, rstate,
+                                     1.0 / qscale, KR);
+    dim3 gg(grid_for(P.Nx * 4, 256 * 4, 64), n);
+    k_dual_grad<<<gg, 256, 0, st>>>(sd, list, P.Nx, NV, P.ring, P.lambda_J, rq, 1.0 / qscale, KR, dv, acc, amax);
+}
+
+void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *dv,
+                      double *dots, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 g(grid_for(P.Nx * 4, 256 * 8, 32), n);
+    k_dual_dots<<<g, 256, 0, st>>>(sd, list, P.Nx, DV_S + 2 * P.ring, P.ring, dv, dots);
+}
+
+void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
+                           const float *R, double *u, double *acc, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 g(grid_for(P.Nx * 4, 256 * 8, 32), n);
+    k_dual_direction<<<g, 256, 0, st>>>(sd, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, P.ring, dv,
+                                        reinterpret_cast<const float4 *>(R), u, acc);
+}
+
+void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
+                        const double *u, double *lbase, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 g(grid_for(P.Nx * 4, 256 * 4, 64), n);
+    k_dual_accept<<<g, 256, 0, st>>>(sd, list, P.Nx, DV_S + 2 * P.ring, dv, u, lbase);
+}
+
+void launch_dual_to_r(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int which,
+                      const double *dv, float *R, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 g(grid_for(P.Nx, 256 * 4, 64), n);
+    k_dual_to_r<<<g, 256, 0, st>>>(sd, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, which, dv,
+                                   reinterpret_cast<float4 *>(R));
+}
+
+void launch_dual_gmax(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *gpool,
+                      double *acc, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 g(grid_for((int64_t)QQ * P.L, 256 * 16, 256), n);
+    k_dual_gmax<<<g, 256, 0, st>>>(sd, list, (int)P.L, P.Dp, gpool, acc);
+}
+
+void launch_dual_digits(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d, const double *dv,
+                        float *R, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 g(grid_for(P.Nx, 256 * 4, 64), n);
+    k_dual_digits<<<g, 256, 0, st>>>(sd, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, d, dv,
+                                     reinterpret_cast<float4 *>(R));
+}
+
+void launch_dual_digit_acc(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d,
+                           const float *gpool, double *J64, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 g(grid_for(P.Dp, 256 * 16, 256), n);
+    k_dual_digit_acc<<<g, 256, 0, st>>>(sd, list, P.Dp, d, gpool, J64);
+}
+
+void launch_dual_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *J64,
+                       float *wa, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 g(grid_for(P.Dp, 256 * 16, 256), n);
+    k_dual_to_wa<<<g, 256, 0, st>>>(sd, list, (int)P.L, P.Dp, J64, wa);
+}
+
+} // namespace sdca
