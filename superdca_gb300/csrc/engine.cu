@@ -49,6 +49,7 @@ enum Phase {
     PH_FINALIZE,    // converged: logits refreshed, needs the final evaluation
     PH_REFRESH,     // logits recomputed from the stored parameters: needs the evaluation there
     PH_READY_REFRESH,  // re-evaluated, waiting for the gradient pass (history kept)
+    PH_CONVERT,     // dual form: stopped, waiting for its parameters to be formed
 };
 
 struct SlotHost {
@@ -144,6 +145,7 @@ struct sdca_handle {
     double refresh_factor = 8.0;
     int refresh_every = 30;
     int tc_refresh_every = 5;   // tensor-core form: recompute logits every this many accepted steps
+    std::vector<int> trace_loci;  // SDCA_TRACE=<locus>[,<locus>...]: per-iteration solver state on stderr
 
     // dual form (kernels_dual.cu)
     double *dv = nullptr, *u64 = nullptr, *KR = nullptr, *amax = nullptr, *J64 = nullptr;
@@ -1232,6 +1234,51 @@ int phase_step(sdca_handle *h)
 
 double dot4h(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3]; }
 
+// Stopped slots of the dual form: x in the engine layout (J = Phi^T a_x,
+// J_rr = 0, h = eta_x), then the final evaluation.  J is formed exactly:
+// the logits K a_x are O(1) while sum_j |K_ij a_j| is hundreds, so a
+// rounding of a in the last bits of single precision would move the gradient
+// at the reported x by far more than the threshold.  A tensor-core pass
+// costs the same for 1 and for 32 slots, so stopped slots wait until 16 of
+// them are ready or no slot is still iterating (`force`: now).
+int dual_convert(sdca_handle *h, bool force)
+{
+    const Problem &P = h->P;
+    std::vector<int32_t> fin;
+    int active = 0;
+    for (int b = 0; b < P.Bmax; ++b) {
+        const int ph = h->slots[b].phase;
+        if (ph == PH_CONVERT) fin.push_back(b);
+        else if (ph != PH_EMPTY && ph != PH_FINALIZE) ++active;
+    }
+    if (fin.empty() || (!force && active > 0 && (int)fin.size() < std::min(16, P.Bmax))) return SDCA_OK;
+    for (int b : fin) {
+        const double am = h->slots[b].amax_x;
+        h->sd_h[b].tc_scale = am > 0.0 ? std::ldexp(1.0, 32) / am : 1.0;
+        for (int a = 0; a < Q; ++a) h->sd_h[b].eta[a] = h->slots[b].eta_x[a];
+    }
+    int rc = upload_slots(h, fin);
+    if (rc) return rc;
+    {
+        Timed t(h, SDCA_K_OTHER, 3 * 4 + 1, (int64_t)fin.size());
+        for (int d = 0; d < 3; ++d) {
+            launch_dual_digits(P, h->sd, h->list, (int)fin.size(), d, h->dv, h->Rchk, h->stream);
+            CK(tc_launch_bwd(h->tc, P, h->sd, h->list, (int)fin.size(), h->Rchk, 1.0f, h->Rhi, h->Rlo, h->gpool,
+                             h->tc_err, h->stream));
+            launch_dual_digit_acc(P, h->sd, h->list, (int)fin.size(), d, h->gpool, h->J64, h->stream);
+        }
+        launch_dual_to_wa(P, h->sd, h->list, (int)fin.size(), h->J64, h->wa, h->stream);
+    }
+    CKL();
+    for (int b : fin) {
+        SlotHost &S = h->slots[b];
+        S.phase = PH_FINALIZE;
+        S.stp = 0.0;
+        S.use_u = false;
+    }
+    return SDCA_OK;
+}
+
 int phase_step_dual(sdca_handle *h)
 {
     const Problem &P = h->P;
@@ -1253,7 +1300,7 @@ int phase_step_dual(sdca_handle *h)
             S.ring_new = -1;
         }
     }
-    if (all.empty()) return SDCA_OK;
+    if (all.empty()) return dual_convert(h, true);
     int rc;
     if (!steps.empty()) {
         if ((rc = upload_slots(h, steps))) return rc;
@@ -1349,7 +1396,9 @@ int phase_step_dual(sdca_handle *h)
         releps_stop[b] = gnorm < releps;
         // the max-norm test needs J = Phi^T a_g: run it when the last check's
         // ratio max|g| / ||g|| predicts a pass, and every 10 iterations
-        const bool due = S.iterations - S.last_check >= 10;
+        // (before the first check the max-norm is far above the threshold
+        // while ||g|| > 200 threshold on the workloads measured: ratio ~0.01)
+        const bool due = S.iterations - S.last_check >= 10 && (S.chk_ratio > 0.0 || gnorm < 200.0 * gtol);
         const bool near = S.chk_ratio > 0.0 && S.chk_ratio * gnorm < 1.5 * gtol;
         if (due || near || gnorm < gtol || releps_stop[b]) chk.push_back(b);
         else if (releps_stop[b]) {
@@ -1391,36 +1440,8 @@ int phase_step_dual(sdca_handle *h)
     }
     for (int b : all) (stop[b] ? fin : cont).push_back(b);
 
-    // Stopped slots: x in the engine layout (J = Phi^T a_x, J_rr = 0,
-    // h = eta_x), then the final evaluation.  J is formed exactly: the
-    // logits K a_x are O(1) while sum_j |K_ij a_j| is hundreds, so a rounding
-    // of a in the last bits of single precision would move the gradient at
-    // the reported x by far more than the threshold.
-    if (!fin.empty()) {
-        for (int b : fin) {
-            const double am = h->slots[b].amax_x;
-            h->sd_h[b].tc_scale = am > 0.0 ? std::ldexp(1.0, 32) / am : 1.0;
-            for (int a = 0; a < Q; ++a) h->sd_h[b].eta[a] = h->slots[b].eta_x[a];
-        }
-        if ((rc = upload_slots(h, fin))) return rc;
-        {
-            Timed t(h, SDCA_K_OTHER, 3 * 4 + 1, (int64_t)fin.size());
-            for (int d = 0; d < 3; ++d) {
-                launch_dual_digits(P, h->sd, h->list, (int)fin.size(), d, h->dv, h->Rchk, h->stream);
-                CK(tc_launch_bwd(h->tc, P, h->sd, h->list, (int)fin.size(), h->Rchk, 1.0f, h->Rhi, h->Rlo, h->gpool,
-                                 h->tc_err, h->stream));
-                launch_dual_digit_acc(P, h->sd, h->list, (int)fin.size(), d, h->gpool, h->J64, h->stream);
-            }
-            launch_dual_to_wa(P, h->sd, h->list, (int)fin.size(), h->J64, h->wa, h->stream);
-        }
-        CKL();
-        for (int b : fin) {
-            SlotHost &S = h->slots[b];
-            S.phase = PH_FINALIZE;
-            S.stp = 0.0;
-            S.use_u = false;
-        }
-    }
+    for (int b : fin) h->slots[b].phase = PH_CONVERT;
+    if ((rc = dual_convert(h, false))) return rc;
     if (cont.empty()) return SDCA_OK;
 
     std::vector<int32_t> withh;
@@ -1531,11 +1552,16 @@ int phase_step_dual(sdca_handle *h)
         return SDCA_OK;
     };
     if ((rc = run_direction(cont))) return rc;
+    // Restart from steepest descent only for a direction that is not
+    // downhill in angle.  The products here are exact, so a small g.d is a
+    // genuine descent: near the optimum it is small because the curvature
+    // along g is large, and a restart there would repeat every iteration
+    // (each steepest-descent step is tiny and so is the next gamma).
     std::vector<int32_t> restart;
     for (int b : cont) {
         SlotHost &S = h->slots[b];
-        const double releps = 1e-4 * std::max(1.0, std::sqrt(S.x2J + S.x2H));
-        if (!S.hist.empty() && (S.force_restart || !(S.gd <= -1e-4 * releps))) restart.push_back(b);
+        const double cosgd = S.gd / std::sqrt(std::max(S.g2, 0.0) * std::max(S.ddJ + S.ddH, 0.0));
+        if (!S.hist.empty() && (S.force_restart || !(cosgd < -1e-10))) restart.push_back(b);
         S.force_restart = false;
     }
     std::vector<char> restarted(P.Bmax, 0);
@@ -1556,6 +1582,11 @@ int phase_step_dual(sdca_handle *h)
         S.use_u = true;
         S.push = false;
         const double d0 = dg0[b] + dl2_along(P, S, 0.0);
+        if (std::find(h->trace_loci.begin(), h->trace_loci.end(), S.locus) != h->trace_loci.end())
+            std::fprintf(stderr, "trace r=%d it=%d f=%.12e |g|=%.4e gmax=%.4e chk=%d ratio=%.3f gd=%.4e dg0=%.4e "
+                                 "x2=%.4e hist=%zu restart=%d stp_prev=%.3e\n",
+                         S.locus, S.iterations, S.f, std::sqrt(S.g2), S.gmax, S.last_check, S.chk_ratio, S.gd, d0,
+                         S.x2J + S.x2H, S.hist.size(), (int)restarted[b], S.stp);
         if (S.ls.start(S.f, d0, alpha_init) == MoreThuente::NEED_EVAL) {
             S.stp = S.ls.stp;
             S.phase = PH_LS;
@@ -1665,6 +1696,13 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
     if (const char *e = std::getenv("SDCA_REFRESH_EVERY")) h->refresh_every = std::max(1, std::atoi(e));
     if (const char *e = std::getenv("SDCA_REFRESH_FACTOR")) h->refresh_factor = std::atof(e);
     if (const char *e = std::getenv("SDCA_TC_REFRESH_EVERY")) h->tc_refresh_every = std::max(1, std::atoi(e));
+    if (const char *e = std::getenv("SDCA_TRACE")) {
+        for (const char *p = e; *p;) {
+            h->trace_loci.push_back(std::atoi(p));
+            while (*p && *p != ',') ++p;
+            if (*p == ',') ++p;
+        }
+    }
     h->slots.resize(P.Bmax);
     int rc = SDCA_OK;
     const size_t B = P.Bmax;
