@@ -153,6 +153,8 @@ struct sdca_handle {
     long long *csum = nullptr;
     float *Rchk = nullptr;
     double qscale = 1.0;
+    KdPlan *kd = nullptr;          // exact K rho on the tensor cores (N <= 4000), else CUDA cores
+    __half *Kd = nullptr, *Rd = nullptr;
 
     // learned warm start (warmstart.cu, mlp.cu)
     float *ws_params = nullptr;
@@ -1324,9 +1326,16 @@ int phase_step_dual(sdca_handle *h)
     CK(cudaMemsetAsync(h->amax, 0, sizeof(double) * 2 * P.Bmax, h->stream));
     if ((rc = zero_acc(h))) return rc;
     {
-        Timed t(h, SDCA_K_BACKWARD, 3, (int64_t)all.size());
-        launch_dual_gradient(P, h->sd, h->list, (int)all.size(), h->R, h->rstate, h->Kmat, h->qscale, h->rq, h->csum,
-                             h->KR, h->dv, h->acc, h->amax, h->stream);
+        Timed t(h, SDCA_K_BACKWARD, h->kd ? 4 : 3, (int64_t)all.size());
+        launch_dual_quant(P, h->sd, h->list, (int)all.size(), h->R, h->rstate, h->qscale, h->rq, h->csum, h->stream);
+        if (h->kd)
+            CK(tc_launch_kdig(h->kd, P, h->list, (int)all.size(), h->rq, h->rstate, h->csum, 1.0 / h->qscale, h->Rd,
+                              h->KR, h->tc_err, h->stream));
+        else
+            launch_dual_kprod(P, h->list, (int)all.size(), h->rstate, h->Kmat, h->qscale, h->rq, h->csum, h->KR,
+                              h->stream);
+        launch_dual_grad(P, h->sd, h->list, (int)all.size(), h->qscale, h->rq, h->KR, h->dv, h->acc, h->amax,
+                         h->stream);
     }
     CKL();
     std::vector<double> amax(2 * P.Bmax);
@@ -1732,7 +1741,10 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
                   (rc = dalloc(h, &h->KR, B * P.Nx * 4)) || (rc = dalloc(h, &h->amax, 2 * B)) ||
                   (rc = dalloc(h, &h->rq, B * P.Nx * 4)) || (rc = dalloc(h, &h->csum, 16 * B)) ||
                   (rc = dalloc(h, &h->Rchk, B * P.Nx * 4)) || (rc = dalloc(h, &h->J64, B * P.Dp)) ||
-                  (rc = dalloc(h, &h->Kmat, (size_t)P.Nx * P.Nx)))) ||
+                  (rc = dalloc(h, &h->Kmat, (size_t)P.Nx * P.Nx)) ||
+                  (P.N <= 4000 && P.L < (1 << 18) &&
+                   ((rc = dalloc(h, &h->Kd, (size_t)3 * kd_nk_rows(P) * P.Nx)) ||
+                    (rc = dalloc(h, &h->Rd, (size_t)5 * kd_nr_rows(P) * P.Nx)))))) ||
         (tcres &&
          ((rc = dalloc(h, &h->Dhi, 4 * B * (size_t)round_up(4 * P.L, 64))) ||
           (rc = dalloc(h, &h->Dlo, 4 * B * (size_t)round_up(4 * P.L, 64))) ||
@@ -1758,6 +1770,8 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
         if (major != 10 || minor != 3) why = "the tensor-core and dual forms need an sm_103 (GB300) device";
         else if (tc_configure() != cudaSuccess) why = "could not reserve the tensor-core kernel's shared memory";
         else if (!(h->tc = tc_plan_create(P, h->X, h->XT, h->Dhi, h->Dlo, h->Rhi, h->Rlo, round_up(4 * P.L, 64))))
+            why = "TMA tensor-map encoding failed";
+        else if (h->Kd && !(h->kd = tc_kdig_plan_create(P, h->Kd, h->Rd)))
             why = "TMA tensor-map encoding failed";
         if (!why.empty()) {
             cudaGetLastError();
@@ -1823,6 +1837,7 @@ int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weig
         }
         launch_distances(h->X, P.Lx, (int)P.N, (int)P.L, packed, dist, h->stream);
         launch_dual_kmat(dist, (int)P.N, P.Nx, (int)P.L, h->Kmat, h->stream);
+        if (h->kd) tc_kdig_fill_k(h->kd, P, h->Kmat, h->Kd, h->stream);
         const cudaError_t e1 = cudaGetLastError();
         const cudaError_t e2 = cudaStreamSynchronize(h->stream);
         cudaFree(packed);
@@ -2109,6 +2124,7 @@ int sdca_destroy(sdca_handle *h)
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (auto e : h->ev_pool) cudaEventDestroy(e);
     if (h->tc) tc_plan_destroy(h->tc);
+    if (h->kd) tc_kdig_plan_destroy(h->kd);
     free_all(h);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     delete h;

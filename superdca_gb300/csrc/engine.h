@@ -157,9 +157,12 @@ void launch_trial64(const Problem &P, const SlotDev *sd, const int32_t *list, in
 
 // dual form (kernels_dual.cu)
 void launch_dual_kmat(const int32_t *dist, int N, int64_t Nx, int L, int32_t *K, cudaStream_t st);
-void launch_dual_gradient(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *R,
-                          const uint8_t *rstate, const int32_t *K, double qscale, int32_t *rq, long long *csum,
-                          double *KR, double *dv, double *acc, double *amax, cudaStream_t st);
+void launch_dual_quant(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *R,
+                       const uint8_t *rstate, double qscale, int32_t *rq, long long *csum, cudaStream_t st);
+void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8_t *rstate, const int32_t *K,
+                       double qscale, const int32_t *rq, const long long *csum, double *KR, cudaStream_t st);
+void launch_dual_grad(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double qscale,
+                      const int32_t *rq, const double *KR, double *dv, double *acc, double *amax, cudaStream_t st);
 void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *dv,
                       double *dots, cudaStream_t st);
 void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
@@ -213,5 +216,15 @@ cudaError_t tc_launch_fwd(const TcPlan *pl, const Problem &P, const SlotDev *sd,
 cudaError_t tc_launch_bwd(const TcPlan *pl, const Problem &P, const SlotDev *sd, const int32_t *list, int n,
                           const float *R, float r_scale, __half *Rhi, __half *Rlo, float *gpool, int *err,
                           cudaStream_t st);
+// dual form: exact K rho on the tensor cores (N <= 4000, L < 2^18)
+struct KdPlan;
+int kd_nk_rows(const Problem &P);
+int kd_nr_rows(const Problem &P);
+KdPlan *tc_kdig_plan_create(const Problem &P, __half *Kd, __half *Rd);
+void tc_kdig_plan_destroy(KdPlan *p);
+void tc_kdig_fill_k(const KdPlan *pl, const Problem &P, const int32_t *K, __half *Kd, cudaStream_t st);
+cudaError_t tc_launch_kdig(const KdPlan *pl, const Problem &P, const int32_t *list, int n, const int32_t *rq,
+                           const uint8_t *rstate, const long long *csum, double inv_qscale, __half *Rd, double *KR,
+                           int *err, cudaStream_t st);
 
 } // namespace sdca

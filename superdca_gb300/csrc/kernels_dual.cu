@@ -396,18 +396,30 @@ void launch_dual_kmat(const int32_t *dist, int N, int64_t Nx, int L, int32_t *K,
     k_dual_kmat<<<grid_for(Nx * Nx, 256 * 8, 4096), 256, 0, st>>>(dist, N, Nx, L, K);
 }
 
-void launch_dual_gradient(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *R,
-                          const uint8_t *rstate, const int32_t *K, double qscale, int32_t *rq, long long *csum,
-                          double *KR, double *dv, double *acc, double *amax, cudaStream_t st)
+void launch_dual_quant(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *R,
+                       const uint8_t *rstate, double qscale, int32_t *rq, long long *csum, cudaStream_t st)
 {
     if (n <= 0) return;
-    const int NV = DV_S + 2 * P.ring;
     dim3 gq(grid_for(P.Nx, 256 * 4, 64), n);
     k_dual_quant<<<gq, 256, 0, st>>>(sd, list, (int)P.N, P.Nx, reinterpret_cast<const float4 *>(R), rstate, qscale,
                                      reinterpret_cast<int4 *>(rq), reinterpret_cast<unsigned long long *>(csum));
+}
+
+// K rho on the CUDA cores (64-bit integer multiply-adds): any N
+void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8_t *rstate, const int32_t *K,
+                       double qscale, const int32_t *rq, const long long *csum, double *KR, cudaStream_t st)
+{
+    if (n <= 0) return;
     dim3 gk((unsigned)(P.Nx / KP_M), (unsigned)((n + KP_S - 1) / KP_S));
     k_dual_kprod<<<gk, 256, 0, st>>>(K, P.Nx, (int)P.N, list, n, reinterpret_cast<const int4 *>(rq), csum, rstate,
                                      1.0 / qscale, KR);
+}
+
+void launch_dual_grad(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double qscale,
+                      const int32_t *rq, const double *KR, double *dv, double *acc, double *amax, cudaStream_t st)
+{
+    if (n <= 0) return;
+    const int NV = DV_S + 2 * P.ring;
     dim3 gg(grid_for(P.Nx * 4, 256 * 4, 64), n);
     k_dual_grad<<<gg, 256, 0, st>>>(sd, list, P.Nx, NV, P.ring, P.lambda_J, rq, 1.0 / qscale, KR, dv, acc, amax);
 }

@@ -406,6 +406,219 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
     }
 }
 
+// ---------------------------------------------------------------------------
+// Exact K rho for the dual form on the tensor cores.
+//
+// K (agreement counts, < 2^18) is held as three fp16 planes of base-64
+// digits (0..63), rho_q (integers, |rho_q| <= 2^30) as five fp16 planes of
+// balanced base-64 digits (|digit| <= 32, the top one <= 65).  Every product
+// of two digits is an integer below 4096 and the sum over at most 4000
+// sequences stays below 2^24, so each of the 15 digit-pair GEMMs is exact in
+// its FP32 TMEM accumulator; the epilogue combines them with their powers of
+// 64 in 64-bit integers (modulo 2^64: the total itself is below 2^62).
+
+constexpr int KD_BM = 128, KD_BN = 32, KD_BK = 64;
+constexpr int KD_KDIG = 3, KD_RDIG = 5;
+constexpr int KD_A_BYTES = KD_BM * KD_BK * 2;  // one K digit plane tile, 16 KB
+constexpr int KD_B_BYTES = KD_BN * KD_BK * 2;  // one rho digit plane tile, 4 KB
+constexpr int KD_STAGE = KD_KDIG * KD_A_BYTES + KD_RDIG * KD_B_BYTES;
+constexpr int KD_STG = 3;
+constexpr int KD_SMEM = KD_STG * KD_STAGE + 1024 + 256;
+constexpr uint32_t KD_TMEM_COLS = 512;  // 15 accumulators of 32 columns
+constexpr uint32_t IDESC_KD = (1u << 4) | ((uint32_t)(KD_BN >> 3) << 17) | ((uint32_t)(KD_BM >> 4) << 24);
+static_assert(KD_STAGE % 1024 == 0, "stage must keep 1024-byte alignment");
+static_assert(KD_KDIG * KD_RDIG * KD_BN <= (int)KD_TMEM_COLS, "accumulators fit TMEM");
+
+__device__ __forceinline__ void mma_f16_kd(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(IDESC_KD), "r"(accumulate)
+        : "memory");
+}
+
+struct KdArgs {
+    int kt_total;        // Nx / 64
+    int nk_rows;         // rows per K digit plane (multiple of 128)
+    int nr_rows;         // rows per rho digit plane (multiple of 32)
+    int N;
+    int64_t Nx;
+    int nlist;
+    const int32_t *list;
+    const uint8_t *rstate;
+    const long long *csum;
+    double inv_qscale;
+    double *KR;
+    int *err;
+};
+
+__global__ void __launch_bounds__(THREADS, 1)
+k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensorMap tmR, const KdArgs args)
+{
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t sbase0 = smem_u32(smem_raw);
+    const uint32_t sbase = (sbase0 + 1023u) & ~1023u;
+    uint8_t *const sgen = smem_raw + (sbase - sbase0);
+    const uint32_t bars = sbase + KD_STG * KD_STAGE;
+    auto full = [&](int s) { return bars + 8u * s; };
+    auto empty = [&](int s) { return bars + 8u * (KD_STG + s); };
+    const uint32_t tmem_full = bars + 8u * (2 * KD_STG);
+    const uint32_t tmem_slot = bars + 8u * (2 * KD_STG + 1);
+    uint32_t *tmem_slot_gen = reinterpret_cast<uint32_t *>(sgen + KD_STG * KD_STAGE + 8 * (2 * KD_STG + 1));
+    constexpr uint32_t BOFF = KD_KDIG * KD_A_BYTES;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m_tile = blockIdx.x, n_tile = blockIdx.y;
+    const int nkt = args.kt_total;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < KD_STG; ++s) {
+            mbar_init(full(s), 1);
+            mbar_init(empty(s), 1);
+        }
+        mbar_init(tmem_full, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tmem_slot),
+                     "r"(KD_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem_base = *tmem_slot_gen;
+    bool failed = false;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            for (int j = 0; j < nkt; ++j) {
+                const int s = j % KD_STG;
+                const uint32_t ph = (uint32_t)((j / KD_STG) & 1);
+                if (!mbar_wait(empty(s), ph ^ 1u)) { failed = true; break; }
+                const uint32_t st = sbase + (uint32_t)s * KD_STAGE;
+                mbar_expect_tx(full(s), KD_STAGE);
+#pragma unroll
+                for (int k = 0; k < KD_KDIG; ++k)
+                    tma_load_2d(st + k * KD_A_BYTES, &tmK, j * KD_BK, k * args.nk_rows + m_tile * KD_BM, full(s));
+#pragma unroll
+                for (int p = 0; p < KD_RDIG; ++p)
+                    tma_load_2d(st + BOFF + p * KD_B_BYTES, &tmR, j * KD_BK, p * args.nr_rows + n_tile * KD_BN,
+                                full(s));
+            }
+            for (int j = max(0, nkt - KD_STG); j < nkt; ++j)
+                if (!mbar_wait(full(j % KD_STG), (uint32_t)((j / KD_STG) & 1))) failed = true;
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            for (int j = 0; j < nkt; ++j) {
+                const int s = j % KD_STG;
+                const uint32_t ph = (uint32_t)((j / KD_STG) & 1);
+                if (!mbar_wait(full(s), ph)) { failed = true; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t st = sbase + (uint32_t)s * KD_STAGE;
+#pragma unroll
+                for (int kk = 0; kk < KD_BK / 16; ++kk) {
+#pragma unroll
+                    for (int k = 0; k < KD_KDIG; ++k) {
+                        const uint64_t ad = smem_desc_sw128(st + k * KD_A_BYTES + kk * 32);
+#pragma unroll
+                        for (int p = 0; p < KD_RDIG; ++p) {
+                            const uint64_t bd = smem_desc_sw128(st + BOFF + p * KD_B_BYTES + kk * 32);
+                            mma_f16_kd(tmem_base + (uint32_t)((k * KD_RDIG + p) * KD_BN), ad, bd,
+                                       (j > 0 || kk > 0) ? 1u : 0u);
+                        }
+                    }
+                }
+                mma_commit(empty(s));
+            }
+            mma_commit(tmem_full);
+        }
+    } else {
+        const bool ok = nkt > 0 && mbar_wait(tmem_full, 0u);
+        if (!ok && nkt > 0) failed = true;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int q = warp & 3;
+        const int row = m_tile * KD_BM + q * 32 + lane;
+        unsigned long long acc[KD_BN];
+#pragma unroll
+        for (int c = 0; c < KD_BN; ++c) acc[c] = 0ull;
+        if (ok) {
+#pragma unroll 1
+            for (int k = 0; k < KD_KDIG; ++k)
+#pragma unroll 1
+                for (int p = 0; p < KD_RDIG; ++p) {
+                    float v[32];
+                    tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)((k * KD_RDIG + p) * KD_BN), v);
+                    const unsigned long long w = 1ull << (6 * (k + p));
+#pragma unroll
+                    for (int c = 0; c < KD_BN; ++c) acc[c] += (unsigned long long)__float2ll_rn(v[c]) * w;
+                }
+#pragma unroll
+            for (int cc = 0; cc < KD_BN; ++cc) {
+                const int P = n_tile * (KD_BN / 4) + cc / 4;
+                if (P >= args.nlist || row >= args.Nx) continue;
+                const int b = args.list[P], c = cc & 3;
+                double val = 0.0;
+                if (row < args.N) {
+                    const int y = args.rstate[(int64_t)b * args.Nx + row] & 3;
+                    const long long tot = (long long)acc[cc] - args.csum[(int64_t)b * 16 + y * 4 + c];
+                    val = (double)tot * args.inv_qscale;
+                }
+                args.KR[((int64_t)b * args.Nx + row) * 4 + c] = val;
+            }
+        }
+    }
+    if (failed) atomicExch(args.err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(KD_TMEM_COLS)
+                     : "memory");
+    }
+}
+
+// K (int32, Nx x Nx) -> three fp16 planes of base-64 digits, rows padded to nk_rows
+__global__ void k_kdig_split_k(const int32_t *__restrict__ K, int64_t Nx, int nk_rows, __half *__restrict__ Kd)
+{
+    const int64_t total = (int64_t)nk_rows * Nx;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / Nx;
+        const int v = i < Nx ? K[t] : 0;
+        Kd[t] = __int2half_rn(v & 63);
+        Kd[(int64_t)nk_rows * Nx + t] = __int2half_rn((v >> 6) & 63);
+        Kd[2 * (int64_t)nk_rows * Nx + t] = __int2half_rn(v >> 12);
+    }
+}
+
+// rho_q of list position P (slot list[P]) -> five fp16 planes of balanced base-64 digits, rows P*4+c
+__global__ void k_kdig_split_r(const int32_t *__restrict__ list, int64_t Nx, int nr_rows,
+                               const int4 *__restrict__ rq, __half *__restrict__ Rd)
+{
+    const int P = blockIdx.y, b = list[P];
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < Nx; j += (int64_t)gridDim.x * blockDim.x) {
+        const int4 q = rq[(int64_t)b * Nx + j];
+        const int qq[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            long long v = qq[c];
+#pragma unroll
+            for (int p = 0; p < KD_RDIG; ++p) {
+                long long d = v;
+                if (p < KD_RDIG - 1) {
+                    d = ((v + 32) & 63) - 32;   // balanced digit, v - d divisible by 64
+                    v = (v - d) / 64;
+                }
+                Rd[((int64_t)p * nr_rows + (int64_t)P * 4 + c) * Nx + j] = __int2half_rn((int)d);
+            }
+        }
+    }
+}
+
 // d (engine layout [n][s][a]) -> B rows p*4+a, columns n*4+s, fp16 hi and lo of d*2^e
 __global__ void k_split_dir(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t L,
                             int64_t Dp, int64_t Kp, const float *__restrict__ vecs, __half *__restrict__ hi,
@@ -578,6 +791,66 @@ TcPlan *tc_plan_create(const Problem &P, const uint8_t *X, const uint8_t *XT, __
 
 void tc_plan_destroy(TcPlan *p) { delete p; }
 
+struct KdPlan {
+    CUtensorMap mK, mR;
+    int nk_rows = 0, nr_rows = 0;
+};
+
+int kd_nk_rows(const Problem &P) { return (int)(((P.Nx + tc::KD_BM - 1) / tc::KD_BM) * tc::KD_BM); }
+int kd_nr_rows(const Problem &P) { return (int)(((4 * P.Bmax + tc::KD_BN - 1) / tc::KD_BN) * tc::KD_BN); }
+
+KdPlan *tc_kdig_plan_create(const Problem &P, __half *Kd, __half *Rd)
+{
+    KdPlan *p = new KdPlan();
+    p->nk_rows = kd_nk_rows(P);
+    p->nr_rows = kd_nr_rows(P);
+    bool ok = make_map(&p->mK, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Kd, (uint64_t)P.Nx, (uint64_t)tc::KD_KDIG * p->nk_rows,
+                       (uint64_t)P.Nx * 2, tc::KD_BK, tc::KD_BM, CU_TENSOR_MAP_SWIZZLE_128B);
+    ok &= make_map(&p->mR, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Rd, (uint64_t)P.Nx, (uint64_t)tc::KD_RDIG * p->nr_rows,
+                   (uint64_t)P.Nx * 2, tc::KD_BK, tc::KD_BN, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (!ok) {
+        delete p;
+        return nullptr;
+    }
+    return p;
+}
+
+void tc_kdig_plan_destroy(KdPlan *p) { delete p; }
+
+void tc_kdig_fill_k(const KdPlan *pl, const Problem &P, const int32_t *K, __half *Kd, cudaStream_t st)
+{
+    const int64_t total = (int64_t)pl->nk_rows * P.Nx;
+    tc::k_kdig_split_k<<<(unsigned)std::min<int64_t>((total + 255) / 256, 8192), 256, 0, st>>>(K, P.Nx, pl->nk_rows,
+                                                                                          Kd);
+}
+
+cudaError_t tc_launch_kdig(const KdPlan *pl, const Problem &P, const int32_t *list, int n, const int32_t *rq,
+                           const uint8_t *rstate, const long long *csum, double inv_qscale, __half *Rd, double *KR,
+                           int *err, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    {
+        dim3 g((unsigned)std::min<int64_t>((P.Nx + 255) / 256, 64), (unsigned)n);
+        tc::k_kdig_split_r<<<g, 256, 0, st>>>(list, P.Nx, pl->nr_rows, reinterpret_cast<const int4 *>(rq), Rd);
+    }
+    tc::KdArgs a{};
+    a.kt_total = (int)(P.Nx / tc::KD_BK);
+    a.nk_rows = pl->nk_rows;
+    a.nr_rows = pl->nr_rows;
+    a.N = (int)P.N;
+    a.Nx = P.Nx;
+    a.nlist = n;
+    a.list = list;
+    a.rstate = rstate;
+    a.csum = csum;
+    a.inv_qscale = inv_qscale;
+    a.KR = KR;
+    a.err = err;
+    dim3 grid((unsigned)(pl->nk_rows / tc::KD_BM), (unsigned)((4 * n + tc::KD_BN - 1) / tc::KD_BN));
+    tc::k_kdig<<<grid, tc::THREADS, tc::KD_SMEM, st>>>(pl->mK, pl->mR, a);
+    return cudaGetLastError();
+}
+
 cudaError_t tc_launch_fwd(const TcPlan *pl, const Problem &P, const SlotDev *sd, const int32_t *list, int n,
                           const float *vecs, __half *Dhi, __half *Dlo, float *partial, int splits, int *err,
                           cudaStream_t st)
@@ -641,6 +914,8 @@ cudaError_t tc_configure()
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(tc::k_gemm<1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  tc::Cfg<1, 4>::SMEM_BYTES);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(tc::k_kdig, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::KD_SMEM);
     return e;
 }
 
