@@ -91,6 +91,7 @@ struct SlotHost {
     double chk_ratio = 0.0;  // max|g| / ||g|| at the last exact max-norm check (0: none yet)
     int last_check = -1000;  // iteration of that check
     double amax_g = 0.0, amax_x = 0.0;  // max |a| of the gradient and of x
+    double f0d = 0.0, dg0d = 0.0;       // data parts of f and of the slope at the current point (step trials)
     MoreThuente ls;
 };
 
@@ -151,7 +152,8 @@ struct sdca_handle {
     double *dv = nullptr, *u64 = nullptr, *KR = nullptr, *amax = nullptr, *J64 = nullptr;
     int32_t *rq = nullptr, *Kmat = nullptr;
     long long *csum = nullptr;
-    float *Rchk = nullptr;
+    float *Rchk = nullptr, *R0 = nullptr;   // R0: R at the current point, base of the step trials
+    float *ud = nullptr;                    // u_a - u_y per sequence (single precision, step trials)
     double qscale = 1.0;
     KdPlan *kd = nullptr;          // exact K rho on the tensor cores (N <= 4000), else CUDA cores
     __half *Kd = nullptr, *Rd = nullptr;
@@ -796,14 +798,30 @@ int phase_trials(sdca_handle *h, Queue &Qu)
         if (rc) return rc;
         rc = zero_acc(h);
         if (rc) return rc;
-        {
+        if (h->form == SDCA_FORM_DUAL) {
+            // step trials as changes from the current point; start and final
+            // evaluations in FP64 from the logits
+            std::vector<int32_t> delta, full;
+            for (int b : lst) {
+                const int ph = h->slots[b].phase;
+                (ph == PH_LS || ph == PH_FINAL_EVAL ? delta : full).push_back(b);
+            }
+            if (!delta.empty()) {
+                if ((rc = upload_list(h, delta))) return rc;
+                Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)delta.size());
+                launch_trial_delta(P, h->sd, h->list, (int)delta.size(), h->lbase, h->u64, h->ud, h->rstate, h->w,
+                                   h->R0, h->R, h->acc, h->stream);
+            }
+            if (!full.empty()) {
+                if ((rc = upload_list(h, full))) return rc;
+                Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)full.size());
+                launch_trial64(P, h->sd, h->list, (int)full.size(), h->lbase, h->u64, h->rstate, h->w, h->R, h->acc,
+                               h->stream);
+            }
+        } else {
             Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)lst.size());
-            if (h->form == SDCA_FORM_DUAL)
-                launch_trial64(P, h->sd, h->list, (int)lst.size(), h->lbase, h->u64, h->rstate, h->w, h->R,
-                               h->acc, h->stream);
-            else
-                launch_trial(P, h->sd, h->list, (int)lst.size(), h->lbase, h->u, h->rstate, h->w, h->R,
-                             h->acc, h->stream);
+            launch_trial(P, h->sd, h->list, (int)lst.size(), h->lbase, h->u, h->rstate, h->w, h->R, h->acc,
+                         h->stream);
         }
         CKL();
         rc = fetch_acc(h);
@@ -823,11 +841,12 @@ int phase_trials(sdca_handle *h, Queue &Qu)
                 S.f_final = fdata + P.lambda_J * S.x2J + P.lambda_h * S.x2H;
                 done.push_back(b);
             } else if (S.phase == PH_FINAL_EVAL) {
-                S.f = fdata + l2_along(P, S, S.stp);
+                S.f = (h->form == SDCA_FORM_DUAL ? S.f0d + fdata : fdata) + l2_along(P, S, S.stp);
                 S.phase = PH_READY_STEP;
             } else {  // PH_LS
-                const double f = fdata + l2_along(P, S, S.stp);
-                const double dg = acc_get(h, b, ACC_DG) + dl2_along(P, S, S.stp);
+                const bool dl = h->form == SDCA_FORM_DUAL;   // trial sums are changes from the current point
+                const double f = (dl ? S.f0d + fdata : fdata) + l2_along(P, S, S.stp);
+                const double dg = (dl ? S.dg0d : 0.0) + acc_get(h, b, ACC_DG) + dl2_along(P, S, S.stp);
                 S.trials++;
                 if (!std::isfinite(f) || !std::isfinite(dg)) {
                     S.f = f;
@@ -1544,7 +1563,8 @@ int phase_step_dual(sdca_handle *h)
         if ((r2 = zero_acc(h))) return r2;
         {
             Timed t(h, SDCA_K_DIRECTION, 1, (int64_t)lst.size());
-            launch_dual_direction(P, h->sd, h->list, (int)lst.size(), h->dv, h->R, h->u64, h->acc, h->stream);
+            launch_dual_direction(P, h->sd, h->list, (int)lst.size(), h->dv, h->R, h->R0, h->w, h->rstate, h->u64,
+                                  h->ud, h->acc, h->stream);
         }
         CKL();
         if ((r2 = fetch_acc(h))) return r2;
@@ -1591,6 +1611,8 @@ int phase_step_dual(sdca_handle *h)
         S.use_u = true;
         S.push = false;
         const double d0 = dg0[b] + dl2_along(P, S, 0.0);
+        S.f0d = S.f - l2_along(P, S, 0.0);
+        S.dg0d = dg0[b];
         if (std::find(h->trace_loci.begin(), h->trace_loci.end(), S.locus) != h->trace_loci.end())
             std::fprintf(stderr, "trace r=%d it=%d f=%.12e |g|=%.4e gmax=%.4e chk=%d ratio=%.3f gd=%.4e dg0=%.4e "
                                  "x2=%.4e hist=%zu restart=%d stp_prev=%.3e\n",
@@ -1741,6 +1763,7 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
                   (rc = dalloc(h, &h->KR, B * P.Nx * 4)) || (rc = dalloc(h, &h->amax, 2 * B)) ||
                   (rc = dalloc(h, &h->rq, B * P.Nx * 4)) || (rc = dalloc(h, &h->csum, 16 * B)) ||
                   (rc = dalloc(h, &h->Rchk, B * P.Nx * 4)) || (rc = dalloc(h, &h->J64, B * P.Dp)) ||
+                  (rc = dalloc(h, &h->R0, B * P.Nx * 4)) || (rc = dalloc(h, &h->ud, B * P.Nx * 4)) ||
                   (rc = dalloc(h, &h->Kmat, (size_t)P.Nx * P.Nx)) ||
                   (P.N <= 4000 && P.L < (1 << 18) &&
                    ((rc = dalloc(h, &h->Kd, (size_t)3 * kd_nk_rows(P) * P.Nx)) ||

@@ -166,7 +166,11 @@ void launch_dual_grad(const Problem &P, const SlotDev *sd, const int32_t *list, 
 void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *dv,
                       double *dots, cudaStream_t st);
 void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
-                           const float *R, double *u, double *acc, cudaStream_t st);
+                           const float *R, float *R0, const double *w, const uint8_t *rstate, double *u, float *ud,
+                           double *acc, cudaStream_t st);
+void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *lbase,
+                        const double *u, const float *ud, const uint8_t *rstate, const double *w, const float *R0,
+                        float *R, double *acc, cudaStream_t st);
 void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
                         const double *u, double *lbase, cudaStream_t st);
 void launch_dual_to_r(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int which,

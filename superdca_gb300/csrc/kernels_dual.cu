@@ -226,13 +226,130 @@ k_dual_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
         atomicAdd(dots + (int64_t)b * 4 * MAXHIST + threadIdx.x, red[threadIdx.x]);
 }
 
+// Base probabilities of a sequence from its R row r = w (p - onehot(y)),
+// normalised to sum 1 (p_y = 1 + r_y / w keeps the precision of 1 - p_y).
+__device__ __forceinline__ void base_probs(float4 r, float w, int y, float p[4])
+{
+    if (!(w > 0.f)) {
+        p[0] = p[1] = p[2] = p[3] = 0.25f;
+        return;
+    }
+    const float iw = 1.f / w;
+    p[0] = r.x * iw + (y == 0 ? 1.f : 0.f);
+    p[1] = r.y * iw + (y == 1 ? 1.f : 0.f);
+    p[2] = r.z * iw + (y == 2 ? 1.f : 0.f);
+    p[3] = r.w * iw + (y == 3 ? 1.f : 0.f);
+#pragma unroll
+    for (int a = 0; a < 4; ++a) p[a] = fmaxf(p[a], 0.f);
+    const float z = p[0] + p[1] + p[2] + p[3];
+    const float iz = z > 0.f ? 1.f / z : 0.f;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) p[a] *= iz;
+}
+
+// A line-search trial as a change from the current point.  With p0 the base
+// probabilities, y the sequence's state at r and t_a = stp (u_a - u_y),
+// per sequence
+//   l(stp) - l(0) = log1p(q),  q = sum_a p0_a expm1(t_a),
+//   p_a(stp) - p0_a = p0_a (expm1(t_a) - q) / (1 + q),
+// and the slope changes by sum_a w (p_a(stp) - p0_a) (u_a - u_y).  Every
+// term is a difference from the sequence's own state, so single precision
+// gives the change with ~1e-7 relative error of the change itself (a
+// well-fitted sequence has q and p0_a, a != y, small), which is what the
+// line search compares; the base values (objective, slope at 0) are FP64.
+// Sequences whose step is large use the FP64 logits.  Sums: ACC_F += w dl,
+// ACC_DG += slope change (against the normalised p0), ACC_RS += R(stp);
+// R <- R(stp).
+constexpr int DT_THREADS = 256;
+
+__global__ void __launch_bounds__(DT_THREADS)
+k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int N, int64_t Nx,
+              const double *__restrict__ lbase, const double *__restrict__ u, const float4 *__restrict__ ud,
+              const uint8_t *__restrict__ rstate, const double *__restrict__ w, const float4 *__restrict__ R0,
+              float4 *__restrict__ R, double *__restrict__ acc)
+{
+    const int b = list[blockIdx.y];
+    const double stp = sd[b].stp;
+    const float stpf = (float)stp;
+    float f = 0.f, dg = 0.f, rs0 = 0.f, rs1 = 0.f, rs2 = 0.f, rs3 = 0.f;
+    double fbig = 0.0, dgbig = 0.0;   // sequences that take the FP64 path
+    for (int i = blockIdx.x * DT_THREADS + threadIdx.x; i < N; i += gridDim.x * DT_THREADS) {
+        const int64_t o = (int64_t)b * Nx + i;
+        const float4 dv4 = ud[o];
+        const float du[4] = {dv4.x, dv4.y, dv4.z, dv4.w};   // u_a - u_y
+        const int y = rstate[o] & 3;
+        const float wi = (float)w[i];
+        float p0[4];
+        base_probs(R0[o], wi, y, p0);
+        float t[4], tmax = 0.f;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            t[a] = stpf * du[a];
+            tmax = fmaxf(tmax, fabsf(t[a]));
+        }
+        float r[4];
+        if (tmax < 30.f) {
+            float e[4], q = 0.f;
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                e[a] = expm1f(t[a]);
+                q = fmaf(p0[a], e[a], q);
+            }
+            const float iq = 1.f / (1.f + q);
+            f = fmaf(wi, log1pf(q), f);
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const float dp = p0[a] * (e[a] - q) * iq;          // p_a(stp) - p0_a
+                dg = fmaf(wi * dp, du[a], dg);
+                r[a] = wi * (p0[a] + dp - (a == y ? 1.f : 0.f));
+            }
+        } else {
+            const double *lb = lbase + o * 4;
+            const double2 ua = reinterpret_cast<const double2 *>(u + o * 4)[0];
+            const double2 ub = reinterpret_cast<const double2 *>(u + o * 4)[1];
+            const double uu[4] = {ua.x, ua.y, ub.x, ub.y};
+            double l0[4], l1[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                l0[a] = lb[a];
+                l1[a] = lb[a] + stp * uu[a];
+            }
+            const double m0 = fmax(fmax(l0[0], l0[1]), fmax(l0[2], l0[3]));
+            const double m1 = fmax(fmax(l1[0], l1[1]), fmax(l1[2], l1[3]));
+            double z0 = 0, z1 = 0, e1[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                z0 += exp(l0[a] - m0);
+                e1[a] = exp(l1[a] - m1);
+                z1 += e1[a];
+            }
+            fbig += (double)wi * ((m1 + log(z1) - l1[y]) - (m0 + log(z0) - l0[y]));
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const double p1 = e1[a] / z1;
+                dgbig += (double)wi * (p1 - (double)p0[a]) * (uu[a] - uu[y]);
+                r[a] = (float)((double)wi * (p1 - (a == y ? 1.0 : 0.0)));
+            }
+        }
+        rs0 += r[0]; rs1 += r[1]; rs2 += r[2]; rs3 += r[3];
+        R[o] = make_float4(r[0], r[1], r[2], r[3]);
+    }
+    // single-precision partial sums per warp, double precision across warps
+    float v[6] = {f, dg, rs0, rs1, rs2, rs3};
+    const int idx[6] = {ACC_F, ACC_DG, ACC_RS0, ACC_RS1, ACC_RS2, ACC_RS3};
+    block_sum_atomic_f<6>(v, acc + (int64_t)b * NACC, idx);
+    if (fbig != 0.0) atomicAdd(acc + (int64_t)b * NACC + ACC_F, fbig);
+    if (dgbig != 0.0) atomicAdd(acc + (int64_t)b * NACC + ACC_DG, dgbig);
+}
+
 // d = coef_g g + sum_j coefS_j s_j + coefY_j y_j (a and k parts); trial
 // logits direction u = k_d + eta_d; sums g.d, d.d, x.d (J parts) and the
 // slope of the search line at 0 from the trial's own numbers, sum_i R_i . u_i
 __global__ void __launch_bounds__(256)
 k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int N, int NV,
-                 int ring, double *__restrict__ dv, const float4 *__restrict__ R, double *__restrict__ u,
-                 double *__restrict__ acc)
+                 int ring, double *__restrict__ dv, const float4 *__restrict__ R, float4 *__restrict__ R0,
+                 const double *__restrict__ w, const uint8_t *__restrict__ rstate, double *__restrict__ u,
+                 float *__restrict__ ud, double *__restrict__ acc)
 {
     const int b = list[blockIdx.y];
     const SlotDev &S = sd[b];
@@ -259,10 +376,20 @@ k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ lis
         const int c = (int)(e & 3);
         const double uu = kk + S.eta[c];
         u[(int64_t)b * Nx * 4 + e] = uu;
+        // the four states of a sequence sit in four consecutive lanes
+        const int64_t o = (int64_t)b * Nx + e / 4;
+        const int y = rstate[o] & 3;
+        const double uy = __shfl_sync(0xffffffffu, uu, (threadIdx.x & ~3) + y);
+        ud[(int64_t)b * Nx * 4 + e] = (float)(uu - uy);
         if (e / 4 < N) {
-            const float4 r = R[(int64_t)b * Nx + e / 4];
-            const float rc = c == 0 ? r.x : c == 1 ? r.y : c == 2 ? r.z : r.w;
-            dg0 += (double)rc * uu;
+            // slope at 0 from the normalised base probabilities, exactly as
+            // the step trials difference against them
+            const float4 r = R[o];
+            const float wi = (float)w[e / 4];
+            float p0[4];
+            base_probs(r, wi, y, p0);
+            if (c == 0) R0[o] = r;
+            dg0 += (double)wi * ((double)p0[c] - (c == y ? 1.0 : 0.0)) * uu;
         }
     }
     double v[4] = {gd, dd, xd, dg0};
@@ -433,12 +560,29 @@ void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, 
 }
 
 void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
-                           const float *R, double *u, double *acc, cudaStream_t st)
+                           const float *R, float *R0, const double *w, const uint8_t *rstate, double *u, float *ud,
+                           double *acc, cudaStream_t st)
 {
     if (n <= 0) return;
     dim3 g(grid_for(P.Nx * 4, 256 * 8, 32), n);
     k_dual_direction<<<g, 256, 0, st>>>(sd, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, P.ring, dv,
-                                        reinterpret_cast<const float4 *>(R), u, acc);
+                                        reinterpret_cast<const float4 *>(R), reinterpret_cast<float4 *>(R0), w,
+                                        rstate, u, ud, acc);
+}
+
+void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *lbase,
+                        const double *u, const float *ud, const uint8_t *rstate, const double *w, const float *R0,
+                        float *R, double *acc, cudaStream_t st)
+{
+    if (n <= 0) return;
+    // a few sequences per thread keep the block sums a small part of the work
+    int gx = (int)((P.N + 4 * DT_THREADS - 1) / (4 * DT_THREADS));
+    if (gx > 32) gx = 32;
+    dim3 grid((unsigned)gx, (unsigned)n);
+    k_trial_delta<<<grid, DT_THREADS, 0, st>>>(sd, list, (int)P.N, P.Nx, lbase, u,
+                                               reinterpret_cast<const float4 *>(ud), rstate, w,
+                                               reinterpret_cast<const float4 *>(R0), reinterpret_cast<float4 *>(R),
+                                               acc);
 }
 
 void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
