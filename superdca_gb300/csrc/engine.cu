@@ -92,6 +92,8 @@ struct SlotHost {
     int last_check = -1000;  // iteration of that check
     double amax_g = 0.0, amax_x = 0.0;  // max |a| of the gradient and of x
     double f0d = 0.0, dg0d = 0.0;       // data parts of f and of the slope at the current point (step trials)
+    double sg_prev[MAXHIST + 1] = {}, yg_prev[MAXHIST + 1] = {};  // s_j.g, y_j.g of the last gradient, by ring position
+    double sy_new = 0.0, yy_new = 0.0;  // s.y and y.y of the newest pair
     MoreThuente ls;
 };
 
@@ -1397,6 +1399,8 @@ int phase_step_dual(sdca_handle *h)
                 if ((int)S.hist.size() == m) S.hist.pop_front();
                 S.hist.push_back(S.ring_new);
                 S.gamma = sy / yy;
+                S.sy_new = sy;
+                S.yy_new = yy;
                 S.iter++;
             } else {
                 S.ring_new = -1;
@@ -1499,19 +1503,23 @@ int phase_step_dual(sdca_handle *h)
                 const int pj = S.hist[j];
                 dt[j] += dot4h(S.eta_s[pj], eg);
                 dt[MAXHIST + j] += dot4h(S.eta_y[pj], eg);
-                if (S.ring_new >= 0) {
-                    dt[2 * MAXHIST + j] += dot4h(S.eta_s[pj], S.eta_y[S.ring_new]);
-                    dt[3 * MAXHIST + j] += dot4h(S.eta_y[pj], S.eta_y[S.ring_new]);
-                }
             }
             if (S.ring_new >= 0) {
+                // the newest pair's column: s_j.y = s_j.g - s_j.g_old, y_j.y likewise,
+                // and its own s.y, y.y from the gradient pass
                 const int pn = S.ring_new;
                 for (int j = 0; j < k; ++j) {
                     const int pj = S.hist[j];
-                    S.SY[pj][pn] = dt[2 * MAXHIST + j];
-                    S.YY[pj][pn] = dt[3 * MAXHIST + j];
-                    S.YY[pn][pj] = dt[3 * MAXHIST + j];
+                    const double syj = pj == pn ? S.sy_new : dt[j] - S.sg_prev[pj];
+                    const double yyj = pj == pn ? S.yy_new : dt[MAXHIST + j] - S.yg_prev[pj];
+                    S.SY[pj][pn] = syj;
+                    S.YY[pj][pn] = yyj;
+                    S.YY[pn][pj] = yyj;
                 }
+            }
+            for (int j = 0; j < k; ++j) {
+                S.sg_prev[S.hist[j]] = dt[j];
+                S.yg_prev[S.hist[j]] = dt[MAXHIST + j];
             }
             double Rm[MAXHIST * MAXHIST], YYm[MAXHIST * MAXHIST], sg[MAXHIST], yg[MAXHIST];
             for (int a = 0; a < k; ++a) {

@@ -183,9 +183,9 @@ k_dual_grad(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
     }
 }
 
-// J-part dots of the history with the gradient and with the newest y:
-// dots[b][j] = a_sj . k_g, [MAXHIST + j] = a_yj . k_g,
-// [2 MAXHIST + j] = a_sj . k_ynew, [3 MAXHIST + j] = a_yj . k_ynew
+// J-part dots of the history with the gradient: dots[b][j] = a_sj . k_g,
+// dots[b][MAXHIST + j] = a_yj . k_g.  (The dots with the newest y follow on
+// the host from these and the previous iteration's: S^T y = S^T g - S^T g_old.)
 __global__ void __launch_bounds__(256)
 k_dual_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
             const double *__restrict__ dv, double *__restrict__ dots)
@@ -193,36 +193,30 @@ k_dual_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
     const int b = list[blockIdx.y];
     const SlotDev &S = sd[b];
     const int k = S.nhist;
-    const bool ynew = S.ring_new >= 0;
     const double *kg = dv + dvo(b, DV_G + S.gcur, 1, NV, Nx);
-    const double *kyn = dv + dvo(b, DV_S + ring + (ynew ? S.ring_new : 0), 1, NV, Nx);
-    double s[4 * MAXHIST];
+    double s[2 * MAXHIST];
 #pragma unroll
-    for (int q = 0; q < 4 * MAXHIST; ++q) s[q] = 0.0;
+    for (int q = 0; q < 2 * MAXHIST; ++q) s[q] = 0.0;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
-        const double g = kg[e], yn = ynew ? kyn[e] : 0.0;
+        const double g = kg[e];
 #pragma unroll
         for (int j = 0; j < MAXHIST; ++j) {
             if (j >= k) break;
-            const double as = dv[dvo(b, DV_S + S.ring[j], 0, NV, Nx) + e];
-            const double ay = dv[dvo(b, DV_S + ring + S.ring[j], 0, NV, Nx) + e];
-            s[j] += as * g;
-            s[MAXHIST + j] += ay * g;
-            s[2 * MAXHIST + j] += as * yn;
-            s[3 * MAXHIST + j] += ay * yn;
+            s[j] += dv[dvo(b, DV_S + S.ring[j], 0, NV, Nx) + e] * g;
+            s[MAXHIST + j] += dv[dvo(b, DV_S + ring + S.ring[j], 0, NV, Nx) + e] * g;
         }
     }
-    __shared__ double red[4 * MAXHIST];
-    if (threadIdx.x < 4 * MAXHIST) red[threadIdx.x] = 0.0;
+    __shared__ double red[2 * MAXHIST];
+    if (threadIdx.x < 2 * MAXHIST) red[threadIdx.x] = 0.0;
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 4 * MAXHIST; ++q) {
+    for (int q = 0; q < 2 * MAXHIST; ++q) {
         if ((q % MAXHIST) >= k) continue;
         const double v = warp_sum(s[q]);
         if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(&red[q], v);
     }
     __syncthreads();
-    if (threadIdx.x < 4 * MAXHIST && red[threadIdx.x] != 0.0)
+    if (threadIdx.x < 2 * MAXHIST && red[threadIdx.x] != 0.0)
         atomicAdd(dots + (int64_t)b * 4 * MAXHIST + threadIdx.x, red[threadIdx.x]);
 }
 

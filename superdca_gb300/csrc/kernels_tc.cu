@@ -425,7 +425,10 @@ constexpr int KD_STAGE = KD_KDIG * KD_A_BYTES + KD_RDIG * KD_B_BYTES;
 constexpr int KD_STG = 3;
 constexpr int KD_SMEM = KD_STG * KD_STAGE + 1024 + 256;
 constexpr uint32_t KD_TMEM_COLS = 512;  // 15 accumulators of 32 columns
-constexpr uint32_t IDESC_KD = (1u << 4) | ((uint32_t)(KD_BN >> 3) << 17) | ((uint32_t)(KD_BM >> 4) << 24);
+// one MMA per K digit covers all five rho digit planes: they are staged
+// back to back, a 160-row B operand, and fill 160 accumulator columns
+constexpr int KD_NB = KD_RDIG * KD_BN;
+constexpr uint32_t IDESC_KD = (1u << 4) | ((uint32_t)(KD_NB >> 3) << 17) | ((uint32_t)(KD_BM >> 4) << 24);
 static_assert(KD_STAGE % 1024 == 0, "stage must keep 1024-byte alignment");
 static_assert(KD_KDIG * KD_RDIG * KD_BN <= (int)KD_TMEM_COLS, "accumulators fit TMEM");
 
@@ -522,15 +525,11 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
                 const uint32_t st = sbase + (uint32_t)s * KD_STAGE;
 #pragma unroll
                 for (int kk = 0; kk < KD_BK / 16; ++kk) {
+                    const uint64_t bd = smem_desc_sw128(st + BOFF + kk * 32);
 #pragma unroll
                     for (int k = 0; k < KD_KDIG; ++k) {
                         const uint64_t ad = smem_desc_sw128(st + k * KD_A_BYTES + kk * 32);
-#pragma unroll
-                        for (int p = 0; p < KD_RDIG; ++p) {
-                            const uint64_t bd = smem_desc_sw128(st + BOFF + p * KD_B_BYTES + kk * 32);
-                            mma_f16_kd(tmem_base + (uint32_t)((k * KD_RDIG + p) * KD_BN), ad, bd,
-                                       (j > 0 || kk > 0) ? 1u : 0u);
-                        }
+                        mma_f16_kd(tmem_base + (uint32_t)(k * KD_NB), ad, bd, (j > 0 || kk > 0) ? 1u : 0u);
                     }
                 }
                 mma_commit(empty(s));
