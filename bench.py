@@ -6,8 +6,11 @@ Workload: the seeded 3000-sequence x 94,000-locus coalescent-tree alignment
 weights (SuperDCA's --no-reweighting path), automatic lambdas, gradient
 threshold 1e-3, zero start.  A step solves one batch of target loci to
 convergence (L-BFGS + More-Thuente, every locus independent); steps take
-disjoint loci.  The alignment (282 MB) and the per-slot solver state are far
-larger than the 129 MB L2, so no L2 flush is needed between steps.
+disjoint loci.  --form picks the engine form: dual (default: the iteration
+kept in the span of the sequences), tc (tensor-core contractions, with the
+learned warm start) or gather (plain).  A step's working set (alignment
+282 MB, agreement digits 54 MB, per-slot solver state) is larger than the
+129 MB L2, so no L2 flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
 
@@ -50,7 +53,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--loci-per-step", type=int, default=0, help="default: batch")
-    ap.add_argument("--form", default="tc", choices=["gather", "tc", "dual"])
+    ap.add_argument("--form", default="dual", choices=["gather", "tc", "dual"])
     ap.add_argument("--history-bf16", action="store_true")
     ap.add_argument("--warm-start", default=os.path.join(ROOT, "superdca_gb300", "warmstart_tree-3000x94000.npy"),
                     help="learned warm-start parameter blob ('none': zero start)")
@@ -154,6 +157,41 @@ def load_workload(args):
     if path:
         np.save(path, st)
     return st
+
+
+def roofline_dual(prof_tot, N, L, m):
+    """Roofline of the dual form's dominant kernel class.
+
+    Work per unit (one target locus through one launch of the class):
+      forward (K rho, exact on the tensor cores): 2 N^2 q FLOP, counted once
+        (the digit expansion issues 15 fp16 products of it on the pipe);
+      backward (one-hot contraction X^T a on the tensor cores: max-norm
+        checks and the final J): 2 N L q^2 FLOP, as in the other forms;
+      history dots: 2k + 1 vectors of N x q doubles read (32 N bytes each);
+      direction: (4k + 3) vectors read, 2 written, u (32 N) and its
+        single-precision differences (16 N) written;
+      line search (step trials): R0, u differences, R (16 N each), states, w."""
+    hbm, tflops, src = measured_peaks()
+    ms, units = prof_tot["kernel_ms"], prof_tot["kernel_units"]
+    cls = max(ms, key=lambda k: ms[k])
+    t = ms[cls] / 1e3
+    if units[cls] == 0 or t <= 0:
+        return None, cls
+    if cls == "forward":
+        ach = 2.0 * N * N * Q * units[cls] / t / 1e12
+        return dict(bound="tensor", achieved=round(ach, 3), peak=tflops, unit="TFLOP/s", frac=round(ach / tflops, 5),
+                    traffic=None, kernel="k_kdig (K rho)", issued_factor=15, peak_source=src), cls
+    if cls == "backward":
+        ach = 2.0 * N * L * Q * Q * units[cls] / t / 1e12
+        return dict(bound="tensor", achieved=round(ach, 3), peak=tflops, unit="TFLOP/s", frac=round(ach / tflops, 5),
+                    traffic=None, kernel="k_gemm (X^T a)", peak_source=src), cls
+    per = {"history": (2 * m + 1) * 32 * N, "direction": ((4 * m + 3) + 2 + 1) * 32 * N + 16 * N,
+           "linesearch": 16 * N * 3 + 9 * N}.get(cls)
+    if per is None:
+        return None, cls
+    ach = per * units[cls] / t / 1e9
+    return dict(bound="hbm", achieved=round(ach, 1), peak=hbm, unit="GB/s", frac=round(ach / hbm, 4),
+                traffic=None, kernel=cls, peak_source=src), cls
 
 
 def roofline(prof_tot, N, L, Dp, m, hist_bytes):
@@ -331,7 +369,10 @@ def engine_arm(args):
               "pair_loci_per_s": float(N * (N - 1) / 2 * L / t_rw), "b_eff": round(float(w_gpu.sum()), 3)}
 
     Dp = ((16 * L + 4 + 63) // 64) * 64
-    rf, dom = roofline(tot, N, L, Dp, 10, 2 if args.history_bf16 else 4)
+    if args.form == "dual":
+        rf, dom = roofline_dual(tot, N, L, 10)
+    else:
+        rf, dom = roofline(tot, N, L, Dp, 10, 2 if args.history_bf16 else 4)
     if rf is not None:
         rf["avg_launch_ms"] = round(tot["kernel_ms"][dom] / max(1, tot["kernel_launches"][dom]), 4)
     out = {
@@ -339,7 +380,9 @@ def engine_arm(args):
         "value": round(value, 4), "unit": "loci/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(t_dev * 1e3 / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp16x2->fp32 (tensor cores), fp64 reductions" if args.form == "tc" else "fp32",
+        "dtype": {"tc": "fp16x2->fp32 (tensor cores), fp64 reductions",
+                  "dual": "exact integer K.rho (fp16 digits, fp32 accumulators), fp64 L-BFGS vectors",
+                  "gather": "fp32"}[args.form],
         "data": "synthetic (seeded coalescent-tree alignment)",
         "config": {"workload": f"{args.workload} seed {args.seed}", "N": int(N), "L": int(L),
                    "batch": B, "loci_per_step": per_step, "form": args.form,

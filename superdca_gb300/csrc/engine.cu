@@ -90,6 +90,7 @@ struct SlotHost {
     double eta_s[MAXHIST + 1][Q] = {}, eta_y[MAXHIST + 1][Q] = {};
     double chk_ratio = 0.0;  // max|g| / ||g|| at the last exact max-norm check (0: none yet)
     int last_check = -1000;  // iteration of that check
+    int chk_wait = 0;        // iterations a wanted check has been deferred
     double amax_g = 0.0, amax_x = 0.0;  // max |a| of the gradient and of x
     double f0d = 0.0, dg0d = 0.0;       // data parts of f and of the slope at the current point (step trials)
     double sg_prev[MAXHIST + 1] = {}, yg_prev[MAXHIST + 1] = {};  // s_j.g, y_j.g of the last gradient, by ring position
@@ -1283,7 +1284,7 @@ int dual_convert(sdca_handle *h, bool force)
     int rc = upload_slots(h, fin);
     if (rc) return rc;
     {
-        Timed t(h, SDCA_K_OTHER, 3 * 4 + 1, (int64_t)fin.size());
+        Timed t(h, SDCA_K_BACKWARD, 3 * 4 + 1, 3 * (int64_t)fin.size());
         for (int d = 0; d < 3; ++d) {
             launch_dual_digits(P, h->sd, h->list, (int)fin.size(), d, h->dv, h->Rchk, h->stream);
             CK(tc_launch_bwd(h->tc, P, h->sd, h->list, (int)fin.size(), h->Rchk, 1.0f, h->Rhi, h->Rlo, h->gpool,
@@ -1346,15 +1347,25 @@ int phase_step_dual(sdca_handle *h)
     CK(cudaMemsetAsync(h->csum, 0, sizeof(long long) * 16 * P.Bmax, h->stream));
     CK(cudaMemsetAsync(h->amax, 0, sizeof(double) * 2 * P.Bmax, h->stream));
     if ((rc = zero_acc(h))) return rc;
+    // Profile classes of this form: "forward" is K rho (a coefficient
+    // vector's logit image, as X d is in the other forms), "backward" the
+    // one-hot contractions X^T a (max-norm checks, final J), "accept" the
+    // iterate update and gradient assembly.
     {
-        Timed t(h, SDCA_K_BACKWARD, h->kd ? 4 : 3, (int64_t)all.size());
+        Timed t(h, SDCA_K_ACCEPT, 1, (int64_t)all.size());
         launch_dual_quant(P, h->sd, h->list, (int)all.size(), h->R, h->rstate, h->qscale, h->rq, h->csum, h->stream);
+    }
+    {
+        Timed t(h, SDCA_K_FORWARD, h->kd ? 2 : 1, (int64_t)all.size());
         if (h->kd)
             CK(tc_launch_kdig(h->kd, P, h->list, (int)all.size(), h->rq, h->rstate, h->csum, 1.0 / h->qscale, h->Rd,
                               h->KR, h->tc_err, h->stream));
         else
             launch_dual_kprod(P, h->list, (int)all.size(), h->rstate, h->Kmat, h->qscale, h->rq, h->csum, h->KR,
                               h->stream);
+    }
+    {
+        Timed t(h, SDCA_K_ACCEPT, 1, (int64_t)all.size());
         launch_dual_grad(P, h->sd, h->list, (int)all.size(), h->qscale, h->rq, h->KR, h->dv, h->acc, h->amax,
                          h->stream);
     }
@@ -1432,11 +1443,27 @@ int phase_step_dual(sdca_handle *h)
         // while ||g|| > 200 threshold on the workloads measured: ratio ~0.01)
         const bool due = S.iterations - S.last_check >= 10 && (S.chk_ratio > 0.0 || gnorm < 200.0 * gtol);
         const bool near = S.chk_ratio > 0.0 && S.chk_ratio * gnorm < 1.5 * gtol;
-        if (due || near || gnorm < gtol || releps_stop[b]) chk.push_back(b);
-        else if (releps_stop[b]) {
-            S.status = 2;
-            stop[b] = 1;
+        if (due || near || gnorm < gtol || releps_stop[b]) {
+            chk.push_back(b);
+            S.chk_wait++;
+        } else {
+            S.chk_wait = 0;
         }
+    }
+    // A check pass costs one tensor-core contraction whether it serves 1 or
+    // 32 slots, while a slot's extra iteration costs a small fraction of
+    // that: slots wanting a check keep iterating until 8 want one, one has
+    // waited 3 iterations, a relative-norm stop is pending, or at most 8
+    // slots are left.
+    if (!chk.empty()) {
+        int active = 0;
+        bool urgent = false;
+        for (int b = 0; b < P.Bmax; ++b) {
+            const int ph = h->slots[b].phase;
+            if (ph != PH_EMPTY && ph != PH_FINALIZE && ph != PH_CONVERT) ++active;
+        }
+        for (int b : chk) urgent = urgent || h->slots[b].chk_wait >= 3 || releps_stop[b];
+        if (!(urgent || (int)chk.size() >= 8 || active <= 8)) chk.clear();
     }
     if (!chk.empty()) {
         double sc = 0.0;
@@ -1461,6 +1488,7 @@ int phase_step_dual(sdca_handle *h)
             S.gmax = gm;
             S.chk_ratio = gnorm > 0.0 ? gm / gnorm : 0.0;
             S.last_check = S.iterations;
+            S.chk_wait = 0;
             if (gm < gtol) {
                 S.status = 0;
                 stop[b] = 1;
