@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="tree-3000x94000")
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--batch", type=int, default=0, help="slots solved together (default: 512 dual, 64 otherwise)")
     ap.add_argument("--loci-per-step", type=int, default=0, help="default: batch")
     ap.add_argument("--form", default="dual", choices=["gather", "tc", "dual"])
     ap.add_argument("--history-bf16", action="store_true")
@@ -275,7 +275,7 @@ def engine_arm(args):
     st = load_workload(args)
     N, L = st.shape
     w = np.ones(N)
-    B = args.batch
+    B = args.batch or (512 if args.form == "dual" else 64)
     per_step = args.loci_per_step or B
     form = {"tc": FORM_TC, "gather": FORM_GATHER, "dual": FORM_DUAL}[args.form]
     E = Engine(N, L, batch=B, device=local, form=form, history_bf16=args.history_bf16)
