@@ -69,10 +69,14 @@ const char *USAGE =
     "  --no-coupling-output               Don't write coupling scores to file.\n"
     "GPU:\n"
     "  --gpu-device arg (=0)              CUDA device.\n"
-    "  --gpu-form arg (=tc)               Contraction form: tc (tensor cores) or plain.\n"
+    "  --gpu-form arg (=dual)             Engine form: dual (span of the sequences), tc (tensor-core\n"
+    "                                     contractions) or plain.\n"
     "  --gpu-batch arg (=64)              Loci solved together.\n"
     "  --gpu-history arg (=fp32)          L-BFGS history storage: fp32 or bf16.\n"
-    "  --gpu-chunk arg (=4096)            Loci per solve call (bounds host memory).\n";
+    "  --gpu-chunk arg (=4096)            Loci per solve call (bounds host memory).\n"
+    "  --gpu-top-k arg (=0)               Write only the K strongest pairs, strongest first.\n"
+    "  --gpu-binary-output                Also write <id>.SuperDCA_couplings.<base>-based.bin:\n"
+    "                                     records of float score, int32 r, int32 n (little endian).\n";
 
 struct Options {
     std::vector<std::string> alignment_files;
@@ -88,9 +92,9 @@ struct Options {
     bool norm_of_mean = false;
     double gradient_threshold = 1e-3, lambda_h = -1.0, lambda_J = -1.0;
     bool no_dca = false, no_coupling_output = false;
-    int device = 0, batch = 64, form = SDCA_FORM_TC;
-    bool history_bf16 = false;
-    long chunk = 4096;
+    int device = 0, batch = 0, form = SDCA_FORM_DUAL;
+    bool history_bf16 = false, binary_output = false;
+    long chunk = 4096, top_k = 0;
 };
 
 [[noreturn]] void fail(const std::string &msg)
@@ -127,7 +131,7 @@ Options parse_options(int argc, char **argv)
         {"output-samplelist-alignment", &o.out_samplelist}, {"no-filter-alignment", &o.no_filter},
         {"no-reweighting", &o.no_reweighting}, {"output-weights", &o.output_weights},
         {"norm-of-mean-scoring", &o.norm_of_mean}, {"no-dca", &o.no_dca},
-        {"no-coupling-output", &o.no_coupling_output},
+        {"no-coupling-output", &o.no_coupling_output}, {"gpu-binary-output", &o.binary_output},
     };
     for (int i = 1; i < argc; ++i) {
         std::string a = argv[i];
@@ -181,10 +185,12 @@ Options parse_options(int argc, char **argv)
         else if (name == "gpu-device") o.device = parse_number<int>(opt, value);
         else if (name == "gpu-batch") o.batch = parse_number<int>(opt, value);
         else if (name == "gpu-chunk") o.chunk = parse_number<long>(opt, value);
+        else if (name == "gpu-top-k") o.top_k = parse_number<long>(opt, value);
         else if (name == "gpu-form") {
             if (value == "tc") o.form = SDCA_FORM_TC;
             else if (value == "plain") o.form = SDCA_FORM_GATHER;
-            else fail("--gpu-form must be tc or plain");
+            else if (value == "dual") o.form = SDCA_FORM_DUAL;
+            else fail("--gpu-form must be dual, tc or plain");
         } else if (name == "gpu-history") {
             if (value == "fp32") o.history_bf16 = false;
             else if (value == "bf16") o.history_bf16 = true;
@@ -195,6 +201,7 @@ Options parse_options(int argc, char **argv)
     if (o.alignment_files.size() > 2) fail("at most two alignment files");
     if (o.gradient_threshold <= 0) fail("--gradient-threshold must be positive");
     if (o.chunk < 1) fail("--gpu-chunk must be positive");
+    if (o.top_k < 0) fail("--gpu-top-k must be >= 0");
     return o;
 }
 
@@ -472,6 +479,149 @@ void write_couplings(const std::string &path, const std::vector<float> &S, const
     if (std::fclose(f) != 0) fail("failed to write \"" + path + "\"");
 }
 
+// ---- norm-of-mean scoring (plmDCA.hpp:335-363, 617-666)
+
+// J_r[n][s][a] in SuperDCA's parameter layout (16-locus blocks, STATES order)
+inline int64_t ref_index(int64_t L, int64_t n, int s, int a)
+{
+    const int64_t b = n / 16, p = n % 16;
+    const int64_t e = b < L / 16 ? 16 : L % 16;
+    return b * 256 + (s * e + p) * 4 + a;
+}
+
+// The reference keeps each block as a float matrix, transposed for n < r
+// (plmDCA.hpp:338-361): rows are then the state of r for n < r and the
+// state of n for n > r.
+void stored_block(const double *x, int64_t L, int64_t r, int64_t n, float M[4][4])
+{
+    for (int s = 0; s < 4; ++s)
+        for (int a = 0; a < 4; ++a) {
+            const float v = (float)x[ref_index(L, n, s, a)];
+            if (n < r) M[a][s] = v;
+            else M[s][a] = v;
+        }
+}
+
+// ising_gauge as SuperDCA evaluates it (plmDCA_utility.hpp:57-83): the row
+// means are spread along columns and the column means along rows.
+void ising_gauge(const float M[4][4], float G[4][4])
+{
+    float rm[4], cm[4], gm = 0.f;
+    for (int i = 0; i < 4; ++i) rm[i] = (M[i][0] + M[i][1] + M[i][2] + M[i][3]) / 4.f;
+    for (int j = 0; j < 4; ++j) cm[j] = (M[0][j] + M[1][j] + M[2][j] + M[3][j]) / 4.f;
+    for (int i = 0; i < 4; ++i) gm += rm[i];
+    gm /= 4.f;
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) G[i][j] = ((M[i][j] - rm[j]) - cm[i]) + gm;
+}
+
+// Frobenius norm without the GAP row and column (Matrix_math.hpp:166-213)
+float frobenius(const float G[4][4], int gap)
+{
+    float sum = 0.f;
+    for (int i = 0; i < 4; ++i) {
+        if (i == gap) continue;
+        for (int j = 0; j < 4; ++j)
+            if (j != gap) sum += G[i][j] * G[i][j];
+    }
+    return std::sqrt(sum);
+}
+
+// Lines of norm-of-mean scoring (plmDCA.hpp:617-666): for r over the loci
+// list and n before it, "|mean of the gauged blocks| r n |J_rn| |J_nr| mean
+// of the two norms".  Blocks: B[k][j] = block (loci[k], loci[j]), 16 floats.
+// (The reference's storage indexes row i from i (d - 1), so block (i, d - 1)
+// shares its memory with (i + 1, 0), plmDCA.hpp:129-137; every block here
+// has its own storage.)
+void write_norm_of_mean(const std::string &path, const std::vector<float> &B, const std::vector<uint32_t> &loci,
+                        const std::vector<int64_t> &translation, int base, int gap)
+{
+    std::FILE *f = std::fopen(path.c_str(), "wb");
+    if (!f) fail("cannot open \"" + path + "\" for writing");
+    const size_t n = loci.size();
+    std::string out;
+    char tmp[64];
+    auto put = [&](double v) {
+        char *p = std::to_chars(tmp, tmp + sizeof tmp, v, std::chars_format::fixed, 8).ptr;
+        out.append(tmp, p);
+    };
+    for (size_t k = 0; k < n; ++k) {
+        out.clear();
+        for (size_t j = 0; j < k; ++j) {
+            const float(*Mrn)[4] = reinterpret_cast<const float(*)[4]>(&B[(k * n + j) * 16]);
+            const float(*Mnr)[4] = reinterpret_cast<const float(*)[4]>(&B[(j * n + k) * 16]);
+            float Ga[4][4], Gb[4][4], Gm[4][4];
+            ising_gauge(Mrn, Ga);
+            ising_gauge(Mnr, Gb);
+            for (int a = 0; a < 4; ++a)
+                for (int c = 0; c < 4; ++c) Gm[a][c] = (Ga[a][c] + Gb[a][c]) * 0.5f;
+            const float jn = frobenius(Gm, gap), jij = frobenius(Ga, gap), jji = frobenius(Gb, gap);
+            put(jn);
+            out += ' ' + std::to_string(translation[loci[k]] + base) + ' ' +
+                   std::to_string(translation[loci[j]] + base) + ' ';
+            put(jij);
+            out += ' ';
+            put(jji);
+            out += ' ';
+            put((double)(jij + jji) * 0.5);
+            out += '\n';
+        }
+        if (!out.empty() && std::fwrite(out.data(), 1, out.size(), f) != out.size())
+            fail("failed to write \"" + path + "\"");
+    }
+    if (std::fclose(f) != 0) fail("failed to write \"" + path + "\"");
+}
+
+// The strongest pairs of mean-of-norms scoring, strongest first (ties by
+// list order), in the text format; optionally every pair as binary records.
+void write_top_and_binary(const std::string &stem, const std::vector<float> &S, const std::vector<uint32_t> &loci,
+                          const std::vector<int64_t> &translation, int base, long top_k, bool binary, bool verbose)
+{
+    const size_t n = loci.size();
+    struct Rec { float v; int32_t r, m; };
+    std::vector<Rec> recs;
+    recs.reserve(n * (n - 1) / 2);
+    for (size_t k = 0; k < n; ++k)
+        for (size_t j = 0; j < k; ++j) {
+            const float sum = S[k * n + j] + S[j * n + k];
+            recs.push_back({(float)((double)sum * 0.5), (int32_t)(translation[loci[k]] + base),
+                            (int32_t)(translation[loci[j]] + base)});
+        }
+    if (binary) {
+        const std::string path = unique_name(stem + ".bin");
+        if (verbose) std::cout << "superdca-gb300: writing binary coupling records to \"" << path << "\"\n";
+        std::FILE *f = std::fopen(path.c_str(), "wb");
+        if (!f) fail("cannot open \"" + path + "\" for writing");
+        for (const Rec &q : recs) {
+            unsigned char buf[12];
+            uint32_t u;
+            std::memcpy(&u, &q.v, 4);
+            const uint32_t w[3] = {u, (uint32_t)q.r, (uint32_t)q.m};
+            for (int t = 0; t < 3; ++t)
+                for (int byte = 0; byte < 4; ++byte) buf[4 * t + byte] = (unsigned char)(w[t] >> (8 * byte));
+            if (std::fwrite(buf, 1, 12, f) != 12) fail("failed to write \"" + path + "\"");
+        }
+        if (std::fclose(f) != 0) fail("failed to write \"" + path + "\"");
+    }
+    if (top_k > 0) {
+        const size_t kk = std::min<size_t>((size_t)top_k, recs.size());
+        std::vector<size_t> idx(recs.size());
+        for (size_t t = 0; t < idx.size(); ++t) idx[t] = t;
+        std::partial_sort(idx.begin(), idx.begin() + kk, idx.end(), [&](size_t a, size_t b) {
+            return recs[a].v > recs[b].v || (recs[a].v == recs[b].v && a < b);
+        });
+        const std::string path = unique_name(stem + ".top" + std::to_string(kk));
+        if (verbose) std::cout << "superdca-gb300: writing the " << kk << " strongest pairs to \"" << path << "\"\n";
+        std::FILE *f = std::fopen(path.c_str(), "wb");
+        if (!f) fail("cannot open \"" + path + "\" for writing");
+        for (size_t t = 0; t < kk; ++t) {
+            const Rec &q = recs[idx[t]];
+            std::fprintf(f, "%.8f %d %d\n", (double)q.v, q.r, q.m);
+        }
+        if (std::fclose(f) != 0) fail("failed to write \"" + path + "\"");
+    }
+}
+
 } // namespace
 
 int main(int argc, char **argv)
@@ -479,8 +629,6 @@ int main(int argc, char **argv)
     const Options o = parse_options(argc, argv);
     if (o.alignment_files.size() > 1)
         fail("the two-alignment scan mode is not supported by this build");
-    if (o.norm_of_mean)
-        fail("--norm-of-mean-scoring is not supported by this build");
     const int threads = o.threads > 0 ? o.threads : (int)std::max(1u, std::thread::hardware_concurrency());
 
     if (o.verbose) std::cout << "superdca-gb300: read alignment \"" << o.alignment_files[0] << "\"\n";
@@ -547,7 +695,13 @@ int main(int argc, char **argv)
         cfg.lambda_h = o.lambda_h;
         cfg.lambda_J = o.lambda_J;
         cfg.gradient_threshold = o.gradient_threshold;
-        cfg.batch = o.batch;
+        cfg.batch = o.batch > 0 ? o.batch : (o.form == SDCA_FORM_DUAL ? 256 : 64);
+        if (cfg.form == SDCA_FORM_DUAL && N > 16383) {
+            // the dual form keeps N x N agreement counts; larger alignments use the tensor cores
+            if (o.verbose) std::cout << "superdca-gb300: " << N << " sequences: using the tensor-core form\n";
+            cfg.form = SDCA_FORM_TC;
+            if (o.batch <= 0) cfg.batch = 64;
+        }
         cfg.form = o.form;
         cfg.flags = o.history_bf16 ? SDCA_FLAG_HISTORY_BF16 : 0;
         cfg.device = o.device;
@@ -580,20 +734,36 @@ int main(int argc, char **argv)
         std::cout << "superdca-gb300: B_eff = " << beff << ", lambda_h = " << lh << ", lambda_J = " << lJ << "\n";
     }
 
-    // Solve the loci list in chunks; keep the scores of the listed columns.
+    // Solve the loci list in chunks; keep the scores of the listed columns
+    // (and, for norm-of-mean scoring, their 4 x 4 blocks).
     const size_t n = loci.size();
-    std::vector<float> S(n * n);
+    const int64_t D = 16 * L + 4;
+    std::vector<float> S(n * n), blocks;
+    if (o.norm_of_mean) blocks.assign(n * n * 16, 0.f);
     std::vector<float> rows;
+    std::vector<double> xs;
     std::vector<sdca_locus_stat> stats;
     size_t not_converged = 0;
-    for (size_t k0 = 0; k0 < n; k0 += (size_t)o.chunk) {
-        const size_t m = std::min(n - k0, (size_t)o.chunk);
+    // solutions are D doubles per locus: keep a chunk of them under ~1 GB
+    const size_t chunk = o.norm_of_mean ? std::max<size_t>(1, std::min<size_t>((size_t)o.chunk, (1ull << 27) / D))
+                                        : (size_t)o.chunk;
+    for (size_t k0 = 0; k0 < n; k0 += chunk) {
+        const size_t m = std::min(n - k0, chunk);
         rows.resize(m * (size_t)L);
         stats.resize(m);
-        check(sdca_solve(H.h, loci.data() + k0, m, rows.data(), stats.data()), H.h, "solve failed");
+        if (o.norm_of_mean) xs.resize(m * (size_t)D);
+        check(sdca_solve_ex(H.h, loci.data() + k0, m, nullptr, o.norm_of_mean ? xs.data() : nullptr, rows.data(),
+                            stats.data()),
+              H.h, "solve failed");
         for (size_t k = 0; k < m; ++k) {
             for (size_t j = 0; j < n; ++j) S[(k0 + k) * n + j] = rows[k * (size_t)L + loci[j]];
             not_converged += stats[k].status != 0;
+            if (o.norm_of_mean)
+                for (size_t j = 0; j < n; ++j) {
+                    if (loci[j] == loci[k0 + k]) continue;
+                    stored_block(xs.data() + k * D, L, loci[k0 + k], loci[j],
+                                 reinterpret_cast<float(*)[4]>(&blocks[((k0 + k) * n + j) * 16]));
+                }
         }
         if (o.verbose)
             std::cout << "superdca-gb300: solved " << k0 + m << " of " << n << " loci\n" << std::flush;
@@ -605,7 +775,11 @@ int main(int argc, char **argv)
         const std::string path =
             unique_name(a.id + ".SuperDCA_couplings." + std::to_string(o.out_base) + "-based.all");
         if (o.verbose) std::cout << "superdca-gb300: writing coupling values to file \"" << path << "\"\n";
-        write_couplings(path, S, loci, translation, o.out_base, threads);
+        if (o.norm_of_mean) write_norm_of_mean(path, blocks, loci, translation, o.out_base, 3);
+        else write_couplings(path, S, loci, translation, o.out_base, threads);
+        if (o.top_k > 0 || o.binary_output)
+            write_top_and_binary(a.id + ".SuperDCA_couplings." + std::to_string(o.out_base) + "-based", S, loci,
+                                 translation, o.out_base, o.top_k, o.binary_output, o.verbose);
     }
     return EXIT_SUCCESS;
 }

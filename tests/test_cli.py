@@ -159,3 +159,65 @@ def test_gpu_cli_couplings_match_oracle(cli, tmp_path, oracle_mod):
     assert idx == [(rr, nn) for _, rr, nn in want]
     assert all(len(g.split()[0].split(".")[1]) == 8 for g in got[:100])
     np.testing.assert_allclose(vals, [v for v, _, _ in want], rtol=0, atol=1e-4)
+
+
+def _gauge(M):
+    """SuperDCA's ising_gauge as it evaluates (row means spread along columns),
+    in single precision."""
+    M = M.astype(np.float32)
+    rm = M.sum(1, dtype=np.float32) / np.float32(4)
+    cm = M.sum(0, dtype=np.float32) / np.float32(4)
+    gm = rm.sum(dtype=np.float32) / np.float32(4)
+    return ((M - rm[None, :]) - cm[:, None]) + gm
+
+
+def _frob(G, gap=3):
+    keep = [i for i in range(4) if i != gap]
+    return float(np.sqrt((G[np.ix_(keep, keep)].astype(np.float64) ** 2).sum()))
+
+
+@pytest.mark.gpu
+def test_gpu_cli_norm_of_mean_top_k_and_binary(cli, tmp_path, oracle_mod):
+    """--norm-of-mean-scoring (plmDCA.hpp:335-363, 617-666) against blocks
+    from the oracle's solutions; --gpu-top-k and --gpu-binary-output against
+    the text file of the same run."""
+    O = oracle_mod
+    nuc, _ = synthetic.independent(N=150, L=90, n_pairs=6, seed=11)
+    A.write_fasta(str(tmp_path / "nm.fasta"), nuc)
+    r = run(cli, ["--no-reweighting", "--norm-of-mean-scoring", "nm.fasta"], tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    states, cols = A.encode(nuc)
+    N, L = states.shape
+    w = np.ones(N)
+    lh, lJ = O.lambdas(w)[:2]
+    _, _, xs = O.Problem(states, w, lh, lJ).solve(np.arange(L), threads=os.cpu_count() or 1, want_x=True)
+    I = O.ref_index(L)
+
+    def block(r, n):
+        J = xs[r][I[n]]                      # [s][a]
+        return (J.T if n < r else J).astype(np.float32)
+
+    got = (tmp_path / "nm.SuperDCA_couplings.1-based.all").read_text().splitlines()
+    assert len(got) == L * (L - 1) // 2
+    k = 0
+    for rr in range(L):
+        for nn in range(rr):
+            f = got[k].split()
+            k += 1
+            assert (int(f[1]), int(f[2])) == (cols[rr] + 1, cols[nn] + 1)
+            Ga, Gb = _gauge(block(rr, nn)), _gauge(block(nn, rr))
+            want = [_frob((Ga + Gb) * np.float32(0.5)), _frob(Ga), _frob(Gb)]
+            np.testing.assert_allclose([float(f[0]), float(f[3]), float(f[4])], want, rtol=0, atol=1e-4)
+            assert abs(float(f[5]) - 0.5 * (float(f[3]) + float(f[4]))) < 2e-8
+
+    r = run(cli, ["--no-reweighting", "--gpu-top-k", "25", "--gpu-binary-output", "nm.fasta"], tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    text = (tmp_path / "nm.SuperDCA_couplings.1-based.all.1").read_text().splitlines()
+    vals = np.array([float(t.split()[0]) for t in text])
+    recs = np.fromfile(tmp_path / "nm.SuperDCA_couplings.1-based.bin", dtype=[("v", "<f4"), ("r", "<i4"), ("n", "<i4")])
+    assert len(recs) == len(text)
+    np.testing.assert_allclose(recs["v"].astype(np.float64), vals, rtol=0, atol=1e-8)
+    assert [(int(t.split()[1]), int(t.split()[2])) for t in text] == list(zip(recs["r"].tolist(), recs["n"].tolist()))
+    top = (tmp_path / "nm.SuperDCA_couplings.1-based.top25").read_text().splitlines()
+    assert len(top) == 25
+    np.testing.assert_allclose([float(t.split()[0]) for t in top], np.sort(vals)[::-1][:25], rtol=0, atol=1e-8)
