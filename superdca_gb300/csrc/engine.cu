@@ -152,7 +152,7 @@ struct sdca_handle {
     std::vector<int> trace_loci;  // SDCA_TRACE=<locus>[,<locus>...]: per-iteration solver state on stderr
 
     // dual form (kernels_dual.cu)
-    double *dv = nullptr, *u64 = nullptr, *KR = nullptr, *amax = nullptr, *J64 = nullptr;
+    double *dv = nullptr, *u64 = nullptr, *KR = nullptr, *amax = nullptr, *J64 = nullptr, *amax_h = nullptr;
     int32_t *rq = nullptr, *Kmat = nullptr;
     long long *csum = nullptr;
     float *Rchk = nullptr, *R0 = nullptr;   // R0: R at the current point, base of the step trials
@@ -1342,10 +1342,21 @@ int phase_step_dual(sdca_handle *h)
             }
         }
     }
-    // gradient at the accepted points
+    // gradient at the accepted points, and its dots with every live history
+    // position (the history and the pair just pushed) in the same round trip
     if ((rc = upload_slots(h, all))) return rc;
+    for (int b : all) {
+        SlotHost &S = h->slots[b];
+        SlotDev &D = h->sd_h[b];
+        int k = 0;
+        for (int p : S.hist) D.ring[k++] = p;
+        if (S.push && S.ring_new >= 0) D.ring[k++] = S.ring_new;
+        D.nhist = k;
+    }
+    if ((rc = staged_h2d(h, h->sd, h->sd_h, sizeof(SlotDev) * P.Bmax))) return rc;
     CK(cudaMemsetAsync(h->csum, 0, sizeof(long long) * 16 * P.Bmax, h->stream));
     CK(cudaMemsetAsync(h->amax, 0, sizeof(double) * 2 * P.Bmax, h->stream));
+    CK(cudaMemsetAsync(h->dots, 0, sizeof(double) * 4 * MAXHIST * P.Bmax, h->stream));
     if ((rc = zero_acc(h))) return rc;
     // Profile classes of this form: "forward" is K rho (a coefficient
     // vector's logit image, as X d is in the other forms), "backward" the
@@ -1369,9 +1380,14 @@ int phase_step_dual(sdca_handle *h)
         launch_dual_grad(P, h->sd, h->list, (int)all.size(), h->qscale, h->rq, h->KR, h->dv, h->acc, h->amax,
                          h->stream);
     }
+    {
+        Timed t(h, SDCA_K_HISTORY, 1, (int64_t)all.size());
+        launch_dual_dots(P, h->sd, h->list, (int)all.size(), 1, h->dv, h->dots, h->stream);
+    }
     CKL();
-    std::vector<double> amax(2 * P.Bmax);
-    CK(cudaMemcpyAsync(amax.data(), h->amax, sizeof(double) * 2 * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
+    const double *amax = h->amax_h;
+    CK(cudaMemcpyAsync(h->amax_h, h->amax, sizeof(double) * 2 * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(h->dots_h, h->dots, sizeof(double) * 4 * MAXHIST * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
     if ((rc = fetch_acc(h))) return rc;
 
     std::vector<int32_t> cont, fin, chk;
@@ -1438,11 +1454,12 @@ int phase_step_dual(sdca_handle *h)
         const double releps = 1e-4 * std::max(1.0, std::sqrt(S.x2J + S.x2H));
         releps_stop[b] = gnorm < releps;
         // the max-norm test needs J = Phi^T a_g: run it when the last check's
-        // ratio max|g| / ||g|| predicts a pass, and every 10 iterations
+        // ratio max|g| / ||g|| predicts a pass, and every 15 iterations (a
+        // check costs about three iterations of the slot)
         // (before the first check the max-norm is far above the threshold
-        // while ||g|| > 200 threshold on the workloads measured: ratio ~0.01)
-        const bool due = S.iterations - S.last_check >= 10 && (S.chk_ratio > 0.0 || gnorm < 200.0 * gtol);
-        const bool near = S.chk_ratio > 0.0 && S.chk_ratio * gnorm < 1.5 * gtol;
+        // while ||g|| > 150 threshold on the workloads measured: ratio ~0.01)
+        const bool due = S.iterations - S.last_check >= 15 && (S.chk_ratio > 0.0 || gnorm < 150.0 * gtol);
+        const bool near = S.chk_ratio > 0.0 && S.chk_ratio * gnorm < 1.1 * gtol;
         if (due || near || gnorm < gtol || releps_stop[b]) {
             chk.push_back(b);
             S.chk_wait++;
@@ -1504,21 +1521,6 @@ int phase_step_dual(sdca_handle *h)
     if ((rc = dual_convert(h, false))) return rc;
     if (cont.empty()) return SDCA_OK;
 
-    std::vector<int32_t> withh;
-    for (int b : cont)
-        if (!h->slots[b].hist.empty()) withh.push_back(b);
-    if (!withh.empty()) {
-        if ((rc = upload_slots(h, withh))) return rc;
-        CK(cudaMemsetAsync(h->dots, 0, sizeof(double) * 4 * MAXHIST * P.Bmax, h->stream));
-        {
-            Timed t(h, SDCA_K_HISTORY, 1, (int64_t)withh.size());
-            launch_dual_dots(P, h->sd, h->list, (int)withh.size(), h->dv, h->dots, h->stream);
-        }
-        CKL();
-        CK(cudaMemcpyAsync(h->dots_h, h->dots, sizeof(double) * 4 * MAXHIST * P.Bmax, cudaMemcpyDeviceToHost,
-                           h->stream));
-        { const int r_ = stream_sync(h); if (r_) return r_; }
-    }
     for (int b : cont) {
         SlotHost &S = h->slots[b];
         SlotDev &D = h->sd_h[b];
@@ -1526,11 +1528,13 @@ int phase_step_dual(sdca_handle *h)
         const double *eg = S.eta_g[S.gcur];
         D.coef_g = -1.0;
         if (k > 0) {
-            double *dt = h->dots_h + (int64_t)b * 4 * MAXHIST;
+            // dots by history index j from the ones by ring position
+            const double *dp = h->dots_h + (int64_t)b * 4 * MAXHIST;
+            double dt[2 * MAXHIST];
             for (int j = 0; j < k; ++j) {
                 const int pj = S.hist[j];
-                dt[j] += dot4h(S.eta_s[pj], eg);
-                dt[MAXHIST + j] += dot4h(S.eta_y[pj], eg);
+                dt[j] = dp[pj] + dot4h(S.eta_s[pj], eg);
+                dt[MAXHIST + j] = dp[DOT_Y + pj] + dot4h(S.eta_y[pj], eg);
             }
             if (S.ring_new >= 0) {
                 // the newest pair's column: s_j.y = s_j.g - s_j.g_old, y_j.y likewise,
@@ -1795,7 +1799,8 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
         (rc = halloc(h, &h->acc_h, B * NACC)) || (rc = halloc(h, &h->dots_h, B * 4 * MAXHIST)) ||
         (rc = halloc(h, &h->rows_h, B * P.L)) || (rc = halloc(h, &h->flag_h, 4)) ||
         (rc = halloc(h, &h->stage, (h->stage_cap = 64 * (((sizeof(SlotDev) + 4) * B + 1024 + 255) & ~(size_t)255)))) ||
-        (dual && ((rc = dalloc(h, &h->dv, B * NV * 2 * P.Nx * 4)) || (rc = dalloc(h, &h->u64, B * P.Nx * 4)) ||
+        (dual && ((rc = halloc(h, &h->amax_h, 2 * B)) ||
+                  (rc = dalloc(h, &h->dv, B * NV * 2 * P.Nx * 4)) || (rc = dalloc(h, &h->u64, B * P.Nx * 4)) ||
                   (rc = dalloc(h, &h->KR, B * P.Nx * 4)) || (rc = dalloc(h, &h->amax, 2 * B)) ||
                   (rc = dalloc(h, &h->rq, B * P.Nx * 4)) || (rc = dalloc(h, &h->csum, 16 * B)) ||
                   (rc = dalloc(h, &h->Rchk, B * P.Nx * 4)) || (rc = dalloc(h, &h->J64, B * P.Dp)) ||

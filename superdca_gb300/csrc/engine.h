@@ -73,7 +73,7 @@ struct SlotDev {
     int32_t gcur;           // g buffer holding the accepted gradient (0/1)
     int32_t ring_new;       // history position written by the last accept, -1 none
     int32_t nhist;          // history pairs in use
-    int32_t ring[MAXHIST];  // history positions, oldest first
+    int32_t ring[MAXHIST + 1];  // history positions, oldest first (dual-form dots: all live positions)
     int32_t flags;          // SLOT_F_*
     int32_t pad_;
     double stp;             // trial (or accepted) step along d
@@ -89,6 +89,7 @@ struct SlotDev {
 // dual form: per slot, vectors (a, k = K a) of N x 4 doubles each:
 // x, d, two gradients, then the s ring and the y ring (P.ring positions each)
 constexpr int DV_X = 0, DV_D = 1, DV_G = 2, DV_S = 4;
+constexpr int DOT_Y = 2 * MAXHIST;  // dual-form dots by ring position: s at [p], y at [DOT_Y + p]
 
 enum SlotFlags {
     SLOT_F_USE_U = 1,       // trial logits use lbase + stp u (else lbase)
@@ -163,7 +164,7 @@ void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8
                        double qscale, const int32_t *rq, const long long *csum, double *KR, cudaStream_t st);
 void launch_dual_grad(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double qscale,
                       const int32_t *rq, const double *KR, double *dv, double *acc, double *amax, cudaStream_t st);
-void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *dv,
+void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int newg, const double *dv,
                       double *dots, cudaStream_t st);
 void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
                            const float *R, float *R0, const double *w, const uint8_t *rstate, double *u, float *ud,

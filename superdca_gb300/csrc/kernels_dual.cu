@@ -183,41 +183,46 @@ k_dual_grad(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
     }
 }
 
-// J-part dots of the history with the gradient: dots[b][j] = a_sj . k_g,
-// dots[b][MAXHIST + j] = a_yj . k_g.  (The dots with the newest y follow on
-// the host from these and the previous iteration's: S^T y = S^T g - S^T g_old.)
+// J-part dots of the history pairs listed in the slot's ring[] with a
+// gradient, stored by ring position p: dots[b][p] = a_sp . k_g,
+// dots[b][DOT_Y + p] = a_yp . k_g.  newg: the gradient just formed (buffer
+// 1 - gcur) instead of the accepted one.  (The dots with the newest y follow
+// on the host from these and the previous iteration's: S^T y = S^T g - S^T g_old.)
 __global__ void __launch_bounds__(256)
 k_dual_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
-            const double *__restrict__ dv, double *__restrict__ dots)
+            int newg, const double *__restrict__ dv, double *__restrict__ dots)
 {
+    constexpr int NP = MAXHIST + 1;   // live positions: a full history and the pair just pushed
     const int b = list[blockIdx.y];
     const SlotDev &S = sd[b];
     const int k = S.nhist;
-    const double *kg = dv + dvo(b, DV_G + S.gcur, 1, NV, Nx);
-    double s[2 * MAXHIST];
+    const double *kg = dv + dvo(b, DV_G + (newg ? 1 - S.gcur : S.gcur), 1, NV, Nx);
+    double s[2 * NP];
 #pragma unroll
-    for (int q = 0; q < 2 * MAXHIST; ++q) s[q] = 0.0;
+    for (int q = 0; q < 2 * NP; ++q) s[q] = 0.0;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
         const double g = kg[e];
 #pragma unroll
-        for (int j = 0; j < MAXHIST; ++j) {
+        for (int j = 0; j < NP; ++j) {
             if (j >= k) break;
             s[j] += dv[dvo(b, DV_S + S.ring[j], 0, NV, Nx) + e] * g;
-            s[MAXHIST + j] += dv[dvo(b, DV_S + ring + S.ring[j], 0, NV, Nx) + e] * g;
+            s[NP + j] += dv[dvo(b, DV_S + ring + S.ring[j], 0, NV, Nx) + e] * g;
         }
     }
-    __shared__ double red[2 * MAXHIST];
-    if (threadIdx.x < 2 * MAXHIST) red[threadIdx.x] = 0.0;
+    __shared__ double red[2 * NP];
+    if (threadIdx.x < 2 * NP) red[threadIdx.x] = 0.0;
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 2 * MAXHIST; ++q) {
-        if ((q % MAXHIST) >= k) continue;
+    for (int q = 0; q < 2 * NP; ++q) {
+        if ((q % NP) >= k) continue;
         const double v = warp_sum(s[q]);
         if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(&red[q], v);
     }
     __syncthreads();
-    if (threadIdx.x < 2 * MAXHIST && red[threadIdx.x] != 0.0)
-        atomicAdd(dots + (int64_t)b * 4 * MAXHIST + threadIdx.x, red[threadIdx.x]);
+    if (threadIdx.x < 2 * NP && (threadIdx.x % NP) < k && red[threadIdx.x] != 0.0) {
+        const int q = threadIdx.x, j = q % NP;
+        atomicAdd(dots + (int64_t)b * 4 * MAXHIST + (q < NP ? 0 : DOT_Y) + S.ring[j], red[q]);
+    }
 }
 
 // Base probabilities of a sequence from its R row r = w (p - onehot(y)),
@@ -545,12 +550,12 @@ void launch_dual_grad(const Problem &P, const SlotDev *sd, const int32_t *list, 
     k_dual_grad<<<gg, 256, 0, st>>>(sd, list, P.Nx, NV, P.ring, P.lambda_J, rq, 1.0 / qscale, KR, dv, acc, amax);
 }
 
-void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *dv,
+void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int newg, const double *dv,
                       double *dots, cudaStream_t st)
 {
     if (n <= 0) return;
     dim3 g(grid_for(P.Nx * 4, 256 * 8, 32), n);
-    k_dual_dots<<<g, 256, 0, st>>>(sd, list, P.Nx, DV_S + 2 * P.ring, P.ring, dv, dots);
+    k_dual_dots<<<g, 256, 0, st>>>(sd, list, P.Nx, DV_S + 2 * P.ring, P.ring, newg, dv, dots);
 }
 
 void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
