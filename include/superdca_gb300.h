@@ -126,6 +126,16 @@ int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weig
 int sdca_compute_weights(sdca_handle *h, const uint8_t *states, const double *mult,
                          double threshold, double *weights_out);
 
+/* Two-alignment scan mode (SuperDCA with two alignment files:
+ * plmDCA_objective.hpp:67, plmDCA.hpp:338-346, 370-377, 484-490): the
+ * targets are the columns of a second alignment of the same sequences
+ * (N x n_target_loci row-major codes), the features are every locus of the
+ * alignment set by sdca_set_alignment, none excluded, and scores are taken
+ * from the blocks as stored (untransposed).  Afterwards the loci of
+ * sdca_solve* and sdca_eval index target columns.  NULL targets return to
+ * the single-alignment mode; sdca_set_alignment does too. */
+int sdca_set_targets(sdca_handle *h, const uint8_t *targets, int64_t n_target_loci);
+
 /* B_eff and the absolute regularisation strengths in force. */
 int sdca_get_lambdas(const sdca_handle *h, double *lambda_h, double *lambda_J,
                      double *b_eff);

@@ -28,7 +28,7 @@ _i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 class OrcProblem(C.Structure):
     _fields_ = [("states", C.c_void_p), ("weights", C.c_void_p), ("N", C.c_int64),
                 ("L", C.c_int64), ("q", C.c_int), ("lambda_h", C.c_double),
-                ("lambda_J", C.c_double)]
+                ("lambda_J", C.c_double), ("targets", C.c_void_p), ("LT", C.c_int64)]
 
 
 class OrcStat(C.Structure):
@@ -110,14 +110,20 @@ def weights(states, threshold=0.9, mult=None):
 class Problem:
     """An alignment (N x L codes 0..q-1), weights and absolute lambdas."""
 
-    def __init__(self, states, weights, lambda_h, lambda_J, q=4):
+    def __init__(self, states, weights, lambda_h, lambda_J, q=4, targets=None):
+        """targets: N x LT target columns for the two-alignment scan mode
+        (plmDCA_objective.hpp:67): locus r is targets[:, r] and every column
+        of states is a feature."""
         self.states = np.ascontiguousarray(states, dtype=np.uint8)
         self.weights = np.ascontiguousarray(weights, dtype=np.float64)
         self.N, self.L = self.states.shape
         self.q = q
         self.lambda_h, self.lambda_J = float(lambda_h), float(lambda_J)
+        self.targets = None if targets is None else np.ascontiguousarray(targets, dtype=np.uint8)
+        LT = 0 if self.targets is None else self.targets.shape[1]
         self._c = OrcProblem(self.states.ctypes.data, self.weights.ctypes.data, self.N,
-                             self.L, q, self.lambda_h, self.lambda_J)
+                             self.L, q, self.lambda_h, self.lambda_J,
+                             None if self.targets is None else self.targets.ctypes.data, LT)
 
     @property
     def D(self):

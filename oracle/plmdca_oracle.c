@@ -52,7 +52,8 @@ double orc_objective(const orc_problem *p, int64_t r, const double *x,
     const int q = p->q;
     const int64_t N = p->N, L = p->L, qq = (int64_t)q * q;
     const int64_t nblocks = (L + ORC_BLOCK - 1) / ORC_BLOCK;
-    const int64_t r_block = r / ORC_BLOCK, r_local = r % ORC_BLOCK;
+    const int scan = p->targets != NULL;   /* scan: r_block is past the last block, nothing excluded */
+    const int64_t r_block = scan ? -1 : r / ORC_BLOCK, r_local = scan ? -1 : r % ORC_BLOCK;
     const double *h = x + qq * L;
     double *lp = (double *)malloc(sizeof(double) * N * q);
     double *nb = (double *)malloc(sizeof(double) * N * q);
@@ -83,7 +84,7 @@ double orc_objective(const orc_problem *p, int64_t r, const double *x,
     /* pseudo-likelihood terms and node beliefs (plmDCA_objective.hpp:126-151) */
     for (int64_t i = 0; i < N; ++i) {
         const double *l = lp + i * q;
-        const int sr = p->states[i * L + r];
+        const int sr = scan ? p->targets[i * p->LT + r] : p->states[i * L + r];
         const double w = p->weights[i];
         for (int a = 0; a < q; ++a) e[a] = exp(l[a]);
         const double z = log(hsum(e, q));
@@ -599,7 +600,9 @@ static void *solve_worker(void *arg)
         orc_stat st;
         orc_minimize(pl->p, r, x, pl->max_iter, pl->gtol, pl->m, &st);
         if (pl->stats) pl->stats[k] = st;
-        if (pl->scores) orc_score_row(x, pl->p->L, pl->p->q, r, pl->gap, pl->scores + k * pl->p->L);
+        /* scan mode scores every block as stored, untransposed (plmDCA.hpp:370-377) */
+        if (pl->scores)
+            orc_score_row(x, pl->p->L, pl->p->q, pl->p->targets ? -1 : r, pl->gap, pl->scores + k * pl->p->L);
         if (pl->x_out) memcpy(pl->x_out + k * D, x, sizeof(double) * D);
     }
     free(x);

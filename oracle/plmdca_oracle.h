@@ -46,6 +46,10 @@ typedef struct {
     int q;                   /* states per locus (4 in SuperDCA) */
     double lambda_h;         /* absolute strengths (already times B_eff) */
     double lambda_J;
+    const uint8_t *targets;  /* two-alignment scan mode (plmDCA_objective.hpp:67): N x LT target
+                                columns; locus r is targets[:, r] and no feature locus is
+                                excluded.  NULL: the target is states[:, r]. */
+    int64_t LT;
 } orc_problem;
 
 typedef struct {

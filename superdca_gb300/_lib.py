@@ -33,7 +33,7 @@ EXPORTS = ["sdca_abi_version", "sdca_config_default", "sdca_create", "sdca_set_a
            "sdca_compute_weights", "sdca_get_lambdas", "sdca_solve", "sdca_solve_ex", "sdca_eval",
            "sdca_get_profile", "sdca_last_error", "sdca_destroy", "sdca_eval_noalloc",
            "sdca_set_warm_start", "sdca_ws_features", "sdca_mlp_blob_size", "sdca_mlp_grad",
-           "sdca_mlp_predict", "sdca_mlp_train", "sdca_mlp_last_error"]
+           "sdca_mlp_predict", "sdca_mlp_train", "sdca_mlp_last_error", "sdca_set_targets"]
 
 
 class Config(C.Structure):
@@ -86,6 +86,7 @@ def load(path: str = LIB_PATH):
     L.sdca_destroy.argtypes = [vp]
     L.sdca_eval_noalloc.argtypes = [vp, i64, i64, vp, dp, dp, C.c_uint32, vp, vp, vp, vp]
     L.sdca_set_warm_start.argtypes = [vp, vp, C.c_size_t]
+    L.sdca_set_targets.argtypes = [vp, vp, i64]
     L.sdca_ws_features.argtypes = [vp, C.c_int, C.c_float, vp, C.c_size_t, vp, C.c_size_t, vp]
     L.sdca_mlp_blob_size.argtypes = []
     L.sdca_mlp_grad.argtypes = [vp, vp, vp, i64, C.POINTER(dp), vp]

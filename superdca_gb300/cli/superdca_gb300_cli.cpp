@@ -627,13 +627,22 @@ void write_top_and_binary(const std::string &stem, const std::vector<float> &S, 
 int main(int argc, char **argv)
 {
     const Options o = parse_options(argc, argv);
-    if (o.alignment_files.size() > 1)
-        fail("the two-alignment scan mode is not supported by this build");
     const int threads = o.threads > 0 ? o.threads : (int)std::max(1u, std::thread::hardware_concurrency());
+    // Two alignment files: the scan mode (SuperDCA.cpp:271-301, plmDCA.hpp:470-493).
+    // The loci of the first are the targets, every locus of the second a
+    // feature; the sequences (rows) are the same.
+    const bool scan = o.alignment_files.size() == 2;
 
     if (o.verbose) std::cout << "superdca-gb300: read alignment \"" << o.alignment_files[0] << "\"\n";
     Alignment a = read_fasta(o.alignment_files[0]);
     if (o.verbose) std::cout << "superdca-gb300: " << a.N << " sequences, " << a.L << " loci\n";
+    Alignment a2;
+    if (scan) {
+        if (o.verbose) std::cout << "superdca-gb300: read alignment \"" << o.alignment_files[1] << "\"\n";
+        a2 = read_fasta(o.alignment_files[1]);
+        if (a2.N != a.N) fail("the two alignments must hold the same sequences (" + std::to_string(a.N) + " and " +
+                              std::to_string(a2.N) + " rows)");
+    }
 
     if (!o.filterlist.empty()) {
         std::vector<int64_t> cols = read_index_list(o.filterlist, o.in_base);
@@ -644,42 +653,66 @@ int main(int argc, char **argv)
         a = select_columns(a, cols);
         if (o.out_filterlist) write_fasta(a, o, "filterlist-selected");
     } else {
-        if (!o.no_filter) a = select_columns(a, filter_columns(a, o.maf, o.gap));
-        if (o.out_filtered) {
-            write_fasta(a, o, "filtered");
-            write_loci(a, o);
+        for (Alignment *al : {&a, &a2}) {
+            if (al == &a2 && !scan) continue;
+            if (!o.no_filter) *al = select_columns(*al, filter_columns(*al, o.maf, o.gap));
+            if (o.out_filtered) {
+                write_fasta(*al, o, "filtered");
+                write_loci(*al, o);
+            }
         }
     }
     if (!o.samplelist.empty()) {
+        // (SuperDCA selects the samples of the first alignment only; the rows
+        // of the two must stay matched, so here both are selected)
         std::vector<int64_t> rows = read_index_list(o.samplelist, o.in_base);
         for (int64_t r : rows)
             if (r >= a.N) fail("sample list index " + std::to_string(r + o.in_base) + " is beyond the alignment");
         a = select_rows(a, rows, stem(o.samplelist));
+        if (scan) a2 = select_rows(a2, rows, a2.id);
         if (o.out_samplelist) write_fasta(a, o, "samplelist-selected");
     }
 
     std::vector<int64_t> kept;
-    const std::vector<uint8_t> states = four_state(a, kept);
+    const std::vector<uint8_t> states1 = four_state(a, kept);
     std::vector<int64_t> translation(kept.size());
     for (size_t k = 0; k < kept.size(); ++k) translation[k] = a.translation[kept[k]];
-    const int64_t N = a.N, L = (int64_t)kept.size();
-    if (o.verbose) std::cout << "superdca-gb300: 4-state alignment has " << N << " sequences and " << L << " loci\n";
+    const int64_t N = a.N, L1 = (int64_t)kept.size();
+    // features: the alignment itself, or the second one in the scan mode
+    std::vector<uint8_t> states2;
+    std::vector<int64_t> translation2;
+    if (scan) {
+        std::vector<int64_t> kept2;
+        states2 = four_state(a2, kept2);
+        translation2.resize(kept2.size());
+        for (size_t k = 0; k < kept2.size(); ++k) translation2[k] = a2.translation[kept2[k]];
+    }
+    const std::vector<uint8_t> &states = scan ? states2 : states1;
+    const int64_t L = scan ? (int64_t)translation2.size() : L1;
+    if (o.verbose) {
+        std::cout << "superdca-gb300: 4-state alignment has " << N << " sequences and " << L1 << " loci\n";
+        if (scan) std::cout << "superdca-gb300: scan against " << L << " loci of the second alignment\n";
+    }
 
     std::vector<uint32_t> loci;
     if (!o.locilist.empty()) {
         for (int64_t v : read_index_list(o.locilist, o.in_base)) {
-            if (v >= L) fail("loci list index " + std::to_string(v + o.in_base) + " is beyond the alignment");
+            if (v >= L1) fail("loci list index " + std::to_string(v + o.in_base) + " is beyond the alignment");
             loci.push_back((uint32_t)v);
         }
     } else {
-        const int64_t end = o.end_locus < 0 ? L : std::min<int64_t>(L, o.end_locus + 1);
+        const int64_t end = o.end_locus < 0 ? L1 : std::min<int64_t>(L1, o.end_locus + 1);
         for (int64_t n = o.begin_locus; n < end; ++n) loci.push_back((uint32_t)n);
     }
-    if (L == 0) {
+    if (L1 == 0 || L == 0) {
         std::cerr << "superdca-gb300: there are no loci to analyze (need at least 2)\n";
         return EXIT_FAILURE;
     }
-    if (loci.size() < 2) {
+    if (scan && loci.empty()) {
+        std::cerr << "superdca-gb300: there are no target loci to analyze\n";
+        return EXIT_FAILURE;
+    }
+    if (!scan && loci.size() < 2) {
         std::cerr << "superdca-gb300: there are not enough loci for plmDCA analysis (found " << loci.size()
                   << " loci that qualify, but need at least 2)\n";
         return EXIT_FAILURE;
@@ -728,10 +761,53 @@ int main(int argc, char **argv)
     }
 
     check(sdca_set_alignment(H.h, states.data(), weights.data()), H.h, "alignment upload failed");
+    if (scan) check(sdca_set_targets(H.h, states1.data(), L1), H.h, "target upload failed");
     if (o.verbose) {
         double lh, lJ, beff;
         sdca_get_lambdas(H.h, &lh, &lJ, &beff);
         std::cout << "superdca-gb300: B_eff = " << beff << ", lambda_h = " << lh << ", lambda_J = " << lJ << "\n";
+    }
+
+    if (scan) {
+        // lines "S[r][n] r n" for r over the target list and every feature
+        // locus n (plmDCA.hpp:638-645, 673-680); the norm-of-mean mode prints
+        // the same norm of the untransposed block
+        std::FILE *f = nullptr;
+        std::string path;
+        if (!o.no_coupling_output) {
+            path = unique_name(a.id + "_scan.SuperDCA_couplings." + std::to_string(o.out_base) + "-based.all");
+            if (o.verbose) std::cout << "superdca-gb300: writing coupling values to file \"" << path << "\"\n";
+            f = std::fopen(path.c_str(), "wb");
+            if (!f) fail("cannot open \"" + path + "\" for writing");
+        }
+        std::vector<float> rows;
+        std::vector<sdca_locus_stat> stats;
+        std::string out;
+        char tmp[64];
+        size_t not_converged = 0;
+        for (size_t k0 = 0; k0 < loci.size(); k0 += (size_t)o.chunk) {
+            const size_t m = std::min(loci.size() - k0, (size_t)o.chunk);
+            rows.resize(m * (size_t)L);
+            stats.resize(m);
+            check(sdca_solve(H.h, loci.data() + k0, m, rows.data(), stats.data()), H.h, "solve failed");
+            for (size_t k = 0; k < m; ++k) {
+                not_converged += stats[k].status != 0;
+                if (!f) continue;
+                out.clear();
+                const std::string rs = std::to_string(translation[loci[k0 + k]] + o.out_base);
+                for (int64_t nn = 0; nn < L; ++nn) {
+                    char *p = std::to_chars(tmp, tmp + sizeof tmp, (double)rows[k * (size_t)L + nn],
+                                            std::chars_format::fixed, 8).ptr;
+                    out.append(tmp, p);
+                    out += ' ' + rs + ' ' + std::to_string(translation2[nn] + o.out_base) + '\n';
+                }
+                if (std::fwrite(out.data(), 1, out.size(), f) != out.size()) fail("failed to write \"" + path + "\"");
+            }
+        }
+        if (f && std::fclose(f) != 0) fail("failed to write \"" + path + "\"");
+        if (not_converged)
+            std::cerr << "superdca-gb300: " << not_converged << " loci stopped before the gradient threshold\n";
+        return EXIT_SUCCESS;
     }
 
     // Solve the loci list in chunks; keep the scores of the listed columns

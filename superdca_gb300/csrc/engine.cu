@@ -161,6 +161,11 @@ struct sdca_handle {
     KdPlan *kd = nullptr;          // exact K rho on the tensor cores (N <= 4000), else CUDA cores
     __half *Kd = nullptr, *Rd = nullptr;
 
+    // two-alignment scan mode: target columns from a second alignment
+    uint8_t *TT = nullptr;        // [LT][Nx] target states, locus-major
+    int64_t LT = 0;
+    bool scan = false;
+
     // learned warm start (warmstart.cu, mlp.cu)
     float *ws_params = nullptr;
     bool ws_on = false;
@@ -396,7 +401,7 @@ int upload_slots(sdca_handle *h, const std::vector<int32_t> &lst)
     for (int b : lst) {
         SlotHost &S = h->slots[b];
         SlotDev &D = h->sd_h[b];
-        D.locus = S.locus;
+        D.locus = h->scan ? -1 : S.locus;   // scan mode: no feature locus is excluded
         D.gcur = S.gcur;
         D.ring_new = S.ring_new;
         D.nhist = (int)S.hist.size();
@@ -497,7 +502,7 @@ int slot_begin(sdca_handle *h, int b, int64_t k, int32_t locus, const float *x0_
     else
         CK(cudaMemsetAsync(wab, 0, sizeof(float) * P.Dp, h->stream));
     CK(cudaMemsetAsync(h->d + (int64_t)b * P.Dp, 0, sizeof(float) * P.Dp, h->stream));
-    CK(cudaMemcpyAsync(h->rstate + (int64_t)b * P.Nx, h->XT + (int64_t)locus * P.Nx, P.Nx,
+    CK(cudaMemcpyAsync(h->rstate + (int64_t)b * P.Nx, (h->scan ? h->TT : h->XT) + (int64_t)locus * P.Nx, P.Nx,
                        cudaMemcpyDeviceToDevice, h->stream));
     if (!x0_engine)
         CK(cudaMemsetAsync(h->lbase + (int64_t)b * P.Nx * 4, 0, sizeof(double) * P.Nx * 4, h->stream));
@@ -705,7 +710,7 @@ int refill(sdca_handle *h, Queue &Qu)
             // the copy reads the staging buffer: finish it before the next slot reuses it
             { const int r_ = stream_sync(h); if (r_) return r_; }
             warm.push_back(b);
-        } else if (h->ws_on && h->form != SDCA_FORM_DUAL) {
+        } else if (h->ws_on && h->form != SDCA_FORM_DUAL && !h->scan) {
             learned.push_back(b);
         }
     }
@@ -1853,6 +1858,7 @@ int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weig
 {
     if (!h) return SDCA_E_ARG;
     h->knn_k = 0;
+    h->scan = false;
     if (!states || !weights) return fail(h, SDCA_E_ARG, "states and weights are required");
     Problem &P = h->P;
     for (int64_t i = 0; i < P.N; ++i)
@@ -1935,8 +1941,9 @@ int sdca_solve_ex(sdca_handle *h, const uint32_t *loci, size_t n_loci, const dou
     int rc = check_ready(h);
     if (rc) return rc;
     if (n_loci > 0 && !loci) return fail(h, SDCA_E_ARG, "null loci list");
+    const int64_t nt = h->scan ? h->LT : h->P.L;   // scan mode: loci are target columns
     for (size_t k = 0; k < n_loci; ++k)
-        if ((int64_t)loci[k] >= h->P.L) return fail(h, SDCA_E_ARG, "locus index out of range");
+        if ((int64_t)loci[k] >= nt) return fail(h, SDCA_E_ARG, "locus index out of range");
     CK(cudaSetDevice(h->cfg.device));
     const int64_t h2d0 = h->prof.h2d_bytes;
     prof_reset(h);
@@ -1986,7 +1993,7 @@ int sdca_eval(sdca_handle *h, uint32_t r, const double *x, double *f, double *g)
     if (rc) return rc;
     if (!x || !f) return fail(h, SDCA_E_ARG, "null argument");
     const Problem &P = h->P;
-    if ((int64_t)r >= P.L) return fail(h, SDCA_E_ARG, "locus index out of range");
+    if ((int64_t)r >= (h->scan ? h->LT : P.L)) return fail(h, SDCA_E_ARG, "locus index out of range");
     CK(cudaSetDevice(h->cfg.device));
     prof_reset(h);
     std::vector<float> xe(P.Dp);
@@ -2095,6 +2102,56 @@ int sdca_compute_weights(sdca_handle *h, const uint8_t *states, const double *mu
     return rc;
 }
 
+int sdca_set_targets(sdca_handle *h, const uint8_t *targets, int64_t n_target_loci)
+{
+    if (!h) return SDCA_E_ARG;
+    if (!h->has_alignment) return fail(h, SDCA_E_STATE, "sdca_set_alignment must come first");
+    if (h->TT) {
+        cudaFree(h->TT);
+        h->TT = nullptr;
+    }
+    h->scan = false;
+    h->LT = 0;
+    if (!targets) return SDCA_OK;
+    const Problem &P = h->P;
+    if (n_target_loci < 1 || n_target_loci > (1LL << 26)) return fail(h, SDCA_E_ARG, "invalid number of target loci");
+    for (int64_t e = 0; e < P.N * n_target_loci; ++e)
+        if (targets[e] >= Q) return fail(h, SDCA_E_ARG, "state codes must be in 0..q-1");
+    CK(cudaSetDevice(h->cfg.device));
+    const int64_t LTx = round_up(n_target_loci, 64);
+    uint8_t *tmp = nullptr;
+    if (cudaMalloc(&tmp, (size_t)P.N * LTx) != cudaSuccess ||
+        cudaMalloc(&h->TT, (size_t)n_target_loci * P.Nx) != cudaSuccess) {
+        cudaGetLastError();
+        if (tmp) cudaFree(tmp);
+        h->TT = nullptr;
+        return fail(h, SDCA_E_NOMEM, "device allocation for the target columns failed");
+    }
+    int rc = SDCA_OK;
+    do {
+        if (cudaMemsetAsync(h->TT, 0, (size_t)n_target_loci * P.Nx, h->stream) != cudaSuccess ||
+            cudaMemcpy2DAsync(tmp, LTx, targets, n_target_loci, n_target_loci, P.N, cudaMemcpyHostToDevice,
+                              h->stream) != cudaSuccess ||
+            cudaMemsetAsync(h->flag, 0, sizeof(int), h->stream) != cudaSuccess) {
+            rc = fail(h, SDCA_E_CUDA, "target upload failed");
+            break;
+        }
+        dim3 grid((unsigned)((n_target_loci + 63) / 64), (unsigned)((P.Nx + 63) / 64));
+        k_transpose<<<grid, 256, 0, h->stream>>>(tmp, LTx, (int)P.N, (int)n_target_loci, h->TT, P.Nx, h->flag);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess)
+            rc = fail(h, SDCA_E_CUDA, "target transpose failed");
+    } while (0);
+    cudaFree(tmp);
+    if (rc) {
+        cudaFree(h->TT);
+        h->TT = nullptr;
+        return rc;
+    }
+    h->LT = n_target_loci;
+    h->scan = true;
+    return SDCA_OK;
+}
+
 int sdca_set_warm_start(sdca_handle *h, const float *params, size_t n_params)
 {
     if (!h) return SDCA_E_ARG;
@@ -2189,6 +2246,7 @@ int sdca_destroy(sdca_handle *h)
     for (auto e : h->ev_pool) cudaEventDestroy(e);
     if (h->tc) tc_plan_destroy(h->tc);
     if (h->kd) tc_kdig_plan_destroy(h->kd);
+    if (h->TT) cudaFree(h->TT);
     free_all(h);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     delete h;

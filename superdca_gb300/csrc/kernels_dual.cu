@@ -40,6 +40,7 @@ k_dual_quant(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, i
              unsigned long long *__restrict__ csum)
 {
     const int b = list[blockIdx.y];
+    const bool own = sd[b].locus >= 0;   // scan mode: no own-agreement correction
     __shared__ unsigned long long red[16];
     if (threadIdx.x < 16) red[threadIdx.x] = 0ull;
     __syncthreads();
@@ -50,7 +51,7 @@ k_dual_quant(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, i
             const float4 v = R[(int64_t)b * Nx + i];
             q = make_int4((int)llrint((double)v.x * qscale), (int)llrint((double)v.y * qscale),
                           (int)llrint((double)v.z * qscale), (int)llrint((double)v.w * qscale));
-            const int y = rstate[(int64_t)b * Nx + i] & 3;
+            const int y = own ? (rstate[(int64_t)b * Nx + i] & 3) : -1;
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
                 if (a != y) continue;

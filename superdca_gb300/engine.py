@@ -133,6 +133,18 @@ class Engine:
             weak_searches=np.array([s.weak_searches for s in st]),
             max_trials=np.array([s.max_trials for s in st]))
 
+    def set_targets(self, targets):
+        """Two-alignment scan mode: solve the columns of `targets` (N x LT codes,
+        the same sequences) against every locus of the alignment; loci of
+        later solves index target columns.  None returns to the usual mode."""
+        if targets is None:
+            self._targets = None
+            self._check(self.lib.sdca_set_targets(self.h, None, 0))
+            return
+        self._targets = np.ascontiguousarray(targets, dtype=np.uint8)
+        assert self._targets.shape[0] == self.N
+        self._check(self.lib.sdca_set_targets(self.h, _ptr(self._targets), self._targets.shape[1]))
+
     def set_warm_start(self, blob):
         """Start later solves (without x_init) from the learned warm start
         given by a parameter blob (superdca_gb300.warmstart); None disables."""

@@ -73,8 +73,11 @@ def test_cli_help_and_option_errors(cli, tmp_path):
     (tmp_path / "bad.fasta").write_text(">a\nACGT\n>b\nACG\n")
     r = run(cli, ["bad.fasta"], tmp_path)
     assert r.returncode == 1 and "has length 3, expected 4" in r.stderr
-    r = run(cli, ["a.fasta", "b.fasta"], tmp_path)
-    assert r.returncode == 1 and "scan mode" in r.stderr
+    r = run(cli, ["a.fasta", "b.fasta", "c.fasta"], tmp_path)
+    assert r.returncode == 1 and "at most two alignment files" in r.stderr
+    (tmp_path / "b.fasta").write_text(">a\nACGT\n")
+    r = run(cli, ["bad.fasta", "b.fasta"], tmp_path)
+    assert r.returncode == 1
 
 
 def test_cli_filter_encode_and_side_outputs(cli, tmp_path):

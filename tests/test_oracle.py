@@ -157,3 +157,35 @@ def test_mlp_oracle_gradient_matches_finite_differences():
         q[i] -= 2 * h
         fm = M.loss_and_grad(q, X, T)[0]
         assert abs((fp - fm) / (2 * h) - g[i]) <= 1e-6 * max(1.0, abs(g[i])), i
+
+
+def test_oracle_scan_objective_matches_direct_statement():
+    """Two-alignment scan mode (plmDCA_objective.hpp:67): the target is a
+    column of the second alignment and no feature locus is excluded.  The
+    oracle against a direct numpy statement of the objective and gradient."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(8)
+    N, L, LT = 40, 21, 3
+    st = rng.integers(0, 4, size=(N, L)).astype(np.uint8)
+    tg = rng.integers(0, 4, size=(N, LT)).astype(np.uint8)
+    w = rng.uniform(0.2, 1.0, N)
+    lh, lJ = 0.7, 0.3
+    P = O.Problem(st, w, lh, lJ, targets=tg)
+    I = O.ref_index(L)
+    oh = np.eye(4)[st]                                  # N L s
+    for r in range(LT):
+        x = rng.normal(size=16 * L + 4) * 0.3
+        J = x[I]                                        # [n][s][a]
+        h = x[16 * L:]
+        l = h + np.einsum('ins,nsa->ia', oh, J)
+        m = l.max(1, keepdims=True)
+        lse = (m + np.log(np.exp(l - m).sum(1, keepdims=True)))[:, 0]
+        y = tg[:, r]
+        f = (w * (lse - l[np.arange(N), y])).sum() + lh * (h ** 2).sum() + lJ * (J ** 2).sum()
+        R = w[:, None] * (np.exp(l - lse[:, None]) - np.eye(4)[y])
+        gJ = np.einsum('ins,ia->nsa', oh, R) + 2 * lJ * J
+        gh = R.sum(0) + 2 * lh * h
+        fo, go = P.objective(r, x)
+        assert fo == pytest.approx(f, rel=1e-12)
+        np.testing.assert_allclose(go[I], gJ, rtol=0, atol=1e-11)
+        np.testing.assert_allclose(go[16 * L:], gh, rtol=0, atol=1e-11)
