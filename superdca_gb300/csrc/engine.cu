@@ -701,7 +701,7 @@ int refill(sdca_handle *h, Queue &Qu)
             return fail(h, SDCA_E_UNSUPPORTED, "the dual form starts every locus from zero (no x_init)");
         if (Qu.x_init) {
             const double *xr = Qu.x_init + k * (QQ * h->P.L + Q);
-            ref_to_engine(h->P, Qu.loci[k], xr, Qu.xbuf.data());
+            ref_to_engine(h->P, h->scan ? -1 : (int64_t)Qu.loci[k], xr, Qu.xbuf.data());
             x0 = Qu.xbuf.data();
         }
         int rc = slot_begin(h, b, k, (int32_t)Qu.loci[k], x0);
@@ -1997,7 +1997,7 @@ int sdca_eval(sdca_handle *h, uint32_t r, const double *x, double *f, double *g)
     CK(cudaSetDevice(h->cfg.device));
     prof_reset(h);
     std::vector<float> xe(P.Dp);
-    ref_to_engine(P, r, x, xe.data());
+    ref_to_engine(P, h->scan ? -1 : (int64_t)r, x, xe.data());
     const int b = 0;
     rc = slot_begin(h, b, 0, (int32_t)r, xe.data());
     if (rc) return rc;
