@@ -155,7 +155,7 @@ struct sdca_handle {
     double *dv = nullptr, *u64 = nullptr, *KR = nullptr, *amax = nullptr, *J64 = nullptr, *amax_h = nullptr;
     int32_t *rq = nullptr, *Kmat = nullptr;
     long long *csum = nullptr;
-    float *Rchk = nullptr, *R0 = nullptr;   // R0: R at the current point, base of the step trials
+    float *Rchk = nullptr, *P0 = nullptr;   // P0: probabilities at the current point, base of the step trials
     float *ud = nullptr;                    // u_a - u_y per sequence (single precision, step trials)
     double qscale = 1.0;
     KdPlan *kd = nullptr;          // exact K rho on the tensor cores (N <= 4000), else CUDA cores
@@ -818,7 +818,7 @@ int phase_trials(sdca_handle *h, Queue &Qu)
                 if ((rc = upload_list(h, delta))) return rc;
                 Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)delta.size());
                 launch_trial_delta(P, h->sd, h->list, (int)delta.size(), h->lbase, h->u64, h->ud, h->rstate, h->w,
-                                   h->R0, h->R, h->acc, h->stream);
+                                   h->P0, h->R, h->acc, h->stream);
             }
             if (!full.empty()) {
                 if ((rc = upload_list(h, full))) return rc;
@@ -1507,6 +1507,9 @@ int phase_step_dual(sdca_handle *h)
             double gm = acc_get(h, b, ACC_GMAX);
             for (int a = 0; a < Q; ++a) gm = std::max(gm, std::fabs(eg[a]));
             const double gnorm = std::sqrt(std::max(S.g2, 0.0));
+            if (std::find(h->trace_loci.begin(), h->trace_loci.end(), S.locus) != h->trace_loci.end())
+                std::fprintf(stderr, "trace r=%d it=%d check max|g_J|=%.4e g_h=%.4e %.4e %.4e %.4e |g|=%.4e\n",
+                             S.locus, S.iterations, acc_get(h, b, ACC_GMAX), eg[0], eg[1], eg[2], eg[3], gnorm);
             S.gmax = gm;
             S.chk_ratio = gnorm > 0.0 ? gm / gnorm : 0.0;
             S.last_check = S.iterations;
@@ -1522,7 +1525,12 @@ int phase_step_dual(sdca_handle *h)
     }
     for (int b : all) (stop[b] ? fin : cont).push_back(b);
 
-    for (int b : fin) h->slots[b].phase = PH_CONVERT;
+    for (int b : fin) {
+        const SlotHost &S = h->slots[b];
+        if (std::find(h->trace_loci.begin(), h->trace_loci.end(), S.locus) != h->trace_loci.end())
+            std::fprintf(stderr, "trace r=%d it=%d stop status=%d f=%.12e\n", S.locus, S.iterations, S.status, S.f);
+        h->slots[b].phase = PH_CONVERT;
+    }
     if ((rc = dual_convert(h, false))) return rc;
     if (cont.empty()) return SDCA_OK;
 
@@ -1608,7 +1616,7 @@ int phase_step_dual(sdca_handle *h)
         if ((r2 = zero_acc(h))) return r2;
         {
             Timed t(h, SDCA_K_DIRECTION, 1, (int64_t)lst.size());
-            launch_dual_direction(P, h->sd, h->list, (int)lst.size(), h->dv, h->R, h->R0, h->w, h->rstate, h->u64,
+            launch_dual_direction(P, h->sd, h->list, (int)lst.size(), h->dv, h->lbase, h->P0, h->w, h->rstate, h->u64,
                                   h->ud, h->acc, h->stream);
         }
         CKL();
@@ -1809,7 +1817,7 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
                   (rc = dalloc(h, &h->KR, B * P.Nx * 4)) || (rc = dalloc(h, &h->amax, 2 * B)) ||
                   (rc = dalloc(h, &h->rq, B * P.Nx * 4)) || (rc = dalloc(h, &h->csum, 16 * B)) ||
                   (rc = dalloc(h, &h->Rchk, B * P.Nx * 4)) || (rc = dalloc(h, &h->J64, B * P.Dp)) ||
-                  (rc = dalloc(h, &h->R0, B * P.Nx * 4)) || (rc = dalloc(h, &h->ud, B * P.Nx * 4)) ||
+                  (rc = dalloc(h, &h->P0, B * P.Nx * 4)) || (rc = dalloc(h, &h->ud, B * P.Nx * 4)) ||
                   (rc = dalloc(h, &h->Kmat, (size_t)P.Nx * P.Nx)) ||
                   (P.N <= 4000 && P.L < (1 << 18) &&
                    ((rc = dalloc(h, &h->Kd, (size_t)3 * kd_nk_rows(P) * P.Nx)) ||

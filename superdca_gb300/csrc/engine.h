@@ -167,10 +167,10 @@ void launch_dual_grad(const Problem &P, const SlotDev *sd, const int32_t *list, 
 void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int newg, const double *dv,
                       double *dots, cudaStream_t st);
 void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
-                           const float *R, float *R0, const double *w, const uint8_t *rstate, double *u, float *ud,
-                           double *acc, cudaStream_t st);
+                           const double *lbase, float *P0, const double *w, const uint8_t *rstate, double *u,
+                           float *ud, double *acc, cudaStream_t st);
 void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *lbase,
-                        const double *u, const float *ud, const uint8_t *rstate, const double *w, const float *R0,
+                        const double *u, const float *ud, const uint8_t *rstate, const double *w, const float *P0,
                         float *R, double *acc, cudaStream_t st);
 void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
                         const double *u, double *lbase, cudaStream_t st);

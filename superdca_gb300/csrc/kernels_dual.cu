@@ -226,46 +226,27 @@ k_dual_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
     }
 }
 
-// Base probabilities of a sequence from its R row r = w (p - onehot(y)),
-// normalised to sum 1 (p_y = 1 + r_y / w keeps the precision of 1 - p_y).
-__device__ __forceinline__ void base_probs(float4 r, float w, int y, float p[4])
-{
-    if (!(w > 0.f)) {
-        p[0] = p[1] = p[2] = p[3] = 0.25f;
-        return;
-    }
-    const float iw = 1.f / w;
-    p[0] = r.x * iw + (y == 0 ? 1.f : 0.f);
-    p[1] = r.y * iw + (y == 1 ? 1.f : 0.f);
-    p[2] = r.z * iw + (y == 2 ? 1.f : 0.f);
-    p[3] = r.w * iw + (y == 3 ? 1.f : 0.f);
-#pragma unroll
-    for (int a = 0; a < 4; ++a) p[a] = fmaxf(p[a], 0.f);
-    const float z = p[0] + p[1] + p[2] + p[3];
-    const float iz = z > 0.f ? 1.f / z : 0.f;
-#pragma unroll
-    for (int a = 0; a < 4; ++a) p[a] *= iz;
-}
-
 // A line-search trial as a change from the current point.  With p0 the base
-// probabilities, y the sequence's state at r and t_a = stp (u_a - u_y),
-// per sequence
-//   l(stp) - l(0) = log1p(q),  q = sum_a p0_a expm1(t_a),
-//   p_a(stp) - p0_a = p0_a (expm1(t_a) - q) / (1 + q),
-// and the slope changes by sum_a w (p_a(stp) - p0_a) (u_a - u_y).  Every
-// term is a difference from the sequence's own state, so single precision
-// gives the change with ~1e-7 relative error of the change itself (a
-// well-fitted sequence has q and p0_a, a != y, small), which is what the
-// line search compares; the base values (objective, slope at 0) are FP64.
-// Sequences whose step is large use the FP64 logits.  Sums: ACC_F += w dl,
-// ACC_DG += slope change (against the normalised p0), ACC_RS += R(stp);
-// R <- R(stp).
+// probabilities (computed from the FP64 logits at the current point), y the
+// sequence's state at r and t_a = stp (u_a - u_y), per sequence
+//   l(stp) - l(0) = log(Z),  Z = sum_a p0_a exp(t_a) = 1 + q,
+//   q = sum_a p0_a expm1(t_a),  p_a(stp) = p0_a exp(t_a) / Z,
+// and the slope changes by sum_a w (p_a(stp) - p0_a) (u_a - u_y), with
+// p_a(stp) - p0_a = p0_a (expm1(t_a) - q) / Z.  Every term is a difference
+// from the sequence's own state, so single precision gives the change with
+// ~1e-7 relative error of the change itself, which is what the line search
+// compares; the base values (objective, slope at 0) are FP64.  Z is a sum of
+// positive terms and the new probabilities are products, so a probability
+// that has become small keeps its relative precision.  Sequences whose step
+// is large use the FP64 logits.  Sums: ACC_F += w dl, ACC_DG += slope change,
+// ACC_RS += R(stp); R <- R(stp) = w (p(stp) - onehot(y)), its y entry as
+// minus the sum of the others.
 constexpr int DT_THREADS = 256;
 
 __global__ void __launch_bounds__(DT_THREADS)
 k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int N, int64_t Nx,
               const double *__restrict__ lbase, const double *__restrict__ u, const float4 *__restrict__ ud,
-              const uint8_t *__restrict__ rstate, const double *__restrict__ w, const float4 *__restrict__ R0,
+              const uint8_t *__restrict__ rstate, const double *__restrict__ w, const float4 *__restrict__ P0,
               float4 *__restrict__ R, double *__restrict__ acc)
 {
     const int b = list[blockIdx.y];
@@ -279,8 +260,8 @@ k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, 
         const float du[4] = {dv4.x, dv4.y, dv4.z, dv4.w};   // u_a - u_y
         const int y = rstate[o] & 3;
         const float wi = (float)w[i];
-        float p0[4];
-        base_probs(R0[o], wi, y, p0);
+        const float4 pv = P0[o];
+        const float p0[4] = {pv.x, pv.y, pv.z, pv.w};
         float t[4], tmax = 0.f;
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
@@ -289,20 +270,24 @@ k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, 
         }
         float r[4];
         if (tmax < 30.f) {
-            float e[4], q = 0.f;
+            float e[4], x[4], q = 0.f, z = 0.f;
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
                 e[a] = expm1f(t[a]);
+                x[a] = p0[a] * expf(t[a]);
                 q = fmaf(p0[a], e[a], q);
+                z += x[a];
             }
-            const float iq = 1.f / (1.f + q);
-            f = fmaf(wi, log1pf(q), f);
+            const float iz = 1.f / z;
+            f = fmaf(wi, fabsf(q) < 0.5f ? log1pf(q) : logf(z), f);
+            float ro = 0.f;
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
-                const float dp = p0[a] * (e[a] - q) * iq;          // p_a(stp) - p0_a
-                dg = fmaf(wi * dp, du[a], dg);
-                r[a] = wi * (p0[a] + dp - (a == y ? 1.f : 0.f));
+                dg = fmaf(wi * (p0[a] * (e[a] - q) * iz), du[a], dg);
+                r[a] = a == y ? 0.f : wi * (x[a] * iz);
+                ro += r[a];
             }
+            r[y] = -ro;
         } else {
             const double *lb = lbase + o * 4;
             const double2 ua = reinterpret_cast<const double2 *>(u + o * 4)[0];
@@ -324,12 +309,16 @@ k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, 
                 z1 += e1[a];
             }
             fbig += (double)wi * ((m1 + log(z1) - l1[y]) - (m0 + log(z0) - l0[y]));
+            double ro = 0.0;
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
                 const double p1 = e1[a] / z1;
                 dgbig += (double)wi * (p1 - (double)p0[a]) * (uu[a] - uu[y]);
-                r[a] = (float)((double)wi * (p1 - (a == y ? 1.0 : 0.0)));
+                const double ra = a == y ? 0.0 : (double)wi * p1;
+                r[a] = (float)ra;
+                ro += ra;
             }
+            r[y] = (float)-ro;
         }
         rs0 += r[0]; rs1 += r[1]; rs2 += r[2]; rs3 += r[3];
         R[o] = make_float4(r[0], r[1], r[2], r[3]);
@@ -343,11 +332,14 @@ k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, 
 }
 
 // d = coef_g g + sum_j coefS_j s_j + coefY_j y_j (a and k parts); trial
-// logits direction u = k_d + eta_d; sums g.d, d.d, x.d (J parts) and the
-// slope of the search line at 0 from the trial's own numbers, sum_i R_i . u_i
+// logits direction u = k_d + eta_d; the base probabilities P0 of the step
+// trials from the FP64 logits at the current point (fresh every iteration,
+// so that rounding does not carry from one iteration to the next); sums g.d,
+// d.d, x.d (J parts) and the slope of the search line at 0 from the trials'
+// own numbers, sum_i w_i sum_c p0_ic (u_ic - u_iy)
 __global__ void __launch_bounds__(256)
 k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int N, int NV,
-                 int ring, double *__restrict__ dv, const float4 *__restrict__ R, float4 *__restrict__ R0,
+                 int ring, double *__restrict__ dv, const double *__restrict__ lbase, float *__restrict__ P0,
                  const double *__restrict__ w, const uint8_t *__restrict__ rstate, double *__restrict__ u,
                  float *__restrict__ ud, double *__restrict__ acc)
 {
@@ -381,16 +373,16 @@ k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ lis
         const int y = rstate[o] & 3;
         const double uy = __shfl_sync(0xffffffffu, uu, (threadIdx.x & ~3) + y);
         ud[(int64_t)b * Nx * 4 + e] = (float)(uu - uy);
-        if (e / 4 < N) {
-            // slope at 0 from the normalised base probabilities, exactly as
-            // the step trials difference against them
-            const float4 r = R[o];
-            const float wi = (float)w[e / 4];
-            float p0[4];
-            base_probs(r, wi, y, p0);
-            if (c == 0) R0[o] = r;
-            dg0 += (double)wi * ((double)p0[c] - (c == y ? 1.0 : 0.0)) * uu;
-        }
+        // p0 = softmax of the four logits of the sequence (lanes 4k..4k+3)
+        const double l = lbase[(int64_t)b * Nx * 4 + e];
+        double m = fmax(l, __shfl_xor_sync(0xffffffffu, l, 1));
+        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, 2));
+        const float ex = expf((float)(l - m));
+        float z = ex + __shfl_xor_sync(0xffffffffu, ex, 1);
+        z += __shfl_xor_sync(0xffffffffu, z, 2);
+        const float p0 = ex / z;
+        P0[(int64_t)b * Nx * 4 + e] = p0;
+        if (e / 4 < N) dg0 += w[e / 4] * (double)p0 * (uu - uy);
     }
     double v[4] = {gd, dd, xd, dg0};
     const int idx[4] = {ACC_GD, ACC_DDJ, ACC_XDJ, ACC_DG0};
@@ -560,18 +552,18 @@ void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, 
 }
 
 void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
-                           const float *R, float *R0, const double *w, const uint8_t *rstate, double *u, float *ud,
-                           double *acc, cudaStream_t st)
+                           const double *lbase, float *P0, const double *w, const uint8_t *rstate, double *u,
+                           float *ud, double *acc, cudaStream_t st)
 {
     if (n <= 0) return;
     dim3 g(grid_for(P.Nx * 4, 256 * 8, 32), n);
     k_dual_direction<<<g, 256, 0, st>>>(sd, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, P.ring, dv,
-                                        reinterpret_cast<const float4 *>(R), reinterpret_cast<float4 *>(R0), w,
+                                        lbase, P0, w,
                                         rstate, u, ud, acc);
 }
 
 void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *lbase,
-                        const double *u, const float *ud, const uint8_t *rstate, const double *w, const float *R0,
+                        const double *u, const float *ud, const uint8_t *rstate, const double *w, const float *P0,
                         float *R, double *acc, cudaStream_t st)
 {
     if (n <= 0) return;
@@ -581,7 +573,7 @@ void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list
     dim3 grid((unsigned)gx, (unsigned)n);
     k_trial_delta<<<grid, DT_THREADS, 0, st>>>(sd, list, (int)P.N, P.Nx, lbase, u,
                                                reinterpret_cast<const float4 *>(ud), rstate, w,
-                                               reinterpret_cast<const float4 *>(R0), reinterpret_cast<float4 *>(R),
+                                               reinterpret_cast<const float4 *>(P0), reinterpret_cast<float4 *>(R),
                                                acc);
 }
 

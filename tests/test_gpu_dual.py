@@ -98,3 +98,24 @@ def test_dual_refuses_start_points_and_warm_start():
             E.set_warm_start(W.new_blob(X, np.ones((10, 16), np.float32)))
         r = E.solve([0, 1, 2])
         assert np.all(r.status == 0)
+
+
+@pytest.mark.parametrize("form", ["dual", "tc"])
+def test_skewed_workload_subset(oracle_mod, form):
+    """The 616 x 78,700 skewed workload (multi-allelic loci, MAF from a Beta
+    distribution, gaps up to 15 %): 12 loci against the FP64 oracle at the
+    engine's parameters, and the oracle's gradient there."""
+    from superdca_gb300 import _lib, synthetic
+    O = oracle_mod
+    states, _, _ = synthetic.workload("skewed-616x78700", seed=2)
+    N, L = states.shape
+    w = O.weights(states, 0.9)
+    loci = np.random.default_rng(6).choice(L, 12, replace=False)
+    fm = _lib.FORM_DUAL if form == "dual" else _lib.FORM_TC
+    res, (lh, lJ, _) = _solve(states, w, loci, fm, batch=12)
+    assert np.all(res.status == 0)
+    P = O.Problem(states, w, lh, lJ)
+    np.testing.assert_allclose(res.f, _f_at(P, loci, res.x), rtol=1e-6)
+    for k in range(3):
+        g = P.objective(int(loci[k]), res.x[k])[1]
+        assert np.abs(g).max() < 1.05e-3
