@@ -51,8 +51,10 @@ def parse():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="tree-3000x94000")
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--batch", type=int, default=0, help="slots solved together (default: 512 dual, 64 otherwise)")
-    ap.add_argument("--loci-per-step", type=int, default=0, help="default: batch")
+    ap.add_argument("--batch", type=int, default=0, help="slots per solver lane (default: 512 dual, 64 otherwise)")
+    ap.add_argument("--lanes", type=int, default=0,
+                    help="solver lanes (own stream and host thread each; default: 3 dual, 1 otherwise)")
+    ap.add_argument("--loci-per-step", type=int, default=0, help="default: 2 x batch x lanes")
     ap.add_argument("--form", default="dual", choices=["gather", "tc", "dual"])
     ap.add_argument("--history-bf16", action="store_true")
     ap.add_argument("--warm-start", default=os.path.join(ROOT, "superdca_gb300", "warmstart_tree-3000x94000.npy"),
@@ -169,8 +171,13 @@ def roofline_dual(prof_tot, N, L, m):
         checks and the final J): 2 N L q^2 FLOP, as in the other forms;
       history dots: 2k + 1 vectors of N x q doubles read (32 N bytes each);
       direction: (4k + 3) vectors read, 2 written, u (32 N) and its
-        single-precision differences (16 N) written;
-      line search (step trials): R0, u differences, R (16 N each), states, w."""
+        single-precision differences (16 N) written, the logits read (32 N)
+        and the base probabilities written (16 N);
+      line search (step trials): base probabilities, u differences, R
+        (16 N each), states, w.
+    With several solver lanes the classes of different lanes overlap in
+    time, and a launch's duration includes the share of the GPU the other
+    lanes' kernels take."""
     hbm, tflops, src = measured_peaks()
     ms, units = prof_tot["kernel_ms"], prof_tot["kernel_units"]
     cls = max(ms, key=lambda k: ms[k])
@@ -185,7 +192,7 @@ def roofline_dual(prof_tot, N, L, m):
         ach = 2.0 * N * L * Q * Q * units[cls] / t / 1e12
         return dict(bound="tensor", achieved=round(ach, 3), peak=tflops, unit="TFLOP/s", frac=round(ach / tflops, 5),
                     traffic=None, kernel="k_gemm (X^T a)", peak_source=src), cls
-    per = {"history": (2 * m + 1) * 32 * N, "direction": ((4 * m + 3) + 2 + 1) * 32 * N + 16 * N,
+    per = {"history": (2 * m + 1) * 32 * N, "direction": ((4 * m + 3) + 2 + 1 + 1) * 32 * N + 32 * N,
            "linesearch": 16 * N * 3 + 9 * N}.get(cls)
     if per is None:
         return None, cls
@@ -276,9 +283,10 @@ def engine_arm(args):
     N, L = st.shape
     w = np.ones(N)
     B = args.batch or (512 if args.form == "dual" else 64)
-    per_step = args.loci_per_step or B
+    lanes = args.lanes or (3 if args.form == "dual" else 1)
+    per_step = args.loci_per_step or 2 * B * lanes   # slots refill once per step
     form = {"tc": FORM_TC, "gather": FORM_GATHER, "dual": FORM_DUAL}[args.form]
-    E = Engine(N, L, batch=B, device=local, form=form, history_bf16=args.history_bf16)
+    E = Engine(N, L, batch=B, device=local, form=form, history_bf16=args.history_bf16, lanes=lanes)
     E.set_alignment(st, w)
     ws = None if args.warm_start in ("", "none") or args.form == "dual" else args.warm_start
     if ws:
@@ -375,6 +383,7 @@ def engine_arm(args):
         rf, dom = roofline(tot, N, L, Dp, 10, 2 if args.history_bf16 else 4)
     if rf is not None:
         rf["avg_launch_ms"] = round(tot["kernel_ms"][dom] / max(1, tot["kernel_launches"][dom]), 4)
+        rf["lanes"] = lanes   # launches of different lanes overlap in time
     out = {
         "metric": "loci/s at N=3000,L=94k (per-locus plmDCA solve, gradient threshold 1e-3)",
         "value": round(value, 4), "unit": "loci/s", "n_gpus": world, "steps": args.steps,
@@ -385,7 +394,7 @@ def engine_arm(args):
                   "gather": "fp32"}[args.form],
         "data": "synthetic (seeded coalescent-tree alignment)",
         "config": {"workload": f"{args.workload} seed {args.seed}", "N": int(N), "L": int(L),
-                   "batch": B, "loci_per_step": per_step, "form": args.form,
+                   "batch": B, "lanes": lanes, "loci_per_step": per_step, "form": args.form,
                    "history": "bf16" if args.history_bf16 else "fp32",
                    "warm_start": os.path.basename(ws) if ws else None,
                    "weights": "unit (--no-reweighting)", "gradient_threshold": 1e-3,

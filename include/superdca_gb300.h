@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define SDCA_ABI_VERSION 1
+#define SDCA_ABI_VERSION 2
 
 /* status codes */
 #define SDCA_OK 0
@@ -65,6 +65,11 @@ typedef struct {
     int32_t flags;             /* SDCA_FLAG_* */
     int32_t device;            /* CUDA device ordinal */
     void *stream;              /* cudaStream_t to run on, or NULL for a private stream */
+    int32_t lanes;             /* solver lanes (1..16; 0 means 1): each lane holds `batch`
+                                  slots with its own stream and host thread, all lanes share
+                                  the resident alignment and draw loci from one queue, so one
+                                  lane's host decisions overlap the others' kernels */
+    int32_t reserved0;         /* 0 */
 } sdca_config;
 
 typedef struct {

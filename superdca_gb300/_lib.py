@@ -41,7 +41,8 @@ class Config(C.Structure):
                 ("gap_state", C.c_int32), ("lambda_h", C.c_double), ("lambda_J", C.c_double),
                 ("gradient_threshold", C.c_double), ("max_iterations", C.c_int32),
                 ("history", C.c_int32), ("batch", C.c_int32), ("form", C.c_int32),
-                ("flags", C.c_int32), ("device", C.c_int32), ("stream", C.c_void_p)]
+                ("flags", C.c_int32), ("device", C.c_int32), ("stream", C.c_void_p),
+                ("lanes", C.c_int32), ("reserved0", C.c_int32)]
 
 
 class LocusStat(C.Structure):

@@ -71,7 +71,9 @@ const char *USAGE =
     "  --gpu-device arg (=0)              CUDA device.\n"
     "  --gpu-form arg (=dual)             Engine form: dual (span of the sequences), tc (tensor-core\n"
     "                                     contractions) or plain.\n"
-    "  --gpu-batch arg (=64)              Loci solved together.\n"
+    "  --gpu-batch arg                    Loci solved together per lane (256 dual, 64 otherwise).\n"
+    "  --gpu-lanes arg                    Solver lanes, each with its own stream and host thread\n"
+    "                                     (3 dual, 1 otherwise).\n"
     "  --gpu-history arg (=fp32)          L-BFGS history storage: fp32 or bf16.\n"
     "  --gpu-chunk arg (=4096)            Loci per solve call (bounds host memory).\n"
     "  --gpu-top-k arg (=0)               Write only the K strongest pairs, strongest first.\n"
@@ -92,7 +94,7 @@ struct Options {
     bool norm_of_mean = false;
     double gradient_threshold = 1e-3, lambda_h = -1.0, lambda_J = -1.0;
     bool no_dca = false, no_coupling_output = false;
-    int device = 0, batch = 0, form = SDCA_FORM_DUAL;
+    int device = 0, batch = 0, lanes = 0, form = SDCA_FORM_DUAL;
     bool history_bf16 = false, binary_output = false;
     long chunk = 4096, top_k = 0;
 };
@@ -184,6 +186,7 @@ Options parse_options(int argc, char **argv)
         else if (name == "lambda-J") o.lambda_J = parse_number<double>(opt, value);
         else if (name == "gpu-device") o.device = parse_number<int>(opt, value);
         else if (name == "gpu-batch") o.batch = parse_number<int>(opt, value);
+        else if (name == "gpu-lanes") o.lanes = parse_number<int>(opt, value);
         else if (name == "gpu-chunk") o.chunk = parse_number<long>(opt, value);
         else if (name == "gpu-top-k") o.top_k = parse_number<long>(opt, value);
         else if (name == "gpu-form") {
@@ -728,14 +731,15 @@ int main(int argc, char **argv)
         cfg.lambda_h = o.lambda_h;
         cfg.lambda_J = o.lambda_J;
         cfg.gradient_threshold = o.gradient_threshold;
-        cfg.batch = o.batch > 0 ? o.batch : (o.form == SDCA_FORM_DUAL ? 256 : 64);
+        cfg.form = o.form;
         if (cfg.form == SDCA_FORM_DUAL && N > 16383) {
             // the dual form keeps N x N agreement counts; larger alignments use the tensor cores
             if (o.verbose) std::cout << "superdca-gb300: " << N << " sequences: using the tensor-core form\n";
             cfg.form = SDCA_FORM_TC;
-            if (o.batch <= 0) cfg.batch = 64;
         }
-        cfg.form = o.form;
+        const bool dual = cfg.form == SDCA_FORM_DUAL;
+        cfg.batch = o.batch > 0 ? o.batch : (dual ? 256 : 64);
+        cfg.lanes = o.lanes > 0 ? o.lanes : (dual ? 3 : 1);
         cfg.flags = o.history_bf16 ? SDCA_FLAG_HISTORY_BF16 : 0;
         cfg.device = o.device;
         check(sdca_create(&cfg, &H.h), nullptr, "engine set-up failed");

@@ -17,6 +17,7 @@
 // Slots whose locus converged are scored and refilled from the queue, so loci
 // retire and enter independently.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -26,6 +27,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "engine.h"
@@ -180,6 +182,13 @@ struct sdca_handle {
     double *ws_xmax = nullptr;
 
     std::vector<SlotHost> slots;
+
+    // solver lanes: sub[i] is a further lane with its own slots, stream and
+    // host thread; its alignment buffers (X, XT, w, K and its digits) are
+    // this handle's (shared_alignment set in the lane, which frees none)
+    std::vector<sdca_handle *> sub;
+    bool shared_alignment = false;
+    cudaEvent_t ev_lanes = nullptr;   // start of a multi-lane solve
 
     // profiling
     std::vector<cudaEvent_t> ev_pool;
@@ -682,7 +691,9 @@ int ws_begin(sdca_handle *h, const std::vector<int32_t> &bs)
 // the per-solve queue
 struct Queue {
     const uint32_t *loci = nullptr;
-    size_t n = 0, next = 0;
+    size_t n = 0;
+    std::atomic<size_t> *next = nullptr;   // shared by the lanes of one solve
+    std::atomic<bool> *abort = nullptr;    // a lane failed: take no further loci
     const double *x_init = nullptr;
     double *x_out = nullptr;
     float *scores = nullptr;
@@ -690,12 +701,21 @@ struct Queue {
     std::vector<float> xbuf;
 };
 
+// next position of the loci list, or -1 when it is exhausted
+int64_t take(Queue &Qu)
+{
+    if (Qu.abort && Qu.abort->load()) return -1;
+    const size_t k = Qu.next->fetch_add(1);
+    return k < Qu.n ? (int64_t)k : -1;
+}
+
 int refill(sdca_handle *h, Queue &Qu)
 {
     std::vector<int32_t> warm, learned;
-    for (int b = 0; b < h->P.Bmax && Qu.next < Qu.n; ++b) {
+    for (int b = 0; b < h->P.Bmax; ++b) {
         if (h->slots[b].phase != PH_EMPTY) continue;
-        const int64_t k = (int64_t)Qu.next++;
+        const int64_t k = take(Qu);
+        if (k < 0) break;
         const float *x0 = nullptr;
         if (Qu.x_init && h->form == SDCA_FORM_DUAL)
             return fail(h, SDCA_E_UNSUPPORTED, "the dual form starts every locus from zero (no x_init)");
@@ -1685,6 +1705,38 @@ int phase_step_dual(sdca_handle *h)
     return SDCA_OK;
 }
 
+// One lane's solve over the shared queue.  Device time runs from t0_common
+// (the multi-lane solve's start) or from this lane's own start event.
+int solve_lane(sdca_handle *h, Queue &Qu, cudaEvent_t t0_common)
+{
+    CK(cudaSetDevice(h->cfg.device));
+    prof_reset(h);
+    h->prof.h2d_bytes = 0;
+    cudaEvent_t t0 = t0_common ? t0_common : take_event(h), t1 = take_event(h);
+    if (!t0 || !t1) return fail(h, SDCA_E_CUDA, "cudaEventCreate failed");
+    if (!t0_common) CK(cudaEventRecord(t0, h->stream));
+    for (auto &S : h->slots) S.phase = PH_EMPTY;
+    int rc = refill(h, Qu);
+    if (rc) return rc;
+    for (;;) {
+        bool any = false;
+        for (auto &S : h->slots)
+            if (S.phase != PH_EMPTY) any = true;
+        if (!any) break;
+        rc = phase_trials(h, Qu);
+        if (rc) return rc;
+        rc = h->form == SDCA_FORM_DUAL ? phase_step_dual(h) : phase_step(h);
+        if (rc) return rc;
+    }
+    CK(cudaEventRecord(t1, h->stream));
+    { const int r_ = stream_sync(h); if (r_) return r_; }
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, t0, t1));
+    h->prof.solve_ms = ms;
+    prof_collect(h);
+    return SDCA_OK;
+}
+
 int check_ready(sdca_handle *h)
 {
     if (!h) return SDCA_E_ARG;
@@ -1717,11 +1769,40 @@ int sdca_config_default(sdca_config *cfg)
     return SDCA_OK;
 }
 
+static int create_lane(const sdca_config *cfg, const sdca_handle *owner, sdca_handle **out);
+
 int sdca_create(const sdca_config *cfg, sdca_handle **out)
 {
-    sdca_handle *h = nullptr;
     if (!cfg || !out) return fail(nullptr, SDCA_E_ARG, "sdca_create: null argument");
     *out = nullptr;
+    if (cfg->lanes < 0 || cfg->lanes > 16) return fail(nullptr, SDCA_E_ARG, "lanes must be in 0..16");
+    sdca_handle *h = nullptr;
+    int rc = create_lane(cfg, nullptr, &h);
+    if (rc) return rc;
+    for (int i = 1; i < cfg->lanes; ++i) {
+        sdca_config c = *cfg;
+        c.lanes = 1;
+        c.stream = nullptr;
+        sdca_handle *s = nullptr;
+        if ((rc = create_lane(&c, h, &s)) == SDCA_OK) {
+            h->sub.push_back(s);
+            continue;
+        }
+        sdca_destroy(h);
+        return rc;
+    }
+    if (!h->sub.empty() && cudaEventCreate(&h->ev_lanes) != cudaSuccess) {
+        sdca_destroy(h);
+        return fail(nullptr, SDCA_E_CUDA, "cudaEventCreate failed");
+    }
+    *out = h;
+    return SDCA_OK;
+}
+
+// one lane; with an owner, the lane uses the owner's alignment buffers
+static int create_lane(const sdca_config *cfg, const sdca_handle *owner, sdca_handle **out)
+{
+    sdca_handle *h = nullptr;
     if (cfg->q != Q) return fail(nullptr, SDCA_E_UNSUPPORTED, "only q = 4 (the triallelic envelope) is supported");
     if (cfg->n_seqs < 1 || cfg->n_loci < 2)
         return fail(nullptr, SDCA_E_ARG, "need at least 1 sequence and 2 loci");
@@ -1796,8 +1877,18 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
     // the dual form keeps its history as N x 4 coefficient pairs, not as D-vectors
     const size_t hist_bytes = dual ? 256 : B * P.ring * P.Dp * hsz;
     const size_t NV = DV_S + 2 * (size_t)P.ring;
-    if ((rc = dalloc(h, &h->X, (size_t)P.N * P.Lx)) || (rc = dalloc(h, &h->XT, (size_t)P.L * P.Nx)) ||
-        (rc = dalloc(h, &h->w, (size_t)P.Nx)) || (rc = dalloc(h, &h->rstate, B * P.Nx)) ||
+    const bool shared = owner != nullptr;
+    if (shared) {
+        h->shared_alignment = true;
+        h->X = owner->X;
+        h->XT = owner->XT;
+        h->w = owner->w;
+        h->Kmat = owner->Kmat;
+        h->Kd = owner->Kd;
+    }
+    if ((!shared && ((rc = dalloc(h, &h->X, (size_t)P.N * P.Lx)) || (rc = dalloc(h, &h->XT, (size_t)P.L * P.Nx)) ||
+                     (rc = dalloc(h, &h->w, (size_t)P.Nx)))) ||
+        (rc = dalloc(h, &h->rstate, B * P.Nx)) ||
         (rc = dalloc(h, &h->wa, B * P.Dp)) || (rc = dalloc(h, &h->d, B * P.Dp)) ||
         (rc = dalloc(h, &h->gpool, 2 * B * P.Dp)) || (rc = dalloc(h, &h->u, B * P.Nx * 4)) ||
         (rc = dalloc(h, &h->R, B * P.Nx * 4)) || (rc = dalloc(h, &h->lbase, B * P.Nx * 4)) ||
@@ -1818,9 +1909,9 @@ int sdca_create(const sdca_config *cfg, sdca_handle **out)
                   (rc = dalloc(h, &h->rq, B * P.Nx * 4)) || (rc = dalloc(h, &h->csum, 16 * B)) ||
                   (rc = dalloc(h, &h->Rchk, B * P.Nx * 4)) || (rc = dalloc(h, &h->J64, B * P.Dp)) ||
                   (rc = dalloc(h, &h->P0, B * P.Nx * 4)) || (rc = dalloc(h, &h->ud, B * P.Nx * 4)) ||
-                  (rc = dalloc(h, &h->Kmat, (size_t)P.Nx * P.Nx)) ||
+                  (!shared && (rc = dalloc(h, &h->Kmat, (size_t)P.Nx * P.Nx))) ||
                   (P.N <= 4000 && P.L < (1 << 18) &&
-                   ((rc = dalloc(h, &h->Kd, (size_t)3 * kd_nk_rows(P) * P.Nx)) ||
+                   ((!shared && (rc = dalloc(h, &h->Kd, (size_t)3 * kd_nk_rows(P) * P.Nx))) ||
                     (rc = dalloc(h, &h->Rd, (size_t)5 * kd_nr_rows(P) * P.Nx)))))) ||
         (tcres &&
          ((rc = dalloc(h, &h->Dhi, 4 * B * (size_t)round_up(4 * P.L, 64))) ||
@@ -1867,6 +1958,11 @@ int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weig
     if (!h) return SDCA_E_ARG;
     h->knn_k = 0;
     h->scan = false;
+    for (sdca_handle *s : h->sub) {
+        s->has_alignment = false;
+        s->knn_k = 0;
+        s->scan = false;
+    }
     if (!states || !weights) return fail(h, SDCA_E_ARG, "states and weights are required");
     Problem &P = h->P;
     for (int64_t i = 0; i < P.N; ++i)
@@ -1931,6 +2027,16 @@ int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weig
     }
     h->has_alignment = true;
     h->prof.h2d_bytes = (int64_t)P.N * P.L + (int64_t)sizeof(double) * P.N;
+    // the other lanes read the same buffers: they take the scalars
+    for (sdca_handle *s : h->sub) {
+        s->w_host = h->w_host;
+        s->P.b_eff = P.b_eff;
+        s->P.lambda_J = P.lambda_J;
+        s->P.lambda_h = P.lambda_h;
+        s->r_scale = h->r_scale;
+        s->qscale = h->qscale;
+        s->has_alignment = true;
+    }
     return SDCA_OK;
 }
 
@@ -1952,40 +2058,64 @@ int sdca_solve_ex(sdca_handle *h, const uint32_t *loci, size_t n_loci, const dou
     const int64_t nt = h->scan ? h->LT : h->P.L;   // scan mode: loci are target columns
     for (size_t k = 0; k < n_loci; ++k)
         if ((int64_t)loci[k] >= nt) return fail(h, SDCA_E_ARG, "locus index out of range");
-    CK(cudaSetDevice(h->cfg.device));
-    const int64_t h2d0 = h->prof.h2d_bytes;
-    prof_reset(h);
-    h->prof.h2d_bytes = 0;
-    (void)h2d0;
-    cudaEvent_t t0 = take_event(h), t1 = take_event(h);
-    CK(cudaEventRecord(t0, h->stream));
-    Queue Qu;
-    Qu.loci = loci;
-    Qu.n = n_loci;
-    Qu.x_init = x_init;
-    Qu.x_out = x_out;
-    Qu.scores = scores;
-    Qu.stats = stats;
-    if (x_init) Qu.xbuf.resize(h->P.Dp);
-    for (auto &S : h->slots) S.phase = PH_EMPTY;
-    rc = refill(h, Qu);
-    if (rc) return rc;
-    for (;;) {
-        bool any = false;
-        for (auto &S : h->slots)
-            if (S.phase != PH_EMPTY) any = true;
-        if (!any) break;
-        rc = phase_trials(h, Qu);
-        if (rc) return rc;
-        rc = h->form == SDCA_FORM_DUAL ? phase_step_dual(h) : phase_step(h);
-        if (rc) return rc;
+    std::atomic<size_t> next{0};
+    std::atomic<bool> abort{false};
+    auto queue_for = [&](sdca_handle *l, Queue &Qu) {
+        Qu.loci = loci;
+        Qu.n = n_loci;
+        Qu.next = &next;
+        Qu.abort = &abort;
+        Qu.x_init = x_init;
+        Qu.x_out = x_out;
+        Qu.scores = scores;
+        Qu.stats = stats;
+        if (x_init) Qu.xbuf.resize(l->P.Dp);
+    };
+    if (h->sub.empty()) {
+        Queue Qu;
+        queue_for(h, Qu);
+        return solve_lane(h, Qu, nullptr);
     }
-    CK(cudaEventRecord(t1, h->stream));
-    { const int r_ = stream_sync(h); if (r_) return r_; }
-    float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, t0, t1));
-    h->prof.solve_ms = ms;
-    prof_collect(h);
+    // lanes: this thread runs lane 0, one thread per further lane; all take
+    // loci from the same queue and write disjoint rows of the outputs
+    CK(cudaSetDevice(h->cfg.device));
+    CK(cudaEventRecord(h->ev_lanes, h->stream));
+    const size_t nl = 1 + h->sub.size();
+    std::vector<int> rcs(nl, SDCA_OK);
+    auto run = [&](size_t i) {
+        sdca_handle *l = i == 0 ? h : h->sub[i - 1];
+        Queue Qu;
+        queue_for(l, Qu);
+        rcs[i] = solve_lane(l, Qu, h->ev_lanes);
+        if (rcs[i]) abort.store(true);
+    };
+    std::vector<std::thread> th;
+    for (size_t i = 1; i < nl; ++i) {
+        try {
+            th.emplace_back(run, i);
+        } catch (...) {
+            // no thread: the lanes that run take this lane's loci
+        }
+    }
+    run(0);
+    for (auto &t : th) t.join();
+    for (size_t i = 0; i < nl; ++i)
+        if (rcs[i]) return i == 0 ? rcs[i] : fail(h, rcs[i], "lane " + std::to_string(i) + ": " + h->sub[i - 1]->err);
+    for (const sdca_handle *l : h->sub) {
+        const sdca_profile &q = l->prof;
+        sdca_profile &p = h->prof;
+        p.solve_ms = std::max(p.solve_ms, q.solve_ms);
+        for (int c = 0; c < 8; ++c) {
+            p.kernel_ms[c] += q.kernel_ms[c];
+            p.kernel_launches[c] += q.kernel_launches[c];
+            p.kernel_units[c] += q.kernel_units[c];
+        }
+        p.gpu_launches += q.gpu_launches;
+        p.iterations += q.iterations;
+        p.contractions += q.contractions;
+        p.h2d_bytes += q.h2d_bytes;
+        p.d2h_bytes += q.d2h_bytes;
+    }
     return SDCA_OK;
 }
 
@@ -2063,6 +2193,10 @@ int sdca_compute_weights(sdca_handle *h, const uint8_t *states, const double *mu
     // sdca_set_alignment overwrites it anyway
     h->has_alignment = false;
     h->knn_k = 0;
+    for (sdca_handle *s : h->sub) {
+        s->has_alignment = false;
+        s->knn_k = 0;
+    }
     const int64_t W = (P.L + 31) / 32;
     uint64_t *packed = nullptr;
     double *d = nullptr;
@@ -2120,7 +2254,10 @@ int sdca_set_targets(sdca_handle *h, const uint8_t *targets, int64_t n_target_lo
     }
     h->scan = false;
     h->LT = 0;
-    if (!targets) return SDCA_OK;
+    if (!targets) {
+        for (sdca_handle *s : h->sub) sdca_set_targets(s, nullptr, 0);
+        return SDCA_OK;
+    }
     const Problem &P = h->P;
     if (n_target_loci < 1 || n_target_loci > (1LL << 26)) return fail(h, SDCA_E_ARG, "invalid number of target loci");
     for (int64_t e = 0; e < P.N * n_target_loci; ++e)
@@ -2157,6 +2294,8 @@ int sdca_set_targets(sdca_handle *h, const uint8_t *targets, int64_t n_target_lo
     }
     h->LT = n_target_loci;
     h->scan = true;
+    for (sdca_handle *s : h->sub)
+        if ((rc = sdca_set_targets(s, targets, n_target_loci))) return fail(h, rc, s->err);
     return SDCA_OK;
 }
 
@@ -2165,6 +2304,7 @@ int sdca_set_warm_start(sdca_handle *h, const float *params, size_t n_params)
     if (!h) return SDCA_E_ARG;
     if (!params) {
         h->ws_on = false;
+        for (sdca_handle *s : h->sub) s->ws_on = false;
         return SDCA_OK;
     }
     if (h->form == SDCA_FORM_DUAL)
@@ -2187,6 +2327,8 @@ int sdca_set_warm_start(sdca_handle *h, const float *params, size_t n_params)
     h->ws_eps = eps;
     h->ws_hfit = params[MLP_HFIT] != 0.f;
     h->ws_on = true;
+    for (sdca_handle *s : h->sub)
+        if ((rc = sdca_set_warm_start(s, params, n_params))) return fail(h, rc, s->err);
     return SDCA_OK;
 }
 
@@ -2249,7 +2391,10 @@ const char *sdca_last_error(const sdca_handle *h)
 int sdca_destroy(sdca_handle *h)
 {
     if (!h) return SDCA_OK;
+    for (sdca_handle *s : h->sub) sdca_destroy(s);   // before the buffers they share
+    h->sub.clear();
     cudaSetDevice(h->cfg.device);
+    if (h->ev_lanes) cudaEventDestroy(h->ev_lanes);
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (auto e : h->ev_pool) cudaEventDestroy(e);
     if (h->tc) tc_plan_destroy(h->tc);

@@ -673,15 +673,16 @@ using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, vo
 
 EncodeFn encode_fn()
 {
-    static EncodeFn fn = nullptr;
-    if (!fn) {
+    // initialised once, thread-safely (solver lanes create plans concurrently)
+    static const EncodeFn fn = []() -> EncodeFn {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeFn>(p);
-    }
+            return reinterpret_cast<EncodeFn>(p);
+        return nullptr;
+    }();
     return fn;
 }
 
@@ -714,11 +715,10 @@ namespace {
 // SDCA_TC_MSUB (1, 2 or 4) overrides the choice for tuning runs.
 int msub_choice()
 {
-    static int v = 0;
-    if (!v) {
+    static const int v = []() {
         const char *e = std::getenv("SDCA_TC_MSUB");
-        v = (e && (e[0] == '1' || e[0] == '2')) ? e[0] - '0' : 4;
-    }
+        return (e && (e[0] == '1' || e[0] == '2')) ? e[0] - '0' : 4;
+    }();
     return v;
 }
 

@@ -47,7 +47,7 @@ class Engine:
                  lambda_J: float = -1.0, gradient_threshold: float = 1e-3,
                  max_iterations: int = 2000, history: int = 10, batch: int = 64,
                  form: int = _lib.FORM_GATHER, history_bf16: bool = False, gap_state: int = 3,
-                 device: int = 0, stream: int | None = None):
+                 device: int = 0, stream: int | None = None, lanes: int = 1):
         self.lib = _lib.load()
         cfg = _lib.Config()
         self.lib.sdca_config_default(C.byref(cfg))
@@ -59,6 +59,7 @@ class Engine:
         cfg.flags = _lib.FLAG_HISTORY_BF16 if history_bf16 else 0
         cfg.gap_state, cfg.device = int(gap_state), int(device)
         cfg.stream = stream
+        cfg.lanes = int(lanes)
         self.cfg = cfg
         h = C.c_void_p()
         rc = self.lib.sdca_create(C.byref(cfg), C.byref(h))

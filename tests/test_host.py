@@ -18,7 +18,7 @@ def test_library_exports_every_declared_symbol(engine_lib):
     assert sorted(_lib.EXPORTS) == declared
     for name in declared:
         assert hasattr(engine_lib, name), name
-    assert engine_lib.sdca_abi_version() == 1
+    assert engine_lib.sdca_abi_version() == 2
 
 
 def test_config_defaults_follow_superdca_options(engine_lib):
