@@ -1,0 +1,94 @@
+// df.cuh -- double-float arithmetic: a value is the unevaluated sum hi + lo
+// of two floats (float2 {x = hi, y = lo}, |lo| <= ulp(hi) / 2), about 48
+// significant bits, computed on the FP32 pipe.  GB300 runs FP64 at a small
+// fraction of its FP32 rate, so the dual form keeps its coefficient vectors
+// in this format: the same 8 bytes per value as a double.
+//
+// Error-free transformations: TwoSum (Knuth, TAOCP vol. 2, 4.2.2), FastTwoSum
+// (Dekker 1971, |a| >= |b|), and TwoProd by a fused multiply-add.  Sums use
+// the "sloppy" double-float addition (Dekker): its error is within a few
+// units of 2^-48 of the larger operand, which is the scale every use here
+// needs (sums of terms, not of cancelled results).  No -use_fast_math: the
+// transformations rely on IEEE round-to-nearest and no reassociation.
+#pragma once
+
+#include <cstdint>
+
+namespace sdca {
+
+__device__ __forceinline__ float2 df_two_sum(float a, float b)
+{
+    const float s = a + b;
+    const float bb = s - a;
+    const float e = (a - (s - bb)) + (b - bb);
+    return make_float2(s, e);
+}
+
+__device__ __forceinline__ float2 df_fast_two_sum(float a, float b)
+{
+    const float s = a + b;
+    return make_float2(s, b - (s - a));
+}
+
+__device__ __forceinline__ float2 df_add(float2 a, float2 b)
+{
+    float2 s = df_two_sum(a.x, b.x);
+    s.y += a.y + b.y;
+    return df_fast_two_sum(s.x, s.y);
+}
+
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+
+__device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, df_neg(b)); }
+
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b)
+{
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return df_fast_two_sum(p, e);
+}
+
+// acc + c x
+__device__ __forceinline__ float2 df_fma(float2 c, float2 x, float2 acc)
+{
+    const float p = c.x * x.x;
+    float e = fmaf(c.x, x.x, -p);
+    e = fmaf(c.x, x.y, e);
+    e = fmaf(c.y, x.x, e);
+    float2 s = df_two_sum(acc.x, p);
+    s.y += acc.y + e;
+    return df_fast_two_sum(s.x, s.y);
+}
+
+// conversions (FP64 instructions: for per-block scalars and the few values
+// that meet FP64 data)
+__device__ __forceinline__ float2 df_from_d(double x)
+{
+    const float hi = __double2float_rn(x);
+    return make_float2(hi, __double2float_rn(x - (double)hi));
+}
+
+__device__ __forceinline__ double df_to_d(float2 a) { return (double)a.x + (double)a.y; }
+
+// exact for |v| < 2^31
+__device__ __forceinline__ float2 df_from_int(int v)
+{
+    const float hi = __int2float_rn(v);
+    return make_float2(hi, __int2float_rn(v - __float2int_rn(hi)));
+}
+
+// 48 bits of a 64-bit integer (|v| < 2^62)
+__device__ __forceinline__ float2 df_from_ll(long long v)
+{
+    const float hi = __ll2float_rn(v);
+    return make_float2(hi, __ll2float_rn(v - __float2ll_rn(hi)));
+}
+
+__device__ __forceinline__ float2 df_zero() { return make_float2(0.f, 0.f); }
+
+// value as a float (rounded)
+__device__ __forceinline__ float df_f(float2 a) { return a.x + a.y; }
+
+} // namespace sdca

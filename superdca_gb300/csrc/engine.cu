@@ -154,7 +154,8 @@ struct sdca_handle {
     std::vector<int> trace_loci;  // SDCA_TRACE=<locus>[,<locus>...]: per-iteration solver state on stderr
 
     // dual form (kernels_dual.cu)
-    double *dv = nullptr, *u64 = nullptr, *KR = nullptr, *amax = nullptr, *J64 = nullptr, *amax_h = nullptr;
+    float2 *dv = nullptr, *KR = nullptr;   // coefficient vectors and K rho, double-float (df.cuh)
+    double *u64 = nullptr, *amax = nullptr, *J64 = nullptr, *amax_h = nullptr;
     int32_t *rq = nullptr, *Kmat = nullptr;
     long long *csum = nullptr;
     float *Rchk = nullptr, *P0 = nullptr;   // P0: probabilities at the current point, base of the step trials

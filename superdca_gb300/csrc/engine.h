@@ -161,24 +161,24 @@ void launch_dual_kmat(const int32_t *dist, int N, int64_t Nx, int L, int32_t *K,
 void launch_dual_quant(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *R,
                        const uint8_t *rstate, double qscale, int32_t *rq, long long *csum, cudaStream_t st);
 void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8_t *rstate, const int32_t *K,
-                       double qscale, const int32_t *rq, const long long *csum, double *KR, cudaStream_t st);
+                       double qscale, const int32_t *rq, const long long *csum, float2 *KR, cudaStream_t st);
 void launch_dual_grad(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double qscale,
-                      const int32_t *rq, const double *KR, double *dv, double *acc, double *amax, cudaStream_t st);
-void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int newg, const double *dv,
+                      const int32_t *rq, const float2 *KR, float2 *dv, double *acc, double *amax, cudaStream_t st);
+void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int newg, const float2 *dv,
                       double *dots, cudaStream_t st);
-void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
+void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float2 *dv,
                            const double *lbase, float *P0, const double *w, const uint8_t *rstate, double *u,
                            float *ud, double *acc, cudaStream_t st);
 void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *lbase,
                         const double *u, const float *ud, const uint8_t *rstate, const double *w, const float *P0,
                         float *R, double *acc, cudaStream_t st);
-void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
+void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float2 *dv,
                         const double *u, double *lbase, cudaStream_t st);
 void launch_dual_to_r(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int which,
-                      const double *dv, float *R, cudaStream_t st);
+                      const float2 *dv, float *R, cudaStream_t st);
 void launch_dual_gmax(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *gpool,
                       double *acc, cudaStream_t st);
-void launch_dual_digits(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d, const double *dv,
+void launch_dual_digits(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d, const float2 *dv,
                         float *R, cudaStream_t st);
 void launch_dual_digit_acc(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d,
                            const float *gpool, double *J64, cudaStream_t st);
@@ -229,7 +229,7 @@ KdPlan *tc_kdig_plan_create(const Problem &P, __half *Kd, __half *Rd);
 void tc_kdig_plan_destroy(KdPlan *p);
 void tc_kdig_fill_k(const KdPlan *pl, const Problem &P, const int32_t *K, __half *Kd, cudaStream_t st);
 cudaError_t tc_launch_kdig(const KdPlan *pl, const Problem &P, const int32_t *list, int n, const int32_t *rq,
-                           const uint8_t *rstate, const long long *csum, double inv_qscale, __half *Rd, double *KR,
+                           const uint8_t *rstate, const long long *csum, double inv_qscale, __half *Rd, float2 *KR,
                            int *err, cudaStream_t st);
 
 } // namespace sdca

@@ -10,7 +10,8 @@
 // (K_ij = number of loci n != r where s_i(n) = s_j(n)) a vector's logit
 // image is K a_v + eta_v and inner products are a_v . K a_w + eta_v . eta_w.
 // So the same iteration runs on N x 4 coefficients; a vector is kept as the
-// pair (a, k = K a) in FP64 and its eta on the host.
+// pair (a, k = K a) in double-float (df.cuh: ~48 bits on the FP32 pipe) and
+// its eta on the host.
 //
 // The one product per iteration, K rho, is exact: rho is rounded to integers
 // rho_q = round(rho * 2^QB / w_max) (the rounded value is the one used, so
@@ -19,6 +20,7 @@
 // the agreement at r itself, a class sum per state of r.
 #include <cstdint>
 
+#include "df.cuh"
 #include "engine.h"
 #include "kernels_common.cuh"
 
@@ -33,10 +35,12 @@ __global__ void k_dual_kmat(const int32_t *__restrict__ dist, int N, int64_t Nx,
     }
 }
 
-// rho_q = round(R * qscale); class sums csum[b][a][c] = sum over i with s_i(r) = a
+// rho_q = round(R * qscale) (R is FP32, so a single-precision product loses
+// nothing: the rounded value is the one every later step uses); class sums
+// csum[b][a][c] = sum over i with s_i(r) = a
 __global__ void __launch_bounds__(256)
 k_dual_quant(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int N, int64_t Nx,
-             const float4 *__restrict__ R, const uint8_t *__restrict__ rstate, double qscale, int4 *__restrict__ rq,
+             const float4 *__restrict__ R, const uint8_t *__restrict__ rstate, float qscale, int4 *__restrict__ rq,
              unsigned long long *__restrict__ csum)
 {
     const int b = list[blockIdx.y];
@@ -49,8 +53,8 @@ k_dual_quant(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, i
         int4 q = make_int4(0, 0, 0, 0);
         if (i < N) {
             const float4 v = R[(int64_t)b * Nx + i];
-            q = make_int4((int)llrint((double)v.x * qscale), (int)llrint((double)v.y * qscale),
-                          (int)llrint((double)v.z * qscale), (int)llrint((double)v.w * qscale));
+            q = make_int4(__float2int_rn(v.x * qscale), __float2int_rn(v.y * qscale), __float2int_rn(v.z * qscale),
+                          __float2int_rn(v.w * qscale));
             const int y = own ? (rstate[(int64_t)b * Nx + i] & 3) : -1;
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
@@ -80,7 +84,7 @@ constexpr int KP_J = 16;   // sequences j per shared-memory stage
 __global__ void __launch_bounds__(256)
 k_dual_kprod(const int32_t *__restrict__ K, int64_t Nx, int N, const int32_t *__restrict__ list, int nlist,
              const int4 *__restrict__ rq, const long long *__restrict__ csum, const uint8_t *__restrict__ rstate,
-             double inv_qscale, double *__restrict__ KR)
+             double inv_qscale, float2 *__restrict__ KR)
 {
     __shared__ __align__(16) int32_t sK[KP_J][KP_M];
     __shared__ __align__(16) int32_t sR[KP_J][KP_S * 4];
@@ -114,18 +118,19 @@ k_dual_kprod(const int32_t *__restrict__ K, int64_t Nx, int N, const int32_t *__
     }
     if (my_slot < 0) return;
     const int b = my_slot;
+    const float2 iq = df_from_d(inv_qscale);
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         const int64_t i = i0 + ty * 4 + a;
-        double *o = KR + ((int64_t)b * Nx + i) * 4;
+        float2 *o = KR + ((int64_t)b * Nx + i) * 4;
         if (i >= N) {
-            o[0] = o[1] = o[2] = o[3] = 0.0;
+            o[0] = o[1] = o[2] = o[3] = df_zero();
             continue;
         }
         const int y = rstate[(int64_t)b * Nx + i] & 3;
         const long long *cs = csum + (int64_t)b * 16 + y * 4;
 #pragma unroll
-        for (int c = 0; c < 4; ++c) o[c] = (double)(acc[a][c] - cs[c]) * inv_qscale;
+        for (int c = 0; c < 4; ++c) o[c] = df_mul(df_from_ll(acc[a][c] - cs[c]), iq);
     }
 }
 
@@ -139,48 +144,49 @@ __device__ __forceinline__ int64_t dvo(int64_t b, int v, int part, int NV, int64
 // J-part sums: g.g, x.x, s.y, y.y, s.s; max |a_g| and max |a_x|
 __global__ void __launch_bounds__(256)
 k_dual_grad(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
-            double lambda_J, const int32_t *__restrict__ rq, double inv_qscale, const double *__restrict__ KR,
-            double *__restrict__ dv, double *__restrict__ acc, double *__restrict__ amax)
+            double lambda_J, const int32_t *__restrict__ rq, double inv_qscale, const float2 *__restrict__ KR,
+            float2 *__restrict__ dv, double *__restrict__ acc, double *__restrict__ amax)
 {
     const int b = list[blockIdx.y];
     const SlotDev &S = sd[b];
     const bool push = (S.flags & SLOT_F_PUSH) && S.ring_new >= 0;
-    const double l2 = 2.0 * lambda_J;
-    const double *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = dv + dvo(b, DV_X, 1, NV, Nx);
-    const double *ago = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kgo = dv + dvo(b, DV_G + S.gcur, 1, NV, Nx);
-    double *agn = dv + dvo(b, DV_G + 1 - S.gcur, 0, NV, Nx), *kgn = dv + dvo(b, DV_G + 1 - S.gcur, 1, NV, Nx);
+    const float2 l2 = df_from_d(2.0 * lambda_J), iq = df_from_d(inv_qscale);
+    const float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = dv + dvo(b, DV_X, 1, NV, Nx);
+    const float2 *ago = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kgo = dv + dvo(b, DV_G + S.gcur, 1, NV, Nx);
+    float2 *agn = dv + dvo(b, DV_G + 1 - S.gcur, 0, NV, Nx), *kgn = dv + dvo(b, DV_G + 1 - S.gcur, 1, NV, Nx);
     const int ps = push ? S.ring_new : 0;
-    const double *as = dv + dvo(b, DV_S + ps, 0, NV, Nx), *ks = dv + dvo(b, DV_S + ps, 1, NV, Nx);
-    double *ay = dv + dvo(b, DV_S + ring + ps, 0, NV, Nx), *ky = dv + dvo(b, DV_S + ring + ps, 1, NV, Nx);
-    double g2 = 0, x2 = 0, sy = 0, yy = 0, ss = 0, mg = 0, mx = 0;
+    const float2 *as = dv + dvo(b, DV_S + ps, 0, NV, Nx), *ks = dv + dvo(b, DV_S + ps, 1, NV, Nx);
+    float2 *ay = dv + dvo(b, DV_S + ring + ps, 0, NV, Nx), *ky = dv + dvo(b, DV_S + ring + ps, 1, NV, Nx);
+    float2 g2 = df_zero(), x2 = df_zero(), sy = df_zero(), yy = df_zero(), ss = df_zero();
+    float mg = 0.f, mx = 0.f;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
-        const double a_x = ax[e], k_x = kx[e];
-        const double a_g = (double)rq[(int64_t)b * Nx * 4 + e] * inv_qscale + l2 * a_x;
-        const double k_g = KR[(int64_t)b * Nx * 4 + e] + l2 * k_x;
-        g2 += a_g * k_g;
-        x2 += a_x * k_x;
-        mg = fmax(mg, fabs(a_g));
-        mx = fmax(mx, fabs(a_x));
+        const float2 a_x = ax[e], k_x = kx[e];
+        const float2 a_g = df_fma(l2, a_x, df_mul(df_from_int(rq[(int64_t)b * Nx * 4 + e]), iq));
+        const float2 k_g = df_fma(l2, k_x, KR[(int64_t)b * Nx * 4 + e]);
+        g2 = df_fma(a_g, k_g, g2);
+        x2 = df_fma(a_x, k_x, x2);
+        mg = fmaxf(mg, fabsf(a_g.x));
+        mx = fmaxf(mx, fabsf(a_x.x));
         if (push) {
-            const double a_y = a_g - ago[e], k_y = k_g - kgo[e];
+            const float2 a_y = df_sub(a_g, ago[e]), k_y = df_sub(k_g, kgo[e]);
             ay[e] = a_y;
             ky[e] = k_y;
-            const double a_s = as[e], k_s = ks[e];
-            sy += a_s * k_y;
-            yy += a_y * k_y;
-            ss += a_s * k_s;
+            const float2 a_s = as[e], k_s = ks[e];
+            sy = df_fma(a_s, k_y, sy);
+            yy = df_fma(a_y, k_y, yy);
+            ss = df_fma(a_s, k_s, ss);
         }
         agn[e] = a_g;
         kgn[e] = k_g;
     }
-    double v[5] = {g2, x2, sy, yy, ss};
+    double v[5] = {df_to_d(g2), df_to_d(x2), df_to_d(sy), df_to_d(yy), df_to_d(ss)};
     const int idx[5] = {ACC_G2, ACC_X2J, ACC_SY, ACC_YY, ACC_SS};
     block_sum_atomic<5>(v, acc + (int64_t)b * NACC, idx);
-    mg = warp_max_d(mg);
-    mx = warp_max_d(mx);
+    mg = warp_max(mg);
+    mx = warp_max(mx);
     if ((threadIdx.x & 31) == 0) {
-        if (mg > 0.0) atomic_max_nonneg(amax + 2 * b, mg);
-        if (mx > 0.0) atomic_max_nonneg(amax + 2 * b + 1, mx);
+        if (mg > 0.f) atomic_max_nonneg(amax + 2 * b, (double)mg);
+        if (mx > 0.f) atomic_max_nonneg(amax + 2 * b + 1, (double)mx);
     }
 }
 
@@ -191,23 +197,23 @@ k_dual_grad(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
 // on the host from these and the previous iteration's: S^T y = S^T g - S^T g_old.)
 __global__ void __launch_bounds__(256)
 k_dual_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
-            int newg, const double *__restrict__ dv, double *__restrict__ dots)
+            int newg, const float2 *__restrict__ dv, double *__restrict__ dots)
 {
     constexpr int NP = MAXHIST + 1;   // live positions: a full history and the pair just pushed
     const int b = list[blockIdx.y];
     const SlotDev &S = sd[b];
     const int k = S.nhist;
-    const double *kg = dv + dvo(b, DV_G + (newg ? 1 - S.gcur : S.gcur), 1, NV, Nx);
-    double s[2 * NP];
+    const float2 *kg = dv + dvo(b, DV_G + (newg ? 1 - S.gcur : S.gcur), 1, NV, Nx);
+    float2 s[2 * NP];
 #pragma unroll
-    for (int q = 0; q < 2 * NP; ++q) s[q] = 0.0;
+    for (int q = 0; q < 2 * NP; ++q) s[q] = df_zero();
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
-        const double g = kg[e];
+        const float2 g = kg[e];
 #pragma unroll
         for (int j = 0; j < NP; ++j) {
             if (j >= k) break;
-            s[j] += dv[dvo(b, DV_S + S.ring[j], 0, NV, Nx) + e] * g;
-            s[NP + j] += dv[dvo(b, DV_S + ring + S.ring[j], 0, NV, Nx) + e] * g;
+            s[j] = df_fma(dv[dvo(b, DV_S + S.ring[j], 0, NV, Nx) + e], g, s[j]);
+            s[NP + j] = df_fma(dv[dvo(b, DV_S + ring + S.ring[j], 0, NV, Nx) + e], g, s[NP + j]);
         }
     }
     __shared__ double red[2 * NP];
@@ -216,7 +222,7 @@ k_dual_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
 #pragma unroll
     for (int q = 0; q < 2 * NP; ++q) {
         if ((q % NP) >= k) continue;
-        const double v = warp_sum(s[q]);
+        const double v = warp_sum(df_to_d(s[q]));
         if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(&red[q], v);
     }
     __syncthreads();
@@ -339,40 +345,53 @@ k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, 
 // own numbers, sum_i w_i sum_c p0_ic (u_ic - u_iy)
 __global__ void __launch_bounds__(256)
 k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int N, int NV,
-                 int ring, double *__restrict__ dv, const double *__restrict__ lbase, float *__restrict__ P0,
+                 int ring, float2 *__restrict__ dv, const double *__restrict__ lbase, float *__restrict__ P0,
                  const double *__restrict__ w, const uint8_t *__restrict__ rstate, double *__restrict__ u,
                  float *__restrict__ ud, double *__restrict__ acc)
 {
     const int b = list[blockIdx.y];
     const SlotDev &S = sd[b];
     const int k = S.nhist;
-    const double *ag = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kg = dv + dvo(b, DV_G + S.gcur, 1, NV, Nx);
-    const double *ax = dv + dvo(b, DV_X, 0, NV, Nx);
-    double *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = dv + dvo(b, DV_D, 1, NV, Nx);
-    double gd = 0, dd = 0, xd = 0, dg0 = 0;
+    const float2 *ag = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kg = dv + dvo(b, DV_G + S.gcur, 1, NV, Nx);
+    const float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx);
+    float2 *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = dv + dvo(b, DV_D, 1, NV, Nx);
+    const int64_t part = Nx * 4;
+    __shared__ float2 cf[2 * MAXHIST + 1 + Q];   // the slot's coefficients and eta_d
+    if (threadIdx.x < k) {
+        cf[threadIdx.x] = df_from_d(S.coefS[threadIdx.x]);
+        cf[MAXHIST + threadIdx.x] = df_from_d(S.coefY[threadIdx.x]);
+    }
+    if (threadIdx.x == 0) cf[2 * MAXHIST] = df_from_d(S.coef_g);
+    if (threadIdx.x < Q) cf[2 * MAXHIST + 1 + threadIdx.x] = df_from_d(S.eta[threadIdx.x]);
+    __syncthreads();
+    const float2 cg = cf[2 * MAXHIST];
+    float2 gd = df_zero(), dd = df_zero(), xd = df_zero(), dg0 = df_zero();
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
-        double a = S.coef_g * ag[e], kk = S.coef_g * kg[e];
+        const float2 g_a = ag[e], g_k = kg[e];
+        float2 a = df_mul(cg, g_a), kk = df_mul(cg, g_k);
 #pragma unroll
         for (int j = 0; j < MAXHIST; ++j) {
             if (j >= k) break;
-            const int64_t os = dvo(b, DV_S + S.ring[j], 0, NV, Nx), oy = dvo(b, DV_S + ring + S.ring[j], 0, NV, Nx);
-            const int64_t part = Nx * 4;
-            a += S.coefS[j] * dv[os + e] + S.coefY[j] * dv[oy + e];
-            kk += S.coefS[j] * dv[os + part + e] + S.coefY[j] * dv[oy + part + e];
+            const float2 *vs = dv + dvo(b, DV_S + S.ring[j], 0, NV, Nx), *vy = dv + dvo(b, DV_S + ring + S.ring[j], 0, NV, Nx);
+            const float2 cs = cf[j], cy = cf[MAXHIST + j];
+            a = df_fma(cy, vy[e], df_fma(cs, vs[e], a));
+            kk = df_fma(cy, vy[part + e], df_fma(cs, vs[part + e], kk));
         }
         ad[e] = a;
         kd[e] = kk;
-        gd += ag[e] * kk;
-        dd += a * kk;
-        xd += ax[e] * kk;
+        gd = df_fma(g_a, kk, gd);
+        dd = df_fma(a, kk, dd);
+        xd = df_fma(ax[e], kk, xd);
         const int c = (int)(e & 3);
-        const double uu = kk + S.eta[c];
-        u[(int64_t)b * Nx * 4 + e] = uu;
+        const float2 uu = df_add(kk, cf[2 * MAXHIST + 1 + c]);
+        u[(int64_t)b * Nx * 4 + e] = df_to_d(uu);
         // the four states of a sequence sit in four consecutive lanes
         const int64_t o = (int64_t)b * Nx + e / 4;
         const int y = rstate[o] & 3;
-        const double uy = __shfl_sync(0xffffffffu, uu, (threadIdx.x & ~3) + y);
-        ud[(int64_t)b * Nx * 4 + e] = (float)(uu - uy);
+        const int src = (threadIdx.x & ~3) + y;
+        const float2 uy = make_float2(__shfl_sync(0xffffffffu, uu.x, src), __shfl_sync(0xffffffffu, uu.y, src));
+        const float2 du = df_sub(uu, uy);
+        ud[(int64_t)b * Nx * 4 + e] = df_f(du);
         // p0 = softmax of the four logits of the sequence (lanes 4k..4k+3)
         const double l = lbase[(int64_t)b * Nx * 4 + e];
         double m = fmax(l, __shfl_xor_sync(0xffffffffu, l, 1));
@@ -382,9 +401,9 @@ k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ lis
         z += __shfl_xor_sync(0xffffffffu, z, 2);
         const float p0 = ex / z;
         P0[(int64_t)b * Nx * 4 + e] = p0;
-        if (e / 4 < N) dg0 += w[e / 4] * (double)p0 * (uu - uy);
+        if (e / 4 < N) dg0 = df_fma(make_float2((float)w[e / 4] * p0, 0.f), du, dg0);
     }
-    double v[4] = {gd, dd, xd, dg0};
+    double v[4] = {df_to_d(gd), df_to_d(dd), df_to_d(xd), df_to_d(dg0)};
     const int idx[4] = {ACC_GD, ACC_DDJ, ACC_XDJ, ACC_DG0};
     block_sum_atomic<4>(v, acc + (int64_t)b * NACC, idx);
 }
@@ -393,24 +412,25 @@ k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ lis
 // logits lbase += stp u
 __global__ void __launch_bounds__(256)
 k_dual_accept(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int NV,
-              double *__restrict__ dv, const double *__restrict__ u, double *__restrict__ lbase)
+              float2 *__restrict__ dv, const double *__restrict__ u, double *__restrict__ lbase)
 {
     const int b = list[blockIdx.y];
     const SlotDev &S = sd[b];
     const double stp = S.stp;
     const bool push = (S.flags & SLOT_F_PUSH) && S.ring_new >= 0;
-    double *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = dv + dvo(b, DV_X, 1, NV, Nx);
-    const double *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = dv + dvo(b, DV_D, 1, NV, Nx);
-    double *as = dv + dvo(b, DV_S + (push ? S.ring_new : 0), 0, NV, Nx);
-    double *ks = dv + dvo(b, DV_S + (push ? S.ring_new : 0), 1, NV, Nx);
+    const float2 sf = df_from_d(stp);
+    float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = dv + dvo(b, DV_X, 1, NV, Nx);
+    const float2 *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = dv + dvo(b, DV_D, 1, NV, Nx);
+    float2 *as = dv + dvo(b, DV_S + (push ? S.ring_new : 0), 0, NV, Nx);
+    float2 *ks = dv + dvo(b, DV_S + (push ? S.ring_new : 0), 1, NV, Nx);
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
-        const double a0 = ax[e], k0 = kx[e];
-        const double a1 = a0 + stp * ad[e], k1 = k0 + stp * kd[e];
+        const float2 a0 = ax[e], k0 = kx[e];
+        const float2 a1 = df_fma(sf, ad[e], a0), k1 = df_fma(sf, kd[e], k0);
         ax[e] = a1;
         kx[e] = k1;
         if (push) {
-            as[e] = a1 - a0;
-            ks[e] = k1 - k0;
+            as[e] = df_sub(a1, a0);
+            ks[e] = df_sub(k1, k0);
         }
         lbase[(int64_t)b * Nx * 4 + e] += stp * u[(int64_t)b * Nx * 4 + e];
     }
@@ -419,14 +439,14 @@ k_dual_accept(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, 
 // FP32 copy of a vector's a part (the current gradient, or x) as the R rows
 // of a tensor-core backward contraction, scaled by `scale`
 __global__ void k_dual_to_r(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int N,
-                            int NV, int which, const double *__restrict__ dv, float4 *__restrict__ R)
+                            int NV, int which, const float2 *__restrict__ dv, float4 *__restrict__ R)
 {
     const int b = list[blockIdx.y];
     const int v = which == 0 ? DV_G + sd[b].gcur : DV_X;
-    const double *a = dv + dvo(b, v, 0, NV, Nx);
+    const float2 *a = dv + dvo(b, v, 0, NV, Nx);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Nx; i += (int64_t)gridDim.x * blockDim.x) {
         float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (i < N) r = make_float4((float)a[4 * i], (float)a[4 * i + 1], (float)a[4 * i + 2], (float)a[4 * i + 3]);
+        if (i < N) r = make_float4(df_f(a[4 * i]), df_f(a[4 * i + 1]), df_f(a[4 * i + 2]), df_f(a[4 * i + 3]));
         R[(int64_t)b * Nx + i] = r;
     }
 }
@@ -436,17 +456,17 @@ __global__ void k_dual_to_r(const SlotDev *__restrict__ sd, const int32_t *__res
 // |D| <= 2^10.  Digits are exact in fp16 and their sums over fewer than
 // 2^14 sequences are exact in FP32, so X^T D is exact on the tensor cores.
 __global__ void k_dual_digits(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int N,
-                              int NV, int d, const double *__restrict__ dv, float4 *__restrict__ R)
+                              int NV, int d, const float2 *__restrict__ dv, float4 *__restrict__ R)
 {
     const int b = list[blockIdx.y];
     const double qa = sd[b].tc_scale;
-    const double *a = dv + dvo(b, DV_X, 0, NV, Nx);
+    const float2 *a = dv + dvo(b, DV_X, 0, NV, Nx);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Nx; i += (int64_t)gridDim.x * blockDim.x) {
         float v[4] = {0.f, 0.f, 0.f, 0.f};
         if (i < N) {
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
-                const long long A = llrint(a[4 * i + c] * qa);
+                const long long A = llrint(df_to_d(a[4 * i + c]) * qa);
                 const long long d0 = (A + (1ll << 21)) >> 22;          // round(A / 2^22)
                 const long long r0 = A - (d0 << 22);
                 const long long d1 = (r0 + (1ll << 10)) >> 11;         // round(r0 / 2^11)
@@ -520,13 +540,14 @@ void launch_dual_quant(const Problem &P, const SlotDev *sd, const int32_t *list,
 {
     if (n <= 0) return;
     dim3 gq(grid_for(P.Nx, 256 * 4, 64), n);
-    k_dual_quant<<<gq, 256, 0, st>>>(sd, list, (int)P.N, P.Nx, reinterpret_cast<const float4 *>(R), rstate, qscale,
+    k_dual_quant<<<gq, 256, 0, st>>>(sd, list, (int)P.N, P.Nx, reinterpret_cast<const float4 *>(R), rstate,
+                                     (float)qscale,
                                      reinterpret_cast<int4 *>(rq), reinterpret_cast<unsigned long long *>(csum));
 }
 
 // K rho on the CUDA cores (64-bit integer multiply-adds): any N
 void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8_t *rstate, const int32_t *K,
-                       double qscale, const int32_t *rq, const long long *csum, double *KR, cudaStream_t st)
+                       double qscale, const int32_t *rq, const long long *csum, float2 *KR, cudaStream_t st)
 {
     if (n <= 0) return;
     dim3 gk((unsigned)(P.Nx / KP_M), (unsigned)((n + KP_S - 1) / KP_S));
@@ -535,7 +556,7 @@ void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8
 }
 
 void launch_dual_grad(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double qscale,
-                      const int32_t *rq, const double *KR, double *dv, double *acc, double *amax, cudaStream_t st)
+                      const int32_t *rq, const float2 *KR, float2 *dv, double *acc, double *amax, cudaStream_t st)
 {
     if (n <= 0) return;
     const int NV = DV_S + 2 * P.ring;
@@ -543,7 +564,7 @@ void launch_dual_grad(const Problem &P, const SlotDev *sd, const int32_t *list, 
     k_dual_grad<<<gg, 256, 0, st>>>(sd, list, P.Nx, NV, P.ring, P.lambda_J, rq, 1.0 / qscale, KR, dv, acc, amax);
 }
 
-void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int newg, const double *dv,
+void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int newg, const float2 *dv,
                       double *dots, cudaStream_t st)
 {
     if (n <= 0) return;
@@ -551,7 +572,7 @@ void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, 
     k_dual_dots<<<g, 256, 0, st>>>(sd, list, P.Nx, DV_S + 2 * P.ring, P.ring, newg, dv, dots);
 }
 
-void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
+void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float2 *dv,
                            const double *lbase, float *P0, const double *w, const uint8_t *rstate, double *u,
                            float *ud, double *acc, cudaStream_t st)
 {
@@ -577,7 +598,7 @@ void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list
                                                acc);
 }
 
-void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double *dv,
+void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float2 *dv,
                         const double *u, double *lbase, cudaStream_t st)
 {
     if (n <= 0) return;
@@ -586,7 +607,7 @@ void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list
 }
 
 void launch_dual_to_r(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int which,
-                      const double *dv, float *R, cudaStream_t st)
+                      const float2 *dv, float *R, cudaStream_t st)
 {
     if (n <= 0) return;
     dim3 g(grid_for(P.Nx, 256 * 4, 64), n);
@@ -602,7 +623,7 @@ void launch_dual_gmax(const Problem &P, const SlotDev *sd, const int32_t *list, 
     k_dual_gmax<<<g, 256, 0, st>>>(sd, list, (int)P.L, P.Dp, gpool, acc);
 }
 
-void launch_dual_digits(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d, const double *dv,
+void launch_dual_digits(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d, const float2 *dv,
                         float *R, cudaStream_t st)
 {
     if (n <= 0) return;

@@ -33,6 +33,7 @@
 #include <cmath>
 #include <cstdlib>
 
+#include "df.cuh"
 #include "engine.h"
 #include "kernels_common.cuh"
 
@@ -453,7 +454,7 @@ struct KdArgs {
     const uint8_t *rstate;
     const long long *csum;
     double inv_qscale;
-    double *KR;
+    float2 *KR;                  // K rho / qscale in double-float
     int *err;
 };
 
@@ -542,6 +543,7 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const int q = warp & 3;
         const int row = m_tile * KD_BM + q * 32 + lane;
+        const float2 iq = df_from_d(args.inv_qscale);
         unsigned long long acc[KD_BN];
 #pragma unroll
         for (int c = 0; c < KD_BN; ++c) acc[c] = 0ull;
@@ -561,11 +563,11 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
                 const int P = n_tile * (KD_BN / 4) + cc / 4;
                 if (P >= args.nlist || row >= args.Nx) continue;
                 const int b = args.list[P], c = cc & 3;
-                double val = 0.0;
+                float2 val = df_zero();
                 if (row < args.N) {
                     const int y = args.rstate[(int64_t)b * args.Nx + row] & 3;
                     const long long tot = (long long)acc[cc] - args.csum[(int64_t)b * 16 + y * 4 + c];
-                    val = (double)tot * args.inv_qscale;
+                    val = df_mul(df_from_ll(tot), iq);
                 }
                 args.KR[((int64_t)b * args.Nx + row) * 4 + c] = val;
             }
@@ -824,7 +826,7 @@ void tc_kdig_fill_k(const KdPlan *pl, const Problem &P, const int32_t *K, __half
 }
 
 cudaError_t tc_launch_kdig(const KdPlan *pl, const Problem &P, const int32_t *list, int n, const int32_t *rq,
-                           const uint8_t *rstate, const long long *csum, double inv_qscale, __half *Rd, double *KR,
+                           const uint8_t *rstate, const long long *csum, double inv_qscale, __half *Rd, float2 *KR,
                            int *err, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
