@@ -91,4 +91,42 @@ __device__ __forceinline__ float2 df_zero() { return make_float2(0.f, 0.f); }
 // value as a float (rounded)
 __device__ __forceinline__ float df_f(float2 a) { return a.x + a.y; }
 
+// sum over the warp, in double-float (lane 0 holds it)
+__device__ __forceinline__ float2 df_warp_sum(float2 v)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float2 o = make_float2(__shfl_xor_sync(0xffffffffu, v.x, off), __shfl_xor_sync(0xffffffffu, v.y, off));
+        v = df_add(v, o);
+    }
+    return v;
+}
+
+// Sum K per-thread double-float values over the block and add them to
+// dst[idx[k]] (FP64 atomics): warp sums in double-float, one conversion per
+// warp, the warps' sums in FP64 by the first warp.
+template <int K>
+__device__ __forceinline__ void block_sum_df(float2 (&v)[K], double *dst, const int *idx)
+{
+    __shared__ double red_df[32][K];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const float2 s = df_warp_sum(v[k]);
+        if (lane == 0) red_df[wid][k] = df_to_d(s);
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double t = lane < nw ? red_df[lane][k] : 0.0;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+            if (lane == 0 && t != 0.0) atomicAdd(dst + idx[k], t);
+        }
+    }
+    __syncthreads();
+}
+
 } // namespace sdca

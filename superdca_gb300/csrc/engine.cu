@@ -122,6 +122,7 @@ struct sdca_handle {
     std::vector<void *> allocs;
     uint8_t *X = nullptr, *XT = nullptr, *rstate = nullptr;
     double *w = nullptr;
+    float *wf = nullptr;           // the weights in FP32 (kernels that need no more)
     float *wa = nullptr, *d = nullptr, *gpool = nullptr, *u = nullptr, *R = nullptr;
     float *partial = nullptr, *rows = nullptr;
     void *Spool = nullptr, *Ypool = nullptr;
@@ -155,7 +156,8 @@ struct sdca_handle {
 
     // dual form (kernels_dual.cu)
     float2 *dv = nullptr, *KR = nullptr;   // coefficient vectors and K rho, double-float (df.cuh)
-    double *u64 = nullptr, *amax = nullptr, *J64 = nullptr, *amax_h = nullptr;
+    float2 *udf = nullptr;                 // logits direction (the dual form's logits are lbase as double-float)
+    double *amax = nullptr, *J64 = nullptr, *amax_h = nullptr;
     int32_t *rq = nullptr, *Kmat = nullptr;
     long long *csum = nullptr;
     float *Rchk = nullptr, *P0 = nullptr;   // P0: probabilities at the current point, base of the step trials
@@ -225,6 +227,9 @@ int fail(sdca_handle *h, int code, const std::string &msg)
     } while (0)
 
 int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
+
+// the dual form keeps its logits in double-float: the same 8 bytes per value
+float2 *lbase_df(sdca_handle *h) { return reinterpret_cast<float2 *>(h->lbase); }
 
 cudaEvent_t take_event(sdca_handle *h)
 {
@@ -519,7 +524,7 @@ int slot_begin(sdca_handle *h, int b, int64_t k, int32_t locus, const float *x0_
     if (h->form == SDCA_FORM_DUAL) {
         const size_t NV = DV_S + 2 * (size_t)P.ring;
         CK(cudaMemsetAsync(h->dv + (size_t)b * NV * 2 * P.Nx * 4, 0, sizeof(double) * NV * 2 * P.Nx * 4, h->stream));
-        CK(cudaMemsetAsync(h->u64 + (size_t)b * P.Nx * 4, 0, sizeof(double) * P.Nx * 4, h->stream));
+        CK(cudaMemsetAsync(h->udf + (size_t)b * P.Nx * 4, 0, sizeof(float2) * P.Nx * 4, h->stream));
     }
     S.stp = 0.0;
     S.use_u = false;
@@ -838,13 +843,13 @@ int phase_trials(sdca_handle *h, Queue &Qu)
             if (!delta.empty()) {
                 if ((rc = upload_list(h, delta))) return rc;
                 Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)delta.size());
-                launch_trial_delta(P, h->sd, h->list, (int)delta.size(), h->lbase, h->u64, h->ud, h->rstate, h->w,
+                launch_trial_delta(P, h->sd, h->list, (int)delta.size(), lbase_df(h), h->udf, h->ud, h->rstate, h->wf,
                                    h->P0, h->R, h->acc, h->stream);
             }
             if (!full.empty()) {
                 if ((rc = upload_list(h, full))) return rc;
                 Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)full.size());
-                launch_trial64(P, h->sd, h->list, (int)full.size(), h->lbase, h->u64, h->rstate, h->w, h->R, h->acc,
+                launch_trial_dual(P, h->sd, h->list, (int)full.size(), lbase_df(h), h->udf, h->rstate, h->w, h->R, h->acc,
                                h->stream);
             }
         } else {
@@ -1356,7 +1361,7 @@ int phase_step_dual(sdca_handle *h)
         if ((rc = upload_slots(h, steps))) return rc;
         {
             Timed t(h, SDCA_K_ACCEPT, 1, (int64_t)steps.size());
-            launch_dual_accept(P, h->sd, h->list, (int)steps.size(), h->dv, h->u64, h->lbase, h->stream);
+            launch_dual_accept(P, h->sd, h->list, (int)steps.size(), h->dv, h->udf, lbase_df(h), h->stream);
         }
         CKL();
         for (int b : steps) {
@@ -1637,7 +1642,7 @@ int phase_step_dual(sdca_handle *h)
         if ((r2 = zero_acc(h))) return r2;
         {
             Timed t(h, SDCA_K_DIRECTION, 1, (int64_t)lst.size());
-            launch_dual_direction(P, h->sd, h->list, (int)lst.size(), h->dv, h->lbase, h->P0, h->w, h->rstate, h->u64,
+            launch_dual_direction(P, h->sd, h->list, (int)lst.size(), h->dv, lbase_df(h), h->P0, h->wf, h->rstate, h->udf,
                                   h->ud, h->acc, h->stream);
         }
         CKL();
@@ -1884,11 +1889,12 @@ static int create_lane(const sdca_config *cfg, const sdca_handle *owner, sdca_ha
         h->X = owner->X;
         h->XT = owner->XT;
         h->w = owner->w;
+        h->wf = owner->wf;
         h->Kmat = owner->Kmat;
         h->Kd = owner->Kd;
     }
     if ((!shared && ((rc = dalloc(h, &h->X, (size_t)P.N * P.Lx)) || (rc = dalloc(h, &h->XT, (size_t)P.L * P.Nx)) ||
-                     (rc = dalloc(h, &h->w, (size_t)P.Nx)))) ||
+                     (rc = dalloc(h, &h->w, (size_t)P.Nx)) || (rc = dalloc(h, &h->wf, (size_t)P.Nx)))) ||
         (rc = dalloc(h, &h->rstate, B * P.Nx)) ||
         (rc = dalloc(h, &h->wa, B * P.Dp)) || (rc = dalloc(h, &h->d, B * P.Dp)) ||
         (rc = dalloc(h, &h->gpool, 2 * B * P.Dp)) || (rc = dalloc(h, &h->u, B * P.Nx * 4)) ||
@@ -1905,7 +1911,7 @@ static int create_lane(const sdca_config *cfg, const sdca_handle *owner, sdca_ha
         (rc = halloc(h, &h->rows_h, B * P.L)) || (rc = halloc(h, &h->flag_h, 4)) ||
         (rc = halloc(h, &h->stage, (h->stage_cap = 64 * (((sizeof(SlotDev) + 4) * B + 1024 + 255) & ~(size_t)255)))) ||
         (dual && ((rc = halloc(h, &h->amax_h, 2 * B)) ||
-                  (rc = dalloc(h, &h->dv, B * NV * 2 * P.Nx * 4)) || (rc = dalloc(h, &h->u64, B * P.Nx * 4)) ||
+                  (rc = dalloc(h, &h->dv, B * NV * 2 * P.Nx * 4)) || (rc = dalloc(h, &h->udf, B * P.Nx * 4)) ||
                   (rc = dalloc(h, &h->KR, B * P.Nx * 4)) || (rc = dalloc(h, &h->amax, 2 * B)) ||
                   (rc = dalloc(h, &h->rq, B * P.Nx * 4)) || (rc = dalloc(h, &h->csum, 16 * B)) ||
                   (rc = dalloc(h, &h->Rchk, B * P.Nx * 4)) || (rc = dalloc(h, &h->J64, B * P.Dp)) ||
@@ -1973,6 +1979,8 @@ int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weig
     h->w_host.assign(weights, weights + P.N);
     CK(cudaMemcpy2DAsync(h->X, P.Lx, states, P.L, P.L, P.N, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->w, weights, sizeof(double) * P.N, cudaMemcpyHostToDevice, h->stream));
+    std::vector<float> wf(weights, weights + P.N);   // the copy completes before the sync below
+    CK(cudaMemcpyAsync(h->wf, wf.data(), sizeof(float) * P.N, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemsetAsync(h->flag, 0, sizeof(int), h->stream));
     {
         dim3 grid((unsigned)((P.L + 63) / 64), (unsigned)((P.Nx + 63) / 64));

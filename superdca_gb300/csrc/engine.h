@@ -152,9 +152,10 @@ void launch_score(const Problem &P, const SlotDev *sd, const int32_t *list, int 
                   const float *wa, int gap, float *rows, cudaStream_t st);
 
 // sequence reweighting (kernels_weights.cu)
-void launch_trial64(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
-                    const double *lbase, const double *u, const uint8_t *rstate, const double *w,
-                    float *R, double *acc, cudaStream_t st);
+// the dual form's FP64 evaluation from its double-float logits (start and final points)
+void launch_trial_dual(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                       const float2 *lbase, const float2 *u, const uint8_t *rstate, const double *w,
+                       float *R, double *acc, cudaStream_t st);
 
 // dual form (kernels_dual.cu)
 void launch_dual_kmat(const int32_t *dist, int N, int64_t Nx, int L, int32_t *K, cudaStream_t st);
@@ -167,13 +168,13 @@ void launch_dual_grad(const Problem &P, const SlotDev *sd, const int32_t *list, 
 void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int newg, const float2 *dv,
                       double *dots, cudaStream_t st);
 void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float2 *dv,
-                           const double *lbase, float *P0, const double *w, const uint8_t *rstate, double *u,
+                           const float2 *lbase, float *P0, const float *w, const uint8_t *rstate, float2 *u,
                            float *ud, double *acc, cudaStream_t st);
-void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *lbase,
-                        const double *u, const float *ud, const uint8_t *rstate, const double *w, const float *P0,
+void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float2 *lbase,
+                        const float2 *u, const float *ud, const uint8_t *rstate, const float *w, const float *P0,
                         float *R, double *acc, cudaStream_t st);
 void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float2 *dv,
-                        const double *u, double *lbase, cudaStream_t st);
+                        const float2 *u, float2 *lbase, cudaStream_t st);
 void launch_dual_to_r(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int which,
                       const float2 *dv, float *R, cudaStream_t st);
 void launch_dual_gmax(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *gpool,

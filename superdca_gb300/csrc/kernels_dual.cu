@@ -179,9 +179,9 @@ k_dual_grad(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
         agn[e] = a_g;
         kgn[e] = k_g;
     }
-    double v[5] = {df_to_d(g2), df_to_d(x2), df_to_d(sy), df_to_d(yy), df_to_d(ss)};
+    float2 v[5] = {g2, x2, sy, yy, ss};
     const int idx[5] = {ACC_G2, ACC_X2J, ACC_SY, ACC_YY, ACC_SS};
-    block_sum_atomic<5>(v, acc + (int64_t)b * NACC, idx);
+    block_sum_df<5>(v, acc + (int64_t)b * NACC, idx);
     mg = warp_max(mg);
     mx = warp_max(mx);
     if ((threadIdx.x & 31) == 0) {
@@ -195,40 +195,34 @@ k_dual_grad(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
 // dots[b][DOT_Y + p] = a_yp . k_g.  newg: the gradient just formed (buffer
 // 1 - gcur) instead of the accepted one.  (The dots with the newest y follow
 // on the host from these and the previous iteration's: S^T y = S^T g - S^T g_old.)
+// A block takes DOT_CHUNK elements of one slot: k_g staged in shared memory,
+// each warp one history vector at a time (one accumulator per lane).
+constexpr int DOT_CHUNK = 1024;
+
 __global__ void __launch_bounds__(256)
 k_dual_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
             int newg, const float2 *__restrict__ dv, double *__restrict__ dots)
 {
-    constexpr int NP = MAXHIST + 1;   // live positions: a full history and the pair just pushed
     const int b = list[blockIdx.y];
     const SlotDev &S = sd[b];
     const int k = S.nhist;
-    const float2 *kg = dv + dvo(b, DV_G + (newg ? 1 - S.gcur : S.gcur), 1, NV, Nx);
-    float2 s[2 * NP];
-#pragma unroll
-    for (int q = 0; q < 2 * NP; ++q) s[q] = df_zero();
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
-        const float2 g = kg[e];
-#pragma unroll
-        for (int j = 0; j < NP; ++j) {
-            if (j >= k) break;
-            s[j] = df_fma(dv[dvo(b, DV_S + S.ring[j], 0, NV, Nx) + e], g, s[j]);
-            s[NP + j] = df_fma(dv[dvo(b, DV_S + ring + S.ring[j], 0, NV, Nx) + e], g, s[NP + j]);
-        }
-    }
-    __shared__ double red[2 * NP];
-    if (threadIdx.x < 2 * NP) red[threadIdx.x] = 0.0;
+    const int64_t E = Nx * 4, e0 = (int64_t)blockIdx.x * DOT_CHUNK;
+    const int ne = E - e0 < DOT_CHUNK ? (int)(E - e0) : DOT_CHUNK;
+    __shared__ float2 g[DOT_CHUNK];
+    const float2 *kg = dv + dvo(b, DV_G + (newg ? 1 - S.gcur : S.gcur), 1, NV, Nx) + e0;
+    for (int t = threadIdx.x; t < ne; t += blockDim.x) g[t] = kg[t];
     __syncthreads();
-#pragma unroll
-    for (int q = 0; q < 2 * NP; ++q) {
-        if ((q % NP) >= k) continue;
-        const double v = warp_sum(df_to_d(s[q]));
-        if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(&red[q], v);
-    }
-    __syncthreads();
-    if (threadIdx.x < 2 * NP && (threadIdx.x % NP) < k && red[threadIdx.x] != 0.0) {
-        const int q = threadIdx.x, j = q % NP;
-        atomicAdd(dots + (int64_t)b * 4 * MAXHIST + (q < NP ? 0 : DOT_Y) + S.ring[j], red[q]);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int q = warp; q < 2 * k; q += nw) {
+        const bool isy = q >= k;
+        const int j = isy ? q - k : q;
+        const float2 *v = dv + dvo(b, DV_S + (isy ? ring : 0) + S.ring[j], 0, NV, Nx) + e0;
+        float2 acc = df_zero();
+#pragma unroll 8
+        for (int t = lane; t < ne; t += 32) acc = df_fma(v[t], g[t], acc);
+        const float2 sum = df_warp_sum(acc);
+        if (lane == 0 && (sum.x != 0.f || sum.y != 0.f))
+            atomicAdd(dots + (int64_t)b * 4 * MAXHIST + (isy ? DOT_Y : 0) + S.ring[j], df_to_d(sum));
     }
 }
 
@@ -247,12 +241,56 @@ k_dual_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
 // is large use the FP64 logits.  Sums: ACC_F += w dl, ACC_DG += slope change,
 // ACC_RS += R(stp); R <- R(stp) = w (p(stp) - onehot(y)), its y entry as
 // minus the sum of the others.
+// a step trial of one sequence from its FP64 logits (large steps): adds to
+// fbig, dgbig and writes the residual row r
+__device__ __noinline__ void trial_fp64(const float2 *lb, const float2 *up, double stp, int y, float wi,
+                                        const float (&p0)[4], float (&r)[4], double &fbig, double &dgbig)
+{
+    const double uu[4] = {df_to_d(up[0]), df_to_d(up[1]), df_to_d(up[2]), df_to_d(up[3])};
+    double l0[4], l1[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        l0[a] = df_to_d(lb[a]);
+        l1[a] = l0[a] + stp * uu[a];
+    }
+    const double m0 = fmax(fmax(l0[0], l0[1]), fmax(l0[2], l0[3]));
+    const double m1 = fmax(fmax(l1[0], l1[1]), fmax(l1[2], l1[3]));
+    double z0 = 0, z1 = 0, e1[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        z0 += exp(l0[a] - m0);
+        e1[a] = exp(l1[a] - m1);
+        z1 += e1[a];
+    }
+    double l0y = l0[0], l1y = l1[0], uuy = uu[0];
+#pragma unroll
+    for (int a = 1; a < 4; ++a)
+        if (a == y) {
+            l0y = l0[a];
+            l1y = l1[a];
+            uuy = uu[a];
+        }
+    fbig += (double)wi * ((m1 + log(z1) - l1y) - (m0 + log(z0) - l0y));
+    double ro = 0.0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const double p1 = e1[a] / z1;
+        dgbig += (double)wi * (p1 - (double)p0[a]) * (uu[a] - uuy);
+        const double ra = a == y ? 0.0 : (double)wi * p1;
+        r[a] = (float)ra;
+        ro += ra;
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+        if (a == y) r[a] = (float)-ro;
+}
+
 constexpr int DT_THREADS = 256;
 
-__global__ void __launch_bounds__(DT_THREADS)
+__global__ void __launch_bounds__(DT_THREADS, 4)
 k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int N, int64_t Nx,
-              const double *__restrict__ lbase, const double *__restrict__ u, const float4 *__restrict__ ud,
-              const uint8_t *__restrict__ rstate, const double *__restrict__ w, const float4 *__restrict__ P0,
+              const float2 *__restrict__ lbase, const float2 *__restrict__ u, const float4 *__restrict__ ud,
+              const uint8_t *__restrict__ rstate, const float *__restrict__ w, const float4 *__restrict__ P0,
               float4 *__restrict__ R, double *__restrict__ acc)
 {
     const int b = list[blockIdx.y];
@@ -260,12 +298,13 @@ k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, 
     const float stpf = (float)stp;
     float f = 0.f, dg = 0.f, rs0 = 0.f, rs1 = 0.f, rs2 = 0.f, rs3 = 0.f;
     double fbig = 0.0, dgbig = 0.0;   // sequences that take the FP64 path
+#pragma unroll 1
     for (int i = blockIdx.x * DT_THREADS + threadIdx.x; i < N; i += gridDim.x * DT_THREADS) {
         const int64_t o = (int64_t)b * Nx + i;
         const float4 dv4 = ud[o];
         const float du[4] = {dv4.x, dv4.y, dv4.z, dv4.w};   // u_a - u_y
         const int y = rstate[o] & 3;
-        const float wi = (float)w[i];
+        const float wi = w[i];
         const float4 pv = P0[o];
         const float p0[4] = {pv.x, pv.y, pv.z, pv.w};
         float t[4], tmax = 0.f;
@@ -293,38 +332,11 @@ k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, 
                 r[a] = a == y ? 0.f : wi * (x[a] * iz);
                 ro += r[a];
             }
-            r[y] = -ro;
+#pragma unroll
+            for (int a = 0; a < 4; ++a)   // (no dynamic index: the arrays stay in registers)
+                if (a == y) r[a] = -ro;
         } else {
-            const double *lb = lbase + o * 4;
-            const double2 ua = reinterpret_cast<const double2 *>(u + o * 4)[0];
-            const double2 ub = reinterpret_cast<const double2 *>(u + o * 4)[1];
-            const double uu[4] = {ua.x, ua.y, ub.x, ub.y};
-            double l0[4], l1[4];
-#pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                l0[a] = lb[a];
-                l1[a] = lb[a] + stp * uu[a];
-            }
-            const double m0 = fmax(fmax(l0[0], l0[1]), fmax(l0[2], l0[3]));
-            const double m1 = fmax(fmax(l1[0], l1[1]), fmax(l1[2], l1[3]));
-            double z0 = 0, z1 = 0, e1[4];
-#pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                z0 += exp(l0[a] - m0);
-                e1[a] = exp(l1[a] - m1);
-                z1 += e1[a];
-            }
-            fbig += (double)wi * ((m1 + log(z1) - l1[y]) - (m0 + log(z0) - l0[y]));
-            double ro = 0.0;
-#pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                const double p1 = e1[a] / z1;
-                dgbig += (double)wi * (p1 - (double)p0[a]) * (uu[a] - uu[y]);
-                const double ra = a == y ? 0.0 : (double)wi * p1;
-                r[a] = (float)ra;
-                ro += ra;
-            }
-            r[y] = (float)-ro;
+            trial_fp64(lbase + o * 4, u + o * 4, stp, y, wi, p0, r, fbig, dgbig);
         }
         rs0 += r[0]; rs1 += r[1]; rs2 += r[2]; rs3 += r[3];
         R[o] = make_float4(r[0], r[1], r[2], r[3]);
@@ -345,8 +357,8 @@ k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, 
 // own numbers, sum_i w_i sum_c p0_ic (u_ic - u_iy)
 __global__ void __launch_bounds__(256)
 k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int N, int NV,
-                 int ring, float2 *__restrict__ dv, const double *__restrict__ lbase, float *__restrict__ P0,
-                 const double *__restrict__ w, const uint8_t *__restrict__ rstate, double *__restrict__ u,
+                 int ring, float2 *__restrict__ dv, const float2 *__restrict__ lbase, float *__restrict__ P0,
+                 const float *__restrict__ w, const uint8_t *__restrict__ rstate, float2 *__restrict__ u,
                  float *__restrict__ ud, double *__restrict__ acc)
 {
     const int b = list[blockIdx.y];
@@ -369,7 +381,7 @@ k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ lis
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
         const float2 g_a = ag[e], g_k = kg[e];
         float2 a = df_mul(cg, g_a), kk = df_mul(cg, g_k);
-#pragma unroll
+#pragma unroll 4   // (a full unroll hoists every load: 116 registers, fewer warps)
         for (int j = 0; j < MAXHIST; ++j) {
             if (j >= k) break;
             const float2 *vs = dv + dvo(b, DV_S + S.ring[j], 0, NV, Nx), *vy = dv + dvo(b, DV_S + ring + S.ring[j], 0, NV, Nx);
@@ -384,7 +396,7 @@ k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ lis
         xd = df_fma(ax[e], kk, xd);
         const int c = (int)(e & 3);
         const float2 uu = df_add(kk, cf[2 * MAXHIST + 1 + c]);
-        u[(int64_t)b * Nx * 4 + e] = df_to_d(uu);
+        u[(int64_t)b * Nx * 4 + e] = uu;
         // the four states of a sequence sit in four consecutive lanes
         const int64_t o = (int64_t)b * Nx + e / 4;
         const int y = rstate[o] & 3;
@@ -392,16 +404,17 @@ k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ lis
         const float2 uy = make_float2(__shfl_sync(0xffffffffu, uu.x, src), __shfl_sync(0xffffffffu, uu.y, src));
         const float2 du = df_sub(uu, uy);
         ud[(int64_t)b * Nx * 4 + e] = df_f(du);
-        // p0 = softmax of the four logits of the sequence (lanes 4k..4k+3)
-        const double l = lbase[(int64_t)b * Nx * 4 + e];
-        double m = fmax(l, __shfl_xor_sync(0xffffffffu, l, 1));
-        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, 2));
-        const float ex = expf((float)(l - m));
+        // p0 = softmax of the four logits of the sequence (lanes 4k..4k+3),
+        // shifted by the largest high part
+        const float2 l = lbase[(int64_t)b * Nx * 4 + e];
+        float m = fmaxf(l.x, __shfl_xor_sync(0xffffffffu, l.x, 1));
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
+        const float ex = expf(df_f(df_sub(l, make_float2(m, 0.f))));
         float z = ex + __shfl_xor_sync(0xffffffffu, ex, 1);
         z += __shfl_xor_sync(0xffffffffu, z, 2);
         const float p0 = ex / z;
         P0[(int64_t)b * Nx * 4 + e] = p0;
-        if (e / 4 < N) dg0 = df_fma(make_float2((float)w[e / 4] * p0, 0.f), du, dg0);
+        if (e / 4 < N) dg0 = df_fma(make_float2(w[e / 4] * p0, 0.f), du, dg0);
     }
     double v[4] = {df_to_d(gd), df_to_d(dd), df_to_d(xd), df_to_d(dg0)};
     const int idx[4] = {ACC_GD, ACC_DDJ, ACC_XDJ, ACC_DG0};
@@ -412,7 +425,7 @@ k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ lis
 // logits lbase += stp u
 __global__ void __launch_bounds__(256)
 k_dual_accept(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int NV,
-              float2 *__restrict__ dv, const double *__restrict__ u, double *__restrict__ lbase)
+              float2 *__restrict__ dv, const float2 *__restrict__ u, float2 *__restrict__ lbase)
 {
     const int b = list[blockIdx.y];
     const SlotDev &S = sd[b];
@@ -432,7 +445,7 @@ k_dual_accept(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, 
             as[e] = df_sub(a1, a0);
             ks[e] = df_sub(k1, k0);
         }
-        lbase[(int64_t)b * Nx * 4 + e] += stp * u[(int64_t)b * Nx * 4 + e];
+        lbase[(int64_t)b * Nx * 4 + e] = df_fma(sf, u[(int64_t)b * Nx * 4 + e], lbase[(int64_t)b * Nx * 4 + e]);
     }
 }
 
@@ -560,7 +573,7 @@ void launch_dual_grad(const Problem &P, const SlotDev *sd, const int32_t *list, 
 {
     if (n <= 0) return;
     const int NV = DV_S + 2 * P.ring;
-    dim3 gg(grid_for(P.Nx * 4, 256 * 4, 64), n);
+    dim3 gg(grid_for(P.Nx * 4, 256 * 8, 64), n);
     k_dual_grad<<<gg, 256, 0, st>>>(sd, list, P.Nx, NV, P.ring, P.lambda_J, rq, 1.0 / qscale, KR, dv, acc, amax);
 }
 
@@ -568,12 +581,12 @@ void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, 
                       double *dots, cudaStream_t st)
 {
     if (n <= 0) return;
-    dim3 g(grid_for(P.Nx * 4, 256 * 8, 32), n);
+    dim3 g((unsigned)((P.Nx * 4 + DOT_CHUNK - 1) / DOT_CHUNK), n);
     k_dual_dots<<<g, 256, 0, st>>>(sd, list, P.Nx, DV_S + 2 * P.ring, P.ring, newg, dv, dots);
 }
 
 void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float2 *dv,
-                           const double *lbase, float *P0, const double *w, const uint8_t *rstate, double *u,
+                           const float2 *lbase, float *P0, const float *w, const uint8_t *rstate, float2 *u,
                            float *ud, double *acc, cudaStream_t st)
 {
     if (n <= 0) return;
@@ -583,8 +596,8 @@ void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *l
                                         rstate, u, ud, acc);
 }
 
-void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *lbase,
-                        const double *u, const float *ud, const uint8_t *rstate, const double *w, const float *P0,
+void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float2 *lbase,
+                        const float2 *u, const float *ud, const uint8_t *rstate, const float *w, const float *P0,
                         float *R, double *acc, cudaStream_t st)
 {
     if (n <= 0) return;
@@ -599,7 +612,7 @@ void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list
 }
 
 void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float2 *dv,
-                        const double *u, double *lbase, cudaStream_t st)
+                        const float2 *u, float2 *lbase, cudaStream_t st)
 {
     if (n <= 0) return;
     dim3 g(grid_for(P.Nx * 4, 256 * 4, 64), n);

@@ -10,6 +10,7 @@
 // that the host evaluates from x.d and d.d).
 #include <algorithm>
 
+#include "df.cuh"
 #include "engine.h"
 #include "kernels_common.cuh"
 
@@ -19,23 +20,31 @@ namespace {
 
 constexpr int TRIAL_THREADS = 256;
 
-// the direction's logits u: float4 (contraction forms) or four doubles (dual form)
-__device__ __forceinline__ double4 load_u(const float4 *u, int64_t o)
+// the direction's logits u and the base logits: float4 / FP64 (contraction
+// forms) or double-float (dual form)
+__device__ __forceinline__ double4 load4(const float4 *u, int64_t o)
 {
     const float4 v = u[o];
     return make_double4(v.x, v.y, v.z, v.w);
 }
-__device__ __forceinline__ double4 load_u(const double *u, int64_t o)
+__device__ __forceinline__ double4 load4(const double *v, int64_t o)
 {
-    const double2 a = reinterpret_cast<const double2 *>(u + o * 4)[0];
-    const double2 b = reinterpret_cast<const double2 *>(u + o * 4)[1];
+    const double2 a = reinterpret_cast<const double2 *>(v + o * 4)[0];
+    const double2 b = reinterpret_cast<const double2 *>(v + o * 4)[1];
     return make_double4(a.x, a.y, b.x, b.y);
 }
+__device__ __forceinline__ double4 load4(const float2 *v, int64_t o)
+{
+    const float4 a = reinterpret_cast<const float4 *>(v + o * 4)[0];
+    const float4 b = reinterpret_cast<const float4 *>(v + o * 4)[1];
+    return make_double4(df_to_d(make_float2(a.x, a.y)), df_to_d(make_float2(a.z, a.w)),
+                        df_to_d(make_float2(b.x, b.y)), df_to_d(make_float2(b.z, b.w)));
+}
 
-template <typename UT>
+template <typename UT, typename LT>
 __global__ void __launch_bounds__(TRIAL_THREADS)
 k_trial(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int N, int64_t Nx,
-        const double *__restrict__ lbase, const UT *__restrict__ u,
+        const LT *__restrict__ lbase, const UT *__restrict__ u,
         const uint8_t *__restrict__ rstate, const double *__restrict__ w, float4 *__restrict__ R,
         double *__restrict__ acc)
 {
@@ -46,10 +55,9 @@ k_trial(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int N,
     double f = 0, dg = 0, rs0 = 0, rs1 = 0, rs2 = 0, rs3 = 0;
     for (int i = blockIdx.x * TRIAL_THREADS + threadIdx.x; i < N; i += gridDim.x * TRIAL_THREADS) {
         const int64_t o = (int64_t)b * Nx + i;
-        const double *lb = lbase + o * 4;
-        const double4 uu = use_u ? load_u(u, o) : make_double4(0.0, 0.0, 0.0, 0.0);
-        double l[4] = {lb[0] + stp * uu.x, lb[1] + stp * uu.y, lb[2] + stp * uu.z,
-                       lb[3] + stp * uu.w};
+        const double4 lb = load4(lbase, o);
+        const double4 uu = use_u ? load4(u, o) : make_double4(0.0, 0.0, 0.0, 0.0);
+        double l[4] = {lb.x + stp * uu.x, lb.y + stp * uu.y, lb.z + stp * uu.z, lb.w + stp * uu.w};
         const double mx = fmax(fmax(l[0], l[1]), fmax(l[2], l[3]));
         double e[4], z = 0;
 #pragma unroll
@@ -387,20 +395,20 @@ void launch_trial(const Problem &P, const SlotDev *sd, const int32_t *list, int 
     int gx = (int)((P.N + TRIAL_THREADS - 1) / TRIAL_THREADS);
     if (gx > 32) gx = 32;
     dim3 grid((unsigned)gx, (unsigned)n);
-    k_trial<float4><<<grid, TRIAL_THREADS, 0, st>>>(sd, list, (int)P.N, P.Nx, lbase,
+    k_trial<float4, double><<<grid, TRIAL_THREADS, 0, st>>>(sd, list, (int)P.N, P.Nx, lbase,
                                                     reinterpret_cast<const float4 *>(u), rstate, w,
                                                     reinterpret_cast<float4 *>(R), acc);
 }
 
-void launch_trial64(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
-                    const double *lbase, const double *u, const uint8_t *rstate, const double *w,
-                    float *R, double *acc, cudaStream_t st)
+void launch_trial_dual(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
+                       const float2 *lbase, const float2 *u, const uint8_t *rstate, const double *w,
+                       float *R, double *acc, cudaStream_t st)
 {
     if (n <= 0) return;
     int gx = (int)((P.N + TRIAL_THREADS - 1) / TRIAL_THREADS);
     if (gx > 32) gx = 32;
     dim3 grid((unsigned)gx, (unsigned)n);
-    k_trial<double><<<grid, TRIAL_THREADS, 0, st>>>(sd, list, (int)P.N, P.Nx, lbase, u, rstate, w,
+    k_trial<float2, float2><<<grid, TRIAL_THREADS, 0, st>>>(sd, list, (int)P.N, P.Nx, lbase, u, rstate, w,
                                                     reinterpret_cast<float4 *>(R), acc);
 }
 
