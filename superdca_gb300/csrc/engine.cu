@@ -1919,7 +1919,7 @@ static int create_lane(const sdca_config *cfg, const sdca_handle *owner, sdca_ha
                   (!shared && (rc = dalloc(h, &h->Kmat, (size_t)P.Nx * P.Nx))) ||
                   (P.N <= 4000 && P.L < (1 << 18) &&
                    ((!shared && (rc = dalloc(h, &h->Kd, (size_t)3 * kd_nk_rows(P) * P.Nx))) ||
-                    (rc = dalloc(h, &h->Rd, (size_t)5 * kd_nr_rows(P) * P.Nx)))))) ||
+                    (rc = dalloc(h, &h->Rd, (size_t)4 * kd_nr_rows(P) * P.Nx)))))) ||
         (tcres &&
          ((rc = dalloc(h, &h->Dhi, 4 * B * (size_t)round_up(4 * P.L, 64))) ||
           (rc = dalloc(h, &h->Dlo, 4 * B * (size_t)round_up(4 * P.L, 64))) ||
@@ -2031,7 +2031,8 @@ int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weig
         }
         double wmax = 0.0;
         for (int64_t i = 0; i < P.N; ++i) wmax = std::max(wmax, weights[i]);
-        const int qb = std::min(30, 62 - (int)std::ceil(std::log2((double)P.N * (double)P.L + 1.0)));
+        // the tensor-core product's four base-128 digit planes hold |rho_q| <= 2^27
+        const int qb = std::min(h->kd ? 27 : 30, 62 - (int)std::ceil(std::log2((double)P.N * (double)P.L + 1.0)));
         h->qscale = wmax > 0.0 ? std::ldexp(1.0, qb) / wmax : 1.0;
     }
     h->has_alignment = true;

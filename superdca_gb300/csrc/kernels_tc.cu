@@ -411,23 +411,23 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
 // Exact K rho for the dual form on the tensor cores.
 //
 // K (agreement counts, < 2^18) is held as three fp16 planes of base-64
-// digits (0..63), rho_q (integers, |rho_q| <= 2^30) as five fp16 planes of
-// balanced base-64 digits (|digit| <= 32, the top one <= 65).  Every product
+// digits (0..63), rho_q (integers, |rho_q| <= 2^27) as four fp16 planes of
+// balanced base-128 digits (|digit| <= 64, the top one <= 65).  Every product
 // of two digits is an integer below 4096 and the sum over at most 4000
-// sequences stays below 2^24, so each of the 15 digit-pair GEMMs is exact in
-// its FP32 TMEM accumulator; the epilogue combines them with their powers of
-// 64 in 64-bit integers (modulo 2^64: the total itself is below 2^62).
+// sequences stays below 2^24, so each of the 12 digit-pair GEMMs is exact in
+// its FP32 TMEM accumulator; the epilogue combines them with their weights
+// 2^(6k + 7p) in 64-bit integers (modulo 2^64: the total is below 2^62).
 
 constexpr int KD_BM = 128, KD_BN = 32, KD_BK = 64;
-constexpr int KD_KDIG = 3, KD_RDIG = 5;
+constexpr int KD_KDIG = 3, KD_RDIG = 4;
 constexpr int KD_A_BYTES = KD_BM * KD_BK * 2;  // one K digit plane tile, 16 KB
 constexpr int KD_B_BYTES = KD_BN * KD_BK * 2;  // one rho digit plane tile, 4 KB
 constexpr int KD_STAGE = KD_KDIG * KD_A_BYTES + KD_RDIG * KD_B_BYTES;
 constexpr int KD_STG = 3;
 constexpr int KD_SMEM = KD_STG * KD_STAGE + 1024 + 256;
-constexpr uint32_t KD_TMEM_COLS = 512;  // 15 accumulators of 32 columns
-// one MMA per K digit covers all five rho digit planes: they are staged
-// back to back, a 160-row B operand, and fill 160 accumulator columns
+constexpr uint32_t KD_TMEM_COLS = 512;  // 12 accumulators of 32 columns
+// one MMA per K digit covers all four rho digit planes: they are staged
+// back to back, a 128-row B operand, and fill 128 accumulator columns
 constexpr int KD_NB = KD_RDIG * KD_BN;
 constexpr uint32_t IDESC_KD = (1u << 4) | ((uint32_t)(KD_NB >> 3) << 17) | ((uint32_t)(KD_BM >> 4) << 24);
 static_assert(KD_STAGE % 1024 == 0, "stage must keep 1024-byte alignment");
@@ -554,7 +554,7 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
                 for (int p = 0; p < KD_RDIG; ++p) {
                     float v[32];
                     tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)((k * KD_RDIG + p) * KD_BN), v);
-                    const unsigned long long w = 1ull << (6 * (k + p));
+                    const unsigned long long w = 1ull << (6 * k + 7 * p);
 #pragma unroll
                     for (int c = 0; c < KD_BN; ++c) acc[c] += (unsigned long long)__float2ll_rn(v[c]) * w;
                 }
@@ -596,7 +596,7 @@ __global__ void k_kdig_split_k(const int32_t *__restrict__ K, int64_t Nx, int nk
     }
 }
 
-// rho_q of list position P (slot list[P]) -> five fp16 planes of balanced base-64 digits, rows P*4+c
+// rho_q of list position P (slot list[P]) -> four fp16 planes of balanced base-128 digits, rows P*4+c
 __global__ void k_kdig_split_r(const int32_t *__restrict__ list, int64_t Nx, int nr_rows,
                                const int4 *__restrict__ rq, __half *__restrict__ Rd)
 {
@@ -611,8 +611,8 @@ __global__ void k_kdig_split_r(const int32_t *__restrict__ list, int64_t Nx, int
             for (int p = 0; p < KD_RDIG; ++p) {
                 long long d = v;
                 if (p < KD_RDIG - 1) {
-                    d = ((v + 32) & 63) - 32;   // balanced digit, v - d divisible by 64
-                    v = (v - d) / 64;
+                    d = ((v + 64) & 127) - 64;   // balanced digit, v - d divisible by 128
+                    v = (v - d) / 128;
                 }
                 Rd[((int64_t)p * nr_rows + (int64_t)P * 4 + c) * Nx + j] = __int2half_rn((int)d);
             }
