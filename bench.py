@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--batch", type=int, default=0, help="slots per solver lane (default: 512 dual, 64 otherwise)")
     ap.add_argument("--lanes", type=int, default=0,
-                    help="solver lanes (own stream and host thread each; default: 3 dual, 1 otherwise)")
+                    help="solver lanes (own stream and host thread each; default: 4 dual, 1 otherwise)")
     ap.add_argument("--loci-per-step", type=int, default=0, help="default: 2 x batch x lanes")
     ap.add_argument("--form", default="dual", choices=["gather", "tc", "dual"])
     ap.add_argument("--history-bf16", action="store_true")
@@ -166,7 +166,7 @@ def roofline_dual(prof_tot, N, L, m):
 
     Work per unit (one target locus through one launch of the class):
       forward (K rho, exact on the tensor cores): 2 N^2 q FLOP, counted once
-        (the digit expansion issues 15 fp16 products of it on the pipe);
+        (the digit expansion issues 12 fp16 products of it on the pipe);
       backward (one-hot contraction X^T a on the tensor cores: max-norm
         checks and the final J): 2 N L q^2 FLOP, as in the other forms;
       history dots: 2k + 1 vectors of N x q doubles read (32 N bytes each);
@@ -187,7 +187,7 @@ def roofline_dual(prof_tot, N, L, m):
     if cls == "forward":
         ach = 2.0 * N * N * Q * units[cls] / t / 1e12
         return dict(bound="tensor", achieved=round(ach, 3), peak=tflops, unit="TFLOP/s", frac=round(ach / tflops, 5),
-                    traffic=None, kernel="k_kdig (K rho)", issued_factor=15, peak_source=src), cls
+                    traffic=None, kernel="k_kdig (K rho)", issued_factor=12, peak_source=src), cls
     if cls == "backward":
         ach = 2.0 * N * L * Q * Q * units[cls] / t / 1e12
         return dict(bound="tensor", achieved=round(ach, 3), peak=tflops, unit="TFLOP/s", frac=round(ach / tflops, 5),
@@ -283,7 +283,7 @@ def engine_arm(args):
     N, L = st.shape
     w = np.ones(N)
     B = args.batch or (512 if args.form == "dual" else 64)
-    lanes = args.lanes or (3 if args.form == "dual" else 1)
+    lanes = args.lanes or (4 if args.form == "dual" else 1)
     per_step = args.loci_per_step or 2 * B * lanes   # slots refill once per step
     form = {"tc": FORM_TC, "gather": FORM_GATHER, "dual": FORM_DUAL}[args.form]
     E = Engine(N, L, batch=B, device=local, form=form, history_bf16=args.history_bf16, lanes=lanes)

@@ -73,7 +73,7 @@ const char *USAGE =
     "                                     contractions) or plain.\n"
     "  --gpu-batch arg                    Loci solved together per lane (256 dual, 64 otherwise).\n"
     "  --gpu-lanes arg                    Solver lanes, each with its own stream and host thread\n"
-    "                                     (3 dual, 1 otherwise).\n"
+    "                                     (4 dual, 1 otherwise).\n"
     "  --gpu-history arg (=fp32)          L-BFGS history storage: fp32 or bf16.\n"
     "  --gpu-chunk arg (=4096)            Loci per solve call (bounds host memory).\n"
     "  --gpu-top-k arg (=0)               Write only the K strongest pairs, strongest first.\n"
@@ -739,7 +739,7 @@ int main(int argc, char **argv)
         }
         const bool dual = cfg.form == SDCA_FORM_DUAL;
         cfg.batch = o.batch > 0 ? o.batch : (dual ? 256 : 64);
-        cfg.lanes = o.lanes > 0 ? o.lanes : (dual ? 3 : 1);
+        cfg.lanes = o.lanes > 0 ? o.lanes : (dual ? 4 : 1);
         cfg.flags = o.history_bf16 ? SDCA_FLAG_HISTORY_BF16 : 0;
         cfg.device = o.device;
         check(sdca_create(&cfg, &H.h), nullptr, "engine set-up failed");
