@@ -420,7 +420,8 @@ def engine_arm(args):
                    "history": "bf16" if args.history_bf16 else "fp32",
                    "warm_start": os.path.basename(ws) if ws else None,
                    "weights": "unit (--no-reweighting)", "gradient_threshold": 1e-3,
-                   "l2": "inputs larger than L2 (282 MB alignment, per-slot solver state)",
+                   "l2": (f"inputs larger than L2 ({N * L / 1e6:.0f} MB alignment; per-slot solver state "
+                          f"{B * lanes} slots)"),
                    "parallelism": f"loci sharded over {world} rank(s)"},
         "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": rf, "reweighting": rw,
         "kernel_ms": {k: round(v, 2) for k, v in tot["kernel_ms"].items()},
