@@ -1319,7 +1319,7 @@ int dual_convert(sdca_handle *h, bool force)
         for (int d = 0; d < 3; ++d) {
             launch_dual_digits(P, h->sd, h->list, (int)fin.size(), d, h->dv, h->Rchk, h->stream);
             CK(tc_launch_bwd(h->tc, P, h->sd, h->list, (int)fin.size(), h->Rchk, 1.0f, h->Rhi, h->Rlo, h->gpool,
-                             h->tc_err, h->stream));
+                             h->tc_err, h->stream, true));   // digits |D| <= 2^10: exact in fp16
             launch_dual_digit_acc(P, h->sd, h->list, (int)fin.size(), d, h->gpool, h->J64, h->stream);
         }
         launch_dual_to_wa(P, h->sd, h->list, (int)fin.size(), h->J64, h->wa, h->stream);

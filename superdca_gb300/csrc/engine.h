@@ -219,9 +219,11 @@ cudaError_t tc_configure();
 cudaError_t tc_launch_fwd(const TcPlan *pl, const Problem &P, const SlotDev *sd, const int32_t *list, int n,
                           const float *vecs, __half *Dhi, __half *Dlo, float *partial, int splits, int *err,
                           cudaStream_t st);
+// exact_fp16: R holds values exact in fp16 (the dual form's digit planes), so
+// the lo half of the split is zero and its MMA is skipped
 cudaError_t tc_launch_bwd(const TcPlan *pl, const Problem &P, const SlotDev *sd, const int32_t *list, int n,
                           const float *R, float r_scale, __half *Rhi, __half *Rlo, float *gpool, int *err,
-                          cudaStream_t st);
+                          cudaStream_t st, bool exact_fp16 = false);
 // dual form: exact K rho on the tensor cores (N <= 4000, L < 2^18)
 struct KdPlan;
 int kd_nk_rows(const Problem &P);

@@ -240,6 +240,7 @@ struct GemmArgs {
     float *gpool;
     int64_t Dp;
     float inv_scale_bwd;
+    int hi_only;          // the slot operand is exact in fp16 (its lo half is zero): skip the lo MMA
     int *err;
 };
 
@@ -300,7 +301,7 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
                 const uint32_t ph = (uint32_t)((j / STG) & 1);
                 if (!mbar_wait(empty(s), ph ^ 1u)) { failed = true; break; }
                 const uint32_t st = sbase + (uint32_t)s * SB;
-                mbar_expect_tx(full_raw(s), MSUB * RAW_BYTES + 2 * B_BYTES);
+                mbar_expect_tx(full_raw(s), MSUB * RAW_BYTES + (args.hi_only ? 1 : 2) * B_BYTES);
                 const int kt = kt0 + j;
 #pragma unroll
                 for (int ms = 0; ms < MSUB; ++ms) {
@@ -311,7 +312,7 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
                         tma_load_2d(st + RAW + ms * RAW_BYTES, &tmRaw, kt * BK, mt * 32, full_raw(s));
                 }
                 tma_load_2d(st + BHI, &tmBhi, kt * BK, n_tile * BN, full_raw(s));
-                tma_load_2d(st + BLO, &tmBlo, kt * BK, n_tile * BN, full_raw(s));
+                if (!args.hi_only) tma_load_2d(st + BLO, &tmBlo, kt * BK, n_tile * BN, full_raw(s));
             }
             // loads still in flight land before the block retires
             for (int j = max(0, nkt - STG); j < nkt; ++j)
@@ -334,7 +335,7 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
                         const uint64_t ad = smem_desc_sw128(st + a_off(ms) + kk * 32);
                         const uint32_t td = tmem_base + (uint32_t)(ms * BN);
                         mma_f16(td, ad, bh, (j > 0 || kk > 0) ? 1u : 0u);
-                        mma_f16(td, ad, bl, 1u);
+                        if (!args.hi_only) mma_f16(td, ad, bl, 1u);
                     }
                 }
                 mma_commit(empty(s));
@@ -880,7 +881,7 @@ cudaError_t tc_launch_fwd(const TcPlan *pl, const Problem &P, const SlotDev *sd,
 
 cudaError_t tc_launch_bwd(const TcPlan *pl, const Problem &P, const SlotDev *sd, const int32_t *list, int n,
                           const float *R, float r_scale, __half *Rhi, __half *Rlo, float *gpool, int *err,
-                          cudaStream_t st)
+                          cudaStream_t st, bool exact_fp16)
 {
     if (n <= 0) return cudaSuccess;
     {
@@ -898,6 +899,7 @@ cudaError_t tc_launch_bwd(const TcPlan *pl, const Problem &P, const SlotDev *sd,
     a.gpool = gpool;
     a.Dp = P.Dp;
     a.inv_scale_bwd = 1.0f / r_scale;
+    a.hi_only = exact_fp16 ? 1 : 0;
     a.Nx = P.Nx;
     a.err = err;
     launch_gemm_any(msub_choice(), (int)((4 * P.L + tc::BM - 1) / tc::BM), (4 * n + tc::BN - 1) / tc::BN, 1,
