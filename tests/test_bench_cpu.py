@@ -1,0 +1,42 @@
+"""The bench's CPU legs (the oracle timed on host cores) and its contract
+helpers, on small inputs: no GPU."""
+import json
+import os
+
+import numpy as np
+
+import bench
+
+
+def test_cpu_eval_rate_runs_at_least_one_batch(oracle_mod):
+    """A zero-second request (the reference arm's warm-up) still times one
+    batch of evaluations instead of dividing by zero."""
+    st = np.random.default_rng(0).integers(0, 4, size=(24, 40)).astype(np.uint8)
+    spe, done, t = bench.cpu_eval_rate(st, 0.0, 2)
+    assert done == 2 and t > 0.0 and np.isfinite(spe) and spe > 0.0
+
+
+def test_nfeval_reference_file_is_consistent():
+    """The evaluations per locus the reference arm divides by come from full
+    oracle solves of the headline workload, committed beside the oracle."""
+    nf, meta = bench.nfeval_reference("tree-3000x94000")
+    assert nf > 100
+    assert len(meta["nfeval"]) == len(meta["loci"])
+    with open(os.path.join(bench.ROOT, "oracle", "nfeval_tree-3000x94000.json")) as fh:
+        assert json.load(fh)["nfeval"] == meta["nfeval"]
+
+
+def test_roofline_dual_picks_the_requested_class():
+    """With overlapping lanes the bench names the class from an isolated step;
+    roofline_dual reports that class, not the one with the most summed time."""
+    keys = ["forward", "backward", "linesearch", "history", "direction", "accept", "score", "other"]
+    tot = {"kernel_ms": {k: 1.0 for k in keys}, "kernel_units": {k: 10 for k in keys},
+           "kernel_launches": {k: 1 for k in keys}}
+    tot["kernel_ms"]["linesearch"] = 50.0
+    rf, cls = bench.roofline_dual(tot, 3000, 94000, 10)
+    assert cls == "linesearch"
+    rf, cls = bench.roofline_dual(tot, 3000, 94000, 10, "direction")
+    assert cls == "direction" and rf["bound"] == "hbm" and rf["kernel"] == "direction"
+    # per unit: (4k + 3) + 4 vectors of 32 N bytes plus 32 N more, over 1 ms for 10 units
+    per = ((4 * 10 + 3) + 2 + 1 + 1) * 32 * 3000 + 32 * 3000
+    assert abs(rf["achieved"] - round(per * 10 / 1e-3 / 1e9, 1)) < 0.2
