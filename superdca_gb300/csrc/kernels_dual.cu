@@ -491,17 +491,18 @@ __global__ void k_dual_digits(const SlotDev *__restrict__ sd, const int32_t *__r
     }
 }
 
-// J64 (=, or +=) weight * (X^T D) from the tensor-core backward output
+// J (=, or +=) 2^(22, 11, 0) (X^T D) in 64-bit integers: every X^T D is an
+// integer below 2^24, exact in the FP32 backward output
 __global__ void k_dual_digit_acc(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Dp,
-                                 int d, const float *__restrict__ gpool, double *__restrict__ J64)
+                                 int d, const float *__restrict__ gpool, long long *__restrict__ J64)
 {
     const int b = list[blockIdx.y];
     const SlotDev &S = sd[b];
     const float *g = gpool + (int64_t)(2 * b + 1 - S.gcur) * Dp;
-    const double wgt = ldexp(1.0, d == 0 ? 22 : d == 1 ? 11 : 0) / S.tc_scale;
-    double *o = J64 + (int64_t)b * Dp;
+    const long long wgt = 1ll << (d == 0 ? 22 : d == 1 ? 11 : 0);
+    long long *o = J64 + (int64_t)b * Dp;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Dp; e += (int64_t)gridDim.x * blockDim.x)
-        o[e] = (d == 0 ? 0.0 : o[e]) + (double)g[e] * wgt;
+        o[e] = (d == 0 ? 0ll : o[e]) + (long long)__float2int_rn(g[e]) * wgt;
 }
 
 // max |Phi^T a| over the J blocks n != r, from the tensor-core backward output
@@ -519,17 +520,20 @@ __global__ void k_dual_gmax(const SlotDev *__restrict__ sd, const int32_t *__res
     if ((threadIdx.x & 31) == 0 && m > 0.f) atomic_max_nonneg(acc + (int64_t)b * NACC + ACC_GMAX, (double)m);
 }
 
-// x in the engine layout from the combined digits: J blocks (J_rr = 0),
-// h = eta (the slot's eta field), padding 0
+// x in the engine layout from the combined digits: J blocks (J_rr = 0) =
+// the integer sum / tc_scale, rounded once to FP32; h = eta (the slot's eta
+// field), padding 0
 __global__ void k_dual_to_wa(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int L, int64_t Dp,
-                             const double *__restrict__ J64, float *__restrict__ wa)
+                             const long long *__restrict__ J64, float *__restrict__ wa)
 {
     const int b = list[blockIdx.y];
     const SlotDev &S = sd[b];
-    const double *g = J64 + (int64_t)b * Dp;
+    const long long *g = J64 + (int64_t)b * Dp;
+    const double inv = 1.0 / S.tc_scale;
+    // (the integer is below 2^47, so its FP64 value is exact)
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Dp; e += (int64_t)gridDim.x * blockDim.x) {
         float v = 0.f;
-        if (e < (int64_t)QQ * L) v = (e / QQ == S.locus) ? 0.f : (float)g[e];
+        if (e < (int64_t)QQ * L) v = (e / QQ == S.locus) ? 0.f : (float)((double)g[e] * inv);
         else if (e < (int64_t)QQ * L + Q) v = (float)S.eta[e - (int64_t)QQ * L];
         wa[(int64_t)b * Dp + e] = v;
     }
@@ -650,7 +654,7 @@ void launch_dual_digit_acc(const Problem &P, const SlotDev *sd, const int32_t *l
 {
     if (n <= 0) return;
     dim3 g(grid_for(P.Dp, 256 * 16, 256), n);
-    k_dual_digit_acc<<<g, 256, 0, st>>>(sd, list, P.Dp, d, gpool, J64);
+    k_dual_digit_acc<<<g, 256, 0, st>>>(sd, list, P.Dp, d, gpool, reinterpret_cast<long long *>(J64));
 }
 
 void launch_dual_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *J64,
@@ -658,7 +662,7 @@ void launch_dual_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list,
 {
     if (n <= 0) return;
     dim3 g(grid_for(P.Dp, 256 * 16, 256), n);
-    k_dual_to_wa<<<g, 256, 0, st>>>(sd, list, (int)P.L, P.Dp, J64, wa);
+    k_dual_to_wa<<<g, 256, 0, st>>>(sd, list, (int)P.L, P.Dp, reinterpret_cast<const long long *>(J64), wa);
 }
 
 } // namespace sdca

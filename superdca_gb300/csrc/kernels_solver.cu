@@ -331,50 +331,52 @@ __global__ void k_score(const SlotDev *__restrict__ sd, const int32_t *__restric
         return;
     }
     const float4 *jp = reinterpret_cast<const float4 *>(wa + (int64_t)b * Dp + n * QQ);
-    double J[4][4];
+    // single precision: the block is stored in FP32 and the score is written
+    // as FP32 (GB300's FP64 rate is a small fraction of its FP32 rate)
+    float J[4][4];
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
         const float4 v = jp[s];
-        const double t[4] = {v.x, v.y, v.z, v.w};
+        const float t[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             if (n < r) J[a][s] = t[a];
             else J[s][a] = t[a];
         }
     }
-    double rm[4], cm[4], gm = 0.0;
+    float rm[4], cm[4], gm = 0.f;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        double t = 0.0;
+        float t = 0.f;
 #pragma unroll
         for (int j = 0; j < 4; ++j) t = t + J[i][j];
-        rm[i] = t / 4.0;
+        rm[i] = t * 0.25f;
     }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        double t = 0.0;
+        float t = 0.f;
 #pragma unroll
         for (int i = 0; i < 4; ++i) t = t + J[i][j];
-        cm[j] = t / 4.0;
+        cm[j] = t * 0.25f;
     }
     {
-        double t = 0.0;
+        float t = 0.f;
 #pragma unroll
         for (int i = 0; i < 4; ++i) t += rm[i];
-        gm = t / 4.0;
+        gm = t * 0.25f;
     }
-    double sum = 0.0;
+    float sum = 0.f;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         if (i == gap) continue;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             if (j == gap) continue;
-            const double gij = ((J[i][j] - rm[j]) - cm[i]) + gm;
-            sum += gij * gij;
+            const float gij = ((J[i][j] - rm[j]) - cm[i]) + gm;
+            sum = fmaf(gij, gij, sum);
         }
     }
-    row[n] = (float)sqrt(sum);
+    row[n] = sqrtf(sum);
 }
 
 // blocks per slot for the D-length passes: at most `cap`, so that every
