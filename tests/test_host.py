@@ -149,3 +149,33 @@ def test_synthetic_workloads_are_seeded():
     assert a.max() <= 3 and a.shape[0] == 200
     t, ct, _ = synthetic.workload("tree-3000x10000", seed=1, N=64, L=300)
     assert t.shape[0] == 64 and t.max() <= 3
+
+
+def test_ctypes_structs_match_the_header_layout(tmp_path):
+    """The ctypes mirrors of sdca_config, sdca_locus_stat and sdca_profile
+    have the C compiler's sizes and field offsets."""
+    import shutil
+    import subprocess
+
+    from superdca_gb300 import _lib
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"sdca_config": _lib.Config, "sdca_locus_stat": _lib.LocusStat, "sdca_profile": _lib.Profile}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "superdca_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
