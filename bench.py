@@ -412,7 +412,7 @@ def engine_arm(args):
         "warmup": args.warmup, "ms_per_step": round(t_dev * 1e3 / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": {"tc": "fp16x2->fp32 (tensor cores), fp64 reductions",
-                  "dual": "exact integer K.rho (fp16 digits, fp32 accumulators), fp64 L-BFGS vectors",
+                  "dual": "exact integer K.rho (fp16 digits, fp32 accumulators), double-float (2 x fp32) L-BFGS vectors",
                   "gather": "fp32"}[args.form],
         "data": "synthetic (seeded coalescent-tree alignment)",
         "config": {"workload": f"{args.workload} seed {args.seed}", "N": int(N), "L": int(L),
