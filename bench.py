@@ -161,6 +161,14 @@ def load_workload(args):
     return st
 
 
+# DRAM bytes per unit (one target locus through one launch) from one ncu
+# capture, scaled to a launch by its units (the traffic grows with the slots):
+#   ncu --set full --clock-control none -k regex:k_dual_direction -s 40 -c 2 ... \
+#       python bench.py --steps 1 --warmup 0 --batch 128 --lanes 1 --loci-per-step 128 --no-cpu --no-e2e
+#   dram__bytes_read.sum 542.7 MB + dram__bytes_write.sum 42.0 MB per launch of 128 slots
+NCU_TRAFFIC_PER_UNIT = {("tree-3000x94000", "direction"): (542.68e6 + 42.05e6) / 128}
+
+
 def roofline_dual(prof_tot, N, L, m, cls=None):
     """Roofline of the dual form's dominant kernel class.
 
@@ -406,6 +414,11 @@ def engine_arm(args):
     if rf is not None:
         rf["avg_launch_ms"] = round(tot["kernel_ms"][dom] / max(1, tot["kernel_launches"][dom]), 4)
         rf["lanes"] = lanes   # launches of different lanes overlap in time
+        per_unit = NCU_TRAFFIC_PER_UNIT.get((args.workload, dom))
+        if per_unit is not None and tot["kernel_launches"][dom] > 0:
+            units = tot["kernel_units"][dom] / tot["kernel_launches"][dom]
+            rf["traffic"] = round(per_unit * units)   # bytes per launch, scaled from a 128-slot capture
+            rf["traffic_source"] = "ncu dram bytes of a 128-slot launch, scaled by the units per launch"
     out = {
         "metric": "loci/s at N=3000,L=94k (per-locus plmDCA solve, gradient threshold 1e-3)",
         "value": round(value, 4), "unit": "loci/s", "n_gpus": world, "steps": args.steps,
