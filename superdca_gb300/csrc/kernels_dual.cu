@@ -226,23 +226,8 @@ k_dual_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
     }
 }
 
-// A line-search trial as a change from the current point.  With p0 the base
-// probabilities (computed from the FP64 logits at the current point), y the
-// sequence's state at r and t_a = stp (u_a - u_y), per sequence
-//   l(stp) - l(0) = log(Z),  Z = sum_a p0_a exp(t_a) = 1 + q,
-//   q = sum_a p0_a expm1(t_a),  p_a(stp) = p0_a exp(t_a) / Z,
-// and the slope changes by sum_a w (p_a(stp) - p0_a) (u_a - u_y), with
-// p_a(stp) - p0_a = p0_a (expm1(t_a) - q) / Z.  Every term is a difference
-// from the sequence's own state, so single precision gives the change with
-// ~1e-7 relative error of the change itself, which is what the line search
-// compares; the base values (objective, slope at 0) are FP64.  Z is a sum of
-// positive terms and the new probabilities are products, so a probability
-// that has become small keeps its relative precision.  Sequences whose step
-// is large use the FP64 logits.  Sums: ACC_F += w dl, ACC_DG += slope change,
-// ACC_RS += R(stp); R <- R(stp) = w (p(stp) - onehot(y)), its y entry as
-// minus the sum of the others.
-// a step trial of one sequence from its FP64 logits (large steps): adds to
-// fbig, dgbig and writes the residual row r
+// A step trial of one sequence in FP64 from its double-float logits (large
+// steps): adds to fbig, dgbig and writes the residual row r.
 __device__ __noinline__ void trial_fp64(const float2 *lb, const float2 *up, double stp, int y, float wi,
                                         const float (&p0)[4], float (&r)[4], double &fbig, double &dgbig)
 {
@@ -285,6 +270,22 @@ __device__ __noinline__ void trial_fp64(const float2 *lb, const float2 *up, doub
         if (a == y) r[a] = (float)-ro;
 }
 
+// A line-search trial as a change from the current point.  With p0 the base
+// probabilities (computed from the logits at the current point), y the
+// sequence's state at r and t_a = stp (u_a - u_y), per sequence
+//   l(stp) - l(0) = log(Z),  Z = sum_a p0_a exp(t_a) = 1 + q,
+//   q = sum_a p0_a expm1(t_a),  p_a(stp) = p0_a exp(t_a) / Z,
+// and the slope changes by sum_a w (p_a(stp) - p0_a) (u_a - u_y), with
+// p_a(stp) - p0_a = p0_a (expm1(t_a) - q) / Z.  Every term is a difference
+// from the sequence's own state, so single precision gives the change with
+// ~1e-7 relative error of the change itself, which is what the line search
+// compares; the base values (objective, slope at 0) are FP64.  Z is a sum of
+// positive terms and the new probabilities are products, so a probability
+// that has become small keeps its relative precision.  Sequences whose step
+// is large take an FP64 log-sum-exp of the logits (trial_fp64).  Sums:
+// ACC_F += w dl, ACC_DG += slope change, ACC_RS += R(stp);
+// R <- R(stp) = w (p(stp) - onehot(y)), its y entry as minus the sum of the
+// others.
 constexpr int DT_THREADS = 256;
 
 __global__ void __launch_bounds__(DT_THREADS, 4)
@@ -351,7 +352,7 @@ k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, 
 
 // d = coef_g g + sum_j coefS_j s_j + coefY_j y_j (a and k parts); trial
 // logits direction u = k_d + eta_d; the base probabilities P0 of the step
-// trials from the FP64 logits at the current point (fresh every iteration,
+// trials from the double-float logits at the current point (fresh every iteration,
 // so that rounding does not carry from one iteration to the next); sums g.d,
 // d.d, x.d (J parts) and the slope of the search line at 0 from the trials'
 // own numbers, sum_i w_i sum_c p0_ic (u_ic - u_iy)
