@@ -41,7 +41,14 @@ class SolveResult:
 
 
 class Engine:
-    """One alignment resident on one GPU; solves batches of target loci."""
+    """One alignment resident on one GPU; solves batches of target loci.
+
+    batch: loci solved together per solver lane (slots).  lanes: solver
+    lanes, each with its own slots, CUDA stream and host thread; they share
+    the resident alignment and take loci from one queue, so one lane's host
+    decisions overlap the other lanes' kernels.  form: FORM_GATHER (plain),
+    FORM_TC (tensor-core contractions) or FORM_DUAL (the span of the
+    sequences, zero start only)."""
 
     def __init__(self, n_seqs: int, n_loci: int, *, lambda_h: float = -1.0,
                  lambda_J: float = -1.0, gradient_threshold: float = 1e-3,
