@@ -69,3 +69,31 @@ def test_combination_reproduces_k_rho():
             assert np.abs(part).max() < 2 ** 24
             total += part * (1 << (6 * k + 7 * p))
     np.testing.assert_array_equal(total, exact)
+
+
+def test_solution_digit_planes_are_exact():
+    """The reported J = Phi^T a_x: A = round(a qa) with |A| <= 2^32 split into
+    A = D0 2^22 + D1 2^11 + D2 (|D| <= 2^10, exact in fp16); each one-hot
+    contraction sum over at most 16383 sequences stays below 2^24, and the
+    64-bit combination gives the integer sum of A."""
+    rng = np.random.default_rng(11)
+    N = 16383
+    A = rng.integers(-2 ** 32, 2 ** 32 + 1, size=N, dtype=np.int64)
+    A[:4] = [2 ** 32, -2 ** 32, 2 ** 32 - 1, -(2 ** 32 - 1)]
+    d0 = (A + (1 << 21)) >> 22
+    r0 = A - (d0 << 22)
+    d1 = (r0 + (1 << 10)) >> 11
+    d2 = r0 - (d1 << 11)
+    for d in (d0, d1, d2):
+        assert np.abs(d).max() <= 1024
+    np.testing.assert_array_equal((d0 << 22) + (d1 << 11) + d2, A)
+    state = rng.integers(0, 4, size=N)
+    for s in range(4):
+        m = state == s
+        G = [np.float32(0.0)] * 3
+        for k, d in enumerate((d0, d1, d2)):
+            G[k] = np.sum(d[m].astype(np.float32), dtype=np.float32)
+            assert abs(int(G[k])) < 2 ** 24 and int(G[k]) == int(d[m].sum())
+        J = int(G[0]) * (1 << 22) + int(G[1]) * (1 << 11) + int(G[2])
+        assert J == int(A[m].sum())
+    assert 16383 * 1024 < 2 ** 24
