@@ -21,6 +21,12 @@ learned warm start) or gather (plain).  A step's working set (alignment
               uploads the alignment from pinned host memory and reads the
               score rows back
   roofline    for the kernel class with the most device time
+  accuracy    the FP64 oracle's objective and max|gradient| at the engine's
+              returned parameters, for a seeded sample of the first timed
+              step's loci (relative objective error; SuperDCA stops at
+              max|g| < 1e-3)
+  vs_plain    the plain GPU form (FP32 gather contractions) timed on loci of
+              the same step in the same process, and value / its loci/s
   cpu_baseline the FP64 C oracle on this host's cores (rank 0, N=1)
 --impl reference times the CPU reference path (the FP64 C oracle restating
 SuperDCA's solve) on all host cores, on rank 0 only.
@@ -41,6 +47,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 Q = 4
+METRIC = "loci/s at N=3000,L=94k: mixed+batched+warm-start vs plain GPU at <=1e-6 rel obj"
 
 
 def parse():
@@ -60,6 +67,10 @@ def parse():
     ap.add_argument("--warm-start", default=os.path.join(ROOT, "superdca_gb300", "warmstart_tree-3000x94000.npy"),
                     help="learned warm-start parameter blob ('none': zero start)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-form arm")
+    ap.add_argument("--plain-loci", type=int, default=64, help="loci timed in the plain-form arm")
+    ap.add_argument("--accuracy-sample", type=int, default=16,
+                    help="loci of the first timed step checked against the FP64 oracle (0: none)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--cache-dir", default="", help="keep the generated alignment here between runs")
@@ -270,6 +281,25 @@ def cpu_eval_rate(st, seconds, threads, seed=5):
     return t_all * threads / done, done, t_all
 
 
+def oracle_check(st, w, lh, lJ, loci, X, threads):
+    """FP64 oracle objective and max |gradient| at each (locus, parameters)
+    pair, evaluated on `threads` host threads (ctypes releases the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+
+    O.build()
+    P = O.Problem(st, w, lh, lJ)
+
+    def one(k):
+        f, g = P.objective(int(loci[k]), X[k])
+        return f, float(np.abs(g).max())
+
+    with ThreadPoolExecutor(max(1, threads)) as ex:
+        out = list(ex.map(one, range(len(loci))))
+    return np.array([o[0] for o in out]), np.array([o[1] for o in out])
+
+
 def nfeval_reference(workload):
     path = os.path.join(ROOT, "oracle", f"nfeval_{workload}.json")
     with open(path) as fh:
@@ -411,6 +441,56 @@ def engine_arm(args):
                                   "measured": f"one untimed step of {B} loci on a single lane"}
     else:
         rf, dom = roofline(tot, N, L, Dp, 10, 2 if args.history_bf16 else 4)
+    # accuracy: the FP64 oracle's objective and gradient at the parameters
+    # the engine returns, for a seeded sample of the first timed step's loci.
+    # The step is solved again after the timed region (same engine, same
+    # queue of loci, so the slots refill as they did), returning solutions
+    # only at the sampled positions.
+    accuracy, f_step = None, None
+    if rank == 0 and args.accuracy_sample > 0:
+        vloci = loci_for(args.warmup)
+        pos = np.sort(np.random.default_rng(1234).choice(len(vloci), min(args.accuracy_sample, len(vloci)),
+                                                         replace=False))
+        rv = E.solve(vloci, x_positions=pos, want_scores=False)
+        f_step = rv.f
+        lh, lJ, _ = E.lambdas()
+        f_orc, g_orc = oracle_check(st, w, lh, lJ, vloci[pos], rv.x, os.cpu_count() or 1)
+        rel = np.abs(rv.f[pos] - f_orc) / np.abs(f_orc)
+        accuracy = {"n": int(len(pos)), "max_rel_obj_err": float(rel.max()),
+                    "median_rel_obj_err": float(np.median(rel)), "max_oracle_gnorm": float(g_orc.max()),
+                    "gradient_threshold": 1e-3, "status_counts": {str(k): int((rv.status[pos] == k).sum())
+                                                                   for k in sorted(set(rv.status[pos].tolist()))},
+                    "loci": [int(v) for v in vloci[pos]],
+                    "how": ("|f_engine - f_oracle(x_engine)| / f_oracle(x_engine), the FP64 oracle evaluated at "
+                            "the engine's returned parameters; max_oracle_gnorm: the oracle's max|g| there "
+                            "(SuperDCA's stop test is max|g| < 1e-3); sampled from the first timed step's loci, "
+                            "re-solved after the timed region in the same queue")}
+    E.close()
+
+    # the plain GPU form (FP32 gather contractions, FP32 L-BFGS history,
+    # zero start) on the same alignment: the spec ratio's denominator
+    vs_plain = None
+    if rank == 0 and args.form != "gather" and not args.no_plain and args.plain_loci > 0:
+        pB = 64
+        Ep = Engine(N, L, batch=pB, device=local, form=FORM_GATHER, lanes=1)
+        Ep.set_alignment(st, w)
+        ploci = loci_for(args.warmup)[:args.plain_loci]
+        Ep.solve(loci_for(args.warmup + args.steps)[:8], want_scores=True)   # warm-up (other loci)
+        rp = Ep.solve(ploci, want_scores=True)
+        pp = Ep.profile()
+        Ep.close()
+        plain = len(ploci) / (pp["solve_ms"] / 1e3)
+        vs_plain = {"plain_loci_s": round(plain, 4), "ratio": round(value / plain, 2),
+                    "plain_form": "gather (FP32 contractions on the CUDA cores, FP32 L-BFGS history, zero start)",
+                    "plain_batch": pB, "plain_loci": int(len(ploci)),
+                    "plain_median_iterations": float(np.median(rp.iterations)),
+                    "plain_status_counts": {str(k): int((rp.status == k).sum()) for k in sorted(set(rp.status.tolist()))},
+                    "how": ("device time (CUDA events) of one solve of the first timed step's first "
+                            f"{len(ploci)} loci, after a warm-up solve; ratio = value / plain_loci_s")}
+        if f_step is not None:
+            fd = f_step[:len(ploci)]
+            vs_plain["max_rel_f_diff_vs_headline"] = float(np.max(np.abs(rp.f - fd) / np.abs(fd)))
+
     if rf is not None:
         rf["avg_launch_ms"] = round(tot["kernel_ms"][dom] / max(1, tot["kernel_launches"][dom]), 4)
         rf["lanes"] = lanes   # launches of different lanes overlap in time
@@ -420,7 +500,7 @@ def engine_arm(args):
             rf["traffic"] = round(per_unit * units)   # bytes per launch, scaled from a 128-slot capture
             rf["traffic_source"] = "ncu dram bytes of a 128-slot launch, scaled by the units per launch"
     out = {
-        "metric": "loci/s at N=3000,L=94k (per-locus plmDCA solve, gradient threshold 1e-3)",
+        "metric": METRIC,
         "value": round(value, 4), "unit": "loci/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(t_dev * 1e3 / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -436,7 +516,8 @@ def engine_arm(args):
                    "l2": (f"inputs larger than L2 ({N * L / 1e6:.0f} MB alignment; per-slot solver state "
                           f"{B * lanes} slots)"),
                    "parallelism": f"loci sharded over {world} rank(s)"},
-        "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": rf, "reweighting": rw,
+        "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": rf,
+        "accuracy": accuracy, "vs_plain": vs_plain, "reweighting": rw,
         "kernel_ms": {k: round(v, 2) for k, v in tot["kernel_ms"].items()},
         "solver": {"median_nfeval": float(np.median(nfe)), "median_iterations": float(np.median(iters)),
                    "p90_iterations": float(np.percentile(iters, 90)), "max_iterations": int(np.max(iters)),
@@ -447,16 +528,21 @@ def engine_arm(args):
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         spe, n_eval, t_cpu = cpu_eval_rate(st, args.cpu_seconds, threads)
-        nf = float(np.median(nfe))
+        try:
+            nf, meta = nfeval_reference(args.workload)
+            nf_src = (f"median of full FP64 oracle solves of {len(meta['loci'])} loci, "
+                      f"oracle/nfeval_{args.workload}.json, as in --impl reference")
+        except OSError:
+            nf = float(np.median(nfe))
+            nf_src = "median of this run's engine solves (no oracle count for this workload)"
         out["cpu_baseline"] = {
             "value": round(threads / (spe * nf), 6), "unit": "loci/s", "cores": threads,
             "kind": "port",
             "sample": (f"{n_eval} full-size FP64 objective+gradient evaluations ({t_cpu:.1f} s) on "
                        f"{threads} threads, {spe:.3f} s each; loci/s = threads / (s per evaluation x "
-                       f"{nf:.0f} evaluations per locus, SuperDCA counting, median of this run)")}
+                       f"{nf:.0f} evaluations per locus, SuperDCA counting, {nf_src})")}
     if rank == 0:
         print(json.dumps(out), flush=True)
-    E.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 
@@ -485,7 +571,7 @@ def reference_arm(args):
               f"{nf:.0f} evaluations per locus, median of full oracle solves of {len(meta['loci'])} loci, "
               f"oracle/nfeval_{args.workload}.json)")
     out = {
-        "metric": "loci/s at N=3000,L=94k (per-locus plmDCA solve, gradient threshold 1e-3)",
+        "metric": METRIC,
         "value": round(value, 6), "unit": "loci/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(wall * 1e3 / args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",

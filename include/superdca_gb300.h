@@ -159,6 +159,16 @@ int sdca_solve(sdca_handle *h, const uint32_t *loci, size_t n_loci, float *score
 int sdca_solve_ex(sdca_handle *h, const uint32_t *loci, size_t n_loci, const double *x_init,
                   double *x_out, float *scores, sdca_locus_stat *stats);
 
+/* As sdca_solve_ex, with solutions for chosen loci only: x_rows[k] is the
+ * row of x_out (n_rows x D, reference layout) that receives the solution of
+ * loci[k], or -1 for none; rows may repeat only for repeated loci.  x_rows
+ * NULL means row k for every k (sdca_solve_ex).  Lets a caller check or keep
+ * a few solutions of a long loci list (SuperDCA keeps each locus's solution
+ * only for its scoring, plmDCA.hpp:298-394) without n_loci x D doubles of
+ * host memory. */
+int sdca_solve_sel(sdca_handle *h, const uint32_t *loci, size_t n_loci, const double *x_init,
+                   const int64_t *x_rows, double *x_out, float *scores, sdca_locus_stat *stats);
+
 /* One objective evaluation for target locus r at x (reference layout):
  * plmDCA_objective_fval_and_gradient (SuperDCA/include/plmDCA_objective.hpp:
  * 38-249) as reached through value_and_gradient
@@ -221,10 +231,11 @@ const char *sdca_mlp_last_error(void);
 #define SDCA_NOALLOC_MAX_LOCI 262144
 
 /* One objective + gradient evaluation that allocates nothing (no counterpart
- * in SuperDCA; same value as sdca_eval).  For callers that cannot call
- * cudaMalloc -- code running while a CUDA graph is captured, or host programs
- * whose own allocator owns all device memory.  Every pointer is a DEVICE
- * pointer the caller allocated: states (n_seqs x n_loci codes 0..3), weights
+ * in SuperDCA; same value as sdca_eval).  For host programs that own all
+ * device memory through their own allocator (a framework's caching
+ * allocator, an embedded runtime with a fixed memory budget) and do not let
+ * a library call cudaMalloc or cudaFree.  Every pointer is a DEVICE pointer
+ * the caller allocated: states (n_seqs x n_loci codes 0..3), weights
  * (n_seqs), x and g (16 n_loci + 4 doubles, SuperDCA's parameter layout) and
  * f (one double).  lambda_h and lambda_J are absolute strengths (as
  * sdca_get_lambdas reports them).  Work is queued on `stream` (a cudaStream_t
@@ -233,8 +244,12 @@ const char *sdca_mlp_last_error(void);
  * (about 2.1 MB, held by every GPU that loads the library until exit), so
  * n_seqs <= SDCA_NOALLOC_MAX_SEQS and n_loci <= SDCA_NOALLOC_MAX_LOCI, else
  * SDCA_E_ARG before any work is queued.  All calls share that array: calls
- * whose work overlaps on the GPU race.  The first call on a device looks up
- * the array's address on that device; make it before any stream capture. */
+ * whose work overlaps on the GPU race.  The first call made with a CUDA
+ * context current looks up the array's address in that context.  The states
+ * are not read on the host, so a code >= 4 cannot be refused here as
+ * sdca_set_alignment refuses it: it makes *f and the h part of g NaN.  An
+ * error already pending in the CUDA runtime when the call starts is left in
+ * place for the caller and reported as SDCA_E_CUDA, with nothing queued. */
 int sdca_eval_noalloc(const uint8_t *states, int64_t n_seqs, int64_t n_loci,
                       const double *weights, double lambda_h, double lambda_J, uint32_t r,
                       const double *x, double *f, double *g, void *stream);

@@ -30,7 +30,7 @@ KERNEL_CLASSES = ["forward", "backward", "linesearch", "history", "direction", "
 
 # every entry point include/superdca_gb300.h declares
 EXPORTS = ["sdca_abi_version", "sdca_config_default", "sdca_create", "sdca_set_alignment",
-           "sdca_compute_weights", "sdca_get_lambdas", "sdca_solve", "sdca_solve_ex", "sdca_eval",
+           "sdca_compute_weights", "sdca_get_lambdas", "sdca_solve", "sdca_solve_ex", "sdca_solve_sel", "sdca_eval",
            "sdca_get_profile", "sdca_last_error", "sdca_destroy", "sdca_eval_noalloc",
            "sdca_set_warm_start", "sdca_ws_features", "sdca_mlp_blob_size", "sdca_mlp_grad",
            "sdca_mlp_predict", "sdca_mlp_train", "sdca_mlp_last_error", "sdca_set_targets"]
@@ -80,6 +80,7 @@ def load(path: str = LIB_PATH):
     L.sdca_get_lambdas.argtypes = [vp, C.POINTER(dp), C.POINTER(dp), C.POINTER(dp)]
     L.sdca_solve.argtypes = [vp, vp, C.c_size_t, vp, vp]
     L.sdca_solve_ex.argtypes = [vp, vp, C.c_size_t, vp, vp, vp, vp]
+    L.sdca_solve_sel.argtypes = [vp, vp, C.c_size_t, vp, vp, vp, vp, vp]
     L.sdca_eval.argtypes = [vp, C.c_uint32, vp, C.POINTER(dp), vp]
     L.sdca_get_profile.argtypes = [vp, C.POINTER(Profile)]
     L.sdca_last_error.restype = C.c_char_p

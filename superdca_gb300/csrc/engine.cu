@@ -702,6 +702,7 @@ struct Queue {
     std::atomic<bool> *abort = nullptr;    // a lane failed: take no further loci
     const double *x_init = nullptr;
     double *x_out = nullptr;
+    const int64_t *x_rows = nullptr;       // row of x_out per list position (-1: none); null: row k
     float *scores = nullptr;
     sdca_locus_stat *stats = nullptr;
     std::vector<float> xbuf;
@@ -771,11 +772,12 @@ int retire(sdca_handle *h, Queue &Qu, const std::vector<int32_t> &done)
     for (size_t j = 0; j < done.size(); ++j) {
         const int b = done[j];
         SlotHost &S = h->slots[b];
-        if (Qu.x_out) {
+        const int64_t row = Qu.x_rows ? Qu.x_rows[S.k] : S.k;
+        if (Qu.x_out && row >= 0) {
             CK(cudaMemcpyAsync(xe.data(), h->wa + (int64_t)b * P.Dp, sizeof(float) * P.Dp,
                                cudaMemcpyDeviceToHost, h->stream));
             { const int r_ = stream_sync(h); if (r_) return r_; }
-            engine_to_ref(P, xe.data(), Qu.x_out + S.k * (QQ * P.L + Q));
+            engine_to_ref(P, xe.data(), Qu.x_out + row * (QQ * P.L + Q));
             h->prof.d2h_bytes += (int64_t)sizeof(float) * P.Dp;
         }
     }
@@ -2059,8 +2061,8 @@ int sdca_get_lambdas(const sdca_handle *h, double *lambda_h, double *lambda_J, d
     return SDCA_OK;
 }
 
-int sdca_solve_ex(sdca_handle *h, const uint32_t *loci, size_t n_loci, const double *x_init,
-                  double *x_out, float *scores, sdca_locus_stat *stats)
+int sdca_solve_sel(sdca_handle *h, const uint32_t *loci, size_t n_loci, const double *x_init,
+                   const int64_t *x_rows, double *x_out, float *scores, sdca_locus_stat *stats)
 {
     int rc = check_ready(h);
     if (rc) return rc;
@@ -2068,6 +2070,10 @@ int sdca_solve_ex(sdca_handle *h, const uint32_t *loci, size_t n_loci, const dou
     const int64_t nt = h->scan ? h->LT : h->P.L;   // scan mode: loci are target columns
     for (size_t k = 0; k < n_loci; ++k)
         if ((int64_t)loci[k] >= nt) return fail(h, SDCA_E_ARG, "locus index out of range");
+    if (x_rows && !x_out) return fail(h, SDCA_E_ARG, "x_rows given without x_out");
+    if (x_rows)
+        for (size_t k = 0; k < n_loci; ++k)
+            if (x_rows[k] < -1) return fail(h, SDCA_E_ARG, "x_rows entries must be -1 or a row index");
     std::atomic<size_t> next{0};
     std::atomic<bool> abort{false};
     auto queue_for = [&](sdca_handle *l, Queue &Qu) {
@@ -2077,6 +2083,7 @@ int sdca_solve_ex(sdca_handle *h, const uint32_t *loci, size_t n_loci, const dou
         Qu.abort = &abort;
         Qu.x_init = x_init;
         Qu.x_out = x_out;
+        Qu.x_rows = x_rows;
         Qu.scores = scores;
         Qu.stats = stats;
         if (x_init) Qu.xbuf.resize(l->P.Dp);
@@ -2127,6 +2134,12 @@ int sdca_solve_ex(sdca_handle *h, const uint32_t *loci, size_t n_loci, const dou
         p.d2h_bytes += q.d2h_bytes;
     }
     return SDCA_OK;
+}
+
+int sdca_solve_ex(sdca_handle *h, const uint32_t *loci, size_t n_loci, const double *x_init,
+                  double *x_out, float *scores, sdca_locus_stat *stats)
+{
+    return sdca_solve_sel(h, loci, n_loci, x_init, nullptr, x_out, scores, stats);
 }
 
 int sdca_solve(sdca_handle *h, const uint32_t *loci, size_t n_loci, float *scores,

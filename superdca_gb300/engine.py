@@ -119,15 +119,26 @@ class Engine:
         self._check(self.lib.sdca_get_lambdas(self.h, C.byref(lh), C.byref(lJ), C.byref(be)))
         return lh.value, lJ.value, be.value
 
-    def solve(self, loci, x_init=None, want_x=False, want_scores=True) -> SolveResult:
+    def solve(self, loci, x_init=None, want_x=False, want_scores=True, x_positions=None) -> SolveResult:
+        """Solve the listed target loci.  want_x: the solution of every locus
+        (n x D doubles); x_positions: solutions of the loci at these list
+        positions only (result.x row j belongs to loci[x_positions[j]])."""
         loci = np.ascontiguousarray(loci, dtype=np.uint32)
         n = len(loci)
         scores = np.zeros((n, self.L), dtype=np.float32) if want_scores else None
         stats = (_lib.LocusStat * max(n, 1))()
-        xo = np.zeros((n, self.D), dtype=np.float64) if want_x else None
         xi = None if x_init is None else np.ascontiguousarray(x_init, dtype=np.float64)
-        self._check(self.lib.sdca_solve_ex(self.h, _ptr(loci), n, _ptr(xi), _ptr(xo), _ptr(scores),
-                                           C.cast(stats, C.c_void_p)))
+        if x_positions is not None:
+            pos = np.asarray(x_positions, dtype=np.int64)
+            rows = np.full(n, -1, dtype=np.int64)
+            rows[pos] = np.arange(len(pos))
+            xo = np.zeros((len(pos), self.D), dtype=np.float64)
+            self._check(self.lib.sdca_solve_sel(self.h, _ptr(loci), n, _ptr(xi), _ptr(rows), _ptr(xo),
+                                                _ptr(scores), C.cast(stats, C.c_void_p)))
+        else:
+            xo = np.zeros((n, self.D), dtype=np.float64) if want_x else None
+            self._check(self.lib.sdca_solve_ex(self.h, _ptr(loci), n, _ptr(xi), _ptr(xo), _ptr(scores),
+                                               C.cast(stats, C.c_void_p)))
         st = stats[:n]
         return SolveResult(
             scores=scores,

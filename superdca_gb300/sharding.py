@@ -52,11 +52,18 @@ def solve_sharded(solve_rows, loci, L: int, group=None, rows_per_message: int = 
         if have:
             buf[:have] = torch.from_numpy(local[m0:m0 + have])
         buf = buf.to(dev)
-        gathered = [torch.empty_like(buf) for _ in range(world)]
-        dist.all_gather(gathered, buf, group=group)
+        # only rank 0 keeps rows: point-to-point sends to it (works on gloo
+        # and NCCL alike), so no other rank receives anyone's rows
         if rank == 0:
             for k, p in enumerate(parts):
+                if k == 0:
+                    got = buf
+                else:
+                    got = torch.empty_like(buf)
+                    dist.recv(got, src=dist.get_global_rank(group, k) if group is not None else k, group=group)
                 n_k = max(0, min(m, (p.stop - p.start) - m0))
                 if n_k:
-                    out[p.start + m0:p.start + m0 + n_k] = gathered[k][:n_k].cpu().numpy()
+                    out[p.start + m0:p.start + m0 + n_k] = got[:n_k].cpu().numpy()
+        else:
+            dist.send(buf, dst=dist.get_global_rank(group, 0) if group is not None else 0, group=group)
     return out
