@@ -85,18 +85,10 @@ struct SlotHost {
     double xmax = 0.0;       // bound on max|x| (sets the fp16 scale of a refresh)
     double dmax = 0.0;       // max|d| of the current direction
     double f_fresh = 0.0;    // pseudo-likelihood part of f at recomputed logits
-    // dual form: h parts of x, d, the two gradients and the history pairs
-    // (their J parts live on the device as coefficient pairs)
-    double eta_x[Q] = {0, 0, 0, 0}, eta_d[Q] = {0, 0, 0, 0};
-    double eta_g[2][Q] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
-    double eta_s[MAXHIST + 1][Q] = {}, eta_y[MAXHIST + 1][Q] = {};
-    double chk_ratio = 0.0;  // max|g| / ||g|| at the last exact max-norm check (0: none yet)
-    int last_check = -1000;  // iteration of that check
-    int chk_wait = 0;        // iterations a wanted check has been deferred
-    double amax_g = 0.0, amax_x = 0.0;  // max |a| of the gradient and of x
-    double f0d = 0.0, dg0d = 0.0;       // data parts of f and of the slope at the current point (step trials)
-    double sg_prev[MAXHIST + 1] = {}, yg_prev[MAXHIST + 1] = {};  // s_j.g, y_j.g of the last gradient, by ring position
-    double sy_new = 0.0, yy_new = 0.0;  // s.y and y.y of the newest pair
+    // dual form: from the device's summary of the slot (its solver state
+    // lives on the device): h part of x, max |a| of the gradient and of x
+    double eta_x[Q] = {0, 0, 0, 0};
+    double amax_g = 0.0, amax_x = 0.0;
     MoreThuente ls;
 };
 
@@ -163,6 +155,12 @@ struct sdca_handle {
     float *Rchk = nullptr, *P0 = nullptr;   // P0: probabilities at the current point, base of the step trials
     float *ud = nullptr;                    // u_a - u_y per sequence (single precision, step trials)
     double qscale = 1.0;
+    DualCtl *ctl = nullptr;        // per-slot solver state, owned by the device while a slot iterates
+    DualSum *sum = nullptr, *sum_h = nullptr;   // per-slot summary the host reads after each round
+    double *dacc = nullptr;        // direction sums for the next line search
+    int32_t *dlist = nullptr;      // the round's slot lists: [evaluations | searching | gradient pass]
+    cudaEvent_t ev_round = nullptr;   // end of a round's control kernel
+    std::vector<int64_t> rows_pending;   // list positions whose score rows are on their way to rows_h
     KdPlan *kd = nullptr;          // exact K rho on the tensor cores (N <= 4000), else CUDA cores
     __half *Kd = nullptr, *Rd = nullptr;
 
@@ -321,7 +319,9 @@ void free_all(sdca_handle *h)
     if (h->rows_h) cudaFreeHost(h->rows_h);
     if (h->flag_h) cudaFreeHost(h->flag_h);
     if (h->stage) cudaFreeHost(h->stage);
+    if (h->sum_h) cudaFreeHost(h->sum_h);
     h->stage = nullptr;
+    h->sum_h = nullptr;
     h->sd_h = nullptr; h->list_h = nullptr; h->acc_h = nullptr; h->dots_h = nullptr;
     h->rows_h = nullptr; h->flag_h = nullptr;
     h->X = h->XT = h->rstate = nullptr;
@@ -500,6 +500,8 @@ int run_forward(sdca_handle *h, const std::vector<int32_t> &lst, const float *ve
 }
 
 // begin a locus in slot b: zero or given start point, logits at the start point
+int dual_ctl_begin(sdca_handle *h, int b);
+
 int slot_begin(sdca_handle *h, int b, int64_t k, int32_t locus, const float *x0_engine)
 {
     SlotHost &S = h->slots[b];
@@ -525,6 +527,8 @@ int slot_begin(sdca_handle *h, int b, int64_t k, int32_t locus, const float *x0_
         const size_t NV = DV_S + 2 * (size_t)P.ring;
         CK(cudaMemsetAsync(h->dv + (size_t)b * NV * 2 * P.Nx * 4, 0, sizeof(double) * NV * 2 * P.Nx * 4, h->stream));
         CK(cudaMemsetAsync(h->udf + (size_t)b * P.Nx * 4, 0, sizeof(float2) * P.Nx * 4, h->stream));
+        const int rc = dual_ctl_begin(h, b);
+        if (rc) return rc;
     }
     S.stp = 0.0;
     S.use_u = false;
@@ -834,27 +838,7 @@ int phase_trials(sdca_handle *h, Queue &Qu)
         if (rc) return rc;
         rc = zero_acc(h);
         if (rc) return rc;
-        if (h->form == SDCA_FORM_DUAL) {
-            // step trials as changes from the current point; start and final
-            // evaluations in FP64 from the logits
-            std::vector<int32_t> delta, full;
-            for (int b : lst) {
-                const int ph = h->slots[b].phase;
-                (ph == PH_LS || ph == PH_FINAL_EVAL ? delta : full).push_back(b);
-            }
-            if (!delta.empty()) {
-                if ((rc = upload_list(h, delta))) return rc;
-                Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)delta.size());
-                launch_trial_delta(P, h->sd, h->list, (int)delta.size(), lbase_df(h), h->udf, h->ud, h->rstate, h->wf,
-                                   h->P0, h->R, h->acc, h->stream);
-            }
-            if (!full.empty()) {
-                if ((rc = upload_list(h, full))) return rc;
-                Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)full.size());
-                launch_trial_dual(P, h->sd, h->list, (int)full.size(), lbase_df(h), h->udf, h->rstate, h->w, h->R, h->acc,
-                               h->stream);
-            }
-        } else {
+        {
             Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)lst.size());
             launch_trial(P, h->sd, h->list, (int)lst.size(), h->lbase, h->u, h->rstate, h->w, h->R, h->acc,
                          h->stream);
@@ -877,12 +861,11 @@ int phase_trials(sdca_handle *h, Queue &Qu)
                 S.f_final = fdata + P.lambda_J * S.x2J + P.lambda_h * S.x2H;
                 done.push_back(b);
             } else if (S.phase == PH_FINAL_EVAL) {
-                S.f = (h->form == SDCA_FORM_DUAL ? S.f0d + fdata : fdata) + l2_along(P, S, S.stp);
+                S.f = fdata + l2_along(P, S, S.stp);
                 S.phase = PH_READY_STEP;
             } else {  // PH_LS
-                const bool dl = h->form == SDCA_FORM_DUAL;   // trial sums are changes from the current point
-                const double f = (dl ? S.f0d + fdata : fdata) + l2_along(P, S, S.stp);
-                const double dg = (dl ? S.dg0d : 0.0) + acc_get(h, b, ACC_DG) + dl2_along(P, S, S.stp);
+                const double f = fdata + l2_along(P, S, S.stp);
+                const double dg = acc_get(h, b, ACC_DG) + dl2_along(P, S, S.stp);
                 S.trials++;
                 if (!std::isfinite(f) || !std::isfinite(dg)) {
                     S.f = f;
@@ -1284,12 +1267,27 @@ int phase_step(sdca_handle *h)
     return SDCA_OK;
 }
 
-// ---- dual form, phase B: accept, gradient through K rho, tests (the
-// max-norm test exactly, on the tensor cores, when the norm says it may
-// pass), history dots, direction.  The host logic is phase_step's; the
-// h parts of all vectors (eta) are kept here.
+// ---- dual form: device-driven rounds.  The L-BFGS iteration of every slot
+// runs on the device (k_dual_linesearch: restart test, More-Thuente search
+// and its trials; k_dual_accept; the gradient through K rho; k_dual_control:
+// history, tests and the next direction's coefficients; k_dual_direction).
+// The host, once per round, reads a summary of every slot (one stream
+// event, taken before the direction kernel so that the host's work overlaps
+// it), batches the exact max-norm checks, forms the solutions of stopped
+// slots, retires finished loci and admits new ones.
 
 double dot4h(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3]; }
+
+// A new locus in slot b: the device state of its solver.
+int dual_ctl_begin(sdca_handle *h, int b)
+{
+    DualCtl c;
+    std::memset(&c, 0, sizeof(c));
+    c.phase = DC_EVAL0;
+    c.ring_new = -1;
+    c.last_check = -1000;
+    return staged_h2d(h, h->ctl + b, &c, sizeof(c));
+}
 
 // Stopped slots of the dual form: x in the engine layout (J = Phi^T a_x,
 // J_rr = 0, h = eta_x), then the final evaluation.  J is formed exactly:
@@ -1310,9 +1308,9 @@ int dual_convert(sdca_handle *h, bool force)
     }
     if (fin.empty() || (!force && active > 0 && (int)fin.size() < std::min(16, P.Bmax))) return SDCA_OK;
     for (int b : fin) {
-        const double am = h->slots[b].amax_x;
-        h->sd_h[b].tc_scale = am > 0.0 ? std::ldexp(1.0, 32) / am : 1.0;
-        for (int a = 0; a < Q; ++a) h->sd_h[b].eta[a] = h->slots[b].eta_x[a];
+        const SlotHost &S = h->slots[b];
+        h->sd_h[b].tc_scale = S.amax_x > 0.0 ? std::ldexp(1.0, 32) / S.amax_x : 1.0;
+        for (int a = 0; a < Q; ++a) h->sd_h[b].eta[a] = S.eta_x[a];
     }
     int rc = upload_slots(h, fin);
     if (rc) return rc;
@@ -1336,183 +1334,217 @@ int dual_convert(sdca_handle *h, bool force)
     return SDCA_OK;
 }
 
-int phase_step_dual(sdca_handle *h)
+// Score rows of retired slots travel to the host without a wait: copied into
+// the caller's array after the next round's event (or at the end).
+int dual_flush_rows(sdca_handle *h, Queue &Qu)
 {
     const Problem &P = h->P;
-    const int m = P.m;
-    const double gtol = h->cfg.gradient_threshold;
-    std::vector<int32_t> all, steps;
-    for (int b = 0; b < P.Bmax; ++b) {
-        SlotHost &S = h->slots[b];
-        if (S.phase == PH_READY_STEP) {
-            steps.push_back(b);
-            all.push_back(b);
-            S.push = true;
-            int pos = 0;
-            while (std::find(S.hist.begin(), S.hist.end(), pos) != S.hist.end()) ++pos;
-            S.ring_new = pos;
-        } else if (S.phase == PH_READY_INIT) {
-            all.push_back(b);
-            S.push = false;
-            S.ring_new = -1;
-        }
-    }
-    if (all.empty()) return dual_convert(h, true);
-    int rc;
-    if (!steps.empty()) {
-        if ((rc = upload_slots(h, steps))) return rc;
+    for (size_t j = 0; j < h->rows_pending.size(); ++j)
+        std::memcpy(Qu.scores + h->rows_pending[j] * P.L, h->rows_h + j * P.L, sizeof(float) * P.L);
+    h->rows_pending.clear();
+    return SDCA_OK;
+}
+
+int dual_retire(sdca_handle *h, Queue &Qu, const std::vector<int32_t> &done)
+{
+    if (done.empty()) return SDCA_OK;
+    const Problem &P = h->P;
+    int rc = upload_slots(h, done);
+    if (rc) return rc;
+    if (Qu.scores) {
         {
-            Timed t(h, SDCA_K_ACCEPT, 1, (int64_t)steps.size());
-            launch_dual_accept(P, h->sd, h->list, (int)steps.size(), h->dv, h->udf, lbase_df(h), h->stream);
+            Timed t(h, SDCA_K_SCORE, 1, (int64_t)done.size());
+            launch_score(P, h->sd, h->list, (int)done.size(), h->wa, h->cfg.gap_state, h->rows, h->stream);
         }
         CKL();
-        for (int b : steps) {
-            SlotHost &S = h->slots[b];
-            for (int a = 0; a < Q; ++a) {
-                const double xn = S.eta_x[a] + S.stp * S.eta_d[a];
-                if (S.ring_new >= 0) S.eta_s[S.ring_new][a] = xn - S.eta_x[a];
-                S.eta_x[a] = xn;
-            }
-        }
+        CK(cudaMemcpyAsync(h->rows_h, h->rows, sizeof(float) * P.L * done.size(), cudaMemcpyDeviceToHost,
+                           h->stream));
+        h->prof.d2h_bytes += (int64_t)sizeof(float) * P.L * done.size();
+        for (int b : done) h->rows_pending.push_back(h->slots[b].k);
     }
-    // gradient at the accepted points, and its dots with every live history
-    // position (the history and the pair just pushed) in the same round trip
-    if ((rc = upload_slots(h, all))) return rc;
-    for (int b : all) {
+    std::vector<float> xe;
+    for (int b : done) {
         SlotHost &S = h->slots[b];
-        SlotDev &D = h->sd_h[b];
-        int k = 0;
-        for (int p : S.hist) D.ring[k++] = p;
-        if (S.push && S.ring_new >= 0) D.ring[k++] = S.ring_new;
-        D.nhist = k;
+        const int64_t row = Qu.x_rows ? Qu.x_rows[S.k] : S.k;
+        if (Qu.x_out && row >= 0) {
+            if (xe.empty()) xe.resize(P.Dp);
+            CK(cudaMemcpyAsync(xe.data(), h->wa + (int64_t)b * P.Dp, sizeof(float) * P.Dp, cudaMemcpyDeviceToHost,
+                               h->stream));
+            { const int r_ = stream_sync(h); if (r_) return r_; }
+            engine_to_ref(P, xe.data(), Qu.x_out + row * (QQ * P.L + Q));
+            h->prof.d2h_bytes += (int64_t)sizeof(float) * P.Dp;
+        }
+        if (Qu.stats) {
+            sdca_locus_stat &st = Qu.stats[S.k];
+            st.f = S.f_final;
+            st.gnorm = S.gmax;
+            st.iterations = S.iterations;
+            st.nfeval = (int32_t)S.nfeval;
+            st.contractions = S.iterations + 1;
+            st.status = S.status;
+            st.restarts = S.restarts;
+            st.skipped_pairs = S.skipped;
+            st.weak_searches = S.weak;
+            st.max_trials = S.max_trials;
+        }
+        h->prof.iterations += S.iterations;
+        h->prof.contractions += S.iterations + 1;
+        S.phase = PH_EMPTY;
     }
-    if ((rc = staged_h2d(h, h->sd, h->sd_h, sizeof(SlotDev) * P.Bmax))) return rc;
-    CK(cudaMemsetAsync(h->csum, 0, sizeof(long long) * 16 * P.Bmax, h->stream));
-    CK(cudaMemsetAsync(h->amax, 0, sizeof(double) * 2 * P.Bmax, h->stream));
-    CK(cudaMemsetAsync(h->dots, 0, sizeof(double) * 4 * MAXHIST * P.Bmax, h->stream));
-    if ((rc = zero_acc(h))) return rc;
-    // Profile classes of this form: "forward" is K rho (a coefficient
-    // vector's logit image, as X d is in the other forms), "backward" the
-    // one-hot contractions X^T a (max-norm checks, final J), "accept" the
-    // iterate update and gradient assembly.
-    {
-        Timed t(h, SDCA_K_ACCEPT, 1, (int64_t)all.size());
-        launch_dual_quant(P, h->sd, h->list, (int)all.size(), h->R, h->rstate, h->qscale, h->rq, h->csum, h->stream);
+    return SDCA_OK;
+}
+
+void dual_take_summary(SlotHost &S, const DualSum &D)
+{
+    S.status = D.status;
+    S.iterations = D.iterations;
+    S.nfeval = D.nfeval;
+    S.restarts = D.restarts;
+    S.skipped = D.skipped;
+    S.weak = D.weak;
+    S.max_trials = D.max_trials;
+    S.f = D.f;
+    S.gmax = D.gmax;
+    S.amax_g = D.amax_g;
+    S.amax_x = D.amax_x;
+    S.x2J = D.x2J;
+    for (int a = 0; a < Q; ++a) S.eta_x[a] = D.eta_x[a];
+}
+
+// One round: start/final evaluations, line searches, accepts, the gradient
+// pass and the control kernel for every slot, then the directions.
+int dual_round(sdca_handle *h, Queue &Qu)
+{
+    const Problem &P = h->P;
+    const double gtol = h->cfg.gradient_threshold;
+    std::vector<int32_t> ef, T, G;
+    for (int b = 0; b < P.Bmax; ++b) {
+        const int ph = h->slots[b].phase;
+        if (ph == PH_INIT || ph == PH_FINALIZE) ef.push_back(b);
+        if (ph == PH_LS) T.push_back(b);   // iterating on the device
     }
+    G = T;
+    for (int b : ef)
+        if (h->slots[b].phase == PH_INIT) G.push_back(b);
+    if (ef.empty() && G.empty()) return dual_convert(h, true);
+    // the lists: [ef | T | G] in one upload
+    const int32_t *l_ef = h->dlist, *l_T = h->dlist + P.Bmax, *l_G = h->dlist + 2 * P.Bmax;
     {
-        Timed t(h, SDCA_K_FORWARD, h->kd ? 2 : 1, (int64_t)all.size());
-        if (h->kd)
-            CK(tc_launch_kdig(h->kd, P, h->list, (int)all.size(), h->rq, h->rstate, h->csum, 1.0 / h->qscale, h->Rd,
-                              h->KR, h->tc_err, h->stream));
-        else
-            launch_dual_kprod(P, h->list, (int)all.size(), h->rstate, h->Kmat, h->qscale, h->rq, h->csum, h->KR,
-                              h->stream);
+        std::vector<int32_t> all(3 * (size_t)P.Bmax, 0);
+        std::copy(ef.begin(), ef.end(), all.begin());
+        std::copy(T.begin(), T.end(), all.begin() + P.Bmax);
+        std::copy(G.begin(), G.end(), all.begin() + 2 * P.Bmax);
+        for (int b : ef) {
+            h->sd_h[b].locus = h->scan ? -1 : h->slots[b].locus;
+            h->sd_h[b].gcur = 0;
+            h->sd_h[b].stp = 0.0;
+            h->sd_h[b].flags = 0;
+        }
+        int rc = staged_h2d(h, h->sd, h->sd_h, sizeof(SlotDev) * P.Bmax);
+        if (rc) return rc;
+        if ((rc = staged_h2d(h, h->dlist, all.data(), sizeof(int32_t) * all.size()))) return rc;
     }
-    {
-        Timed t(h, SDCA_K_ACCEPT, 1, (int64_t)all.size());
-        launch_dual_grad(P, h->sd, h->list, (int)all.size(), h->qscale, h->rq, h->KR, h->dv, h->acc, h->amax,
-                         h->stream);
+    int rc = zero_acc(h);
+    if (rc) return rc;
+    if (!ef.empty()) {
+        Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)ef.size());
+        launch_trial_dual(P, h->sd, l_ef, (int)ef.size(), lbase_df(h), h->udf, h->rstate, h->w, h->R, h->acc,
+                          h->stream);
     }
-    {
-        Timed t(h, SDCA_K_HISTORY, 1, (int64_t)all.size());
-        launch_dual_dots(P, h->sd, h->list, (int)all.size(), 1, h->dv, h->dots, h->stream);
+    if (!T.empty()) {
+        {
+            Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)T.size());
+            launch_dual_linesearch(P, h->ctl, l_T, (int)T.size(), h->dacc, h->dv, lbase_df(h), h->udf, h->ud,
+                                   h->rstate, h->wf, h->P0, h->R, h->acc, h->stream);
+        }
+        Timed t(h, SDCA_K_ACCEPT, 1, (int64_t)T.size());
+        launch_dual_accept(P, h->ctl, l_T, (int)T.size(), h->dv, h->udf, lbase_df(h), h->stream);
     }
     CKL();
-    const double *amax = h->amax_h;
-    CK(cudaMemcpyAsync(h->amax_h, h->amax, sizeof(double) * 2 * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(h->dots_h, h->dots, sizeof(double) * 4 * MAXHIST * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
-    if ((rc = fetch_acc(h))) return rc;
+    const int nG = (int)G.size();
+    if (nG > 0) {
+        CK(cudaMemsetAsync(h->csum, 0, sizeof(long long) * 16 * P.Bmax, h->stream));
+        CK(cudaMemsetAsync(h->amax, 0, sizeof(double) * 2 * P.Bmax, h->stream));
+        CK(cudaMemsetAsync(h->dots, 0, sizeof(double) * 4 * MAXHIST * P.Bmax, h->stream));
+        // Profile classes of this form: "forward" is K rho (a coefficient
+        // vector's logit image, as X d is in the other forms), "backward" the
+        // one-hot contractions X^T a (max-norm checks, final J), "accept" the
+        // iterate update and gradient assembly, "other" the control kernel.
+        {
+            Timed t(h, SDCA_K_ACCEPT, 1, nG);
+            launch_dual_quant(P, h->sd, l_G, nG, h->R, h->rstate, h->qscale, h->rq, h->csum, h->stream);
+        }
+        {
+            Timed t(h, SDCA_K_FORWARD, h->kd ? 2 : 1, nG);
+            if (h->kd)
+                CK(tc_launch_kdig(h->kd, P, l_G, nG, h->rq, h->rstate, h->csum, 1.0 / h->qscale, h->Rd, h->KR,
+                                  h->tc_err, h->stream));
+            else
+                launch_dual_kprod(P, l_G, nG, h->rstate, h->Kmat, h->qscale, h->rq, h->csum, h->KR, h->stream);
+        }
+        {
+            Timed t(h, SDCA_K_ACCEPT, 1, nG);
+            launch_dual_grad(P, h->ctl, l_G, nG, h->qscale, h->rq, h->KR, h->dv, h->acc, h->amax, h->stream);
+        }
+        {
+            Timed t(h, SDCA_K_HISTORY, 1, nG);
+            launch_dual_dots(P, h->ctl, l_G, nG, 1, h->dv, h->dots, h->stream);
+        }
+        {
+            Timed t(h, SDCA_K_OTHER, 1, nG);
+            launch_dual_control(P, h->ctl, h->sum, l_G, nG, h->cfg.max_iterations, gtol, h->acc, h->amax, h->dots,
+                                h->stream);
+        }
+        CKL();
+    }
+    CK(cudaMemcpyAsync(h->sum_h, h->sum, sizeof(DualSum) * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(h->acc_h, h->acc, sizeof(double) * NACC * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
+    if (h->tc_err) CK(cudaMemcpyAsync(h->flag_h + 1, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaEventRecord(h->ev_round, h->stream));
+    if (nG > 0) {
+        CK(cudaMemsetAsync(h->dacc, 0, sizeof(double) * NDACC * P.Bmax, h->stream));
+        Timed t(h, SDCA_K_DIRECTION, 1, nG);
+        launch_dual_direction(P, h->ctl, l_G, nG, h->dv, lbase_df(h), h->P0, h->wf, h->rstate, h->udf, h->ud,
+                              h->dacc, h->stream);
+    }
+    CKL();
+    CK(cudaEventSynchronize(h->ev_round));
+    // every staged host-to-device copy was queued before the event
+    h->stage_off = 0;
+    if (h->tc_err && h->flag_h[1])
+        return fail(h, SDCA_E_CUDA, "tensor-core pipeline wait timed out (kernel abandoned its tile)");
+    if (Qu.scores) dual_flush_rows(h, Qu);
 
-    std::vector<int32_t> cont, fin, chk;
-    std::vector<char> stop(P.Bmax, 0), releps_stop(P.Bmax, 0);
-    for (int b : all) {
+    std::vector<int32_t> done, chk;
+    for (int b : ef) {
         SlotHost &S = h->slots[b];
-        S.contractions++;
-        const int gn = 1 - S.gcur;
-        double eg[Q];
-        for (int a = 0; a < Q; ++a) eg[a] = S.rs[a] + 2.0 * P.lambda_h * S.eta_x[a];
-        const bool pushed = S.push && S.ring_new >= 0;
-        if (pushed)
-            for (int a = 0; a < Q; ++a) S.eta_y[S.ring_new][a] = eg[a] - S.eta_g[S.gcur][a];
-        for (int a = 0; a < Q; ++a) S.eta_g[gn][a] = eg[a];
-        S.gcur = gn;
-        S.g2 = acc_get(h, b, ACC_G2) + dot4h(eg, eg);
-        S.x2J = acc_get(h, b, ACC_X2J);
-        S.x2H = dot4h(S.eta_x, S.eta_x);
-        S.amax_g = amax[2 * b];
-        S.amax_x = amax[2 * b + 1];
-        const double gnorm = std::sqrt(std::max(S.g2, 0.0));
-        S.gmax = S.chk_ratio > 0.0 ? S.chk_ratio * gnorm : gnorm;   // estimate until checked
-        bool st = false;
-        if (S.phase == PH_READY_INIT) {
-            S.f += P.lambda_J * S.x2J + P.lambda_h * S.x2H;
-            S.nfeval = 1;
-        } else {
-            S.iterations++;
-            S.nfeval += 2 + S.trials;
-            const double *es = S.eta_s[S.ring_new >= 0 ? S.ring_new : 0];
-            const double *ey = S.eta_y[S.ring_new >= 0 ? S.ring_new : 0];
-            const double sy = acc_get(h, b, ACC_SY) + (pushed ? dot4h(es, ey) : 0.0);
-            const double yy = acc_get(h, b, ACC_YY) + (pushed ? dot4h(ey, ey) : 0.0);
-            const double ss = acc_get(h, b, ACC_SS) + (pushed ? dot4h(es, es) : 0.0);
-            if (pushed && sy > 1e-3 * std::sqrt(ss * yy) && yy > 0.0 && std::isfinite(sy) && std::isfinite(yy)) {
-                if ((int)S.hist.size() == m) S.hist.pop_front();
-                S.hist.push_back(S.ring_new);
-                S.gamma = sy / yy;
-                S.sy_new = sy;
-                S.yy_new = yy;
-                S.iter++;
-            } else {
-                S.ring_new = -1;
-                S.skipped++;
-            }
-            if (S.iterations > h->cfg.max_iterations) {
-                S.status = 1;
-                st = true;
-            } else if (S.stalled) {
-                S.status = 2;
-                st = true;
-            }
-        }
-        if (!std::isfinite(S.f) || !std::isfinite(S.g2)) {
-            S.status = -1;
-            st = true;
-        }
-        if (st) {
-            stop[b] = 1;
+        if (S.phase != PH_FINALIZE) continue;
+        S.f_final = acc_get(h, b, ACC_F) + P.lambda_J * S.x2J + P.lambda_h * dot4h(S.eta_x, S.eta_x);
+        done.push_back(b);
+    }
+    for (int b : G) {
+        SlotHost &S = h->slots[b];
+        const DualSum &D = h->sum_h[b];
+        dual_take_summary(S, D);
+        if (D.phase == DC_STOP) {
+            S.phase = PH_CONVERT;
             continue;
         }
-        // the relative-norm stop, decided after the max-norm test as in the
-        // other forms (status 0 when both hold)
-        const double releps = 1e-4 * std::max(1.0, std::sqrt(S.x2J + S.x2H));
-        releps_stop[b] = gnorm < releps;
-        // the max-norm test needs J = Phi^T a_g: run it when the last check's
-        // ratio max|g| / ||g|| predicts a pass, and every 15 iterations (a
-        // check costs about three iterations of the slot)
-        // (before the first check the max-norm is far above the threshold
-        // while ||g|| > 150 threshold on the workloads measured: ratio ~0.01)
-        const bool due = S.iterations - S.last_check >= 15 && (S.chk_ratio > 0.0 || gnorm < 150.0 * gtol);
-        const bool near = S.chk_ratio > 0.0 && S.chk_ratio * gnorm < 1.1 * gtol;
-        if (due || near || gnorm < gtol || releps_stop[b]) {
-            chk.push_back(b);
-            S.chk_wait++;
-        } else {
-            S.chk_wait = 0;
-        }
+        S.phase = PH_LS;
+        if (D.want_check) chk.push_back(b);
     }
     // A check pass costs one tensor-core contraction whether it serves 1 or
     // 32 slots, while a slot's extra iteration costs a small fraction of
     // that: slots wanting a check keep iterating until 8 want one, one has
     // waited 3 iterations, a relative-norm stop is pending, or at most 8
-    // slots are left.
+    // slots are left.  The check's verdict reaches the host with the next
+    // round's summary; meanwhile the slot's kernels see it on the device.
     if (!chk.empty()) {
         int active = 0;
         bool urgent = false;
-        for (int b = 0; b < P.Bmax; ++b) {
-            const int ph = h->slots[b].phase;
-            if (ph != PH_EMPTY && ph != PH_FINALIZE && ph != PH_CONVERT) ++active;
-        }
-        for (int b : chk) urgent = urgent || h->slots[b].chk_wait >= 3 || releps_stop[b];
+        for (int b = 0; b < P.Bmax; ++b)
+            if (h->slots[b].phase == PH_LS) ++active;
+        for (int b : chk) urgent = urgent || h->sum_h[b].chk_wait >= 3 || h->sum_h[b].releps_stop;
         if (!(urgent || (int)chk.size() >= 8 || active <= 8)) chk.clear();
     }
     if (!chk.empty()) {
@@ -1522,194 +1554,19 @@ int phase_step_dual(sdca_handle *h)
         if ((rc = zero_acc(h))) return rc;
         {
             Timed t(h, SDCA_K_BACKWARD, 5, (int64_t)chk.size());
-            launch_dual_to_r(P, h->sd, h->list, (int)chk.size(), 0, h->dv, h->Rchk, h->stream);
+            launch_dual_to_r(P, h->ctl, h->list, (int)chk.size(), 0, h->dv, h->Rchk, h->stream);
             CK(tc_launch_bwd(h->tc, P, h->sd, h->list, (int)chk.size(), h->Rchk, (float)pow2_scale(sc), h->Rhi,
                              h->Rlo, h->gpool, h->tc_err, h->stream));
             launch_dual_gmax(P, h->sd, h->list, (int)chk.size(), h->gpool, h->acc, h->stream);
+            launch_dual_check_apply(h->ctl, h->sum, h->list, (int)chk.size(), gtol, h->acc, h->stream);
         }
         CKL();
-        if ((rc = fetch_acc(h))) return rc;
-        for (int b : chk) {
-            SlotHost &S = h->slots[b];
-            const double *eg = S.eta_g[S.gcur];
-            double gm = acc_get(h, b, ACC_GMAX);
-            for (int a = 0; a < Q; ++a) gm = std::max(gm, std::fabs(eg[a]));
-            const double gnorm = std::sqrt(std::max(S.g2, 0.0));
-            if (std::find(h->trace_loci.begin(), h->trace_loci.end(), S.locus) != h->trace_loci.end())
-                std::fprintf(stderr, "trace r=%d it=%d check max|g_J|=%.4e g_h=%.4e %.4e %.4e %.4e |g|=%.4e\n",
-                             S.locus, S.iterations, acc_get(h, b, ACC_GMAX), eg[0], eg[1], eg[2], eg[3], gnorm);
-            S.gmax = gm;
-            S.chk_ratio = gnorm > 0.0 ? gm / gnorm : 0.0;
-            S.last_check = S.iterations;
-            S.chk_wait = 0;
-            if (gm < gtol) {
-                S.status = 0;
-                stop[b] = 1;
-            } else if (releps_stop[b]) {
-                S.status = 2;
-                stop[b] = 1;
-            }
-        }
     }
-    for (int b : all) (stop[b] ? fin : cont).push_back(b);
-
-    for (int b : fin) {
-        const SlotHost &S = h->slots[b];
-        if (std::find(h->trace_loci.begin(), h->trace_loci.end(), S.locus) != h->trace_loci.end())
-            std::fprintf(stderr, "trace r=%d it=%d stop status=%d f=%.12e\n", S.locus, S.iterations, S.status, S.f);
-        h->slots[b].phase = PH_CONVERT;
-    }
-    if ((rc = dual_convert(h, false))) return rc;
-    if (cont.empty()) return SDCA_OK;
-
-    for (int b : cont) {
-        SlotHost &S = h->slots[b];
-        SlotDev &D = h->sd_h[b];
-        const int k = (int)S.hist.size();
-        const double *eg = S.eta_g[S.gcur];
-        D.coef_g = -1.0;
-        if (k > 0) {
-            // dots by history index j from the ones by ring position
-            const double *dp = h->dots_h + (int64_t)b * 4 * MAXHIST;
-            double dt[2 * MAXHIST];
-            for (int j = 0; j < k; ++j) {
-                const int pj = S.hist[j];
-                dt[j] = dp[pj] + dot4h(S.eta_s[pj], eg);
-                dt[MAXHIST + j] = dp[DOT_Y + pj] + dot4h(S.eta_y[pj], eg);
-            }
-            if (S.ring_new >= 0) {
-                // the newest pair's column: s_j.y = s_j.g - s_j.g_old, y_j.y likewise,
-                // and its own s.y, y.y from the gradient pass
-                const int pn = S.ring_new;
-                for (int j = 0; j < k; ++j) {
-                    const int pj = S.hist[j];
-                    const double syj = pj == pn ? S.sy_new : dt[j] - S.sg_prev[pj];
-                    const double yyj = pj == pn ? S.yy_new : dt[MAXHIST + j] - S.yg_prev[pj];
-                    S.SY[pj][pn] = syj;
-                    S.YY[pj][pn] = yyj;
-                    S.YY[pn][pj] = yyj;
-                }
-            }
-            for (int j = 0; j < k; ++j) {
-                S.sg_prev[S.hist[j]] = dt[j];
-                S.yg_prev[S.hist[j]] = dt[MAXHIST + j];
-            }
-            double Rm[MAXHIST * MAXHIST], YYm[MAXHIST * MAXHIST], sg[MAXHIST], yg[MAXHIST];
-            for (int a = 0; a < k; ++a) {
-                sg[a] = dt[a];
-                yg[a] = dt[MAXHIST + a];
-                for (int c = 0; c < k; ++c) {
-                    Rm[a * k + c] = (a <= c) ? S.SY[S.hist[a]][S.hist[c]] : 0.0;
-                    YYm[a * k + c] = S.YY[S.hist[a]][S.hist[c]];
-                }
-            }
-            double cg, cS[MAXHIST], cY[MAXHIST];
-            if (lbfgs_compact_coeffs(k, Rm, YYm, sg, yg, S.gamma, &cg, cS, cY)) {
-                D.coef_g = cg;
-                for (int a = 0; a < k; ++a) {
-                    D.coefS[a] = cS[a];
-                    D.coefY[a] = cY[a];
-                }
-            } else {
-                S.hist.clear();
-                S.iter = 0;
-            }
-        }
-    }
-    auto set_eta_d = [&](int b) {
-        SlotHost &S = h->slots[b];
-        SlotDev &D = h->sd_h[b];
-        const double *eg = S.eta_g[S.gcur];
-        for (int a = 0; a < Q; ++a) {
-            double v = D.coef_g * eg[a];
-            for (size_t j = 0; j < S.hist.size(); ++j)
-                v += D.coefS[j] * S.eta_s[S.hist[j]][a] + D.coefY[j] * S.eta_y[S.hist[j]][a];
-            S.eta_d[a] = v;
-            D.eta[a] = v;
-        }
-    };
-    std::vector<double> dg0(P.Bmax, 0.0);
-    auto run_direction = [&](const std::vector<int32_t> &lst) -> int {
-        for (int b : lst) {
-            SlotHost &S = h->slots[b];
-            SlotDev &D = h->sd_h[b];
-            D.nhist = (int)S.hist.size();
-            for (int j = 0; j < D.nhist; ++j) D.ring[j] = S.hist[j];
-            D.gcur = S.gcur;
-            set_eta_d(b);
-        }
-        int r2 = staged_h2d(h, h->sd, h->sd_h, sizeof(SlotDev) * P.Bmax);
-        if (r2) return r2;
-        if ((r2 = upload_list(h, lst))) return r2;
-        if ((r2 = zero_acc(h))) return r2;
-        {
-            Timed t(h, SDCA_K_DIRECTION, 1, (int64_t)lst.size());
-            launch_dual_direction(P, h->sd, h->list, (int)lst.size(), h->dv, lbase_df(h), h->P0, h->wf, h->rstate, h->udf,
-                                  h->ud, h->acc, h->stream);
-        }
-        CKL();
-        if ((r2 = fetch_acc(h))) return r2;
-        for (int b : lst) {
-            SlotHost &S = h->slots[b];
-            const double *eg = S.eta_g[S.gcur];
-            S.gd = acc_get(h, b, ACC_GD) + dot4h(eg, S.eta_d);
-            S.ddJ = acc_get(h, b, ACC_DDJ);
-            S.ddH = dot4h(S.eta_d, S.eta_d);
-            S.xdJ = acc_get(h, b, ACC_XDJ);
-            S.xdH = dot4h(S.eta_x, S.eta_d);
-            dg0[b] = acc_get(h, b, ACC_DG0);
-        }
-        return SDCA_OK;
-    };
-    if ((rc = run_direction(cont))) return rc;
-    // Restart from steepest descent only for a direction that is not
-    // downhill in angle.  The products here are exact, so a small g.d is a
-    // genuine descent: near the optimum it is small because the curvature
-    // along g is large, and a restart there would repeat every iteration
-    // (each steepest-descent step is tiny and so is the next gamma).
-    std::vector<int32_t> restart;
-    for (int b : cont) {
-        SlotHost &S = h->slots[b];
-        const double cosgd = S.gd / std::sqrt(std::max(S.g2, 0.0) * std::max(S.ddJ + S.ddH, 0.0));
-        if (!S.hist.empty() && (S.force_restart || !(cosgd < -1e-10))) restart.push_back(b);
-        S.force_restart = false;
-    }
-    std::vector<char> restarted(P.Bmax, 0);
-    if (!restart.empty()) {
-        for (int b : restart) {
-            h->slots[b].hist.clear();
-            h->slots[b].iter = 0;
-            h->slots[b].restarts++;
-            h->sd_h[b].coef_g = -1.0;
-            restarted[b] = 1;
-        }
-        if ((rc = run_direction(restart))) return rc;
-    }
-    for (int b : cont) {
-        SlotHost &S = h->slots[b];
-        const double alpha_init = restarted[b] ? 1.0 : 1.0 / std::sqrt(S.g2);
-        S.trials = 0;
-        S.use_u = true;
-        S.push = false;
-        const double d0 = dg0[b] + dl2_along(P, S, 0.0);
-        S.f0d = S.f - l2_along(P, S, 0.0);
-        S.dg0d = dg0[b];
-        if (std::find(h->trace_loci.begin(), h->trace_loci.end(), S.locus) != h->trace_loci.end())
-            std::fprintf(stderr, "trace r=%d it=%d f=%.12e |g|=%.4e gmax=%.4e chk=%d ratio=%.3f gd=%.4e dg0=%.4e "
-                                 "x2=%.4e hist=%zu restart=%d stp_prev=%.3e\n",
-                         S.locus, S.iterations, S.f, std::sqrt(S.g2), S.gmax, S.last_check, S.chk_ratio, S.gd, d0,
-                         S.x2J + S.x2H, S.hist.size(), (int)restarted[b], S.stp);
-        if (S.ls.start(S.f, d0, alpha_init) == MoreThuente::NEED_EVAL) {
-            S.stp = S.ls.stp;
-            S.phase = PH_LS;
-        } else {
-            S.stp = 0.0;
-            S.phase = PH_FINAL_EVAL;
-            if (S.hist.empty()) S.stalled = true;
-            else S.force_restart = true;
-            S.weak++;
-        }
-    }
+    if ((rc = dual_retire(h, Qu, done))) return rc;
+    bool any_active = false;
+    for (int b = 0; b < P.Bmax; ++b) any_active = any_active || h->slots[b].phase == PH_LS;
+    if ((rc = dual_convert(h, !any_active))) return rc;
+    if (!done.empty()) return refill(h, Qu);
     return SDCA_OK;
 }
 
@@ -1731,13 +1588,19 @@ int solve_lane(sdca_handle *h, Queue &Qu, cudaEvent_t t0_common)
         for (auto &S : h->slots)
             if (S.phase != PH_EMPTY) any = true;
         if (!any) break;
+        if (h->form == SDCA_FORM_DUAL) {
+            rc = dual_round(h, Qu);
+            if (rc) return rc;
+            continue;
+        }
         rc = phase_trials(h, Qu);
         if (rc) return rc;
-        rc = h->form == SDCA_FORM_DUAL ? phase_step_dual(h) : phase_step(h);
+        rc = phase_step(h);
         if (rc) return rc;
     }
     CK(cudaEventRecord(t1, h->stream));
     { const int r_ = stream_sync(h); if (r_) return r_; }
+    if (Qu.scores) dual_flush_rows(h, Qu);
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, t0, t1));
     h->prof.solve_ms = ms;
@@ -1912,7 +1775,9 @@ static int create_lane(const sdca_config *cfg, const sdca_handle *owner, sdca_ha
         (rc = halloc(h, &h->acc_h, B * NACC)) || (rc = halloc(h, &h->dots_h, B * 4 * MAXHIST)) ||
         (rc = halloc(h, &h->rows_h, B * P.L)) || (rc = halloc(h, &h->flag_h, 4)) ||
         (rc = halloc(h, &h->stage, (h->stage_cap = 64 * (((sizeof(SlotDev) + 4) * B + 1024 + 255) & ~(size_t)255)))) ||
-        (dual && ((rc = halloc(h, &h->amax_h, 2 * B)) ||
+        (dual && ((rc = halloc(h, &h->amax_h, 2 * B)) || (rc = halloc(h, &h->sum_h, B)) ||
+                  (rc = dalloc(h, &h->ctl, B)) || (rc = dalloc(h, &h->sum, B)) ||
+                  (rc = dalloc(h, &h->dacc, B * NDACC)) || (rc = dalloc(h, &h->dlist, 3 * B)) ||
                   (rc = dalloc(h, &h->dv, B * NV * 2 * P.Nx * 4)) || (rc = dalloc(h, &h->udf, B * P.Nx * 4)) ||
                   (rc = dalloc(h, &h->KR, B * P.Nx * 4)) || (rc = dalloc(h, &h->amax, 2 * B)) ||
                   (rc = dalloc(h, &h->rq, B * P.Nx * 4)) || (rc = dalloc(h, &h->csum, 16 * B)) ||
@@ -1933,7 +1798,8 @@ static int create_lane(const sdca_config *cfg, const sdca_handle *owner, sdca_ha
         delete h;
         return fail(nullptr, rc, msg);
     }
-    if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess ||
+        (dual && cudaEventCreateWithFlags(&h->ev_round, cudaEventDisableTiming) != cudaSuccess)) {
         free_all(h);
         if (h->own_stream) cudaStreamDestroy(h->stream);
         delete h;
@@ -2419,6 +2285,7 @@ int sdca_destroy(sdca_handle *h)
     cudaSetDevice(h->cfg.device);
     if (h->ev_lanes) cudaEventDestroy(h->ev_lanes);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->ev_round) cudaEventDestroy(h->ev_round);
     for (auto e : h->ev_pool) cudaEventDestroy(e);
     if (h->tc) tc_plan_destroy(h->tc);
     if (h->kd) tc_kdig_plan_destroy(h->kd);

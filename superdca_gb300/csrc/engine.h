@@ -91,6 +91,59 @@ struct SlotDev {
 constexpr int DV_X = 0, DV_D = 1, DV_G = 2, DV_S = 4;
 constexpr int DOT_Y = 2 * MAXHIST;  // dual-form dots by ring position: s at [p], y at [DOT_Y + p]
 
+// Dual form: the solver state of one slot, owned by the device while the
+// slot iterates.  The host writes it once when a locus enters the slot and
+// reads the DualSum summary after each round; the line-search kernel, the
+// accept and gradient kernels and the control kernel advance it.
+enum DualPhase {
+    DC_EVAL0 = 0,   // start point evaluated by k_trial_dual: the next gradient pass is the first
+    DC_STEP = 1,    // a direction is ready: line search, accept, gradient pass
+    DC_STOP = 2,    // stopped (status set): the host forms the solution
+};
+
+struct DualCtl {
+    int32_t phase;          // DualPhase
+    int32_t gcur;           // gradient buffer holding the accepted gradient (0/1)
+    int32_t ring_new;       // ring position of the pair the next accept forms, -1 none
+    int32_t push;           // the next accept pushes s (and the gradient pass y)
+    int32_t nhist;          // live history pairs, oldest first in hist[]
+    int32_t hist[MAXHIST];
+    int32_t iter;           // pairs since the last restart
+    int32_t iterations, nfeval, restarts, skipped, weak, max_trials, trials;
+    int32_t status;         // 0 gradient tolerance, 1 iteration limit, 2 relative-epsilon stop, -1 non-finite
+    int32_t force_restart, stalled;
+    int32_t last_check, chk_wait, want_check, releps_stop;
+    double f;               // objective at the accepted point
+    double g2, g2J;         // ||g||^2 (all, J part)
+    double x2J;             // ||x_J||^2
+    double gmax;            // max|g| (exact at a check, else the estimate chk_ratio ||g||)
+    double chk_ratio;       // max|g| / ||g|| at the last check (0: none yet)
+    double amax_g, amax_x;  // max |a| of the gradient and of x (FP32 scales of a check and of the solution)
+    double gamma, sy_new, yy_new;
+    double stp;             // accepted step of the last search
+    double coef_g, coefS[MAXHIST], coefY[MAXHIST];
+    double eta_x[Q], eta_d[Q], eta_g[2][Q], eta_s[MAXHIST + 1][Q], eta_y[MAXHIST + 1][Q];
+    double SY[MAXHIST + 1][MAXHIST + 1], YY[MAXHIST + 1][MAXHIST + 1];
+    double sg_prev[MAXHIST + 1], yg_prev[MAXHIST + 1];
+};
+
+// What the host reads of each slot after a round (a copy of DualCtl fields).
+struct DualSum {
+    int32_t phase, status, want_check, chk_wait, releps_stop, iterations, nfeval, restarts, skipped, weak,
+        max_trials, pad_;
+    double f, gmax, amax_g, amax_x, x2J;
+    double eta_x[Q];
+};
+
+// per-slot line-search and direction sums (doubles) of the dual form
+enum DualAcc {
+    DA_GD = 0,      // g.d, J part (direction kernel)
+    DA_DDJ,         // d_J . d_J
+    DA_XDJ,         // x_J . d_J
+    DA_DG0,         // slope of the search line at 0, data part
+    NDACC = 4
+};
+
 enum SlotFlags {
     SLOT_F_USE_U = 1,       // trial logits use lbase + stp u (else lbase)
     SLOT_F_PUSH = 2,        // accept pushes an (s, y) pair into the history
@@ -163,20 +216,26 @@ void launch_dual_quant(const Problem &P, const SlotDev *sd, const int32_t *list,
                        const uint8_t *rstate, double qscale, int32_t *rq, long long *csum, cudaStream_t st);
 void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8_t *rstate, const int32_t *K,
                        double qscale, const int32_t *rq, const long long *csum, float2 *KR, cudaStream_t st);
-void launch_dual_grad(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double qscale,
+void launch_dual_grad(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, double qscale,
                       const int32_t *rq, const float2 *KR, float2 *dv, double *acc, double *amax, cudaStream_t st);
-void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int newg, const float2 *dv,
+void launch_dual_dots(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int newg, const float2 *dv,
                       double *dots, cudaStream_t st);
-void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float2 *dv,
+void launch_dual_direction(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
                            const float2 *lbase, float *P0, const float *w, const uint8_t *rstate, float2 *u,
-                           float *ud, double *acc, cudaStream_t st);
-void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float2 *lbase,
-                        const float2 *u, const float *ud, const uint8_t *rstate, const float *w, const float *P0,
-                        float *R, double *acc, cudaStream_t st);
-void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float2 *dv,
+                           float *ud, double *dacc, cudaStream_t st);
+void launch_dual_accept(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
                         const float2 *u, float2 *lbase, cudaStream_t st);
-void launch_dual_to_r(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int which,
+void launch_dual_to_r(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int which,
                       const float2 *dv, float *R, cudaStream_t st);
+// the per-iteration decisions of the dual form on the device
+void launch_dual_linesearch(const Problem &P, DualCtl *ctl, const int32_t *list, int n, const double *dacc,
+                            float2 *dv, const float2 *lbase, float2 *u, float *ud, const uint8_t *rstate,
+                            const float *w, const float *P0, float *R, double *acc, cudaStream_t st);
+void launch_dual_control(const Problem &P, DualCtl *ctl, DualSum *sum, const int32_t *list, int n,
+                         int max_iterations, double gtol, const double *acc, const double *amax, const double *dots,
+                         cudaStream_t st);
+void launch_dual_check_apply(DualCtl *ctl, DualSum *sum, const int32_t *list, int n, double gtol, const double *acc,
+                             cudaStream_t st);
 void launch_dual_gmax(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *gpool,
                       double *acc, cudaStream_t st);
 void launch_dual_digits(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d, const float2 *dv,

@@ -19,10 +19,13 @@
 // are taken in 64-bit integers; QB keeps them below 2^62.  K = K_all minus
 // the agreement at r itself, a class sum per state of r.
 #include <cstdint>
+#include <new>
 
 #include "df.cuh"
 #include "engine.h"
 #include "kernels_common.cuh"
+#include "lbfgs_host.h"
+#include "linesearch.h"
 
 namespace sdca {
 namespace {
@@ -143,13 +146,14 @@ __device__ __forceinline__ int64_t dvo(int64_t b, int v, int part, int NV, int64
 // y = g_new - g_old into the history when the slot pushes a pair;
 // J-part sums: g.g, x.x, s.y, y.y, s.s; max |a_g| and max |a_x|
 __global__ void __launch_bounds__(256)
-k_dual_grad(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
+k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
             double lambda_J, const int32_t *__restrict__ rq, double inv_qscale, const float2 *__restrict__ KR,
             float2 *__restrict__ dv, double *__restrict__ acc, double *__restrict__ amax)
 {
     const int b = list[blockIdx.y];
-    const SlotDev &S = sd[b];
-    const bool push = (S.flags & SLOT_F_PUSH) && S.ring_new >= 0;
+    const DualCtl &S = ctl[b];
+    if (S.phase == DC_STOP) return;
+    const bool push = S.push && S.ring_new >= 0;
     const float2 l2 = df_from_d(2.0 * lambda_J), iq = df_from_d(inv_qscale);
     const float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = dv + dvo(b, DV_X, 1, NV, Nx);
     const float2 *ago = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kgo = dv + dvo(b, DV_G + S.gcur, 1, NV, Nx);
@@ -200,29 +204,33 @@ k_dual_grad(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, in
 constexpr int DOT_CHUNK = 1024;
 
 __global__ void __launch_bounds__(256)
-k_dual_dots(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
+k_dual_dots(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
             int newg, const float2 *__restrict__ dv, double *__restrict__ dots)
 {
     const int b = list[blockIdx.y];
-    const SlotDev &S = sd[b];
-    const int k = S.nhist;
+    const DualCtl &S = ctl[b];
+    if (S.phase == DC_STOP) return;
+    // the live history and the pair the last accept pushed
+    const bool pushed = S.push && S.ring_new >= 0;
+    const int k = S.nhist + (pushed ? 1 : 0);
     const int64_t E = Nx * 4, e0 = (int64_t)blockIdx.x * DOT_CHUNK;
     const int ne = E - e0 < DOT_CHUNK ? (int)(E - e0) : DOT_CHUNK;
     __shared__ float2 g[DOT_CHUNK];
-    const float2 *kg = dv + dvo(b, DV_G + (newg ? 1 - S.gcur : S.gcur), 1, NV, Nx) + e0;
+    const float2 *kg = dv + dvo(b, DV_G + (newg ? 1 - S.gcur : S.gcur), 1, NV, Nx) + e0;   // (gcur flips in the control kernel)
     for (int t = threadIdx.x; t < ne; t += blockDim.x) g[t] = kg[t];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int q = warp; q < 2 * k; q += nw) {
         const bool isy = q >= k;
         const int j = isy ? q - k : q;
-        const float2 *v = dv + dvo(b, DV_S + (isy ? ring : 0) + S.ring[j], 0, NV, Nx) + e0;
+        const int pos = j < S.nhist ? S.hist[j] : S.ring_new;
+        const float2 *v = dv + dvo(b, DV_S + (isy ? ring : 0) + pos, 0, NV, Nx) + e0;
         float2 acc = df_zero();
 #pragma unroll 8
         for (int t = lane; t < ne; t += 32) acc = df_fma(v[t], g[t], acc);
         const float2 sum = df_warp_sum(acc);
         if (lane == 0 && (sum.x != 0.f || sum.y != 0.f))
-            atomicAdd(dots + (int64_t)b * 4 * MAXHIST + (isy ? DOT_Y : 0) + S.ring[j], df_to_d(sum));
+            atomicAdd(dots + (int64_t)b * 4 * MAXHIST + (isy ? DOT_Y : 0) + pos, df_to_d(sum));
     }
 }
 
@@ -282,74 +290,10 @@ __device__ __noinline__ void trial_fp64(const float2 *lb, const float2 *up, doub
 // compares; the base values (objective, slope at 0) are FP64.  Z is a sum of
 // positive terms and the new probabilities are products, so a probability
 // that has become small keeps its relative precision.  Sequences whose step
-// is large take an FP64 log-sum-exp of the logits (trial_fp64).  Sums:
-// ACC_F += w dl, ACC_DG += slope change, ACC_RS += R(stp);
-// R <- R(stp) = w (p(stp) - onehot(y)), its y entry as minus the sum of the
-// others.
-constexpr int DT_THREADS = 256;
-
-__global__ void __launch_bounds__(DT_THREADS, 4)
-k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int N, int64_t Nx,
-              const float2 *__restrict__ lbase, const float2 *__restrict__ u, const float4 *__restrict__ ud,
-              const uint8_t *__restrict__ rstate, const float *__restrict__ w, const float4 *__restrict__ P0,
-              float4 *__restrict__ R, double *__restrict__ acc)
-{
-    const int b = list[blockIdx.y];
-    const double stp = sd[b].stp;
-    const float stpf = (float)stp;
-    float f = 0.f, dg = 0.f, rs0 = 0.f, rs1 = 0.f, rs2 = 0.f, rs3 = 0.f;
-    double fbig = 0.0, dgbig = 0.0;   // sequences that take the FP64 path
-#pragma unroll 1
-    for (int i = blockIdx.x * DT_THREADS + threadIdx.x; i < N; i += gridDim.x * DT_THREADS) {
-        const int64_t o = (int64_t)b * Nx + i;
-        const float4 dv4 = ud[o];
-        const float du[4] = {dv4.x, dv4.y, dv4.z, dv4.w};   // u_a - u_y
-        const int y = rstate[o] & 3;
-        const float wi = w[i];
-        const float4 pv = P0[o];
-        const float p0[4] = {pv.x, pv.y, pv.z, pv.w};
-        float t[4], tmax = 0.f;
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            t[a] = stpf * du[a];
-            tmax = fmaxf(tmax, fabsf(t[a]));
-        }
-        float r[4];
-        if (tmax < 30.f) {
-            float e[4], x[4], q = 0.f, z = 0.f;
-#pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                e[a] = expm1f(t[a]);
-                x[a] = p0[a] * expf(t[a]);
-                q = fmaf(p0[a], e[a], q);
-                z += x[a];
-            }
-            const float iz = 1.f / z;
-            f = fmaf(wi, fabsf(q) < 0.5f ? log1pf(q) : logf(z), f);
-            float ro = 0.f;
-#pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                dg = fmaf(wi * (p0[a] * (e[a] - q) * iz), du[a], dg);
-                r[a] = a == y ? 0.f : wi * (x[a] * iz);
-                ro += r[a];
-            }
-#pragma unroll
-            for (int a = 0; a < 4; ++a)   // (no dynamic index: the arrays stay in registers)
-                if (a == y) r[a] = -ro;
-        } else {
-            trial_fp64(lbase + o * 4, u + o * 4, stp, y, wi, p0, r, fbig, dgbig);
-        }
-        rs0 += r[0]; rs1 += r[1]; rs2 += r[2]; rs3 += r[3];
-        R[o] = make_float4(r[0], r[1], r[2], r[3]);
-    }
-    // single-precision partial sums per warp, double precision across warps
-    float v[6] = {f, dg, rs0, rs1, rs2, rs3};
-    const int idx[6] = {ACC_F, ACC_DG, ACC_RS0, ACC_RS1, ACC_RS2, ACC_RS3};
-    block_sum_atomic_f<6>(v, acc + (int64_t)b * NACC, idx);
-    if (fbig != 0.0) atomicAdd(acc + (int64_t)b * NACC + ACC_F, fbig);
-    if (dgbig != 0.0) atomicAdd(acc + (int64_t)b * NACC + ACC_DG, dgbig);
-}
-
+// is large take an FP64 log-sum-exp of the logits (trial_fp64).  Per trial:
+// the sums of w dl, of the slope change and of R(stp), and the rows
+// R <- R(stp) = w (p(stp) - onehot(y)), the y entry as minus the sum of the
+// others (trial_seq, in the line-search kernel below).
 // d = coef_g g + sum_j coefS_j s_j + coefY_j y_j (a and k parts); trial
 // logits direction u = k_d + eta_d; the base probabilities P0 of the step
 // trials from the double-float logits at the current point (fresh every iteration,
@@ -357,13 +301,14 @@ k_trial_delta(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, 
 // d.d, x.d (J parts) and the slope of the search line at 0 from the trials'
 // own numbers, sum_i w_i sum_c p0_ic (u_ic - u_iy)
 __global__ void __launch_bounds__(256)
-k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int N, int NV,
+k_dual_direction(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int N, int NV,
                  int ring, float2 *__restrict__ dv, const float2 *__restrict__ lbase, float *__restrict__ P0,
                  const float *__restrict__ w, const uint8_t *__restrict__ rstate, float2 *__restrict__ u,
-                 float *__restrict__ ud, double *__restrict__ acc)
+                 float *__restrict__ ud, double *__restrict__ dacc)
 {
     const int b = list[blockIdx.y];
-    const SlotDev &S = sd[b];
+    const DualCtl &S = ctl[b];
+    if (S.phase == DC_STOP) return;
     const int k = S.nhist;
     const float2 *ag = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kg = dv + dvo(b, DV_G + S.gcur, 1, NV, Nx);
     const float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx);
@@ -375,7 +320,7 @@ k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ lis
         cf[MAXHIST + threadIdx.x] = df_from_d(S.coefY[threadIdx.x]);
     }
     if (threadIdx.x == 0) cf[2 * MAXHIST] = df_from_d(S.coef_g);
-    if (threadIdx.x < Q) cf[2 * MAXHIST + 1 + threadIdx.x] = df_from_d(S.eta[threadIdx.x]);
+    if (threadIdx.x < Q) cf[2 * MAXHIST + 1 + threadIdx.x] = df_from_d(S.eta_d[threadIdx.x]);
     __syncthreads();
     const float2 cg = cf[2 * MAXHIST];
     float2 gd = df_zero(), dd = df_zero(), xd = df_zero(), dg0 = df_zero();
@@ -385,7 +330,7 @@ k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ lis
 #pragma unroll 4   // (a full unroll hoists every load: 116 registers, fewer warps)
         for (int j = 0; j < MAXHIST; ++j) {
             if (j >= k) break;
-            const float2 *vs = dv + dvo(b, DV_S + S.ring[j], 0, NV, Nx), *vy = dv + dvo(b, DV_S + ring + S.ring[j], 0, NV, Nx);
+            const float2 *vs = dv + dvo(b, DV_S + S.hist[j], 0, NV, Nx), *vy = dv + dvo(b, DV_S + ring + S.hist[j], 0, NV, Nx);
             const float2 cs = cf[j], cy = cf[MAXHIST + j];
             a = df_fma(cy, vy[e], df_fma(cs, vs[e], a));
             kk = df_fma(cy, vy[part + e], df_fma(cs, vs[part + e], kk));
@@ -418,20 +363,21 @@ k_dual_direction(const SlotDev *__restrict__ sd, const int32_t *__restrict__ lis
         if (e / 4 < N) dg0 = df_fma(make_float2(w[e / 4] * p0, 0.f), du, dg0);
     }
     double v[4] = {df_to_d(gd), df_to_d(dd), df_to_d(xd), df_to_d(dg0)};
-    const int idx[4] = {ACC_GD, ACC_DDJ, ACC_XDJ, ACC_DG0};
-    block_sum_atomic<4>(v, acc + (int64_t)b * NACC, idx);
+    const int idx[4] = {DA_GD, DA_DDJ, DA_XDJ, DA_DG0};
+    block_sum_atomic<4>(v, dacc + (int64_t)b * NDACC, idx);
 }
 
 // x += stp d (a and k parts), s = x_new - x_old into the history on a push,
 // logits lbase += stp u
 __global__ void __launch_bounds__(256)
-k_dual_accept(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int NV,
+k_dual_accept(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int NV,
               float2 *__restrict__ dv, const float2 *__restrict__ u, float2 *__restrict__ lbase)
 {
     const int b = list[blockIdx.y];
-    const SlotDev &S = sd[b];
+    const DualCtl &S = ctl[b];
+    if (S.phase != DC_STEP) return;
     const double stp = S.stp;
-    const bool push = (S.flags & SLOT_F_PUSH) && S.ring_new >= 0;
+    const bool push = S.push && S.ring_new >= 0;
     const float2 sf = df_from_d(stp);
     float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = dv + dvo(b, DV_X, 1, NV, Nx);
     const float2 *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = dv + dvo(b, DV_D, 1, NV, Nx);
@@ -452,11 +398,11 @@ k_dual_accept(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, 
 
 // FP32 copy of a vector's a part (the current gradient, or x) as the R rows
 // of a tensor-core backward contraction, scaled by `scale`
-__global__ void k_dual_to_r(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Nx, int N,
+__global__ void k_dual_to_r(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int N,
                             int NV, int which, const float2 *__restrict__ dv, float4 *__restrict__ R)
 {
     const int b = list[blockIdx.y];
-    const int v = which == 0 ? DV_G + sd[b].gcur : DV_X;
+    const int v = which == 0 ? DV_G + ctl[b].gcur : DV_X;
     const float2 *a = dv + dvo(b, v, 0, NV, Nx);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Nx; i += (int64_t)gridDim.x * blockDim.x) {
         float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -540,6 +486,490 @@ __global__ void k_dual_to_wa(const SlotDev *__restrict__ sd, const int32_t *__re
     }
 }
 
+// ---- the per-iteration decisions on the device
+
+// One sequence of a step trial as a change from the current point (the
+// derivation above): adds w dl, the slope change and the new residual row's
+// sums, and writes the row.
+__device__ __forceinline__ void trial_seq(int64_t o, int i, double stp, float stpf, const float2 *__restrict__ lbase,
+                                          const float2 *__restrict__ u, const float4 *__restrict__ ud,
+                                          const uint8_t *__restrict__ rstate, const float *__restrict__ w,
+                                          const float4 *__restrict__ P0, float4 *__restrict__ R, float &f, float &dg,
+                                          float (&rs)[4], double &fbig, double &dgbig)
+{
+    const float4 dv4 = ud[o];
+    const float du[4] = {dv4.x, dv4.y, dv4.z, dv4.w};   // u_a - u_y
+    const int y = rstate[o] & 3;
+    const float wi = w[i];
+    const float4 pv = P0[o];
+    const float p0[4] = {pv.x, pv.y, pv.z, pv.w};
+    float t[4], tmax = 0.f;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        t[a] = stpf * du[a];
+        tmax = fmaxf(tmax, fabsf(t[a]));
+    }
+    float r[4];
+    if (tmax < 30.f) {
+        float e[4], x[4], q = 0.f, z = 0.f;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            e[a] = expm1f(t[a]);
+            x[a] = p0[a] * expf(t[a]);
+            q = fmaf(p0[a], e[a], q);
+            z += x[a];
+        }
+        const float iz = 1.f / z;
+        f = fmaf(wi, fabsf(q) < 0.5f ? log1pf(q) : logf(z), f);
+        float ro = 0.f;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            dg = fmaf(wi * (p0[a] * (e[a] - q) * iz), du[a], dg);
+            r[a] = a == y ? 0.f : wi * (x[a] * iz);
+            ro += r[a];
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+            if (a == y) r[a] = -ro;
+    } else {
+        trial_fp64(lbase + o * 4, u + o * 4, stp, y, wi, p0, r, fbig, dgbig);
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) rs[a] += r[a];
+    R[o] = make_float4(r[0], r[1], r[2], r[3]);
+}
+
+__device__ __forceinline__ double dot4d(const double *a, const double *b)
+{
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3];
+}
+
+constexpr int LS_THREADS = 256;
+
+// The whole line search of one slot in one thread block (SuperDCA: the
+// More-Thuente search of CppNumericalSolvers' LbfgsSolver, one
+// value_and_gradient per trial, LBFGS_interface_CppNumericalSolvers.hpp:
+// 111-117).  Thread 0 holds the More-Thuente state machine (FP64, in shared
+// memory); all threads evaluate each trial over the slot's sequences and
+// reduce it (FP32 per thread and warp, FP64 across warps).
+//   1. Restart test: a direction that is not downhill in angle
+//      (cos(g, d) >= -1e-10), or one the last search asked to restart,
+//      becomes steepest descent: d = -g, its logit direction, differences
+//      and slope at 0 are formed here and the history is dropped.
+//   2. More-Thuente start from f, the slope at 0 (data part from the
+//      direction kernel's base probabilities, L2 part exact) and the initial
+//      step (1 after a restart, else 1 / ||g||).  A start that is not downhill
+//      evaluates the point itself (step 0) and marks the slot to restart, or
+//      to stop when it has no history.
+//   3. Trials until the search accepts one: the accepted point is the last
+//      trial, so R holds its residual rows, acc[ACC_RS*] their sums and the
+//      slot's f, stp the point's objective and step.
+__global__ void __launch_bounds__(LS_THREADS, 3)
+k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int N, int64_t Nx, int NV,
+                  double lambda_J, double lambda_h, const double *__restrict__ dacc, float2 *__restrict__ dv,
+                  const float2 *__restrict__ lbase, float2 *__restrict__ u, float4 *__restrict__ ud,
+                  const uint8_t *__restrict__ rstate, const float *__restrict__ w, const float4 *__restrict__ P0,
+                  float4 *__restrict__ R, double *__restrict__ acc)
+{
+    const int b = list[blockIdx.x];
+    DualCtl &S = ctl[b];
+    if (S.phase != DC_STEP) return;   // (the same for the whole block)
+    __shared__ __align__(16) unsigned char mt_raw[sizeof(MoreThuente)];
+    __shared__ double red[LS_THREADS / 32][8];
+    __shared__ double s_stp;
+    __shared__ int s_restart, s_done;
+    MoreThuente &mt = *reinterpret_cast<MoreThuente *>(mt_raw);
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const double *da = dacc + (int64_t)b * NDACC;
+    // FP64 scalars of the search, thread 0's (in shared memory, so that they
+    // hold no registers of the other threads through the trial loop)
+    __shared__ double sc[9];
+    double &xdJ = sc[0], &xdH = sc[1], &ddJ = sc[2], &ddH = sc[3], &dg0 = sc[4], &f0d = sc[5], &dg0d = sc[6],
+           &x2H = sc[7];
+    __shared__ int s_mode;   // 0 searching, 1 evaluating the current point (start not downhill)
+    if (tid == 0) {
+        const double *eg = S.eta_g[S.gcur];
+        const double gd = da[DA_GD] + dot4d(eg, S.eta_d);
+        ddJ = da[DA_DDJ];
+        ddH = dot4d(S.eta_d, S.eta_d);
+        const double cosgd = gd / sqrt(fmax(S.g2, 0.0) * fmax(ddJ + ddH, 0.0));
+        s_restart = (S.nhist > 0 && (S.force_restart || !(cosgd < -1e-10))) ? 1 : 0;
+        S.force_restart = 0;
+        xdJ = da[DA_XDJ];
+        dg0 = da[DA_DG0];
+        s_mode = 0;
+    }
+    __syncthreads();
+    const bool restart = s_restart != 0;
+    if (restart) {
+        const int gc = S.gcur;
+        float2 ed[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) ed[c] = df_from_d(-S.eta_g[gc][c]);
+        const float2 *ag = dv + dvo(b, DV_G + gc, 0, NV, Nx), *kg = dv + dvo(b, DV_G + gc, 1, NV, Nx);
+        const float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx);
+        float2 *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = dv + dvo(b, DV_D, 1, NV, Nx);
+        float2 xd = df_zero(), d0 = df_zero();
+        for (int64_t i = tid; i < Nx; i += LS_THREADS) {
+            const int64_t o = (int64_t)b * Nx + i;
+            float2 uu[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float2 a_d = df_neg(ag[4 * i + c]), k_d = df_neg(kg[4 * i + c]);
+                ad[4 * i + c] = a_d;
+                kd[4 * i + c] = k_d;
+                uu[c] = df_add(k_d, ed[c]);
+                u[o * 4 + c] = uu[c];
+                xd = df_fma(ax[4 * i + c], k_d, xd);
+            }
+            const int y = rstate[o] & 3;
+            float2 uy = uu[0];
+#pragma unroll
+            for (int c = 1; c < 4; ++c)
+                if (c == y) uy = uu[c];
+            float du[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) du[c] = df_f(df_sub(uu[c], uy));
+            ud[o] = make_float4(du[0], du[1], du[2], du[3]);
+            if (i < N) {
+                const float4 pv = P0[o];
+                const float p0[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+                for (int c = 0; c < 4; ++c) d0 = df_fma(make_float2(w[i] * p0[c], 0.f), df_sub(uu[c], uy), d0);
+            }
+        }
+        const float2 sx = df_warp_sum(xd), s0 = df_warp_sum(d0);
+        if (lane == 0) {
+            red[wid][0] = df_to_d(sx);
+            red[wid][1] = df_to_d(s0);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double t0 = 0, t1 = 0;
+            for (int k = 0; k < LS_THREADS / 32; ++k) {
+                t0 += red[k][0];
+                t1 += red[k][1];
+            }
+            xdJ = t0;
+            dg0 = t1;
+            ddJ = S.g2J;
+            for (int c = 0; c < 4; ++c) S.eta_d[c] = -S.eta_g[gc][c];
+            ddH = dot4d(S.eta_d, S.eta_d);
+            S.nhist = 0;
+            S.iter = 0;
+            S.restarts++;
+            S.coef_g = -1.0;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        xdH = dot4d(S.eta_x, S.eta_d);
+        x2H = dot4d(S.eta_x, S.eta_x);
+        const double l20 = lambda_J * S.x2J + lambda_h * x2H;
+        const double d0 = dg0 + 2.0 * lambda_J * xdJ + 2.0 * lambda_h * xdH;
+        f0d = S.f - l20;
+        dg0d = dg0;
+        const double alpha = restart ? 1.0 : 1.0 / sqrt(S.g2);
+        S.trials = 0;
+        new (mt_raw) MoreThuente();
+        if (mt.start(S.f, d0, alpha) == MoreThuente::NEED_EVAL) {
+            s_stp = mt.stp;
+        } else {
+            s_stp = 0.0;
+            s_mode = 1;
+            S.weak++;
+            if (S.nhist == 0) S.stalled = 1;
+            else S.force_restart = 1;
+        }
+        s_done = 0;
+    }
+    // More-Thuente stops within 20 trials; the bound only guards the loop
+    for (int it = 0; it < 64; ++it) {
+        __syncthreads();
+        const double stp = s_stp;
+        const float stpf = (float)stp;
+        float f = 0.f, dg = 0.f, rs[4] = {0.f, 0.f, 0.f, 0.f};
+        double fbig = 0.0, dgbig = 0.0;
+#pragma unroll 1
+        for (int i = tid; i < N; i += LS_THREADS)
+            trial_seq((int64_t)b * Nx + i, i, stp, stpf, lbase, u, ud, rstate, w, P0, R, f, dg, rs, fbig, dgbig);
+        const float v[6] = {warp_sum_f(f), warp_sum_f(dg), warp_sum_f(rs[0]), warp_sum_f(rs[1]), warp_sum_f(rs[2]),
+                            warp_sum_f(rs[3])};
+        fbig = warp_sum(fbig);
+        dgbig = warp_sum(dgbig);
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) red[wid][k] = (double)v[k];
+            red[wid][6] = fbig;
+            red[wid][7] = dgbig;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double tot[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int k = 0; k < LS_THREADS / 32; ++k)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) tot[j] += red[k][j];
+            const double l2 = lambda_J * (S.x2J + 2.0 * stp * xdJ + stp * stp * ddJ) +
+                              lambda_h * (x2H + 2.0 * stp * xdH + stp * stp * ddH);
+            const double dl2 = 2.0 * lambda_J * (xdJ + stp * ddJ) + 2.0 * lambda_h * (xdH + stp * ddH);
+            const double ff = f0d + (tot[0] + tot[6]) + l2;
+            const double dd = dg0d + (tot[1] + tot[7]) + dl2;
+            S.trials++;
+            bool done = s_mode == 1 || it == 63;
+            if (!done && (!isfinite(ff) || !isfinite(dd))) done = true;
+            if (!done) {
+                if (mt.feed(ff, dd) == MoreThuente::DONE) {
+                    done = true;
+                    if (mt.info != 1) S.weak++;
+                    S.max_trials = max(S.max_trials, S.trials);
+                } else {
+                    s_stp = mt.stp;
+                }
+            }
+            if (done) {
+                S.stp = stp;   // the accepted point is the last trial
+                S.f = ff;
+                double *ac = acc + (int64_t)b * NACC;
+                for (int a = 0; a < 4; ++a) ac[ACC_RS0 + a] = tot[2 + a];
+                s_done = 1;
+            }
+        }
+        __syncthreads();
+        if (s_done) break;
+    }
+}
+
+constexpr int CTL_WORDS = (int)(sizeof(DualCtl) / 8);
+static_assert(sizeof(DualCtl) % 8 == 0, "DualCtl is copied as 8-byte words");
+
+__device__ void write_summary(const DualCtl &S, DualSum &o)
+{
+    o.phase = S.phase;
+    o.status = S.status;
+    o.want_check = S.want_check;
+    o.chk_wait = S.chk_wait;
+    o.releps_stop = S.releps_stop;
+    o.iterations = S.iterations;
+    o.nfeval = S.nfeval;
+    o.restarts = S.restarts;
+    o.skipped = S.skipped;
+    o.weak = S.weak;
+    o.max_trials = S.max_trials;
+    o.f = S.f;
+    o.gmax = S.gmax;
+    o.amax_g = S.amax_g;
+    o.amax_x = S.amax_x;
+    o.x2J = S.x2J;
+    for (int a = 0; a < Q; ++a) o.eta_x[a] = S.eta_x[a];
+}
+
+// After the gradient pass: the L-BFGS bookkeeping of one slot per warp, in
+// FP64 by lane 0 on a shared-memory copy of the slot's state (SuperDCA's
+// LbfgsSolver iteration, driven from plmDCA.hpp:298-304; stop on max|g| <
+// threshold or the iteration limit, plmDCA.hpp:218-221):
+//   h gradient from the residual sums, the (s, y) pair kept when
+//   s.y > 1e-3 |s| |y|, the iteration limit and stall stops, the wish for an
+//   exact max-norm check (the host batches those), the newest column of the
+//   Gram matrices S^T Y and Y^T Y from the history dots, the compact-form
+//   coefficients of the next direction and its h part, and the ring
+//   position the next accepted step will fill.
+__global__ void __launch_bounds__(32)
+k_dual_control(DualCtl *__restrict__ ctl, DualSum *__restrict__ sum, const int32_t *__restrict__ list, int m,
+               int max_iterations, double gtol, double lambda_J, double lambda_h, const double *__restrict__ acc,
+               const double *__restrict__ amax, const double *__restrict__ dots)
+{
+    const int b = list[blockIdx.x];
+    __shared__ DualCtl S;
+    {
+        const unsigned long long *src = reinterpret_cast<const unsigned long long *>(ctl + b);
+        unsigned long long *dst = reinterpret_cast<unsigned long long *>(&S);
+        for (int k = threadIdx.x; k < CTL_WORDS; k += 32) dst[k] = src[k];
+    }
+    __syncwarp();
+    if (threadIdx.x == 0 && S.phase != DC_STOP) {
+        const double *ac = acc + (int64_t)b * NACC;
+        const bool init = S.phase == DC_EVAL0;
+        if (!init) {
+            // the accepted step's h part: x_h += stp d_h, s_h
+            for (int a = 0; a < Q; ++a) {
+                const double xn = S.eta_x[a] + S.stp * S.eta_d[a];
+                if (S.push && S.ring_new >= 0) S.eta_s[S.ring_new][a] = xn - S.eta_x[a];
+                S.eta_x[a] = xn;
+            }
+        }
+        const int gn = 1 - S.gcur;
+        double eg[Q];
+        for (int a = 0; a < Q; ++a) eg[a] = ac[ACC_RS0 + a] + 2.0 * lambda_h * S.eta_x[a];
+        const bool pushed = S.push && S.ring_new >= 0;
+        if (pushed)
+            for (int a = 0; a < Q; ++a) S.eta_y[S.ring_new][a] = eg[a] - S.eta_g[S.gcur][a];
+        for (int a = 0; a < Q; ++a) S.eta_g[gn][a] = eg[a];
+        S.gcur = gn;
+        S.g2J = ac[ACC_G2];
+        S.g2 = S.g2J + dot4d(eg, eg);
+        S.x2J = ac[ACC_X2J];
+        const double x2H = dot4d(S.eta_x, S.eta_x);
+        S.amax_g = amax[2 * b];
+        S.amax_x = amax[2 * b + 1];
+        const double gnorm = sqrt(fmax(S.g2, 0.0));
+        S.gmax = S.chk_ratio > 0.0 ? S.chk_ratio * gnorm : gnorm;   // estimate until checked
+        bool st = false;
+        if (init) {
+            S.f = ac[ACC_F] + lambda_J * S.x2J + lambda_h * x2H;
+            S.nfeval = 1;
+        } else {
+            S.iterations++;
+            S.nfeval += 2 + S.trials;
+            const int pr = S.ring_new >= 0 ? S.ring_new : 0;
+            const double sy = ac[ACC_SY] + (pushed ? dot4d(S.eta_s[pr], S.eta_y[pr]) : 0.0);
+            const double yy = ac[ACC_YY] + (pushed ? dot4d(S.eta_y[pr], S.eta_y[pr]) : 0.0);
+            const double ss = ac[ACC_SS] + (pushed ? dot4d(S.eta_s[pr], S.eta_s[pr]) : 0.0);
+            if (pushed && sy > 1e-3 * sqrt(ss * yy) && yy > 0.0 && isfinite(sy) && isfinite(yy)) {
+                if (S.nhist == m) {
+                    for (int j = 1; j < m; ++j) S.hist[j - 1] = S.hist[j];
+                    S.nhist--;
+                }
+                S.hist[S.nhist++] = S.ring_new;
+                S.gamma = sy / yy;
+                S.sy_new = sy;
+                S.yy_new = yy;
+                S.iter++;
+            } else {
+                S.ring_new = -1;
+                S.skipped++;
+            }
+            if (S.iterations > max_iterations) {
+                S.status = 1;
+                st = true;
+            } else if (S.stalled) {
+                S.status = 2;
+                st = true;
+            }
+        }
+        if (!isfinite(S.f) || !isfinite(S.g2)) {
+            S.status = -1;
+            st = true;
+        }
+        if (st) {
+            S.phase = DC_STOP;
+            S.want_check = 0;
+        } else {
+            // the relative-norm stop is decided after the max-norm test (by the host's check pass)
+            const double releps = 1e-4 * fmax(1.0, sqrt(S.x2J + x2H));
+            S.releps_stop = gnorm < releps;
+            // the max-norm test needs J = Phi^T a_g: wanted when the last check's
+            // ratio max|g| / ||g|| predicts a pass, and every 15 iterations
+            const bool due = S.iterations - S.last_check >= 15 && (S.chk_ratio > 0.0 || gnorm < 150.0 * gtol);
+            const bool near = S.chk_ratio > 0.0 && S.chk_ratio * gnorm < 1.1 * gtol;
+            S.want_check = (due || near || gnorm < gtol || S.releps_stop) ? 1 : 0;
+            S.chk_wait = S.want_check ? S.chk_wait + 1 : 0;
+            // compact-form coefficients of the next direction
+            const int k = S.nhist;
+            S.coef_g = -1.0;
+            if (k > 0) {
+                const double *dp = dots + (int64_t)b * 4 * MAXHIST;
+                double dt[2 * MAXHIST];
+                for (int j = 0; j < k; ++j) {
+                    const int pj = S.hist[j];
+                    dt[j] = dp[pj] + dot4d(S.eta_s[pj], eg);
+                    dt[MAXHIST + j] = dp[DOT_Y + pj] + dot4d(S.eta_y[pj], eg);
+                }
+                if (S.ring_new >= 0) {
+                    // the newest pair's column: s_j.y = s_j.g - s_j.g_old, y_j.y likewise,
+                    // and its own s.y, y.y from the gradient pass
+                    const int pn = S.ring_new;
+                    for (int j = 0; j < k; ++j) {
+                        const int pj = S.hist[j];
+                        const double syj = pj == pn ? S.sy_new : dt[j] - S.sg_prev[pj];
+                        const double yyj = pj == pn ? S.yy_new : dt[MAXHIST + j] - S.yg_prev[pj];
+                        S.SY[pj][pn] = syj;
+                        S.YY[pj][pn] = yyj;
+                        S.YY[pn][pj] = yyj;
+                    }
+                }
+                for (int j = 0; j < k; ++j) {
+                    S.sg_prev[S.hist[j]] = dt[j];
+                    S.yg_prev[S.hist[j]] = dt[MAXHIST + j];
+                }
+                double Rm[MAXHIST * MAXHIST], YYm[MAXHIST * MAXHIST], sg[MAXHIST], yg[MAXHIST];
+                for (int a = 0; a < k; ++a) {
+                    sg[a] = dt[a];
+                    yg[a] = dt[MAXHIST + a];
+                    for (int c = 0; c < k; ++c) {
+                        Rm[a * k + c] = (a <= c) ? S.SY[S.hist[a]][S.hist[c]] : 0.0;
+                        YYm[a * k + c] = S.YY[S.hist[a]][S.hist[c]];
+                    }
+                }
+                double cg, cS[MAXHIST], cY[MAXHIST];
+                if (lbfgs_compact_coeffs(k, Rm, YYm, sg, yg, S.gamma, &cg, cS, cY)) {
+                    S.coef_g = cg;
+                    for (int a = 0; a < k; ++a) {
+                        S.coefS[a] = cS[a];
+                        S.coefY[a] = cY[a];
+                    }
+                } else {
+                    S.nhist = 0;
+                    S.iter = 0;
+                }
+            }
+            for (int a = 0; a < Q; ++a) {
+                double v = S.coef_g * eg[a];
+                for (int j = 0; j < S.nhist; ++j)
+                    v += S.coefS[j] * S.eta_s[S.hist[j]][a] + S.coefY[j] * S.eta_y[S.hist[j]][a];
+                S.eta_d[a] = v;
+            }
+            // the next accepted step fills a ring position outside the live history
+            int pos = 0;
+            for (bool used = true; used;) {
+                used = false;
+                for (int j = 0; j < S.nhist; ++j) used = used || S.hist[j] == pos;
+                if (used) ++pos;
+            }
+            S.ring_new = pos;
+            S.push = 1;
+            S.phase = DC_STEP;
+        }
+    }
+    __syncwarp();
+    {
+        unsigned long long *dst = reinterpret_cast<unsigned long long *>(ctl + b);
+        const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&S);
+        for (int k = threadIdx.x; k < CTL_WORDS; k += 32) dst[k] = src[k];
+    }
+    if (threadIdx.x == 0) write_summary(S, sum[b]);
+}
+
+// After an exact max-norm check (k_dual_gmax): the slot's max|g| is the J
+// part's maximum and |g_h|; stop with status 0 below the threshold, or with
+// status 2 on a pending relative-norm stop (SuperDCA: plmDCA.hpp:218-221).
+__global__ void k_dual_check_apply(DualCtl *__restrict__ ctl, DualSum *__restrict__ sum,
+                                   const int32_t *__restrict__ list, int n, double gtol,
+                                   const double *__restrict__ acc)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int b = list[t];
+    DualCtl &S = ctl[b];
+    if (S.phase == DC_STOP) return;
+    const double *eg = S.eta_g[S.gcur];
+    double gm = acc[(int64_t)b * NACC + ACC_GMAX];
+    for (int a = 0; a < Q; ++a) gm = fmax(gm, fabs(eg[a]));
+    const double gnorm = sqrt(fmax(S.g2, 0.0));
+    S.gmax = gm;
+    S.chk_ratio = gnorm > 0.0 ? gm / gnorm : 0.0;
+    S.last_check = S.iterations;
+    S.chk_wait = 0;
+    S.want_check = 0;
+    if (gm < gtol) {
+        S.status = 0;
+        S.phase = DC_STOP;
+    } else if (S.releps_stop) {
+        S.status = 2;
+        S.phase = DC_STOP;
+    }
+    write_summary(S, sum[b]);
+}
+
 unsigned grid_for(int64_t elems, int per_block_elems, int cap)
 {
     const int64_t g = (elems + per_block_elems - 1) / per_block_elems;
@@ -573,63 +1003,48 @@ void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8
                                      1.0 / qscale, KR);
 }
 
-void launch_dual_grad(const Problem &P, const SlotDev *sd, const int32_t *list, int n, double qscale,
+void launch_dual_grad(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, double qscale,
                       const int32_t *rq, const float2 *KR, float2 *dv, double *acc, double *amax, cudaStream_t st)
 {
     if (n <= 0) return;
     const int NV = DV_S + 2 * P.ring;
     dim3 gg(grid_for(P.Nx * 4, 256 * 8, 64), n);
-    k_dual_grad<<<gg, 256, 0, st>>>(sd, list, P.Nx, NV, P.ring, P.lambda_J, rq, 1.0 / qscale, KR, dv, acc, amax);
+    k_dual_grad<<<gg, 256, 0, st>>>(ctl, list, P.Nx, NV, P.ring, P.lambda_J, rq, 1.0 / qscale, KR, dv, acc, amax);
 }
 
-void launch_dual_dots(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int newg, const float2 *dv,
+void launch_dual_dots(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int newg, const float2 *dv,
                       double *dots, cudaStream_t st)
 {
     if (n <= 0) return;
     dim3 g((unsigned)((P.Nx * 4 + DOT_CHUNK - 1) / DOT_CHUNK), n);
-    k_dual_dots<<<g, 256, 0, st>>>(sd, list, P.Nx, DV_S + 2 * P.ring, P.ring, newg, dv, dots);
+    k_dual_dots<<<g, 256, 0, st>>>(ctl, list, P.Nx, DV_S + 2 * P.ring, P.ring, newg, dv, dots);
 }
 
-void launch_dual_direction(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float2 *dv,
+void launch_dual_direction(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
                            const float2 *lbase, float *P0, const float *w, const uint8_t *rstate, float2 *u,
-                           float *ud, double *acc, cudaStream_t st)
+                           float *ud, double *dacc, cudaStream_t st)
 {
     if (n <= 0) return;
     dim3 g(grid_for(P.Nx * 4, 256 * 8, 32), n);
-    k_dual_direction<<<g, 256, 0, st>>>(sd, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, P.ring, dv,
+    k_dual_direction<<<g, 256, 0, st>>>(ctl, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, P.ring, dv,
                                         lbase, P0, w,
-                                        rstate, u, ud, acc);
+                                        rstate, u, ud, dacc);
 }
 
-void launch_trial_delta(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float2 *lbase,
-                        const float2 *u, const float *ud, const uint8_t *rstate, const float *w, const float *P0,
-                        float *R, double *acc, cudaStream_t st)
-{
-    if (n <= 0) return;
-    // a few sequences per thread keep the block sums a small part of the work
-    int gx = (int)((P.N + 4 * DT_THREADS - 1) / (4 * DT_THREADS));
-    if (gx > 32) gx = 32;
-    dim3 grid((unsigned)gx, (unsigned)n);
-    k_trial_delta<<<grid, DT_THREADS, 0, st>>>(sd, list, (int)P.N, P.Nx, lbase, u,
-                                               reinterpret_cast<const float4 *>(ud), rstate, w,
-                                               reinterpret_cast<const float4 *>(P0), reinterpret_cast<float4 *>(R),
-                                               acc);
-}
-
-void launch_dual_accept(const Problem &P, const SlotDev *sd, const int32_t *list, int n, float2 *dv,
+void launch_dual_accept(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
                         const float2 *u, float2 *lbase, cudaStream_t st)
 {
     if (n <= 0) return;
     dim3 g(grid_for(P.Nx * 4, 256 * 4, 64), n);
-    k_dual_accept<<<g, 256, 0, st>>>(sd, list, P.Nx, DV_S + 2 * P.ring, dv, u, lbase);
+    k_dual_accept<<<g, 256, 0, st>>>(ctl, list, P.Nx, DV_S + 2 * P.ring, dv, u, lbase);
 }
 
-void launch_dual_to_r(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int which,
+void launch_dual_to_r(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int which,
                       const float2 *dv, float *R, cudaStream_t st)
 {
     if (n <= 0) return;
     dim3 g(grid_for(P.Nx, 256 * 4, 64), n);
-    k_dual_to_r<<<g, 256, 0, st>>>(sd, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, which, dv,
+    k_dual_to_r<<<g, 256, 0, st>>>(ctl, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, which, dv,
                                    reinterpret_cast<float4 *>(R));
 }
 
@@ -664,6 +1079,33 @@ void launch_dual_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list,
     if (n <= 0) return;
     dim3 g(grid_for(P.Dp, 256 * 16, 256), n);
     k_dual_to_wa<<<g, 256, 0, st>>>(sd, list, (int)P.L, P.Dp, reinterpret_cast<const long long *>(J64), wa);
+}
+
+void launch_dual_linesearch(const Problem &P, DualCtl *ctl, const int32_t *list, int n, const double *dacc,
+                            float2 *dv, const float2 *lbase, float2 *u, float *ud, const uint8_t *rstate,
+                            const float *w, const float *P0, float *R, double *acc, cudaStream_t st)
+{
+    if (n <= 0) return;
+    k_dual_linesearch<<<n, LS_THREADS, 0, st>>>(ctl, list, (int)P.N, P.Nx, DV_S + 2 * P.ring, P.lambda_J,
+                                               P.lambda_h, dacc, dv, lbase, u, reinterpret_cast<float4 *>(ud),
+                                               rstate, w, reinterpret_cast<const float4 *>(P0),
+                                               reinterpret_cast<float4 *>(R), acc);
+}
+
+void launch_dual_control(const Problem &P, DualCtl *ctl, DualSum *sum, const int32_t *list, int n,
+                         int max_iterations, double gtol, const double *acc, const double *amax, const double *dots,
+                         cudaStream_t st)
+{
+    if (n <= 0) return;
+    k_dual_control<<<n, 32, 0, st>>>(ctl, sum, list, P.m, max_iterations, gtol, P.lambda_J, P.lambda_h, acc, amax,
+                                     dots);
+}
+
+void launch_dual_check_apply(DualCtl *ctl, DualSum *sum, const int32_t *list, int n, double gtol, const double *acc,
+                             cudaStream_t st)
+{
+    if (n <= 0) return;
+    k_dual_check_apply<<<(n + 63) / 64, 64, 0, st>>>(ctl, sum, list, n, gtol, acc);
 }
 
 } // namespace sdca

@@ -11,8 +11,16 @@
 // with R = upper triangle of S^T Y (diagonal D).  Mathematically identical to
 // the two-loop recursion; it needs only the dot products S^T g, Y^T g and the
 // small Gram matrices, so the device reads the history twice per iteration
-// (dots, then the direction) instead of 4m times.
+// (dots, then the direction) instead of 4m times.  The same code runs on the
+// host (tensor-core and plain forms) and on the device (the dual form's
+// control kernel).
 #pragma once
+
+#ifdef __CUDACC__
+#define SDCA_HD_L __host__ __device__
+#else
+#define SDCA_HD_L
+#endif
 
 namespace sdca {
 
@@ -20,7 +28,7 @@ namespace sdca {
 // YY: k x k, YY[a*k+b] = y_a . y_b.  sg[a] = s_a . g, yg[a] = y_a . g.
 // Output d = coef_g g + sum_a coefS[a] s_a + coefY[a] y_a  (= -H g).
 // Returns false if R is singular.
-inline bool lbfgs_compact_coeffs(int k, const double *R, const double *YY, const double *sg,
+SDCA_HD_L inline bool lbfgs_compact_coeffs(int k, const double *R, const double *YY, const double *sg,
                                  const double *yg, double gamma, double *coef_g, double *coefS,
                                  double *coefY)
 {

@@ -11,13 +11,25 @@
 // The search is written as a state machine so that every slot of a batch can
 // hold its own search: start() gives the first trial step, each feed() takes
 // f and g.s at the last trial and either asks for another step or finishes.
-// The accepted point is always the last trial evaluated.
+// The accepted point is always the last trial evaluated.  The same code runs
+// on the host (tensor-core and plain forms) and on the device (the dual
+// form's line-search kernel, one search per thread block).
 #pragma once
 
-#include <algorithm>
-#include <cmath>
+#include <math.h>
+
+#ifdef __CUDACC__
+#define SDCA_HD __host__ __device__
+#else
+#define SDCA_HD
+#endif
 
 namespace sdca {
+
+// std::min / std::max semantics (the first operand wins ties and NaN
+// comparisons), usable in device code
+SDCA_HD inline double mt_min(double a, double b) { return (b < a) ? b : a; }
+SDCA_HD inline double mt_max(double a, double b) { return (a < b) ? b : a; }
 
 class MoreThuente {
 public:
@@ -27,7 +39,7 @@ public:
     int nfev = 0;    // trials evaluated
     int info = 0;
 
-    Result start(double f0, double dg0, double stp0)
+    SDCA_HD Result start(double f0, double dg0, double stp0)
     {
         stp = stp0;
         nfev = 0;
@@ -47,7 +59,7 @@ public:
         return NEED_EVAL;
     }
 
-    Result feed(double f, double dg)
+    SDCA_HD Result feed(double f, double dg)
     {
         nfev++;
         const double ftest1 = finit + stp * dgtest;
@@ -56,9 +68,9 @@ public:
         if ((stp == kStpmin) && ((f > ftest1) || (dg >= dgtest))) info = 4;
         if (nfev >= kMaxfev) info = 3;
         if (brackt && (stmax - stmin <= kXtol * stmax)) info = 2;
-        if ((f <= ftest1) && (std::fabs(dg) <= kGtol * (-dginit))) info = 1;
+        if ((f <= ftest1) && (fabs(dg) <= kGtol * (-dginit))) info = 1;
         if (info != 0) return DONE;
-        if (stage1 && (f <= ftest1) && (dg >= std::min(kFtol, kGtol) * dginit)) stage1 = false;
+        if (stage1 && (f <= ftest1) && (dg >= mt_min(kFtol, kGtol) * dginit)) stage1 = false;
         if (stage1 && (f <= fx) && (f > ftest1)) {
             // modified function psi(stp) = f(stp) - f(0) - stp * dgtest
             const double fm = f - stp * dgtest;
@@ -74,9 +86,9 @@ public:
             step(stx, fx, dgx, sty, fy, dgy, stp, f, dg);
         }
         if (brackt) {
-            if (std::fabs(sty - stx) >= 0.66 * width1) stp = stx + 0.5 * (sty - stx);
+            if (fabs(sty - stx) >= 0.66 * width1) stp = stx + 0.5 * (sty - stx);
             width1 = width;
-            width = std::fabs(sty - stx);
+            width = fabs(sty - stx);
         }
         prepare();
         return NEED_EVAL;
@@ -93,62 +105,62 @@ private:
     double stx = 0, fx = 0, dgx = 0, sty = 0, fy = 0, dgy = 0, stmin = 0, stmax = 0;
 
     // interval of uncertainty and safeguards for the next trial
-    void prepare()
+    SDCA_HD void prepare()
     {
         if (brackt) {
-            stmin = std::min(stx, sty);
-            stmax = std::max(stx, sty);
+            stmin = mt_min(stx, sty);
+            stmax = mt_max(stx, sty);
         } else {
             stmin = stx;
             stmax = stp + kXtrapf * (stp - stx);
         }
-        stp = std::max(stp, kStpmin);
-        stp = std::min(stp, kStpmax);
+        stp = mt_max(stp, kStpmin);
+        stp = mt_min(stp, kStpmax);
         if ((brackt && ((stp <= stmin) || (stp >= stmax))) || (nfev >= kMaxfev - 1) ||
             (infoc == 0) || (brackt && ((stmax - stmin) <= (kXtol * stmax))))
             stp = stx;
     }
 
     // safeguarded step: minimiser of a cubic or quadratic interpolant
-    void step(double &sx, double &fxv, double &dx, double &sy, double &fyv, double &dy,
-              double &st, double fp, double dp)
+    SDCA_HD void step(double &sx, double &fxv, double &dx, double &sy, double &fyv, double &dy,
+                      double &st, double fp, double dp)
     {
         infoc = 0;
-        if ((brackt && ((st <= std::min(sx, sy)) || (st >= std::max(sx, sy)))) ||
+        if ((brackt && ((st <= mt_min(sx, sy)) || (st >= mt_max(sx, sy)))) ||
             (dx * (st - sx) >= 0.0) || (stmax < stmin))
             return;
         bool bound = false;
-        const double sgnd = dp * (dx / std::fabs(dx));
+        const double sgnd = dp * (dx / fabs(dx));
         double stpf, stpc, stpq;
         if (fp > fxv) {
             infoc = 1;
             bound = true;
             const double theta = 3.0 * (fxv - fp) / (st - sx) + dx + dp;
-            const double s = std::max(std::fabs(theta), std::max(std::fabs(dx), std::fabs(dp)));
-            double gamma = s * std::sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+            const double s = mt_max(fabs(theta), mt_max(fabs(dx), fabs(dp)));
+            double gamma = s * sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
             if (st < sx) gamma = -gamma;
             const double p = (gamma - dx) + theta, q = ((gamma - dx) + gamma) + dp;
             stpc = sx + (p / q) * (st - sx);
             stpq = sx + ((dx / ((fxv - fp) / (st - sx) + dx)) / 2.0) * (st - sx);
-            stpf = (std::fabs(stpc - sx) < std::fabs(stpq - sx)) ? stpc : stpc + (stpq - stpc) / 2.0;
+            stpf = (fabs(stpc - sx) < fabs(stpq - sx)) ? stpc : stpc + (stpq - stpc) / 2.0;
             brackt = true;
         } else if (sgnd < 0.0) {
             infoc = 2;
             const double theta = 3.0 * (fxv - fp) / (st - sx) + dx + dp;
-            const double s = std::max(std::fabs(theta), std::max(std::fabs(dx), std::fabs(dp)));
-            double gamma = s * std::sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+            const double s = mt_max(fabs(theta), mt_max(fabs(dx), fabs(dp)));
+            double gamma = s * sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
             if (st > sx) gamma = -gamma;
             const double p = (gamma - dp) + theta, q = ((gamma - dp) + gamma) + dx;
             stpc = st + (p / q) * (sx - st);
             stpq = st + (dp / (dp - dx)) * (sx - st);
-            stpf = (std::fabs(stpc - st) > std::fabs(stpq - st)) ? stpc : stpq;
+            stpf = (fabs(stpc - st) > fabs(stpq - st)) ? stpc : stpq;
             brackt = true;
-        } else if (std::fabs(dp) < std::fabs(dx)) {
+        } else if (fabs(dp) < fabs(dx)) {
             infoc = 3;
             bound = true;
             const double theta = 3.0 * (fxv - fp) / (st - sx) + dx + dp;
-            const double s = std::max(std::fabs(theta), std::max(std::fabs(dx), std::fabs(dp)));
-            double gamma = s * std::sqrt(std::max(0.0, (theta / s) * (theta / s) - (dx / s) * (dp / s)));
+            const double s = mt_max(fabs(theta), mt_max(fabs(dx), fabs(dp)));
+            double gamma = s * sqrt(mt_max(0.0, (theta / s) * (theta / s) - (dx / s) * (dp / s)));
             if (st > sx) gamma = -gamma;
             const double p = (gamma - dp) + theta, q = (gamma + (dx - dp)) + gamma;
             const double r = p / q;
@@ -156,14 +168,14 @@ private:
             else if (st > sx) stpc = stmax;
             else stpc = stmin;
             stpq = st + (dp / (dp - dx)) * (sx - st);
-            if (brackt) stpf = (std::fabs(st - stpc) < std::fabs(st - stpq)) ? stpc : stpq;
-            else stpf = (std::fabs(st - stpc) > std::fabs(st - stpq)) ? stpc : stpq;
+            if (brackt) stpf = (fabs(st - stpc) < fabs(st - stpq)) ? stpc : stpq;
+            else stpf = (fabs(st - stpc) > fabs(st - stpq)) ? stpc : stpq;
         } else {
             infoc = 4;
             if (brackt) {
                 const double theta = 3.0 * (fp - fyv) / (sy - st) + dy + dp;
-                const double s = std::max(std::fabs(theta), std::max(std::fabs(dy), std::fabs(dp)));
-                double gamma = s * std::sqrt((theta / s) * (theta / s) - (dy / s) * (dp / s));
+                const double s = mt_max(fabs(theta), mt_max(fabs(dy), fabs(dp)));
+                double gamma = s * sqrt((theta / s) * (theta / s) - (dy / s) * (dp / s));
                 if (st > sy) gamma = -gamma;
                 const double p = (gamma - dp) + theta, q = ((gamma - dp) + gamma) + dy;
                 stpc = st + (p / q) * (sy - st);
@@ -178,12 +190,12 @@ private:
             if (sgnd < 0.0) { sy = sx; fyv = fxv; dy = dx; }
             sx = st; fxv = fp; dx = dp;
         }
-        stpf = std::min(stmax, stpf);
-        stpf = std::max(stmin, stpf);
+        stpf = mt_min(stmax, stpf);
+        stpf = mt_max(stmin, stpf);
         st = stpf;
         if (brackt && bound) {
-            if (sy > sx) st = std::min(sx + 0.66 * (sy - sx), st);
-            else st = std::max(sx + 0.66 * (sy - sx), st);
+            if (sy > sx) st = mt_min(sx + 0.66 * (sy - sx), st);
+            else st = mt_max(sx + 0.66 * (sy - sx), st);
         }
     }
 };
