@@ -71,6 +71,12 @@ def parse():
     ap.add_argument("--plain-loci", type=int, default=64, help="loci timed in the plain-form arm")
     ap.add_argument("--accuracy-sample", type=int, default=16,
                     help="loci of the first timed step checked against the FP64 oracle (0: none)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the autotuner (default when --batch/--lanes are not given: measure them on a "
+                         "probe list of loci outside the timed steps)")
+    ap.add_argument("--tune-loci", type=int, default=16384, help="loci the autotuner may solve as probes")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the skewed 616 x 78,700 workload measured after the headline")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--cache-dir", default="", help="keep the generated alignment here between runs")
@@ -307,6 +313,45 @@ def nfeval_reference(workload):
     return float(np.median(d["nfeval"])), d
 
 
+def secondary_skewed(args, local, steps=3, warmup=1, seed=2):
+    """The uneven-convergence workload: 616 sequences x 78,700 generated loci
+    (MAF from Beta(0.5, 2), 10 % multi-allelic loci, gaps up to 15 %), GPU
+    sequence weights, autotuned batch and lanes, and the distribution of
+    iterations per locus.  Device time from CUDA events, as the headline."""
+    from superdca_gb300 import Engine, FORM_DUAL, autotune, synthetic
+
+    t0 = time.time()
+    st, _, _ = synthetic.workload("skewed-616x78700", seed=seed)
+    N, L = st.shape
+    with Engine(N, L, batch=64, device=local, form=FORM_DUAL) as E0:
+        w = E0.compute_weights(st, 0.9)
+    order = (np.arange(L) * 7919) % L
+    tr = autotune(st, w, order[L - min(16384, L // 4):], form=FORM_DUAL, max_fraction=1.0, device=local,
+                  want_scores=False)
+    B, lanes = (tr.batch, tr.lanes) if tr.batch > 0 else (512, 4)
+    per_step = 2 * B * lanes
+    iters, statuses, dev_ms = [], [], 0.0
+    with Engine(N, L, batch=B, lanes=lanes, device=local, form=FORM_DUAL) as E:
+        E.set_alignment(st, w)
+        for s in range(warmup + steps):
+            res = E.solve(order[s * per_step:(s + 1) * per_step], want_scores=True)
+            if s >= warmup:
+                dev_ms += E.profile()["solve_ms"]
+                iters += res.iterations.tolist()
+                statuses += res.status.tolist()
+    it = np.array(iters)
+    return {"workload": f"skewed-616x78700 seed {seed}", "N": int(N), "L": int(L), "batch": B, "lanes": lanes,
+            "value": round(steps * per_step / (dev_ms / 1e3), 2), "unit": "loci/s", "steps": steps,
+            "warmup": warmup, "loci_per_step": per_step, "weights": "GPU reweighting, threshold 0.9",
+            "iterations": {"median": float(np.median(it)), "p10": float(np.percentile(it, 10)),
+                           "p90": float(np.percentile(it, 90)), "max": int(it.max()), "min": int(it.min())},
+            "status_counts": {str(k): statuses.count(k) for k in sorted(set(statuses))},
+            "autotune": {"chosen": [tr.batch, tr.lanes], "probe_loci": tr.n_done,
+                         "candidates": [{k: (round(v, 1) if isinstance(v, float) else v) for k, v in e.items()}
+                                        for e in tr.entries]},
+            "seconds": round(time.time() - t0, 1)}
+
+
 def engine_arm(args):
     world, rank, local = dist()
     import torch
@@ -316,15 +361,30 @@ def engine_arm(args):
 
         torch.cuda.set_device(local)
         tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from superdca_gb300 import Engine, FORM_DUAL, FORM_GATHER, FORM_TC
+    from superdca_gb300 import Engine, FORM_DUAL, FORM_GATHER, FORM_TC, autotune
 
     st = load_workload(args)
     N, L = st.shape
     w = np.ones(N)
+    form = {"tc": FORM_TC, "gather": FORM_GATHER, "dual": FORM_DUAL}[args.form]
+    tune = None
+    if not args.no_autotune and not args.batch and not args.lanes and args.tune_loci > 0:
+        # batch and lanes measured on probe loci taken from the end of the
+        # locus order the steps walk (the timed steps start at its front)
+        t_tune = time.time()
+        order = (np.arange(L) * 7919) % L
+        probe = order[L - min(args.tune_loci, L):]
+        tr = autotune(st, w, probe, form=form, max_fraction=1.0, device=local, want_scores=False)
+        tune = {"chosen": [tr.batch, tr.lanes], "probe_loci": tr.n_done, "seconds": round(time.time() - t_tune, 2),
+                "candidates": [{k: (round(v, 1) if isinstance(v, float) else v) for k, v in e.items()}
+                               for e in tr.entries],
+                "how": ("sdca_autotune: each candidate (batch, lanes) solves 2 x its slots of the probe loci; the "
+                        "most L-BFGS iterations per device second wins; untimed, before the warm-up")}
+        if tr.batch > 0 and tr.lanes > 0:
+            args.batch, args.lanes = tr.batch, tr.lanes
     B = args.batch or (512 if args.form == "dual" else 64)
     lanes = args.lanes or (4 if args.form == "dual" else 1)
     per_step = args.loci_per_step or 2 * B * lanes   # slots refill once per step
-    form = {"tc": FORM_TC, "gather": FORM_GATHER, "dual": FORM_DUAL}[args.form]
     E = Engine(N, L, batch=B, device=local, form=form, history_bf16=args.history_bf16, lanes=lanes)
     E.set_alignment(st, w)
     ws = None if args.warm_start in ("", "none") or args.form == "dual" else args.warm_start
@@ -517,14 +577,17 @@ def engine_arm(args):
                           f"{B * lanes} slots)"),
                    "parallelism": f"loci sharded over {world} rank(s)"},
         "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": rf,
-        "accuracy": accuracy, "vs_plain": vs_plain, "reweighting": rw,
+        "accuracy": accuracy, "vs_plain": vs_plain, "autotune": tune, "reweighting": rw,
         "kernel_ms": {k: round(v, 2) for k, v in tot["kernel_ms"].items()},
+        "kernel_launches": dict(tot["kernel_launches"]), "kernel_units": dict(tot["kernel_units"]),
         "solver": {"median_nfeval": float(np.median(nfe)), "median_iterations": float(np.median(iters)),
                    "p90_iterations": float(np.percentile(iters, 90)), "max_iterations": int(np.max(iters)),
                    "median_contractions": float(np.median(contr)),
                    "status_counts": {str(k): statuses.count(k) for k in sorted(set(statuses))},
                    "wall_s": round(wall, 2), "wall_s_per_step": [round(v, 3) for v in walls]},
     }
+    if rank == 0 and world == 1 and not args.no_secondary and args.form == "dual":
+        out["secondary"] = secondary_skewed(args, local)
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         spe, n_eval, t_cpu = cpu_eval_rate(st, args.cpu_seconds, threads)

@@ -176,6 +176,38 @@ int sdca_solve_sel(sdca_handle *h, const uint32_t *loci, size_t n_loci, const do
  * g may be NULL. */
 int sdca_eval(sdca_handle *h, uint32_t r, const double *x, double *f, double *g);
 
+/* ---- Autotuner.  SuperDCA balances its loci with TBB, grain 1
+ * (SuperDCA/include/plmDCA.hpp:581-586); the engine's counterpart is the
+ * choice of sdca_config.batch (slots per lane) and sdca_config.lanes.
+ * sdca_autotune solves the first loci of `loci` with candidate (batch,
+ * lanes) pairs in turn -- each probe holds twice its candidate's slots --
+ * and picks the pair that ran the most L-BFGS iterations per device second.
+ * The probe loci are solved for real: their score rows (n_loci x L, may be
+ * NULL) and statistics (may be NULL) are written, and *n_done tells how many
+ * leading entries of `loci` are done (at most max_fraction of n_loci;
+ * candidates whose probe does not fit in that budget are skipped).  *best
+ * is *base with the chosen batch and lanes.  cache_path (may be NULL): a
+ * text file that keeps one choice per (N, L, form, device, free-memory
+ * class); a cached choice is returned at once with *n_done = 0.  entries
+ * (may be NULL; SDCA_TUNE_MAX_ENTRIES of them) and *n_entries report every
+ * candidate: status SDCA_OK (measured), SDCA_E_NOMEM (did not fit on the
+ * device) or SDCA_E_ARG (no room left in the probe budget). */
+#define SDCA_TUNE_MAX_ENTRIES 16
+
+typedef struct {
+    int32_t batch;             /* slots per lane */
+    int32_t lanes;             /* solver lanes */
+    int32_t n_loci;            /* loci its probe solved (0: not measured) */
+    int32_t status;            /* SDCA_OK, or why it was not measured */
+    double device_ms;          /* device time of the probe (CUDA events) */
+    double iterations_per_s;   /* L-BFGS iterations of the probe per device second */
+} sdca_tune_entry;
+
+int sdca_autotune(const sdca_config *base, const uint8_t *states, const double *weights,
+                  const uint32_t *loci, size_t n_loci, double max_fraction, const char *cache_path,
+                  float *scores, sdca_locus_stat *stats, size_t *n_done, sdca_config *best,
+                  sdca_tune_entry *entries, int32_t *n_entries);
+
 /* Device timings and counters of the last sdca_solve* call. */
 int sdca_get_profile(const sdca_handle *h, sdca_profile *out);
 

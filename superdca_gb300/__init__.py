@@ -6,4 +6,4 @@ alignment encoding and the seeded synthetic workloads used by the tests and
 the benchmark.
 """
 from ._lib import EngineError, FORM_DUAL, FORM_GATHER, FORM_TC  # noqa: F401
-from .engine import Engine, SolveResult, coupling_lines, format_coupling_lines  # noqa: F401
+from .engine import Engine, SolveResult, TuneResult, autotune, coupling_lines, format_coupling_lines  # noqa: F401

@@ -33,7 +33,7 @@ EXPORTS = ["sdca_abi_version", "sdca_config_default", "sdca_create", "sdca_set_a
            "sdca_compute_weights", "sdca_get_lambdas", "sdca_solve", "sdca_solve_ex", "sdca_solve_sel", "sdca_eval",
            "sdca_get_profile", "sdca_last_error", "sdca_destroy", "sdca_eval_noalloc",
            "sdca_set_warm_start", "sdca_ws_features", "sdca_mlp_blob_size", "sdca_mlp_grad",
-           "sdca_mlp_predict", "sdca_mlp_train", "sdca_mlp_last_error", "sdca_set_targets"]
+           "sdca_mlp_predict", "sdca_mlp_train", "sdca_mlp_last_error", "sdca_set_targets", "sdca_autotune"]
 
 
 class Config(C.Structure):
@@ -50,6 +50,14 @@ class LocusStat(C.Structure):
                 ("nfeval", C.c_int32), ("contractions", C.c_int32), ("status", C.c_int32),
                 ("restarts", C.c_int32), ("skipped_pairs", C.c_int32), ("weak_searches", C.c_int32),
                 ("max_trials", C.c_int32)]
+
+
+class TuneEntry(C.Structure):
+    _fields_ = [("batch", C.c_int32), ("lanes", C.c_int32), ("n_loci", C.c_int32), ("status", C.c_int32),
+                ("device_ms", C.c_double), ("iterations_per_s", C.c_double)]
+
+
+TUNE_MAX_ENTRIES = 16
 
 
 class Profile(C.Structure):
@@ -89,6 +97,8 @@ def load(path: str = LIB_PATH):
     L.sdca_eval_noalloc.argtypes = [vp, i64, i64, vp, dp, dp, C.c_uint32, vp, vp, vp, vp]
     L.sdca_set_warm_start.argtypes = [vp, vp, C.c_size_t]
     L.sdca_set_targets.argtypes = [vp, vp, i64]
+    L.sdca_autotune.argtypes = [C.POINTER(Config), vp, vp, vp, C.c_size_t, dp, C.c_char_p, vp, vp,
+                                C.POINTER(C.c_size_t), C.POINTER(Config), vp, C.POINTER(C.c_int32)]
     L.sdca_ws_features.argtypes = [vp, C.c_int, C.c_float, vp, C.c_size_t, vp, C.c_size_t, vp]
     L.sdca_mlp_blob_size.argtypes = []
     L.sdca_mlp_grad.argtypes = [vp, vp, vp, i64, C.POINTER(dp), vp]

@@ -21,7 +21,7 @@ CLI = os.path.join(HERE, "superdca-gb300")
 CLI_SOURCES = [os.path.join(HERE, "cli", "superdca_gb300_cli.cpp")]
 
 SOURCES = ["engine.cu", "kernels_gather.cu", "kernels_solver.cu", "kernels_tc.cu", "kernels_weights.cu",
-           "noalloc.cu", "mlp.cu", "warmstart.cu", "kernels_dual.cu"]
+           "noalloc.cu", "mlp.cu", "warmstart.cu", "kernels_dual.cu", "autotune.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr",
          "-I" + os.path.join(ROOT, "include")]

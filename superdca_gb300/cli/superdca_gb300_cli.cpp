@@ -71,9 +71,12 @@ const char *USAGE =
     "  --gpu-device arg (=0)              CUDA device.\n"
     "  --gpu-form arg (=dual)             Engine form: dual (span of the sequences), tc (tensor-core\n"
     "                                     contractions) or plain.\n"
-    "  --gpu-batch arg                    Loci solved together per lane (256 dual, 64 otherwise).\n"
+    "  --gpu-batch arg                    Loci solved together per lane (default: autotuned;\n"
+    "                                     512 dual, 64 otherwise without the autotuner).\n"
     "  --gpu-lanes arg                    Solver lanes, each with its own stream and host thread\n"
-    "                                     (4 dual, 1 otherwise).\n"
+    "                                     (default: autotuned; 4 dual, 1 otherwise without it).\n"
+    "  --gpu-no-autotune                  Do not measure batch and lanes on the first loci.\n"
+    "  --gpu-tune-cache arg               File that keeps the autotuner's choice per shape.\n"
     "  --gpu-history arg (=fp32)          L-BFGS history storage: fp32 or bf16.\n"
     "  --gpu-chunk arg (=4096)            Loci per solve call (bounds host memory).\n"
     "  --gpu-top-k arg (=0)               Write only the K strongest pairs, strongest first.\n"
@@ -97,6 +100,8 @@ struct Options {
     int device = 0, batch = 0, lanes = 0, form = SDCA_FORM_DUAL;
     bool history_bf16 = false, binary_output = false;
     long chunk = 4096, top_k = 0;
+    bool no_autotune = false;
+    std::string tune_cache;
 };
 
 [[noreturn]] void fail(const std::string &msg)
@@ -134,6 +139,7 @@ Options parse_options(int argc, char **argv)
         {"no-reweighting", &o.no_reweighting}, {"output-weights", &o.output_weights},
         {"norm-of-mean-scoring", &o.norm_of_mean}, {"no-dca", &o.no_dca},
         {"no-coupling-output", &o.no_coupling_output}, {"gpu-binary-output", &o.binary_output},
+        {"gpu-no-autotune", &o.no_autotune},
     };
     for (int i = 1; i < argc; ++i) {
         std::string a = argv[i];
@@ -187,6 +193,7 @@ Options parse_options(int argc, char **argv)
         else if (name == "gpu-device") o.device = parse_number<int>(opt, value);
         else if (name == "gpu-batch") o.batch = parse_number<int>(opt, value);
         else if (name == "gpu-lanes") o.lanes = parse_number<int>(opt, value);
+        else if (name == "gpu-tune-cache") o.tune_cache = value;
         else if (name == "gpu-chunk") o.chunk = parse_number<long>(opt, value);
         else if (name == "gpu-top-k") o.top_k = parse_number<long>(opt, value);
         else if (name == "gpu-form") {
@@ -723,9 +730,9 @@ int main(int argc, char **argv)
 
     const bool need_gpu = !o.no_reweighting || !o.no_dca;
     Handle H;
+    sdca_config cfg;
+    sdca_config_default(&cfg);
     if (need_gpu) {
-        sdca_config cfg;
-        sdca_config_default(&cfg);
         cfg.n_seqs = N;
         cfg.n_loci = L;
         cfg.lambda_h = o.lambda_h;
@@ -738,7 +745,7 @@ int main(int argc, char **argv)
             cfg.form = SDCA_FORM_TC;
         }
         const bool dual = cfg.form == SDCA_FORM_DUAL;
-        cfg.batch = o.batch > 0 ? o.batch : (dual ? 256 : 64);
+        cfg.batch = o.batch > 0 ? o.batch : (dual ? 512 : 64);
         cfg.lanes = o.lanes > 0 ? o.lanes : (dual ? 4 : 1);
         cfg.flags = o.history_bf16 ? SDCA_FLAG_HISTORY_BF16 : 0;
         cfg.device = o.device;
@@ -824,10 +831,48 @@ int main(int argc, char **argv)
     std::vector<double> xs;
     std::vector<sdca_locus_stat> stats;
     size_t not_converged = 0;
+    size_t start = 0;
+    // Without --gpu-batch / --gpu-lanes the first loci (at most a quarter of
+    // the list, and at most 4 GB of score rows) are solved with candidate
+    // configurations in turn, and the rest with the fastest.  Norm-of-mean
+    // scoring needs every solution, which the probes do not return.
+    if (!o.no_autotune && o.batch <= 0 && o.lanes <= 0 && !o.norm_of_mean) {
+        const size_t prefix = std::min(n / 4, (size_t)((1ull << 30) / (uint64_t)L));
+        rows.resize(prefix * (size_t)L);
+        stats.resize(std::max<size_t>(prefix, 1));
+        sdca_config best;
+        size_t done = 0;
+        sdca_tune_entry ents[SDCA_TUNE_MAX_ENTRIES];
+        int32_t nent = 0;
+        check(sdca_autotune(&cfg, states.data(), weights.data(), loci.data(), prefix, 1.0,
+                            o.tune_cache.empty() ? nullptr : o.tune_cache.c_str(), rows.data(), stats.data(), &done,
+                            &best, ents, &nent),
+              nullptr, "autotuning failed");
+        for (size_t k = 0; k < done; ++k) {
+            for (size_t j = 0; j < n; ++j) S[k * n + j] = rows[k * (size_t)L + loci[j]];
+            not_converged += stats[k].status != 0;
+        }
+        if (o.verbose) {
+            for (int e = 0; e < nent; ++e)
+                if (ents[e].status == SDCA_OK)
+                    std::cout << "superdca-gb300: autotune batch " << ents[e].batch << " x " << ents[e].lanes
+                              << " lanes: " << ents[e].iterations_per_s << " iterations/s (" << ents[e].n_loci
+                              << " loci)\n";
+            std::cout << "superdca-gb300: using batch " << best.batch << " x " << best.lanes << " lanes\n";
+        }
+        if (best.batch != cfg.batch || best.lanes != cfg.lanes) {
+            sdca_destroy(H.h);
+            H.h = nullptr;
+            cfg = best;
+            check(sdca_create(&cfg, &H.h), nullptr, "engine set-up failed");
+            check(sdca_set_alignment(H.h, states.data(), weights.data()), H.h, "alignment upload failed");
+        }
+        start = done;
+    }
     // solutions are D doubles per locus: keep a chunk of them under ~1 GB
     const size_t chunk = o.norm_of_mean ? std::max<size_t>(1, std::min<size_t>((size_t)o.chunk, (1ull << 27) / D))
                                         : (size_t)o.chunk;
-    for (size_t k0 = 0; k0 < n; k0 += chunk) {
+    for (size_t k0 = start; k0 < n; k0 += chunk) {
         const size_t m = std::min(n - k0, chunk);
         rows.resize(m * (size_t)L);
         stats.resize(m);

@@ -86,6 +86,23 @@ __device__ __forceinline__ float2 df_from_ll(long long v)
     return make_float2(hi, __ll2float_rn(v - __float2ll_rn(hi)));
 }
 
+// 48 bits of a 64-bit integer (|v| < 2^62) from its 32-bit halves, with
+// 32-bit conversions and FP32 arithmetic only: v = hi 2^32 + lo, lo in
+// [0, 2^32) as 2^16 lo_h + lo_l, each part exact as a float or a
+// double-float, summed in double-float.
+__device__ __forceinline__ float2 df_from_ll_fast(long long v)
+{
+    const int hi = (int)(v >> 32);
+    const unsigned lo = (unsigned)(v & 0xffffffffll);
+    const float hh = __int2float_rn(hi);
+    const float hl = __int2float_rn(hi - __float2int_rn(hh));        // hi = hh + hl exactly (|hi| < 2^30)
+    const float lh = __uint2float_rn(lo >> 16) * 65536.0f;           // exact: < 2^32, 16 significant bits
+    const float ll = __uint2float_rn(lo & 0xffffu);                  // exact
+    float2 r = df_two_sum(hh * 4294967296.0f, hl * 4294967296.0f);   // powers of two: exact products
+    r = df_add(r, df_two_sum(lh, ll));
+    return r;
+}
+
 __device__ __forceinline__ float2 df_zero() { return make_float2(0.f, 0.f); }
 
 // value as a float (rounded)

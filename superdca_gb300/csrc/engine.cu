@@ -1307,6 +1307,10 @@ int dual_convert(sdca_handle *h, bool force)
         else if (ph != PH_EMPTY && ph != PH_FINALIZE) ++active;
     }
     if (fin.empty() || (!force && active > 0 && (int)fin.size() < std::min(16, P.Bmax))) return SDCA_OK;
+    // the three digit planes of up to Bmax / 3 slots go through one tensor-core
+    // pass (the one-hot operand is streamed once for all of them)
+    const int per_pass = P.Bmax / 3;
+    if (per_pass >= 1 && (int)fin.size() > per_pass) fin.resize(per_pass);
     for (int b : fin) {
         const SlotHost &S = h->slots[b];
         h->sd_h[b].tc_scale = S.amax_x > 0.0 ? std::ldexp(1.0, 32) / S.amax_x : 1.0;
@@ -1314,7 +1318,15 @@ int dual_convert(sdca_handle *h, bool force)
     }
     int rc = upload_slots(h, fin);
     if (rc) return rc;
-    {
+    if (per_pass >= 1) {
+        Timed t(h, SDCA_K_BACKWARD, 5, 3 * (int64_t)fin.size());
+        const int nf = (int)fin.size();
+        launch_dual_digits3(P, h->sd, h->list, nf, h->dv, h->Rchk, h->stream);
+        CK(tc_launch_bwd(h->tc, P, h->sd, h->list, nf, h->Rchk, 1.0f, h->Rhi, h->Rlo, h->gpool, h->tc_err,
+                         h->stream, true, nullptr, 0, 3));   // digits |D| <= 2^10: exact in fp16
+        launch_dual_digit_acc3(P, h->list, nf, h->gpool, h->J64, h->stream);
+        launch_dual_to_wa(P, h->sd, h->list, nf, h->J64, h->wa, h->stream);
+    } else {
         Timed t(h, SDCA_K_BACKWARD, 3 * 4 + 1, 3 * (int64_t)fin.size());
         for (int d = 0; d < 3; ++d) {
             launch_dual_digits(P, h->sd, h->list, (int)fin.size(), d, h->dv, h->Rchk, h->stream);
@@ -1553,11 +1565,11 @@ int dual_round(sdca_handle *h, Queue &Qu)
         if ((rc = upload_slots(h, chk))) return rc;
         if ((rc = zero_acc(h))) return rc;
         {
-            Timed t(h, SDCA_K_BACKWARD, 5, (int64_t)chk.size());
+            // X^T a_g on the tensor cores with a max-only epilogue: no gradient is written
+            Timed t(h, SDCA_K_BACKWARD, 4, (int64_t)chk.size());
             launch_dual_to_r(P, h->ctl, h->list, (int)chk.size(), 0, h->dv, h->Rchk, h->stream);
             CK(tc_launch_bwd(h->tc, P, h->sd, h->list, (int)chk.size(), h->Rchk, (float)pow2_scale(sc), h->Rhi,
-                             h->Rlo, h->gpool, h->tc_err, h->stream));
-            launch_dual_gmax(P, h->sd, h->list, (int)chk.size(), h->gpool, h->acc, h->stream);
+                             h->Rlo, h->gpool, h->tc_err, h->stream, false, h->acc + ACC_GMAX, NACC));
             launch_dual_check_apply(h->ctl, h->sum, h->list, (int)chk.size(), gtol, h->acc, h->stream);
         }
         CKL();

@@ -125,6 +125,11 @@ struct DualCtl {
     double eta_x[Q], eta_d[Q], eta_g[2][Q], eta_s[MAXHIST + 1][Q], eta_y[MAXHIST + 1][Q];
     double SY[MAXHIST + 1][MAXHIST + 1], YY[MAXHIST + 1][MAXHIST + 1];
     double sg_prev[MAXHIST + 1], yg_prev[MAXHIST + 1];
+    // the direction's coefficients as double-float for the direction kernel:
+    // [0, m) coefS, [MAXHIST, MAXHIST + m) coefY, [2 MAXHIST] coef_g,
+    // [2 MAXHIST + 1, + Q) eta_d
+    float2 cdf[2 * MAXHIST + 1 + Q];
+    int32_t cdf_pad_[2];
 };
 
 // What the host reads of each slot after a round (a copy of DualCtl fields).
@@ -236,12 +241,16 @@ void launch_dual_control(const Problem &P, DualCtl *ctl, DualSum *sum, const int
                          cudaStream_t st);
 void launch_dual_check_apply(DualCtl *ctl, DualSum *sum, const int32_t *list, int n, double gtol, const double *acc,
                              cudaStream_t st);
-void launch_dual_gmax(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *gpool,
-                      double *acc, cudaStream_t st);
 void launch_dual_digits(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d, const float2 *dv,
                         float *R, cudaStream_t st);
 void launch_dual_digit_acc(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d,
                            const float *gpool, double *J64, cudaStream_t st);
+// all three digit planes of x's a part in one pass: R rows d n + s, and their
+// combination from gpool buffers d n + s
+void launch_dual_digits3(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float2 *dv, float *R,
+                         cudaStream_t st);
+void launch_dual_digit_acc3(const Problem &P, const int32_t *list, int n, const float *gpool, double *J64,
+                            cudaStream_t st);
 void launch_dual_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *J64,
                        float *wa, cudaStream_t st);
 
@@ -280,9 +289,15 @@ cudaError_t tc_launch_fwd(const TcPlan *pl, const Problem &P, const SlotDev *sd,
                           cudaStream_t st);
 // exact_fp16: R holds values exact in fp16 (the dual form's digit planes), so
 // the lo half of the split is zero and its MMA is skipped
+// gmax_acc: max-only backward (no gradient written): each slot's max |g|
+// over the blocks n != locus into gmax_acc[slot * gmax_stride].
+// planes > 1: R holds planes x n rows by position (plane d of list position
+// s at row d n + s) and row P's product goes to gpool buffer P; needs
+// planes x n <= Bmax.
 cudaError_t tc_launch_bwd(const TcPlan *pl, const Problem &P, const SlotDev *sd, const int32_t *list, int n,
                           const float *R, float r_scale, __half *Rhi, __half *Rlo, float *gpool, int *err,
-                          cudaStream_t st, bool exact_fp16 = false);
+                          cudaStream_t st, bool exact_fp16 = false, double *gmax_acc = nullptr,
+                          int gmax_stride = 0, int planes = 1);
 // dual form: exact K rho on the tensor cores (N <= 4000, L < 2^18)
 struct KdPlan;
 int kd_nk_rows(const Problem &P);

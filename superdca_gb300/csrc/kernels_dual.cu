@@ -142,6 +142,19 @@ __device__ __forceinline__ int64_t dvo(int64_t b, int v, int part, int NV, int64
     return (((b * NV + v) * 2 + part) * Nx) * 4;
 }
 
+// two consecutive double-float entries (t: the pair's index) in one 16-byte access
+__device__ __forceinline__ void df2_load(const float2 *p, int64_t t, float2 (&v)[2])
+{
+    const float4 q = reinterpret_cast<const float4 *>(p)[t];
+    v[0] = make_float2(q.x, q.y);
+    v[1] = make_float2(q.z, q.w);
+}
+
+__device__ __forceinline__ void df2_store(float2 *p, int64_t t, const float2 (&v)[2])
+{
+    reinterpret_cast<float4 *>(p)[t] = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+}
+
 // new gradient (a, k) = (rho_q / qscale + 2 lambda_J a_x, K rho + 2 lambda_J k_x),
 // y = g_new - g_old into the history when the slot pushes a pair;
 // J-part sums: g.g, x.x, s.y, y.y, s.s; max |a_g| and max |a_x|
@@ -155,33 +168,53 @@ k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
     if (S.phase == DC_STOP) return;
     const bool push = S.push && S.ring_new >= 0;
     const float2 l2 = df_from_d(2.0 * lambda_J), iq = df_from_d(inv_qscale);
-    const float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = dv + dvo(b, DV_X, 1, NV, Nx);
-    const float2 *ago = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kgo = dv + dvo(b, DV_G + S.gcur, 1, NV, Nx);
-    float2 *agn = dv + dvo(b, DV_G + 1 - S.gcur, 0, NV, Nx), *kgn = dv + dvo(b, DV_G + 1 - S.gcur, 1, NV, Nx);
+    const int64_t part = Nx * 4;
+    const float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = ax + part;
+    const float2 *ago = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kgo = ago + part;
+    float2 *agn = dv + dvo(b, DV_G + 1 - S.gcur, 0, NV, Nx), *kgn = agn + part;
     const int ps = push ? S.ring_new : 0;
-    const float2 *as = dv + dvo(b, DV_S + ps, 0, NV, Nx), *ks = dv + dvo(b, DV_S + ps, 1, NV, Nx);
-    float2 *ay = dv + dvo(b, DV_S + ring + ps, 0, NV, Nx), *ky = dv + dvo(b, DV_S + ring + ps, 1, NV, Nx);
+    const float2 *as = dv + dvo(b, DV_S + ps, 0, NV, Nx), *ks = as + part;
+    float2 *ay = dv + dvo(b, DV_S + ring + ps, 0, NV, Nx), *ky = ay + part;
+    const int2 *rq2 = reinterpret_cast<const int2 *>(rq + (int64_t)b * Nx * 4);
+    const float2 *KRb = KR + (int64_t)b * Nx * 4;
     float2 g2 = df_zero(), x2 = df_zero(), sy = df_zero(), yy = df_zero(), ss = df_zero();
     float mg = 0.f, mx = 0.f;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
-        const float2 a_x = ax[e], k_x = kx[e];
-        const float2 a_g = df_fma(l2, a_x, df_mul(df_from_int(rq[(int64_t)b * Nx * 4 + e]), iq));
-        const float2 k_g = df_fma(l2, k_x, KR[(int64_t)b * Nx * 4 + e]);
-        g2 = df_fma(a_g, k_g, g2);
-        x2 = df_fma(a_x, k_x, x2);
-        mg = fmaxf(mg, fabsf(a_g.x));
-        mx = fmaxf(mx, fabsf(a_x.x));
-        if (push) {
-            const float2 a_y = df_sub(a_g, ago[e]), k_y = df_sub(k_g, kgo[e]);
-            ay[e] = a_y;
-            ky[e] = k_y;
-            const float2 a_s = as[e], k_s = ks[e];
-            sy = df_fma(a_s, k_y, sy);
-            yy = df_fma(a_y, k_y, yy);
-            ss = df_fma(a_s, k_s, ss);
+    // entry pairs (2t, 2t+1): 16-byte loads of every stream
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < Nx * 2; t += (int64_t)gridDim.x * blockDim.x) {
+        float2 a_x[2], k_x[2], kr[2], a_g[2], k_g[2];
+        df2_load(ax, t, a_x);
+        df2_load(kx, t, k_x);
+        df2_load(KRb, t, kr);
+        const int2 r2 = rq2[t];
+        const int rr[2] = {r2.x, r2.y};
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            a_g[q] = df_fma(l2, a_x[q], df_mul(df_from_int(rr[q]), iq));
+            k_g[q] = df_fma(l2, k_x[q], kr[q]);
+            g2 = df_fma(a_g[q], k_g[q], g2);
+            x2 = df_fma(a_x[q], k_x[q], x2);
+            mg = fmaxf(mg, fabsf(a_g[q].x));
+            mx = fmaxf(mx, fabsf(a_x[q].x));
         }
-        agn[e] = a_g;
-        kgn[e] = k_g;
+        if (push) {
+            float2 a_o[2], k_o[2], a_s[2], k_s[2], a_y[2], k_y[2];
+            df2_load(ago, t, a_o);
+            df2_load(kgo, t, k_o);
+            df2_load(as, t, a_s);
+            df2_load(ks, t, k_s);
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                a_y[q] = df_sub(a_g[q], a_o[q]);
+                k_y[q] = df_sub(k_g[q], k_o[q]);
+                sy = df_fma(a_s[q], k_y[q], sy);
+                yy = df_fma(a_y[q], k_y[q], yy);
+                ss = df_fma(a_s[q], k_s[q], ss);
+            }
+            df2_store(ay, t, a_y);
+            df2_store(ky, t, k_y);
+        }
+        df2_store(agn, t, a_g);
+        df2_store(kgn, t, k_g);
     }
     float2 v[5] = {g2, x2, sy, yy, ss};
     const int idx[5] = {ACC_G2, ACC_X2J, ACC_SY, ACC_YY, ACC_SS};
@@ -194,14 +227,16 @@ k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
     }
 }
 
-// J-part dots of the history pairs listed in the slot's ring[] with a
-// gradient, stored by ring position p: dots[b][p] = a_sp . k_g,
-// dots[b][DOT_Y + p] = a_yp . k_g.  newg: the gradient just formed (buffer
-// 1 - gcur) instead of the accepted one.  (The dots with the newest y follow
-// on the host from these and the previous iteration's: S^T y = S^T g - S^T g_old.)
-// A block takes DOT_CHUNK elements of one slot: k_g staged in shared memory,
-// each warp one history vector at a time (one accumulator per lane).
-constexpr int DOT_CHUNK = 1024;
+// J-part dots of the live history pairs (and the pair the last accept
+// pushed) with a gradient, stored by ring position p: dots[b][p] =
+// a_sp . k_g, dots[b][DOT_Y + p] = a_yp . k_g.  newg: the gradient just
+// formed (buffer 1 - gcur) instead of the accepted one.  (The dots with the
+// newest y follow in the control kernel from these and the previous
+// iteration's: S^T y = S^T g - S^T g_old.)
+// A block takes DOT_CHUNK entries of one slot: k_g staged in shared memory,
+// each warp one history vector at a time, 16-byte loads (one accumulator
+// per lane).
+constexpr int DOT_CHUNK = 2048;
 
 __global__ void __launch_bounds__(256)
 k_dual_dots(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
@@ -214,68 +249,80 @@ k_dual_dots(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
     const bool pushed = S.push && S.ring_new >= 0;
     const int k = S.nhist + (pushed ? 1 : 0);
     const int64_t E = Nx * 4, e0 = (int64_t)blockIdx.x * DOT_CHUNK;
-    const int ne = E - e0 < DOT_CHUNK ? (int)(E - e0) : DOT_CHUNK;
-    __shared__ float2 g[DOT_CHUNK];
+    const int ne = E - e0 < DOT_CHUNK ? (int)(E - e0) : DOT_CHUNK;   // a multiple of 4 (Nx is of 64)
+    const int nq = ne / 2;                                            // float4 pairs
+    __shared__ float4 g[DOT_CHUNK / 2];
     const float2 *kg = dv + dvo(b, DV_G + (newg ? 1 - S.gcur : S.gcur), 1, NV, Nx) + e0;   // (gcur flips in the control kernel)
-    for (int t = threadIdx.x; t < ne; t += blockDim.x) g[t] = kg[t];
+    for (int t = threadIdx.x; t < nq; t += blockDim.x) g[t] = reinterpret_cast<const float4 *>(kg)[t];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int q = warp; q < 2 * k; q += nw) {
-        const bool isy = q >= k;
-        const int j = isy ? q - k : q;
+    for (int qv = warp; qv < 2 * k; qv += nw) {
+        const bool isy = qv >= k;
+        const int j = isy ? qv - k : qv;
         const int pos = j < S.nhist ? S.hist[j] : S.ring_new;
-        const float2 *v = dv + dvo(b, DV_S + (isy ? ring : 0) + pos, 0, NV, Nx) + e0;
+        const float4 *v = reinterpret_cast<const float4 *>(dv + dvo(b, DV_S + (isy ? ring : 0) + pos, 0, NV, Nx) + e0);
         float2 acc = df_zero();
 #pragma unroll 8
-        for (int t = lane; t < ne; t += 32) acc = df_fma(v[t], g[t], acc);
+        for (int t = lane; t < nq; t += 32) {
+            const float4 x = v[t], y = g[t];
+            acc = df_fma(make_float2(x.x, x.y), make_float2(y.x, y.y), acc);
+            acc = df_fma(make_float2(x.z, x.w), make_float2(y.z, y.w), acc);
+        }
         const float2 sum = df_warp_sum(acc);
         if (lane == 0 && (sum.x != 0.f || sum.y != 0.f))
             atomicAdd(dots + (int64_t)b * 4 * MAXHIST + (isy ? DOT_Y : 0) + pos, df_to_d(sum));
     }
 }
 
-// A step trial of one sequence in FP64 from its double-float logits (large
-// steps): adds to fbig, dgbig and writes the residual row r.
-__device__ __noinline__ void trial_fp64(const float2 *lb, const float2 *up, double stp, int y, float wi,
-                                        const float (&p0)[4], float (&r)[4], double &fbig, double &dgbig)
+// A step trial of one sequence with a large step (|t| >= 30), from its
+// double-float logits without FP64 arithmetic: l1 = l0 + stp u in
+// double-float, each log-sum-exp shifted by its largest high part and taken
+// in FP32 (the shifted terms are O(1)), the change of w (lse(l) - l_y)
+// assembled in double-float.  Adds to fbig, dgbig and writes the residual
+// row r.
+__device__ __noinline__ void trial_big(const float2 *lb, const float2 *up, float2 stp, int y, float wi,
+                                       const float (&p0)[4], float (&r)[4], float2 &fbig, float2 &dgbig)
 {
-    const double uu[4] = {df_to_d(up[0]), df_to_d(up[1]), df_to_d(up[2]), df_to_d(up[3])};
-    double l0[4], l1[4];
+    float2 l0[4], l1[4], uu[4];
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-        l0[a] = df_to_d(lb[a]);
-        l1[a] = l0[a] + stp * uu[a];
+        l0[a] = lb[a];
+        uu[a] = up[a];
+        l1[a] = df_fma(stp, uu[a], l0[a]);
     }
-    const double m0 = fmax(fmax(l0[0], l0[1]), fmax(l0[2], l0[3]));
-    const double m1 = fmax(fmax(l1[0], l1[1]), fmax(l1[2], l1[3]));
-    double z0 = 0, z1 = 0, e1[4];
+    const float m0 = fmaxf(fmaxf(l0[0].x, l0[1].x), fmaxf(l0[2].x, l0[3].x));
+    const float m1 = fmaxf(fmaxf(l1[0].x, l1[1].x), fmaxf(l1[2].x, l1[3].x));
+    float z0 = 0.f, z1 = 0.f, e1[4];
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-        z0 += exp(l0[a] - m0);
-        e1[a] = exp(l1[a] - m1);
+        z0 += expf(df_f(df_sub(l0[a], make_float2(m0, 0.f))));
+        e1[a] = expf(df_f(df_sub(l1[a], make_float2(m1, 0.f))));
         z1 += e1[a];
     }
-    double l0y = l0[0], l1y = l1[0], uuy = uu[0];
+    float2 l0y = l0[0], l1y = l1[0], uy = uu[0];
 #pragma unroll
     for (int a = 1; a < 4; ++a)
         if (a == y) {
             l0y = l0[a];
             l1y = l1[a];
-            uuy = uu[a];
+            uy = uu[a];
         }
-    fbig += (double)wi * ((m1 + log(z1) - l1y) - (m0 + log(z0) - l0y));
-    double ro = 0.0;
+    float2 d = df_sub(df_sub(make_float2(m1, 0.f), l1y), df_sub(make_float2(m0, 0.f), l0y));
+    d = df_add(d, make_float2(logf(z1) - logf(z0), 0.f));
+    fbig = df_fma(make_float2(wi, 0.f), d, fbig);
+    const float iz1 = 1.f / z1;
+    float ro = 0.f;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-        const double p1 = e1[a] / z1;
-        dgbig += (double)wi * (p1 - (double)p0[a]) * (uu[a] - uuy);
-        const double ra = a == y ? 0.0 : (double)wi * p1;
-        r[a] = (float)ra;
+        const float p1 = e1[a] * iz1;
+        dgbig = df_fma(make_float2(wi * (p1 - p0[a]), 0.f), df_sub(uu[a], uy), dgbig);
+        const float ra = a == y ? 0.f : wi * p1;
+        r[a] = ra;
         ro += ra;
     }
 #pragma unroll
     for (int a = 0; a < 4; ++a)
-        if (a == y) r[a] = (float)-ro;
+        if (a == y) r[a] = -ro;
 }
 
 // A line-search trial as a change from the current point.  With p0 the base
@@ -290,7 +337,7 @@ __device__ __noinline__ void trial_fp64(const float2 *lb, const float2 *up, doub
 // compares; the base values (objective, slope at 0) are FP64.  Z is a sum of
 // positive terms and the new probabilities are products, so a probability
 // that has become small keeps its relative precision.  Sequences whose step
-// is large take an FP64 log-sum-exp of the logits (trial_fp64).  Per trial:
+// is large take a log-sum-exp of the double-float logits (trial_big).  Per trial:
 // the sums of w dl, of the slope change and of R(stp), and the rows
 // R <- R(stp) = w (p(stp) - onehot(y)), the y entry as minus the sum of the
 // others (trial_seq, in the line-search kernel below).
@@ -299,8 +346,14 @@ __device__ __noinline__ void trial_fp64(const float2 *lb, const float2 *up, doub
 // trials from the double-float logits at the current point (fresh every iteration,
 // so that rounding does not carry from one iteration to the next); sums g.d,
 // d.d, x.d (J parts) and the slope of the search line at 0 from the trials'
-// own numbers, sum_i w_i sum_c p0_ic (u_ic - u_iy)
-__global__ void __launch_bounds__(256)
+// own numbers, sum_i w_i sum_c p0_ic (u_ic - u_iy).
+// Each thread takes two consecutive entries (16-byte loads of every stream);
+// a sequence's four states sit in a lane pair.  History loads of two vectors
+// are issued before their multiply-adds.  One pass per thread: the grid
+// covers the slot's N x 4 entries.
+constexpr int DIR_THREADS = 256;
+
+__global__ void __launch_bounds__(DIR_THREADS, 5)
 k_dual_direction(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int N, int NV,
                  int ring, float2 *__restrict__ dv, const float2 *__restrict__ lbase, float *__restrict__ P0,
                  const float *__restrict__ w, const uint8_t *__restrict__ rstate, float2 *__restrict__ u,
@@ -310,61 +363,111 @@ k_dual_direction(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ li
     const DualCtl &S = ctl[b];
     if (S.phase == DC_STOP) return;
     const int k = S.nhist;
-    const float2 *ag = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kg = dv + dvo(b, DV_G + S.gcur, 1, NV, Nx);
-    const float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx);
-    float2 *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = dv + dvo(b, DV_D, 1, NV, Nx);
-    const int64_t part = Nx * 4;
-    __shared__ float2 cf[2 * MAXHIST + 1 + Q];   // the slot's coefficients and eta_d
+    __shared__ float2 cf[2 * MAXHIST + 1 + Q];   // the slot's coefficients and eta_d (double-float)
+    __shared__ int64_t hoff[2 * MAXHIST];        // history vector offsets (a parts; k part at + Nx*4)
+    if (threadIdx.x < 2 * MAXHIST + 1 + Q) cf[threadIdx.x] = S.cdf[threadIdx.x];
     if (threadIdx.x < k) {
-        cf[threadIdx.x] = df_from_d(S.coefS[threadIdx.x]);
-        cf[MAXHIST + threadIdx.x] = df_from_d(S.coefY[threadIdx.x]);
+        hoff[threadIdx.x] = dvo(b, DV_S + S.hist[threadIdx.x], 0, NV, Nx);
+        hoff[MAXHIST + threadIdx.x] = dvo(b, DV_S + ring + S.hist[threadIdx.x], 0, NV, Nx);
     }
-    if (threadIdx.x == 0) cf[2 * MAXHIST] = df_from_d(S.coef_g);
-    if (threadIdx.x < Q) cf[2 * MAXHIST + 1 + threadIdx.x] = df_from_d(S.eta_d[threadIdx.x]);
     __syncthreads();
-    const float2 cg = cf[2 * MAXHIST];
+    const int64_t part = Nx * 4;                 // a part -> k part, in float2 entries
+    const int64_t t = (int64_t)blockIdx.x * DIR_THREADS + threadIdx.x;   // entry pair: entries 2t, 2t+1
+    const bool live = t < Nx * 2;
     float2 gd = df_zero(), dd = df_zero(), xd = df_zero(), dg0 = df_zero();
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
-        const float2 g_a = ag[e], g_k = kg[e];
-        float2 a = df_mul(cg, g_a), kk = df_mul(cg, g_k);
-#pragma unroll 4   // (a full unroll hoists every load: 116 registers, fewer warps)
-        for (int j = 0; j < MAXHIST; ++j) {
-            if (j >= k) break;
-            const float2 *vs = dv + dvo(b, DV_S + S.hist[j], 0, NV, Nx), *vy = dv + dvo(b, DV_S + ring + S.hist[j], 0, NV, Nx);
-            const float2 cs = cf[j], cy = cf[MAXHIST + j];
-            a = df_fma(cy, vy[e], df_fma(cs, vs[e], a));
-            kk = df_fma(cy, vy[part + e], df_fma(cs, vs[part + e], kk));
+    // (the whole warp reaches the shuffles below: Nx*2 is a multiple of 128)
+    if (live) {
+        const float2 *ag = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kg = ag + part;
+        const float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx);
+        float2 *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = ad + part;
+        const float2 cg = cf[2 * MAXHIST];
+        float2 g_a[2], g_k[2], a[2], kk[2];
+        df2_load(ag, t, g_a);
+        df2_load(kg, t, g_k);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            a[q] = df_mul(cg, g_a[q]);
+            kk[q] = df_mul(cg, g_k[q]);
         }
-        ad[e] = a;
-        kd[e] = kk;
-        gd = df_fma(g_a, kk, gd);
-        dd = df_fma(a, kk, dd);
-        xd = df_fma(ax[e], kk, xd);
-        const int c = (int)(e & 3);
-        const float2 uu = df_add(kk, cf[2 * MAXHIST + 1 + c]);
-        u[(int64_t)b * Nx * 4 + e] = uu;
-        // the four states of a sequence sit in four consecutive lanes
-        const int64_t o = (int64_t)b * Nx + e / 4;
-        const int y = rstate[o] & 3;
-        const int src = (threadIdx.x & ~3) + y;
-        const float2 uy = make_float2(__shfl_sync(0xffffffffu, uu.x, src), __shfl_sync(0xffffffffu, uu.y, src));
-        const float2 du = df_sub(uu, uy);
-        ud[(int64_t)b * Nx * 4 + e] = df_f(du);
-        // p0 = softmax of the four logits of the sequence (lanes 4k..4k+3),
-        // shifted by the largest high part
-        const float2 l = lbase[(int64_t)b * Nx * 4 + e];
-        float m = fmaxf(l.x, __shfl_xor_sync(0xffffffffu, l.x, 1));
-        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
-        const float ex = expf(df_f(df_sub(l, make_float2(m, 0.f))));
-        float z = ex + __shfl_xor_sync(0xffffffffu, ex, 1);
-        z += __shfl_xor_sync(0xffffffffu, z, 2);
-        const float p0 = ex / z;
-        P0[(int64_t)b * Nx * 4 + e] = p0;
-        if (e / 4 < N) dg0 = df_fma(make_float2(w[e / 4] * p0, 0.f), du, dg0);
+        int j = 0;
+        for (; j + 1 < k; j += 2) {
+            float2 sa0[2], sk0[2], ya0[2], yk0[2], sa1[2], sk1[2], ya1[2], yk1[2];
+            const float2 *s0 = dv + hoff[j], *y0 = dv + hoff[MAXHIST + j];
+            const float2 *s1 = dv + hoff[j + 1], *y1 = dv + hoff[MAXHIST + j + 1];
+            df2_load(s0, t, sa0);
+            df2_load(s0 + part, t, sk0);
+            df2_load(y0, t, ya0);
+            df2_load(y0 + part, t, yk0);
+            df2_load(s1, t, sa1);
+            df2_load(s1 + part, t, sk1);
+            df2_load(y1, t, ya1);
+            df2_load(y1 + part, t, yk1);
+            const float2 cs0 = cf[j], cy0 = cf[MAXHIST + j], cs1 = cf[j + 1], cy1 = cf[MAXHIST + j + 1];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                a[q] = df_fma(cy0, ya0[q], df_fma(cs0, sa0[q], a[q]));
+                kk[q] = df_fma(cy0, yk0[q], df_fma(cs0, sk0[q], kk[q]));
+                a[q] = df_fma(cy1, ya1[q], df_fma(cs1, sa1[q], a[q]));
+                kk[q] = df_fma(cy1, yk1[q], df_fma(cs1, sk1[q], kk[q]));
+            }
+        }
+        if (j < k) {
+            float2 sa0[2], sk0[2], ya0[2], yk0[2];
+            const float2 *s0 = dv + hoff[j], *y0 = dv + hoff[MAXHIST + j];
+            df2_load(s0, t, sa0);
+            df2_load(s0 + part, t, sk0);
+            df2_load(y0, t, ya0);
+            df2_load(y0 + part, t, yk0);
+            const float2 cs0 = cf[j], cy0 = cf[MAXHIST + j];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                a[q] = df_fma(cy0, ya0[q], df_fma(cs0, sa0[q], a[q]));
+                kk[q] = df_fma(cy0, yk0[q], df_fma(cs0, sk0[q], kk[q]));
+            }
+        }
+        df2_store(ad, t, a);
+        df2_store(kd, t, kk);
+        float2 x_a[2], l[2];
+        df2_load(ax, t, x_a);
+        df2_load(lbase + (int64_t)b * Nx * 4, t, l);
+        const int c0 = (int)((2 * t) & 3);        // state of the first entry: 0 or 2
+        const int64_t i = t >> 1;                  // the sequence
+        float2 uu[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            gd = df_fma(g_a[q], kk[q], gd);
+            dd = df_fma(a[q], kk[q], dd);
+            xd = df_fma(x_a[q], kk[q], xd);
+            uu[q] = df_add(kk[q], cf[2 * MAXHIST + 1 + c0 + q]);
+        }
+        df2_store(u + (int64_t)b * Nx * 4, t, uu);
+        // u at the sequence's own state y, from whichever lane of the pair holds it
+        const int y = rstate[(int64_t)b * Nx + i] & 3;
+        const float2 mine = (y & 1) ? uu[1] : uu[0];
+        const float2 other = make_float2(__shfl_xor_sync(0xffffffffu, mine.x, 1), __shfl_xor_sync(0xffffffffu, mine.y, 1));
+        const float2 uy = ((y & 2) == c0) ? mine : other;
+        float2 du[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) du[q] = df_sub(uu[q], uy);
+        reinterpret_cast<float2 *>(ud + (int64_t)b * Nx * 4)[t] = make_float2(df_f(du[0]), df_f(du[1]));
+        // p0 = softmax of the sequence's four logits, shifted by the largest high part
+        float m = fmaxf(l[0].x, l[1].x);
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
+        const float e0 = expf(df_f(df_sub(l[0], make_float2(m, 0.f))));
+        const float e1 = expf(df_f(df_sub(l[1], make_float2(m, 0.f))));
+        float z = e0 + e1;
+        z += __shfl_xor_sync(0xffffffffu, z, 1);
+        const float p00 = e0 / z, p01 = e1 / z;
+        reinterpret_cast<float2 *>(P0 + (int64_t)b * Nx * 4)[t] = make_float2(p00, p01);
+        if (i < N) {
+            const float wi = w[i];
+            dg0 = df_fma(make_float2(wi * p00, 0.f), du[0], dg0);
+            dg0 = df_fma(make_float2(wi * p01, 0.f), du[1], dg0);
+        }
     }
-    double v[4] = {df_to_d(gd), df_to_d(dd), df_to_d(xd), df_to_d(dg0)};
+    float2 v[4] = {gd, dd, xd, dg0};
     const int idx[4] = {DA_GD, DA_DDJ, DA_XDJ, DA_DG0};
-    block_sum_atomic<4>(v, dacc + (int64_t)b * NDACC, idx);
+    block_sum_df<4>(v, dacc + (int64_t)b * NDACC, idx);
 }
 
 // x += stp d (a and k parts), s = x_new - x_old into the history on a push,
@@ -379,20 +482,39 @@ k_dual_accept(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list,
     const double stp = S.stp;
     const bool push = S.push && S.ring_new >= 0;
     const float2 sf = df_from_d(stp);
-    float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = dv + dvo(b, DV_X, 1, NV, Nx);
-    const float2 *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = dv + dvo(b, DV_D, 1, NV, Nx);
-    float2 *as = dv + dvo(b, DV_S + (push ? S.ring_new : 0), 0, NV, Nx);
-    float2 *ks = dv + dvo(b, DV_S + (push ? S.ring_new : 0), 1, NV, Nx);
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
-        const float2 a0 = ax[e], k0 = kx[e];
-        const float2 a1 = df_fma(sf, ad[e], a0), k1 = df_fma(sf, kd[e], k0);
-        ax[e] = a1;
-        kx[e] = k1;
-        if (push) {
-            as[e] = df_sub(a1, a0);
-            ks[e] = df_sub(k1, k0);
+    const int64_t part = Nx * 4;
+    float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = ax + part;
+    const float2 *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = ad + part;
+    float2 *as = dv + dvo(b, DV_S + (push ? S.ring_new : 0), 0, NV, Nx), *ks = as + part;
+    const float2 *ub = u + (int64_t)b * Nx * 4;
+    float2 *lb = lbase + (int64_t)b * Nx * 4;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < Nx * 2; t += (int64_t)gridDim.x * blockDim.x) {
+        float2 a0[2], k0[2], a_d[2], k_d[2], a1[2], k1[2], uu[2], l[2];
+        df2_load(ax, t, a0);
+        df2_load(kx, t, k0);
+        df2_load(ad, t, a_d);
+        df2_load(kd, t, k_d);
+        df2_load(ub, t, uu);
+        df2_load(lb, t, l);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            a1[q] = df_fma(sf, a_d[q], a0[q]);
+            k1[q] = df_fma(sf, k_d[q], k0[q]);
+            l[q] = df_fma(sf, uu[q], l[q]);
         }
-        lbase[(int64_t)b * Nx * 4 + e] = df_fma(sf, u[(int64_t)b * Nx * 4 + e], lbase[(int64_t)b * Nx * 4 + e]);
+        df2_store(ax, t, a1);
+        df2_store(kx, t, k1);
+        df2_store(lb, t, l);
+        if (push) {
+            float2 sa[2], sk[2];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                sa[q] = df_sub(a1[q], a0[q]);
+                sk[q] = df_sub(k1[q], k0[q]);
+            }
+            df2_store(as, t, sa);
+            df2_store(ks, t, sk);
+        }
     }
 }
 
@@ -438,6 +560,45 @@ __global__ void k_dual_digits(const SlotDev *__restrict__ sd, const int32_t *__r
     }
 }
 
+// The three digits at once: plane d of list position s into R row d n + s.
+__global__ void k_dual_digits3(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int n, int64_t Nx,
+                               int N, int NV, const float2 *__restrict__ dv, float4 *__restrict__ R)
+{
+    const int s = blockIdx.y, b = list[s];
+    const double qa = sd[b].tc_scale;
+    const float2 *a = dv + dvo(b, DV_X, 0, NV, Nx);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Nx; i += (int64_t)gridDim.x * blockDim.x) {
+        float v[3][4] = {};
+        if (i < N) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const long long A = llrint(df_to_d(a[4 * i + c]) * qa);
+                const long long d0 = (A + (1ll << 21)) >> 22;          // round(A / 2^22)
+                const long long r0 = A - (d0 << 22);
+                const long long d1 = (r0 + (1ll << 10)) >> 11;         // round(r0 / 2^11)
+                v[0][c] = (float)d0;
+                v[1][c] = (float)d1;
+                v[2][c] = (float)(r0 - (d1 << 11));
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) R[((int64_t)d * n + s) * Nx + i] = make_float4(v[d][0], v[d][1], v[d][2], v[d][3]);
+    }
+}
+
+// J = 2^22 X^T D0 + 2^11 X^T D1 + X^T D2 in 64-bit integers, the three
+// products from gpool buffers s, n + s, 2n + s
+__global__ void k_dual_digit_acc3(const int32_t *__restrict__ list, int n, int64_t Dp, const float *__restrict__ gpool,
+                                  long long *__restrict__ J64)
+{
+    const int s = blockIdx.y, b = list[s];
+    const float *g0 = gpool + (int64_t)s * Dp, *g1 = gpool + (int64_t)(n + s) * Dp, *g2 = gpool + (int64_t)(2 * n + s) * Dp;
+    long long *o = J64 + (int64_t)b * Dp;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Dp; e += (int64_t)gridDim.x * blockDim.x)
+        o[e] = ((long long)__float2int_rn(g0[e]) << 22) + ((long long)__float2int_rn(g1[e]) << 11) +
+               (long long)__float2int_rn(g2[e]);
+}
+
 // J (=, or +=) 2^(22, 11, 0) (X^T D) in 64-bit integers: every X^T D is an
 // integer below 2^24, exact in the FP32 backward output
 __global__ void k_dual_digit_acc(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int64_t Dp,
@@ -450,21 +611,6 @@ __global__ void k_dual_digit_acc(const SlotDev *__restrict__ sd, const int32_t *
     long long *o = J64 + (int64_t)b * Dp;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Dp; e += (int64_t)gridDim.x * blockDim.x)
         o[e] = (d == 0 ? 0ll : o[e]) + (long long)__float2int_rn(g[e]) * wgt;
-}
-
-// max |Phi^T a| over the J blocks n != r, from the tensor-core backward output
-__global__ void k_dual_gmax(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int L, int64_t Dp,
-                            const float *__restrict__ gpool, double *__restrict__ acc)
-{
-    const int b = list[blockIdx.y];
-    const SlotDev &S = sd[b];
-    const float *g = gpool + (int64_t)(2 * b + 1 - S.gcur) * Dp;
-    float m = 0.f;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < (int64_t)QQ * L;
-         e += (int64_t)gridDim.x * blockDim.x)
-        if (e / QQ != S.locus) m = fmaxf(m, fabsf(g[e]));
-    m = warp_max(m);
-    if ((threadIdx.x & 31) == 0 && m > 0.f) atomic_max_nonneg(acc + (int64_t)b * NACC + ACC_GMAX, (double)m);
 }
 
 // x in the engine layout from the combined digits: J blocks (J_rr = 0) =
@@ -491,11 +637,11 @@ __global__ void k_dual_to_wa(const SlotDev *__restrict__ sd, const int32_t *__re
 // One sequence of a step trial as a change from the current point (the
 // derivation above): adds w dl, the slope change and the new residual row's
 // sums, and writes the row.
-__device__ __forceinline__ void trial_seq(int64_t o, int i, double stp, float stpf, const float2 *__restrict__ lbase,
+__device__ __forceinline__ void trial_seq(int64_t o, int i, float2 stp, float stpf, const float2 *__restrict__ lbase,
                                           const float2 *__restrict__ u, const float4 *__restrict__ ud,
                                           const uint8_t *__restrict__ rstate, const float *__restrict__ w,
                                           const float4 *__restrict__ P0, float4 *__restrict__ R, float &f, float &dg,
-                                          float (&rs)[4], double &fbig, double &dgbig)
+                                          float (&rs)[4], float2 &fbig, float2 &dgbig)
 {
     const float4 dv4 = ud[o];
     const float du[4] = {dv4.x, dv4.y, dv4.z, dv4.w};   // u_a - u_y
@@ -532,7 +678,7 @@ __device__ __forceinline__ void trial_seq(int64_t o, int i, double stp, float st
         for (int a = 0; a < 4; ++a)
             if (a == y) r[a] = -ro;
     } else {
-        trial_fp64(lbase + o * 4, u + o * 4, stp, y, wi, p0, r, fbig, dgbig);
+        trial_big(lbase + o * 4, u + o * 4, stp, y, wi, p0, r, fbig, dgbig);
     }
 #pragma unroll
     for (int a = 0; a < 4; ++a) rs[a] += r[a];
@@ -577,6 +723,8 @@ k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
     __shared__ __align__(16) unsigned char mt_raw[sizeof(MoreThuente)];
     __shared__ double red[LS_THREADS / 32][8];
     __shared__ double s_stp;
+    __shared__ float2 s_stp_df;
+    __shared__ double s_tot[8];
     __shared__ int s_restart, s_done;
     MoreThuente &mt = *reinterpret_cast<MoreThuente *>(mt_raw);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -653,12 +801,16 @@ k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
             xdJ = t0;
             dg0 = t1;
             ddJ = S.g2J;
-            for (int c = 0; c < 4; ++c) S.eta_d[c] = -S.eta_g[gc][c];
+            for (int c = 0; c < 4; ++c) {
+                S.eta_d[c] = -S.eta_g[gc][c];
+                S.cdf[2 * MAXHIST + 1 + c] = df_from_d(S.eta_d[c]);
+            }
             ddH = dot4d(S.eta_d, S.eta_d);
             S.nhist = 0;
             S.iter = 0;
             S.restarts++;
             S.coef_g = -1.0;
+            S.cdf[2 * MAXHIST] = make_float2(-1.f, 0.f);
         }
         __syncthreads();
     }
@@ -674,8 +826,10 @@ k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
         new (mt_raw) MoreThuente();
         if (mt.start(S.f, d0, alpha) == MoreThuente::NEED_EVAL) {
             s_stp = mt.stp;
+            s_stp_df = df_from_d(mt.stp);
         } else {
             s_stp = 0.0;
+            s_stp_df = df_zero();
             s_mode = 1;
             S.weak++;
             if (S.nhist == 0) S.stalled = 1;
@@ -687,28 +841,34 @@ k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
     for (int it = 0; it < 64; ++it) {
         __syncthreads();
         const double stp = s_stp;
-        const float stpf = (float)stp;
+        const float2 stpd = s_stp_df;
+        const float stpf = stpd.x + stpd.y;
         float f = 0.f, dg = 0.f, rs[4] = {0.f, 0.f, 0.f, 0.f};
-        double fbig = 0.0, dgbig = 0.0;
+        float2 fbig = df_zero(), dgbig = df_zero();
 #pragma unroll 1
         for (int i = tid; i < N; i += LS_THREADS)
-            trial_seq((int64_t)b * Nx + i, i, stp, stpf, lbase, u, ud, rstate, w, P0, R, f, dg, rs, fbig, dgbig);
+            trial_seq((int64_t)b * Nx + i, i, stpd, stpf, lbase, u, ud, rstate, w, P0, R, f, dg, rs, fbig, dgbig);
+        // FP32 sums per warp (each lane's value is an FP32 partial over a few
+        // sequences), double-float for the large-step terms, FP64 across warps
         const float v[6] = {warp_sum_f(f), warp_sum_f(dg), warp_sum_f(rs[0]), warp_sum_f(rs[1]), warp_sum_f(rs[2]),
                             warp_sum_f(rs[3])};
-        fbig = warp_sum(fbig);
-        dgbig = warp_sum(dgbig);
+        fbig = df_warp_sum(fbig);
+        dgbig = df_warp_sum(dgbig);
         if (lane == 0) {
 #pragma unroll
             for (int k = 0; k < 6; ++k) red[wid][k] = (double)v[k];
-            red[wid][6] = fbig;
-            red[wid][7] = dgbig;
+            red[wid][6] = df_to_d(fbig);
+            red[wid][7] = df_to_d(dgbig);
+        }
+        __syncthreads();
+        if (tid < 8) {
+            double t = 0.0;
+            for (int k = 0; k < LS_THREADS / 32; ++k) t += red[k][tid];
+            s_tot[tid] = t;
         }
         __syncthreads();
         if (tid == 0) {
-            double tot[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            for (int k = 0; k < LS_THREADS / 32; ++k)
-#pragma unroll
-                for (int j = 0; j < 8; ++j) tot[j] += red[k][j];
+            const double *tot = s_tot;
             const double l2 = lambda_J * (S.x2J + 2.0 * stp * xdJ + stp * stp * ddJ) +
                               lambda_h * (x2H + 2.0 * stp * xdH + stp * stp * ddH);
             const double dl2 = 2.0 * lambda_J * (xdJ + stp * ddJ) + 2.0 * lambda_h * (xdH + stp * ddH);
@@ -724,6 +884,7 @@ k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
                     S.max_trials = max(S.max_trials, S.trials);
                 } else {
                     s_stp = mt.stp;
+                    s_stp_df = df_from_d(mt.stp);
                 }
             }
             if (done) {
@@ -918,6 +1079,12 @@ k_dual_control(DualCtl *__restrict__ ctl, DualSum *__restrict__ sum, const int32
                     v += S.coefS[j] * S.eta_s[S.hist[j]][a] + S.coefY[j] * S.eta_y[S.hist[j]][a];
                 S.eta_d[a] = v;
             }
+            for (int j = 0; j < S.nhist; ++j) {
+                S.cdf[j] = df_from_d(S.coefS[j]);
+                S.cdf[MAXHIST + j] = df_from_d(S.coefY[j]);
+            }
+            S.cdf[2 * MAXHIST] = df_from_d(S.coef_g);
+            for (int a = 0; a < Q; ++a) S.cdf[2 * MAXHIST + 1 + a] = df_from_d(S.eta_d[a]);
             // the next accepted step fills a ring position outside the live history
             int pos = 0;
             for (bool used = true; used;) {
@@ -939,8 +1106,9 @@ k_dual_control(DualCtl *__restrict__ ctl, DualSum *__restrict__ sum, const int32
     if (threadIdx.x == 0) write_summary(S, sum[b]);
 }
 
-// After an exact max-norm check (k_dual_gmax): the slot's max|g| is the J
-// part's maximum and |g_h|; stop with status 0 below the threshold, or with
+// After an exact max-norm check (the tensor-core backward X^T a_g with its
+// max-only epilogue): the slot's max|g| is the J part's maximum and |g_h|;
+// stop with status 0 below the threshold, or with
 // status 2 on a pending relative-norm stop (SuperDCA: plmDCA.hpp:218-221).
 __global__ void k_dual_check_apply(DualCtl *__restrict__ ctl, DualSum *__restrict__ sum,
                                    const int32_t *__restrict__ list, int n, double gtol,
@@ -1008,7 +1176,7 @@ void launch_dual_grad(const Problem &P, const DualCtl *ctl, const int32_t *list,
 {
     if (n <= 0) return;
     const int NV = DV_S + 2 * P.ring;
-    dim3 gg(grid_for(P.Nx * 4, 256 * 8, 64), n);
+    dim3 gg(grid_for(P.Nx * 2, 256 * 2, 64), n);
     k_dual_grad<<<gg, 256, 0, st>>>(ctl, list, P.Nx, NV, P.ring, P.lambda_J, rq, 1.0 / qscale, KR, dv, acc, amax);
 }
 
@@ -1025,17 +1193,16 @@ void launch_dual_direction(const Problem &P, const DualCtl *ctl, const int32_t *
                            float *ud, double *dacc, cudaStream_t st)
 {
     if (n <= 0) return;
-    dim3 g(grid_for(P.Nx * 4, 256 * 8, 32), n);
-    k_dual_direction<<<g, 256, 0, st>>>(ctl, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, P.ring, dv,
-                                        lbase, P0, w,
-                                        rstate, u, ud, dacc);
+    dim3 g((unsigned)((P.Nx * 2 + DIR_THREADS - 1) / DIR_THREADS), n);
+    k_dual_direction<<<g, DIR_THREADS, 0, st>>>(ctl, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, P.ring, dv, lbase, P0,
+                                                w, rstate, u, ud, dacc);
 }
 
 void launch_dual_accept(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
                         const float2 *u, float2 *lbase, cudaStream_t st)
 {
     if (n <= 0) return;
-    dim3 g(grid_for(P.Nx * 4, 256 * 4, 64), n);
+    dim3 g(grid_for(P.Nx * 2, 256 * 2, 64), n);
     k_dual_accept<<<g, 256, 0, st>>>(ctl, list, P.Nx, DV_S + 2 * P.ring, dv, u, lbase);
 }
 
@@ -1046,14 +1213,6 @@ void launch_dual_to_r(const Problem &P, const DualCtl *ctl, const int32_t *list,
     dim3 g(grid_for(P.Nx, 256 * 4, 64), n);
     k_dual_to_r<<<g, 256, 0, st>>>(ctl, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, which, dv,
                                    reinterpret_cast<float4 *>(R));
-}
-
-void launch_dual_gmax(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *gpool,
-                      double *acc, cudaStream_t st)
-{
-    if (n <= 0) return;
-    dim3 g(grid_for((int64_t)QQ * P.L, 256 * 16, 256), n);
-    k_dual_gmax<<<g, 256, 0, st>>>(sd, list, (int)P.L, P.Dp, gpool, acc);
 }
 
 void launch_dual_digits(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d, const float2 *dv,
@@ -1071,6 +1230,23 @@ void launch_dual_digit_acc(const Problem &P, const SlotDev *sd, const int32_t *l
     if (n <= 0) return;
     dim3 g(grid_for(P.Dp, 256 * 16, 256), n);
     k_dual_digit_acc<<<g, 256, 0, st>>>(sd, list, P.Dp, d, gpool, reinterpret_cast<long long *>(J64));
+}
+
+void launch_dual_digits3(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float2 *dv, float *R,
+                         cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 g(grid_for(P.Nx, 256 * 4, 64), n);
+    k_dual_digits3<<<g, 256, 0, st>>>(sd, list, n, P.Nx, (int)P.N, DV_S + 2 * P.ring, dv,
+                                      reinterpret_cast<float4 *>(R));
+}
+
+void launch_dual_digit_acc3(const Problem &P, const int32_t *list, int n, const float *gpool, double *J64,
+                            cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 g(grid_for(P.Dp, 256 * 16, 256), n);
+    k_dual_digit_acc3<<<g, 256, 0, st>>>(list, n, P.Dp, gpool, reinterpret_cast<long long *>(J64));
 }
 
 void launch_dual_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *J64,

@@ -241,6 +241,15 @@ struct GemmArgs {
     int64_t Dp;
     float inv_scale_bwd;
     int hi_only;          // the slot operand is exact in fp16 (its lo half is zero): skip the lo MMA
+    // backward, max only: instead of writing the gradient, each slot's
+    // max |g| over the blocks n != locus goes to gmax_acc[slot * gmax_stride]
+    // (non-negative double bits, atomicMax)
+    double *gmax_acc;
+    int gmax_stride;
+    // backward, digit planes: the list holds nslot slots and the B operand
+    // planes x nslot virtual columns (plane d of list position s at virtual
+    // position d * nslot + s); virtual position P is written to gpool buffer P
+    int planes, nslot;
     int *err;
 };
 
@@ -378,7 +387,7 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
                 for (int tt = 0; tt < 8; ++tt) {
                     const int P = (n_tile * BN + cj * 32) / 4 + tt;
                     if (P >= args.nlist) continue;
-                    const int b = args.list[P];
+                    const int b = args.planes > 1 ? args.list[P % args.nslot] : args.list[P];
                     if (args.mode == MODE_FWD) {
                         if (row < args.Nx) {
                             const float sc = (float)args.sd[b].tc_inv_scale;
@@ -386,11 +395,22 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
                                 make_float4(v[4 * tt] * sc, v[4 * tt + 1] * sc, v[4 * tt + 2] * sc,
                                             v[4 * tt + 3] * sc);
                         }
+                    } else if (args.gmax_acc) {
+                        // (the list position P is the same in every lane of the warp)
+                        float mv = 0.f;
+                        if (row < args.m_rows && (row >> 2) != args.sd[b].locus)
+                            mv = fmaxf(fmaxf(fabsf(v[4 * tt]), fabsf(v[4 * tt + 1])),
+                                       fmaxf(fabsf(v[4 * tt + 2]), fabsf(v[4 * tt + 3]))) * args.inv_scale_bwd;
+                        const unsigned mask = __activemask();
+                        const unsigned mb = __reduce_max_sync(mask, __float_as_uint(mv));
+                        if (lane == __ffs(mask) - 1 && mb != 0u)
+                            atomicMax(reinterpret_cast<unsigned long long *>(args.gmax_acc +
+                                                                             (int64_t)b * args.gmax_stride),
+                                      (unsigned long long)__double_as_longlong((double)__uint_as_float(mb)));
                     } else if (row < args.m_rows) {
                         const float sc = args.inv_scale_bwd;
-                        const int gb = args.sd[b].gcur;
-                        float *gn = args.gpool + (int64_t)(2 * b + 1 - gb) * args.Dp + (int64_t)(row >> 2) * QQ +
-                                    (row & 3) * Q;
+                        const int64_t buf = args.planes > 1 ? (int64_t)P : (int64_t)(2 * b + 1 - args.sd[b].gcur);
+                        float *gn = args.gpool + buf * args.Dp + (int64_t)(row >> 2) * QQ + (row & 3) * Q;
                         *reinterpret_cast<float4 *>(gn) = make_float4(v[4 * tt] * sc, v[4 * tt + 1] * sc,
                                                                       v[4 * tt + 2] * sc, v[4 * tt + 3] * sc);
                     }
@@ -545,9 +565,13 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
         const int q = warp & 3;
         const int row = m_tile * KD_BM + q * 32 + lane;
         const float2 iq = df_from_d(args.inv_qscale);
-        unsigned long long acc[KD_BN];
+        // The 12 digit products are integers below 2^24 in magnitude (exact
+        // in the FP32 accumulators): each is converted with a 32-bit
+        // conversion and shifted into place in 64-bit integers (no 64-bit
+        // conversion or multiply, which run on GB300's narrow FP64 pipe).
+        long long acc[KD_BN];
 #pragma unroll
-        for (int c = 0; c < KD_BN; ++c) acc[c] = 0ull;
+        for (int c = 0; c < KD_BN; ++c) acc[c] = 0ll;
         if (ok) {
 #pragma unroll 1
             for (int k = 0; k < KD_KDIG; ++k)
@@ -555,9 +579,9 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
                 for (int p = 0; p < KD_RDIG; ++p) {
                     float v[32];
                     tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)((k * KD_RDIG + p) * KD_BN), v);
-                    const unsigned long long w = 1ull << (6 * k + 7 * p);
+                    const int sh = 6 * k + 7 * p;
 #pragma unroll
-                    for (int c = 0; c < KD_BN; ++c) acc[c] += (unsigned long long)__float2ll_rn(v[c]) * w;
+                    for (int c = 0; c < KD_BN; ++c) acc[c] += (long long)__float2int_rn(v[c]) << sh;
                 }
 #pragma unroll
             for (int cc = 0; cc < KD_BN; ++cc) {
@@ -567,8 +591,8 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
                 float2 val = df_zero();
                 if (row < args.N) {
                     const int y = args.rstate[(int64_t)b * args.Nx + row] & 3;
-                    const long long tot = (long long)acc[cc] - args.csum[(int64_t)b * 16 + y * 4 + c];
-                    val = df_mul(df_from_ll(tot), iq);
+                    const long long tot = acc[cc] - args.csum[(int64_t)b * 16 + y * 4 + c];
+                    val = df_mul(df_from_ll_fast(tot), iq);
                 }
                 args.KR[((int64_t)b * args.Nx + row) * 4 + c] = val;
             }
@@ -645,10 +669,10 @@ __global__ void k_split_dir(const SlotDev *__restrict__ sd, const int32_t *__res
 
 // R (float4 per sequence) -> B rows p*4+a, columns i, fp16 hi and lo of R*2^e
 __global__ void k_split_R(const int32_t *__restrict__ list, int64_t Nx, const float4 *__restrict__ R, float sc,
-                          __half *__restrict__ hi, __half *__restrict__ lo)
+                          __half *__restrict__ hi, __half *__restrict__ lo, int direct)
 {
     const int P = blockIdx.y;
-    const int b = list[P];
+    const int b = direct ? P : list[P];   // direct: R rows by list position (digit planes)
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Nx; i += (int64_t)gridDim.x * blockDim.x) {
         const float4 v = R[(int64_t)b * Nx + i];
         const float vv[4] = {v.x * sc, v.y * sc, v.z * sc, v.w * sc};
@@ -881,12 +905,18 @@ cudaError_t tc_launch_fwd(const TcPlan *pl, const Problem &P, const SlotDev *sd,
 
 cudaError_t tc_launch_bwd(const TcPlan *pl, const Problem &P, const SlotDev *sd, const int32_t *list, int n,
                           const float *R, float r_scale, __half *Rhi, __half *Rlo, float *gpool, int *err,
-                          cudaStream_t st, bool exact_fp16)
+                          cudaStream_t st, bool exact_fp16, double *gmax_acc, int gmax_stride, int planes)
 {
     if (n <= 0) return cudaSuccess;
+    const int nslot = n;
+    if (planes > 1) {
+        if ((int64_t)planes * n > P.Bmax) return cudaErrorInvalidValue;   // B operand rows and gpool buffers
+        n *= planes;
+    }
     {
         dim3 g((unsigned)std::min<int64_t>((P.Nx + 255) / 256, 64), (unsigned)n);
-        tc::k_split_R<<<g, 256, 0, st>>>(list, P.Nx, reinterpret_cast<const float4 *>(R), r_scale, Rhi, Rlo);
+        tc::k_split_R<<<g, 256, 0, st>>>(list, P.Nx, reinterpret_cast<const float4 *>(R), r_scale, Rhi, Rlo,
+                                          planes > 1 ? 1 : 0);
     }
     tc::GemmArgs a{};
     a.mode = tc::MODE_BWD;
@@ -900,6 +930,10 @@ cudaError_t tc_launch_bwd(const TcPlan *pl, const Problem &P, const SlotDev *sd,
     a.Dp = P.Dp;
     a.inv_scale_bwd = 1.0f / r_scale;
     a.hi_only = exact_fp16 ? 1 : 0;
+    a.gmax_acc = gmax_acc;
+    a.gmax_stride = gmax_stride;
+    a.planes = planes > 1 ? planes : 1;
+    a.nslot = nslot;
     a.Nx = P.Nx;
     a.err = err;
     launch_gemm_any(msub_choice(), (int)((4 * P.L + tc::BM - 1) / tc::BM), (4 * n + tc::BN - 1) / tc::BN, 1,

@@ -208,6 +208,65 @@ class Engine:
                     h2d_bytes=p.h2d_bytes, d2h_bytes=p.d2h_bytes)
 
 
+@dataclass
+class TuneResult:
+    batch: int               # chosen slots per lane
+    lanes: int               # chosen solver lanes
+    n_done: int              # leading loci of the list solved by the probes
+    scores: np.ndarray | None  # their score rows (n_done x L)
+    stats: list              # their per-locus statistics (dicts)
+    entries: list            # per candidate: batch, lanes, n_loci, status, device_ms, iterations_per_s
+    cached: bool             # the choice came from the cache file (no probe ran)
+
+
+def autotune(states: np.ndarray, weights: np.ndarray, loci, *, form: int = _lib.FORM_DUAL,
+             max_fraction: float = 0.25, cache_path: str | None = None, device: int = 0,
+             lambda_h: float = -1.0, lambda_J: float = -1.0, gradient_threshold: float = 1e-3,
+             want_scores: bool = True) -> TuneResult:
+    """Choose batch and lanes for this alignment shape by solving the first
+    loci of `loci` with candidate configurations (sdca_autotune).  The probe
+    loci are solved for real: result.scores / result.stats hold their rows
+    and statistics; continue with loci[result.n_done:] on an Engine built
+    with result.batch and result.lanes."""
+    lib = _lib.load()
+    st = np.ascontiguousarray(states, dtype=np.uint8)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    loci = np.ascontiguousarray(loci, dtype=np.uint32)
+    N, L = st.shape
+    cfg = _lib.Config()
+    lib.sdca_config_default(C.byref(cfg))
+    cfg.n_seqs, cfg.n_loci = N, L
+    cfg.lambda_h, cfg.lambda_J, cfg.gradient_threshold = float(lambda_h), float(lambda_J), float(gradient_threshold)
+    cfg.form, cfg.device = int(form), int(device)
+    n = len(loci)
+    budget = int(max_fraction * n)
+    scores = np.zeros((budget, L), dtype=np.float32) if want_scores and budget > 0 else None
+    sc_full = None
+    if scores is not None:
+        # the library writes rows by list position; the probes stay within the budget
+        sc_full = scores
+    stats = (_lib.LocusStat * max(budget, 1))()
+    best = _lib.Config()
+    done = C.c_size_t()
+    ents = (_lib.TuneEntry * _lib.TUNE_MAX_ENTRIES)()
+    nent = C.c_int32()
+    rc = lib.sdca_autotune(C.byref(cfg), _ptr(st), _ptr(w), _ptr(loci), min(n, budget if budget > 0 else 0),
+                           1.0 if budget > 0 else 0.0,
+                           None if cache_path is None else cache_path.encode(), _ptr(sc_full),
+                           C.cast(stats, C.c_void_p), C.byref(done), C.byref(best), C.cast(ents, C.c_void_p),
+                           C.byref(nent))
+    if rc != 0:
+        raise EngineError(rc, lib.sdca_last_error(None).decode())
+    nd = int(done.value)
+    st_list = [dict(f=s.f, gnorm=s.gnorm, iterations=s.iterations, nfeval=s.nfeval, status=s.status)
+               for s in stats[:nd]]
+    entries = [dict(batch=e.batch, lanes=e.lanes, n_loci=e.n_loci, status=e.status, device_ms=e.device_ms,
+                    iterations_per_s=e.iterations_per_s) for e in ents[:nent.value]]
+    return TuneResult(batch=best.batch, lanes=best.lanes, n_done=nd,
+                      scores=None if scores is None else scores[:nd], stats=st_list, entries=entries,
+                      cached=nent.value == 0)
+
+
 def coupling_lines(scores: np.ndarray, loci, translation=None, base: int = 1):
     """The lines SuperDCA writes for mean-of-norms scoring
     (SuperDCA/include/plmDCA.hpp:667-693): for each r in the loci list and each

@@ -152,8 +152,8 @@ def test_synthetic_workloads_are_seeded():
 
 
 def test_ctypes_structs_match_the_header_layout(tmp_path):
-    """The ctypes mirrors of sdca_config, sdca_locus_stat and sdca_profile
-    have the C compiler's sizes and field offsets."""
+    """The ctypes mirrors of sdca_config, sdca_locus_stat, sdca_profile and
+    sdca_tune_entry have the C compiler's sizes and field offsets."""
     import shutil
     import subprocess
 
@@ -162,7 +162,8 @@ def test_ctypes_structs_match_the_header_layout(tmp_path):
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no C compiler")
-    structs = {"sdca_config": _lib.Config, "sdca_locus_stat": _lib.LocusStat, "sdca_profile": _lib.Profile}
+    structs = {"sdca_config": _lib.Config, "sdca_locus_stat": _lib.LocusStat, "sdca_profile": _lib.Profile,
+               "sdca_tune_entry": _lib.TuneEntry}
     lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "superdca_gb300.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
