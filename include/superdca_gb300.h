@@ -43,7 +43,8 @@ extern "C" {
 #define SDCA_FORM_TC 1        /* tcgen05 one-hot GEMMs, fp16 hi+lo, FP32 accumulate */
 #define SDCA_FORM_DUAL 2      /* the same L-BFGS iteration kept in the span of the sequences:
                                  N x 4 coefficients, one exact integer product with the
-                                 N x N agreement matrix per iteration; zero start only */
+                                 N x N agreement matrix per iteration; starts from zero
+                                 or from the per-sequence learned start (version-2 blob) */
 
 /* sdca_config.flags */
 #define SDCA_FLAG_HISTORY_BF16 0x1 /* keep L-BFGS (s, y) history in BF16 */
@@ -225,7 +226,7 @@ int sdca_abi_version(void);
  * an initial block J_rn (and optionally h fitted with J fixed).  The optimum is
  * unchanged (the objective is strictly convex); only the start moves.
  * The parameter blob holds sdca_mlp_blob_size() floats:
- *   [0] version (1), [1] neighbours k (1..8), [2] smoothing eps,
+ *   [0] version (1), [1] neighbours k (1..16), [2] smoothing eps,
  *   [3] 1: fit h by Newton's method with J fixed, 0: start from h = 0,
  *   [4, 44) input mean, [44, 84) input scale, W1 (128 x 40), b1 (128),
  *   W2 (128 x 128), b2 (128), W3 (16 x 128), b3 (16), output scale (16).
@@ -236,8 +237,29 @@ int sdca_abi_version(void);
  * output[s][a] * scale[s*4+a] * B_eff / (2 lambda_J). */
 
 /* Enable the warm start with this blob for later sdca_solve* calls whose
- * x_init is NULL; params = NULL disables it. */
+ * x_init is NULL; params = NULL disables it.  The tensor-core and plain
+ * forms take the per-pair blob above (version 1).  The dual form takes a
+ * per-sequence blob (version 2, the same network and layout; [1] = 16
+ * neighbours, [2] = shrinkage alpha in (0, 1], [3] = 0): from statistics of
+ * each sequence at the target column -- onehot(s_i(r)), the column's weighted
+ * state frequencies, the state frequencies among its 1, 3, 8 and 16 nearest
+ * neighbours in Hamming distance and those neighbours' distances over L
+ * (inputs 0..27; 28..39 are 0) -- the network predicts the sequence's
+ * converged residual p_i - onehot(s_i(r)) (outputs 0..3 times the output
+ * scale), centred over the states and scaled into [-1, 1] where larger.
+ * The start is x0 = (Phi^T a0, 0) with a0 = -alpha w_i (predicted residual)
+ * / (2 lambda_J), the form an optimum has in the span of the sequences, and
+ * K a0 is formed exactly, so the iteration stays exact.  The network runs on
+ * the tensor cores with BF16 weights (an image of the blob's FP32 weights). */
 int sdca_set_warm_start(sdca_handle *h, const float *params, size_t n_params);
+
+/* Training data for the dual form's per-sequence start: for each listed
+ * locus, the statistics above for every sequence (feats: n_loci x N x 40
+ * floats) and, from a solve of the loci (stats as sdca_solve), the
+ * converged residual rows w_i (p_i - onehot(s_i(r))) (rho: n_loci x N x 4
+ * floats).  Dual form only. */
+int sdca_ws_dual_data(sdca_handle *h, const uint32_t *loci, size_t n_loci, float *feats, float *rho,
+                      sdca_locus_stat *stats);
 
 /* Pair statistics of target loci (for training): out holds n_loci x n_sel x
  * 40 floats for pairs (loci[k], sel[k*n_sel + j]), or n_loci x L x 40 when

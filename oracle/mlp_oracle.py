@@ -54,3 +54,25 @@ def loss_and_grad(p, X, T):
     g[W1:B1] = (d1.T @ xn).ravel()
     g[B1:W2] = d1.sum(0)
     return loss, g
+
+
+def bf16(a):
+    """Round float32 values to bfloat16 (nearest, ties to even), returned as float32."""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000).astype(np.uint32)
+    return r.view(np.float32)
+
+
+def forward_bf16(p, X):
+    """The tensor-core forward's arithmetic: normalised inputs, weights and
+    hidden activations rounded to bfloat16, sums and biases in full
+    precision (the kernel accumulates in FP32)."""
+    q = unpack(np.asarray(p, dtype=np.float32))
+    xn = (np.asarray(X, dtype=np.float32) - q["mean"].astype(np.float32)) * q["scale"].astype(np.float32)
+    a1 = bf16(xn).astype(np.float64)
+    h1 = np.maximum(a1 @ bf16(q["W1"]).astype(np.float64).T + q["b1"], 0.0)
+    a2 = bf16(h1).astype(np.float64)
+    h2 = np.maximum(a2 @ bf16(q["W2"]).astype(np.float64).T + q["b2"], 0.0)
+    a3 = bf16(h2).astype(np.float64)
+    return a3 @ bf16(q["W3"]).astype(np.float64).T + q["b3"]

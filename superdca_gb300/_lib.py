@@ -33,7 +33,8 @@ EXPORTS = ["sdca_abi_version", "sdca_config_default", "sdca_create", "sdca_set_a
            "sdca_compute_weights", "sdca_get_lambdas", "sdca_solve", "sdca_solve_ex", "sdca_solve_sel", "sdca_eval",
            "sdca_get_profile", "sdca_last_error", "sdca_destroy", "sdca_eval_noalloc",
            "sdca_set_warm_start", "sdca_ws_features", "sdca_mlp_blob_size", "sdca_mlp_grad",
-           "sdca_mlp_predict", "sdca_mlp_train", "sdca_mlp_last_error", "sdca_set_targets", "sdca_autotune"]
+           "sdca_mlp_predict", "sdca_mlp_train", "sdca_mlp_last_error", "sdca_set_targets", "sdca_autotune",
+           "sdca_ws_dual_data"]
 
 
 class Config(C.Structure):
@@ -97,6 +98,7 @@ def load(path: str = LIB_PATH):
     L.sdca_eval_noalloc.argtypes = [vp, i64, i64, vp, dp, dp, C.c_uint32, vp, vp, vp, vp]
     L.sdca_set_warm_start.argtypes = [vp, vp, C.c_size_t]
     L.sdca_set_targets.argtypes = [vp, vp, i64]
+    L.sdca_ws_dual_data.argtypes = [vp, vp, C.c_size_t, vp, vp, vp]
     L.sdca_autotune.argtypes = [C.POINTER(Config), vp, vp, vp, C.c_size_t, dp, C.c_char_p, vp, vp,
                                 C.POINTER(C.c_size_t), C.POINTER(Config), vp, C.POINTER(C.c_int32)]
     L.sdca_ws_features.argtypes = [vp, C.c_int, C.c_float, vp, C.c_size_t, vp, C.c_size_t, vp]

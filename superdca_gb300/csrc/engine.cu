@@ -52,6 +52,7 @@ enum Phase {
     PH_REFRESH,     // logits recomputed from the stored parameters: needs the evaluation there
     PH_READY_REFRESH,  // re-evaluated, waiting for the gradient pass (history kept)
     PH_CONVERT,     // dual form: stopped, waiting for its parameters to be formed
+    PH_WARM,        // dual form: its learned start is formed this round (then PH_INIT)
 };
 
 struct SlotHost {
@@ -171,14 +172,21 @@ struct sdca_handle {
 
     // learned warm start (warmstart.cu, mlp.cu)
     float *ws_params = nullptr;
+    uint16_t *ws_wb = nullptr;     // BF16 image of the network's weights (tensor-core forward)
+    int *ws_err = nullptr;         // set when a wait of the tensor-core forward gives up
     bool ws_on = false;
     int ws_k = 0;
     float ws_eps = 0.f;
     bool ws_hfit = false;          // fit h to the predicted J (blob flag) or start from h = 0
-    int32_t *knn = nullptr;
+    int32_t *knn = nullptr, *knn_d = nullptr;   // neighbours and their Hamming distances
     int knn_k = 0;                 // k of the nearest-neighbour table held (0: none)
+    // the dual form's learned start (blob version 2): shrinkage and buffers
+    // for up to dws_cap slots per network pass
+    bool ws_dual = false;
+    float ws_alpha = 0.f;
+    float *dws_feats = nullptr, *dws_out = nullptr;
+    int dws_cap = 0;
     float *ws_R = nullptr, *ws_feats = nullptr, *ws_out = nullptr;
-    float *ws_xn = nullptr, *ws_h1 = nullptr, *ws_h2 = nullptr;
     int32_t *ws_idx = nullptr;     // [0, WS_G): slots, [WS_G, 2 WS_G): loci
     double *ws_xmax = nullptr;
 
@@ -546,13 +554,9 @@ int ws_buffers(sdca_handle *h)
 {
     if (h->ws_feats) return SDCA_OK;
     const Problem &P = h->P;
-    const size_t rows = (size_t)std::min<int64_t>(WS_ROWS, WS_G * P.L);
     int rc;
     if ((rc = dalloc(h, &h->ws_R, (size_t)WS_G * P.Nx * 8))) return rc;   // [g][Nx][8], or R2 [g][Nx][4]
     if ((rc = dalloc(h, &h->ws_out, (size_t)WS_G * P.L * MLP_OUT))) return rc;
-    if ((rc = dalloc(h, &h->ws_xn, rows * MLP_IN))) return rc;
-    if ((rc = dalloc(h, &h->ws_h1, rows * MLP_H))) return rc;
-    if ((rc = dalloc(h, &h->ws_h2, rows * MLP_H))) return rc;
     if ((rc = dalloc(h, &h->ws_idx, 2 * WS_G))) return rc;
     if ((rc = dalloc(h, &h->ws_xmax, WS_G))) return rc;
     return dalloc(h, &h->ws_feats, (size_t)WS_G * P.L * MLP_IN);
@@ -567,6 +571,7 @@ int ws_knn(sdca_handle *h, int k)
     if (P.N > 32768) return fail(h, SDCA_E_UNSUPPORTED, "the warm start supports at most 32768 sequences");
     int rc;
     if (!h->knn && (rc = dalloc(h, &h->knn, (size_t)P.N * WS_MAX_K))) return rc;
+    if (!h->knn_d && (rc = dalloc(h, &h->knn_d, (size_t)P.N * WS_MAX_K))) return rc;
     const int64_t W = (P.L + 31) / 32;
     uint64_t *packed = nullptr;
     int32_t *dist = nullptr;
@@ -577,7 +582,7 @@ int ws_knn(sdca_handle *h, int k)
         return fail(h, SDCA_E_NOMEM, "device allocation for the neighbour table failed");
     }
     launch_distances(h->X, P.Lx, (int)P.N, (int)P.L, packed, dist, h->stream);
-    launch_knn(dist, (int)P.N, k, h->knn, h->stream);
+    launch_knn(dist, (int)P.N, k, h->knn, h->stream, h->knn_d);
     const cudaError_t e1 = cudaGetLastError();
     const cudaError_t e2 = cudaStreamSynchronize(h->stream);
     cudaFree(packed);
@@ -661,10 +666,10 @@ int ws_begin(sdca_handle *h, const std::vector<int32_t> &bs)
         CK(cudaMemsetAsync(h->ws_xmax, 0, sizeof(double) * WS_G, h->stream));
         {
             const int64_t M = (int64_t)G * P.L, rows = std::min<int64_t>(WS_ROWS, WS_G * P.L);
-            Timed t(h, SDCA_K_OTHER, (int)(4 * ((M + rows - 1) / rows) + 1), G);
+            Timed t(h, SDCA_K_OTHER, (int)((M + rows - 1) / rows + 1), G);
             for (int64_t r0 = 0; r0 < M; r0 += rows)
-                mlp_infer(h->ws_params, h->ws_feats + r0 * MLP_IN, std::min(rows, M - r0), h->ws_xn, h->ws_h1,
-                          h->ws_h2, h->ws_out + r0 * MLP_OUT, h->stream);
+                mlp_infer(h->ws_params, h->ws_wb, h->ws_feats + r0 * MLP_IN, std::min(rows, M - r0),
+                          h->ws_out + r0 * MLP_OUT, h->ws_err, h->stream);
             launch_ws_scatter((int)P.L, P.Dp, h->ws_idx, h->ws_idx + WS_G, G, h->ws_out, h->ws_params,
                               P.b_eff / (2.0 * P.lambda_J), h->wa, h->ws_xmax, h->stream);
         }
@@ -672,8 +677,10 @@ int ws_begin(sdca_handle *h, const std::vector<int32_t> &bs)
         std::vector<double> xm(G);
         auto fetch_xmax = [&]() -> int {
             CK(cudaMemcpyAsync(xm.data(), h->ws_xmax, sizeof(double) * G, cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaMemcpyAsync(h->flag_h + 2, h->ws_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
             const int r_ = stream_sync(h);
             if (r_) return r_;
+            if (h->flag_h[2]) return fail(h, SDCA_E_CUDA, "warm start: a tensor-core pipeline wait gave up");
             for (int g = 0; g < G; ++g) {
                 const int b = grp[g];
                 h->slots[b].xmax = xm[g];
@@ -707,6 +714,7 @@ struct Queue {
     const double *x_init = nullptr;
     double *x_out = nullptr;
     const int64_t *x_rows = nullptr;       // row of x_out per list position (-1: none); null: row k
+    float *rho_out = nullptr;              // dual form: converged residual rows (n x N x 4) or null
     float *scores = nullptr;
     sdca_locus_stat *stats = nullptr;
     std::vector<float> xbuf;
@@ -729,7 +737,8 @@ int refill(sdca_handle *h, Queue &Qu)
         if (k < 0) break;
         const float *x0 = nullptr;
         if (Qu.x_init && h->form == SDCA_FORM_DUAL)
-            return fail(h, SDCA_E_UNSUPPORTED, "the dual form starts every locus from zero (no x_init)");
+            return fail(h, SDCA_E_UNSUPPORTED,
+                        "the dual form takes no arbitrary start point (x_init): it starts from zero or learned");
         if (Qu.x_init) {
             const double *xr = Qu.x_init + k * (QQ * h->P.L + Q);
             ref_to_engine(h->P, h->scan ? -1 : (int64_t)Qu.loci[k], xr, Qu.xbuf.data());
@@ -737,6 +746,7 @@ int refill(sdca_handle *h, Queue &Qu)
         }
         int rc = slot_begin(h, b, k, (int32_t)Qu.loci[k], x0);
         if (rc) return rc;
+        if (h->form == SDCA_FORM_DUAL && h->ws_dual) h->slots[b].phase = PH_WARM;
         if (x0) {
             // the copy reads the staging buffer: finish it before the next slot reuses it
             { const int r_ = stream_sync(h); if (r_) return r_; }
@@ -1386,6 +1396,12 @@ int dual_retire(sdca_handle *h, Queue &Qu, const std::vector<int32_t> &done)
             engine_to_ref(P, xe.data(), Qu.x_out + row * (QQ * P.L + Q));
             h->prof.d2h_bytes += (int64_t)sizeof(float) * P.Dp;
         }
+        if (Qu.rho_out) {
+            // the final evaluation's residual rows w_i (p_i - onehot(y_i))
+            CK(cudaMemcpyAsync(Qu.rho_out + S.k * P.N * 4, h->R + (int64_t)b * P.Nx * 4, sizeof(float) * P.N * 4,
+                               cudaMemcpyDeviceToHost, h->stream));
+            { const int r_ = stream_sync(h); if (r_) return r_; }
+        }
         if (Qu.stats) {
             sdca_locus_stat &st = Qu.stats[S.k];
             st.f = S.f_final;
@@ -1423,29 +1439,53 @@ void dual_take_summary(SlotHost &S, const DualSum &D)
     for (int a = 0; a < Q; ++a) S.eta_x[a] = D.eta_x[a];
 }
 
+// The dual form's learned start, first half: per-sequence statistics of the
+// slots' target columns, the network, and its residual prediction into the
+// slots' R rows (the round's K rho pass and k_dual_ws_init finish it).
+int dual_ws_rows(sdca_handle *h, int nW, const int32_t *l_W)
+{
+    const Problem &P = h->P;
+    int rc;
+    if (h->knn_k != DWS_K && (rc = ws_knn(h, DWS_K))) return rc;
+    Timed t(h, SDCA_K_OTHER, 3 * ((nW + h->dws_cap - 1) / h->dws_cap), nW);   // statistics, network, rows
+    for (int c0 = 0; c0 < nW; c0 += h->dws_cap) {
+        const int n = std::min(h->dws_cap, nW - c0);
+        launch_dual_ws_feats(h->rstate, l_W + c0, n, (int)P.N, P.Nx, (int)P.L, h->w, h->knn, h->knn_d, h->dws_feats,
+                             h->stream);
+        mlp_infer(h->ws_params, h->ws_wb, h->dws_feats, (int64_t)n * P.Nx, h->dws_out, h->ws_err, h->stream);
+        launch_dual_ws_r(l_W + c0, n, (int)P.N, P.Nx, h->dws_out, h->ws_params, h->ws_alpha, h->wf, h->R, h->stream);
+    }
+    CKL();
+    return SDCA_OK;
+}
+
 // One round: start/final evaluations, line searches, accepts, the gradient
 // pass and the control kernel for every slot, then the directions.
 int dual_round(sdca_handle *h, Queue &Qu)
 {
     const Problem &P = h->P;
     const double gtol = h->cfg.gradient_threshold;
-    std::vector<int32_t> ef, T, G;
+    std::vector<int32_t> ef, T, G, W;
     for (int b = 0; b < P.Bmax; ++b) {
         const int ph = h->slots[b].phase;
         if (ph == PH_INIT || ph == PH_FINALIZE) ef.push_back(b);
         if (ph == PH_LS) T.push_back(b);   // iterating on the device
+        if (ph == PH_WARM) W.push_back(b); // learned start formed this round
     }
     G = T;
     for (int b : ef)
         if (h->slots[b].phase == PH_INIT) G.push_back(b);
-    if (ef.empty() && G.empty()) return dual_convert(h, true);
-    // the lists: [ef | T | G] in one upload
+    if (ef.empty() && G.empty() && W.empty()) return dual_convert(h, true);
+    // the lists: [ef | T | G, W] in one upload (the K rho pass takes G and W)
     const int32_t *l_ef = h->dlist, *l_T = h->dlist + P.Bmax, *l_G = h->dlist + 2 * P.Bmax;
+    const int32_t *l_W = l_G + G.size();
     {
         std::vector<int32_t> all(3 * (size_t)P.Bmax, 0);
         std::copy(ef.begin(), ef.end(), all.begin());
         std::copy(T.begin(), T.end(), all.begin() + P.Bmax);
         std::copy(G.begin(), G.end(), all.begin() + 2 * P.Bmax);
+        std::copy(W.begin(), W.end(), all.begin() + 2 * P.Bmax + G.size());
+        for (int b : W) h->sd_h[b].locus = h->scan ? -1 : h->slots[b].locus;
         for (int b : ef) {
             h->sd_h[b].locus = h->scan ? -1 : h->slots[b].locus;
             h->sd_h[b].gcur = 0;
@@ -1456,8 +1496,9 @@ int dual_round(sdca_handle *h, Queue &Qu)
         if (rc) return rc;
         if ((rc = staged_h2d(h, h->dlist, all.data(), sizeof(int32_t) * all.size()))) return rc;
     }
-    int rc = zero_acc(h);
-    if (rc) return rc;
+    int rc;
+    if (!W.empty() && (rc = dual_ws_rows(h, (int)W.size(), l_W))) return rc;
+    if ((rc = zero_acc(h))) return rc;
     if (!ef.empty()) {
         Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)ef.size());
         launch_trial_dual(P, h->sd, l_ef, (int)ef.size(), lbase_df(h), h->udf, h->rstate, h->w, h->R, h->acc,
@@ -1473,8 +1514,8 @@ int dual_round(sdca_handle *h, Queue &Qu)
         launch_dual_accept(P, h->ctl, l_T, (int)T.size(), h->dv, h->udf, lbase_df(h), h->stream);
     }
     CKL();
-    const int nG = (int)G.size();
-    if (nG > 0) {
+    const int nG = (int)G.size(), nGW = nG + (int)W.size();
+    if (nGW > 0) {
         CK(cudaMemsetAsync(h->csum, 0, sizeof(long long) * 16 * P.Bmax, h->stream));
         CK(cudaMemsetAsync(h->amax, 0, sizeof(double) * 2 * P.Bmax, h->stream));
         CK(cudaMemsetAsync(h->dots, 0, sizeof(double) * 4 * MAXHIST * P.Bmax, h->stream));
@@ -1483,17 +1524,25 @@ int dual_round(sdca_handle *h, Queue &Qu)
         // one-hot contractions X^T a (max-norm checks, final J), "accept" the
         // iterate update and gradient assembly, "other" the control kernel.
         {
-            Timed t(h, SDCA_K_ACCEPT, 1, nG);
-            launch_dual_quant(P, h->sd, l_G, nG, h->R, h->rstate, h->qscale, h->rq, h->csum, h->stream);
+            Timed t(h, SDCA_K_ACCEPT, 1, nGW);
+            launch_dual_quant(P, h->sd, l_G, nGW, h->R, h->rstate, h->qscale, h->rq, h->csum, h->stream);
         }
         {
-            Timed t(h, SDCA_K_FORWARD, h->kd ? 2 : 1, nG);
+            Timed t(h, SDCA_K_FORWARD, h->kd ? 2 : 1, nGW);
             if (h->kd)
-                CK(tc_launch_kdig(h->kd, P, l_G, nG, h->rq, h->rstate, h->csum, 1.0 / h->qscale, h->Rd, h->KR,
+                CK(tc_launch_kdig(h->kd, P, l_G, nGW, h->rq, h->rstate, h->csum, 1.0 / h->qscale, h->Rd, h->KR,
                                   h->tc_err, h->stream));
             else
-                launch_dual_kprod(P, l_G, nG, h->rstate, h->Kmat, h->qscale, h->rq, h->csum, h->KR, h->stream);
+                launch_dual_kprod(P, l_G, nGW, h->rstate, h->Kmat, h->qscale, h->rq, h->csum, h->KR, h->stream);
         }
+        if (!W.empty()) {
+            // the learned start: a_x = -rho^ / (2 lambda_J), K a_x exactly from the pass above
+            Timed t(h, SDCA_K_OTHER, 1, (int64_t)W.size());
+            launch_dual_ws_init(P, l_W, (int)W.size(), -0.5 / P.lambda_J, h->qscale, h->rq, h->KR, h->dv, lbase_df(h),
+                                h->stream);
+        }
+    }
+    if (nG > 0) {
         {
             Timed t(h, SDCA_K_ACCEPT, 1, nG);
             launch_dual_grad(P, h->ctl, l_G, nG, h->qscale, h->rq, h->KR, h->dv, h->acc, h->amax, h->stream);
@@ -1512,6 +1561,7 @@ int dual_round(sdca_handle *h, Queue &Qu)
     CK(cudaMemcpyAsync(h->sum_h, h->sum, sizeof(DualSum) * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaMemcpyAsync(h->acc_h, h->acc, sizeof(double) * NACC * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
     if (h->tc_err) CK(cudaMemcpyAsync(h->flag_h + 1, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    if (!W.empty()) CK(cudaMemcpyAsync(h->flag_h + 2, h->ws_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaEventRecord(h->ev_round, h->stream));
     if (nG > 0) {
         CK(cudaMemsetAsync(h->dacc, 0, sizeof(double) * NDACC * P.Bmax, h->stream));
@@ -1525,9 +1575,12 @@ int dual_round(sdca_handle *h, Queue &Qu)
     h->stage_off = 0;
     if (h->tc_err && h->flag_h[1])
         return fail(h, SDCA_E_CUDA, "tensor-core pipeline wait timed out (kernel abandoned its tile)");
+    if (!W.empty() && h->flag_h[2])
+        return fail(h, SDCA_E_CUDA, "warm start: a tensor-core pipeline wait gave up");
     if (Qu.scores) dual_flush_rows(h, Qu);
 
     std::vector<int32_t> done, chk;
+    for (int b : W) h->slots[b].phase = PH_INIT;   // start evaluation next round
     for (int b : ef) {
         SlotHost &S = h->slots[b];
         if (S.phase != PH_FINALIZE) continue;
@@ -1628,6 +1681,100 @@ int check_ready(sdca_handle *h)
 }
 
 } // namespace
+
+// the network on the device: the parameter blob, its BF16 weight image and
+// the error word of the tensor-core forward
+static int ws_network(sdca_handle *h, const float *params)
+{
+    int rc;
+    if (!h->ws_params && (rc = dalloc(h, &h->ws_params, MLP_BLOB_SIZE))) return rc;
+    if (!h->ws_wb && (rc = dalloc(h, &h->ws_wb, MLP_WB_ELEMS))) return rc;
+    if (!h->ws_err && (rc = dalloc(h, &h->ws_err, 1))) return rc;
+    CK(cudaMemcpyAsync(h->ws_params, params, sizeof(float) * MLP_BLOB_SIZE, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(h->ws_err, 0, sizeof(int), h->stream));
+    mlp_pack(h->ws_params, h->ws_wb, h->stream);
+    CKL();
+    return stream_sync(h);
+}
+
+// the solve of a loci list over the handle's lanes (sdca_solve_sel, and the
+// training data of the dual form's start with rho_out)
+static int solve_queue(sdca_handle *h, const uint32_t *loci, size_t n_loci, const double *x_init,
+                       const int64_t *x_rows, double *x_out, float *scores, sdca_locus_stat *stats, float *rho_out)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (n_loci > 0 && !loci) return fail(h, SDCA_E_ARG, "null loci list");
+    const int64_t nt = h->scan ? h->LT : h->P.L;   // scan mode: loci are target columns
+    for (size_t k = 0; k < n_loci; ++k)
+        if ((int64_t)loci[k] >= nt) return fail(h, SDCA_E_ARG, "locus index out of range");
+    if (x_rows && !x_out) return fail(h, SDCA_E_ARG, "x_rows given without x_out");
+    if (x_rows)
+        for (size_t k = 0; k < n_loci; ++k)
+            if (x_rows[k] < -1) return fail(h, SDCA_E_ARG, "x_rows entries must be -1 or a row index");
+    std::atomic<size_t> next{0};
+    std::atomic<bool> abort{false};
+    auto queue_for = [&](sdca_handle *l, Queue &Qu) {
+        Qu.loci = loci;
+        Qu.n = n_loci;
+        Qu.next = &next;
+        Qu.abort = &abort;
+        Qu.x_init = x_init;
+        Qu.x_out = x_out;
+        Qu.x_rows = x_rows;
+        Qu.rho_out = rho_out;
+        Qu.scores = scores;
+        Qu.stats = stats;
+        if (x_init) Qu.xbuf.resize(l->P.Dp);
+    };
+    if (h->sub.empty()) {
+        Queue Qu;
+        queue_for(h, Qu);
+        return solve_lane(h, Qu, nullptr);
+    }
+    // lanes: this thread runs lane 0, one thread per further lane; all take
+    // loci from the same queue and write disjoint rows of the outputs
+    CK(cudaSetDevice(h->cfg.device));
+    CK(cudaEventRecord(h->ev_lanes, h->stream));
+    const size_t nl = 1 + h->sub.size();
+    std::vector<int> rcs(nl, SDCA_OK);
+    auto run = [&](size_t i) {
+        sdca_handle *l = i == 0 ? h : h->sub[i - 1];
+        Queue Qu;
+        queue_for(l, Qu);
+        rcs[i] = solve_lane(l, Qu, h->ev_lanes);
+        if (rcs[i]) abort.store(true);
+    };
+    std::vector<std::thread> th;
+    for (size_t i = 1; i < nl; ++i) {
+        try {
+            th.emplace_back(run, i);
+        } catch (...) {
+            // no thread: the lanes that run take this lane's loci
+        }
+    }
+    run(0);
+    for (auto &t : th) t.join();
+    for (size_t i = 0; i < nl; ++i)
+        if (rcs[i]) return i == 0 ? rcs[i] : fail(h, rcs[i], "lane " + std::to_string(i) + ": " + h->sub[i - 1]->err);
+    for (const sdca_handle *l : h->sub) {
+        const sdca_profile &q = l->prof;
+        sdca_profile &p = h->prof;
+        p.solve_ms = std::max(p.solve_ms, q.solve_ms);
+        for (int c = 0; c < 8; ++c) {
+            p.kernel_ms[c] += q.kernel_ms[c];
+            p.kernel_launches[c] += q.kernel_launches[c];
+            p.kernel_units[c] += q.kernel_units[c];
+        }
+        p.gpu_launches += q.gpu_launches;
+        p.iterations += q.iterations;
+        p.contractions += q.contractions;
+        p.h2d_bytes += q.h2d_bytes;
+        p.d2h_bytes += q.d2h_bytes;
+    }
+    return SDCA_OK;
+}
+
 
 extern "C" {
 
@@ -1942,76 +2089,57 @@ int sdca_get_lambdas(const sdca_handle *h, double *lambda_h, double *lambda_J, d
 int sdca_solve_sel(sdca_handle *h, const uint32_t *loci, size_t n_loci, const double *x_init,
                    const int64_t *x_rows, double *x_out, float *scores, sdca_locus_stat *stats)
 {
+    return solve_queue(h, loci, n_loci, x_init, x_rows, x_out, scores, stats, nullptr);
+}
+
+int sdca_ws_dual_data(sdca_handle *h, const uint32_t *loci, size_t n_loci, float *feats, float *rho,
+                      sdca_locus_stat *stats)
+{
     int rc = check_ready(h);
     if (rc) return rc;
-    if (n_loci > 0 && !loci) return fail(h, SDCA_E_ARG, "null loci list");
-    const int64_t nt = h->scan ? h->LT : h->P.L;   // scan mode: loci are target columns
+    if (h->form != SDCA_FORM_DUAL) return fail(h, SDCA_E_UNSUPPORTED, "training data of the dual form's start");
+    if (n_loci > 0 && (!loci || !feats || !rho)) return fail(h, SDCA_E_ARG, "null loci, feats or rho");
+    const Problem &P = h->P;
+    const int64_t nt = h->scan ? h->LT : P.L;
     for (size_t k = 0; k < n_loci; ++k)
         if ((int64_t)loci[k] >= nt) return fail(h, SDCA_E_ARG, "locus index out of range");
-    if (x_rows && !x_out) return fail(h, SDCA_E_ARG, "x_rows given without x_out");
-    if (x_rows)
-        for (size_t k = 0; k < n_loci; ++k)
-            if (x_rows[k] < -1) return fail(h, SDCA_E_ARG, "x_rows entries must be -1 or a row index");
-    std::atomic<size_t> next{0};
-    std::atomic<bool> abort{false};
-    auto queue_for = [&](sdca_handle *l, Queue &Qu) {
-        Qu.loci = loci;
-        Qu.n = n_loci;
-        Qu.next = &next;
-        Qu.abort = &abort;
-        Qu.x_init = x_init;
-        Qu.x_out = x_out;
-        Qu.x_rows = x_rows;
-        Qu.scores = scores;
-        Qu.stats = stats;
-        if (x_init) Qu.xbuf.resize(l->P.Dp);
-    };
-    if (h->sub.empty()) {
-        Queue Qu;
-        queue_for(h, Qu);
-        return solve_lane(h, Qu, nullptr);
-    }
-    // lanes: this thread runs lane 0, one thread per further lane; all take
-    // loci from the same queue and write disjoint rows of the outputs
     CK(cudaSetDevice(h->cfg.device));
-    CK(cudaEventRecord(h->ev_lanes, h->stream));
-    const size_t nl = 1 + h->sub.size();
-    std::vector<int> rcs(nl, SDCA_OK);
-    auto run = [&](size_t i) {
-        sdca_handle *l = i == 0 ? h : h->sub[i - 1];
-        Queue Qu;
-        queue_for(l, Qu);
-        rcs[i] = solve_lane(l, Qu, h->ev_lanes);
-        if (rcs[i]) abort.store(true);
-    };
-    std::vector<std::thread> th;
-    for (size_t i = 1; i < nl; ++i) {
-        try {
-            th.emplace_back(run, i);
-        } catch (...) {
-            // no thread: the lanes that run take this lane's loci
-        }
+    if ((rc = ws_knn(h, DWS_K))) return rc;
+    // statistics: the target columns of the listed loci, in chunks
+    const int cap = 32;
+    float *fe = nullptr;
+    int32_t *idx = nullptr;
+    if (cudaMalloc(&fe, sizeof(float) * cap * P.Nx * MLP_IN) != cudaSuccess ||
+        cudaMalloc(&idx, sizeof(int32_t) * cap) != cudaSuccess) {
+        cudaGetLastError();
+        if (fe) cudaFree(fe);
+        return fail(h, SDCA_E_NOMEM, "device allocation for the statistics failed");
     }
-    run(0);
-    for (auto &t : th) t.join();
-    for (size_t i = 0; i < nl; ++i)
-        if (rcs[i]) return i == 0 ? rcs[i] : fail(h, rcs[i], "lane " + std::to_string(i) + ": " + h->sub[i - 1]->err);
-    for (const sdca_handle *l : h->sub) {
-        const sdca_profile &q = l->prof;
-        sdca_profile &p = h->prof;
-        p.solve_ms = std::max(p.solve_ms, q.solve_ms);
-        for (int c = 0; c < 8; ++c) {
-            p.kernel_ms[c] += q.kernel_ms[c];
-            p.kernel_launches[c] += q.kernel_launches[c];
-            p.kernel_units[c] += q.kernel_units[c];
+    std::vector<float> buf((size_t)cap * P.Nx * MLP_IN);
+    int err = SDCA_OK;
+    for (size_t c0 = 0; c0 < n_loci && err == SDCA_OK; c0 += cap) {
+        const int n = (int)std::min<size_t>(cap, n_loci - c0);
+        std::vector<int32_t> li(loci + c0, loci + c0 + n);
+        if (cudaMemcpyAsync(idx, li.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) {
+            err = fail(h, SDCA_E_CUDA, "statistics upload failed");
+            break;
         }
-        p.gpu_launches += q.gpu_launches;
-        p.iterations += q.iterations;
-        p.contractions += q.contractions;
-        p.h2d_bytes += q.h2d_bytes;
-        p.d2h_bytes += q.d2h_bytes;
+        launch_dual_ws_feats(h->scan ? h->TT : h->XT, idx, n, (int)P.N, P.Nx, (int)P.L, h->w, h->knn, h->knn_d, fe,
+                             h->stream);
+        if (cudaMemcpyAsync(buf.data(), fe, sizeof(float) * n * P.Nx * MLP_IN, cudaMemcpyDeviceToHost, h->stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(h->stream) != cudaSuccess) {
+            err = fail(h, SDCA_E_CUDA, "statistics kernel failed");
+            break;
+        }
+        for (int g = 0; g < n; ++g)
+            std::memcpy(feats + ((c0 + g) * (size_t)P.N) * MLP_IN, buf.data() + (size_t)g * P.Nx * MLP_IN,
+                        sizeof(float) * P.N * MLP_IN);
     }
-    return SDCA_OK;
+    cudaFree(fe);
+    cudaFree(idx);
+    if (err) return err;
+    return solve_queue(h, loci, n_loci, nullptr, nullptr, nullptr, nullptr, stats, rho);
 }
 
 int sdca_solve_ex(sdca_handle *h, const uint32_t *loci, size_t n_loci, const double *x_init,
@@ -2205,25 +2333,45 @@ int sdca_set_warm_start(sdca_handle *h, const float *params, size_t n_params)
     if (!h) return SDCA_E_ARG;
     if (!params) {
         h->ws_on = false;
-        for (sdca_handle *s : h->sub) s->ws_on = false;
+        h->ws_dual = false;
+        for (sdca_handle *s : h->sub) s->ws_on = s->ws_dual = false;
         return SDCA_OK;
     }
-    if (h->form == SDCA_FORM_DUAL)
-        return fail(h, SDCA_E_UNSUPPORTED, "the dual form starts every locus from zero (no warm start)");
     if (n_params != (size_t)MLP_BLOB_SIZE)
         return fail(h, SDCA_E_ARG, "warm-start parameters: expected " + std::to_string(MLP_BLOB_SIZE) + " floats");
-    if (params[MLP_VERSION] != (float)MLP_BLOB_VERSION)
-        return fail(h, SDCA_E_ARG, "warm-start parameters: unknown version");
-    const float kf = params[MLP_KNN], eps = params[MLP_EPS];
-    if (!(kf >= 1.f && kf <= (float)WS_MAX_K && kf == std::floor(kf)) || !(eps >= 0.f) || !std::isfinite(eps))
-        return fail(h, SDCA_E_ARG, "warm-start parameters: neighbours must be 1..8 and eps >= 0");
     for (size_t i = 0; i < n_params; ++i)
         if (!std::isfinite(params[i])) return fail(h, SDCA_E_ARG, "warm-start parameters must be finite");
-    CK(cudaSetDevice(h->cfg.device));
     int rc;
-    if (!h->ws_params && (rc = dalloc(h, &h->ws_params, MLP_BLOB_SIZE))) return rc;
-    CK(cudaMemcpyAsync(h->ws_params, params, sizeof(float) * MLP_BLOB_SIZE, cudaMemcpyHostToDevice, h->stream));
-    if ((rc = stream_sync(h))) return rc;
+    if (h->form == SDCA_FORM_DUAL) {
+        // per-sequence blob (version 2): the start a0 = -alpha rho^ / (2 lambda_J)
+        if (params[MLP_VERSION] != (float)MLP_BLOB_VERSION_DUAL)
+            return fail(h, SDCA_E_ARG, "the dual form takes a per-sequence warm-start blob (version 2)");
+        if (params[MLP_KNN] != (float)DWS_K) return fail(h, SDCA_E_ARG, "warm-start parameters: neighbours must be 16");
+        const float alpha = params[MLP_ALPHA];
+        if (!(alpha > 0.f && alpha <= 1.f))
+            return fail(h, SDCA_E_ARG, "warm-start parameters: shrinkage must be in (0, 1]");
+        CK(cudaSetDevice(h->cfg.device));
+        if ((rc = ws_network(h, params))) return rc;
+        if (!h->dws_feats) {
+            const int cap = 32;
+            const size_t rows = (size_t)cap * h->P.Nx;
+            if ((rc = dalloc(h, &h->dws_feats, rows * MLP_IN)) || (rc = dalloc(h, &h->dws_out, rows * MLP_OUT)))
+                return rc;
+            h->dws_cap = cap;
+        }
+        h->ws_alpha = alpha;
+        h->ws_dual = true;
+        for (sdca_handle *s : h->sub)
+            if ((rc = sdca_set_warm_start(s, params, n_params))) return fail(h, rc, s->err);
+        return SDCA_OK;
+    }
+    if (params[MLP_VERSION] != (float)MLP_BLOB_VERSION)
+        return fail(h, SDCA_E_ARG, "warm-start parameters: this form takes a per-pair blob (version 1)");
+    const float kf = params[MLP_KNN], eps = params[MLP_EPS];
+    if (!(kf >= 1.f && kf <= (float)WS_MAX_K && kf == std::floor(kf)) || !(eps >= 0.f))
+        return fail(h, SDCA_E_ARG, "warm-start parameters: neighbours must be 1..16 and eps >= 0");
+    CK(cudaSetDevice(h->cfg.device));
+    if ((rc = ws_network(h, params))) return rc;
     h->ws_k = (int)kf;
     h->ws_eps = eps;
     h->ws_hfit = params[MLP_HFIT] != 0.f;
@@ -2239,7 +2387,7 @@ int sdca_ws_features(sdca_handle *h, int k, float eps, const uint32_t *loci, siz
     if (!h) return SDCA_E_ARG;
     if (!h->has_alignment) return fail(h, SDCA_E_STATE, "sdca_set_alignment must come first");
     if (!loci || !out) return fail(h, SDCA_E_ARG, "loci and out are required");
-    if (k < 1 || k > WS_MAX_K || !(eps >= 0.f)) return fail(h, SDCA_E_ARG, "k must be 1..8 and eps >= 0");
+    if (k < 1 || k > WS_MAX_K || !(eps >= 0.f)) return fail(h, SDCA_E_ARG, "k must be 1..16 and eps >= 0");
     const Problem &P = h->P;
     for (size_t i = 0; i < n_loci; ++i)
         if (loci[i] >= (uint32_t)P.L) return fail(h, SDCA_E_ARG, "locus index out of range");

@@ -42,7 +42,13 @@ constexpr int MLP_B3 = MLP_W3 + MLP_OUT * MLP_H;
 constexpr int MLP_TRAIN_END = MLP_B3 + MLP_OUT;
 constexpr int MLP_OUT_SCALE = MLP_TRAIN_END;
 constexpr int MLP_BLOB_SIZE = MLP_OUT_SCALE + MLP_OUT;
-constexpr int WS_MAX_K = 8;       // nearest neighbours per sequence, at most
+constexpr int MLP_WB_ELEMS = MLP_H * 64 + MLP_H * MLP_H + MLP_OUT * MLP_H;   // BF16 weight image
+constexpr int WS_MAX_K = 16;      // nearest neighbours per sequence, at most
+// Dual form's learned start (blob version 2, same network): per-sequence
+// statistics of a target column, DWS_K nearest neighbours
+constexpr int MLP_BLOB_VERSION_DUAL = 2;
+constexpr int DWS_K = 16;
+constexpr int MLP_ALPHA = 2;      // version 2: the shrinkage of the predicted residuals (blob[2])
 
 // per-slot accumulators (doubles), zeroed by the host before each use
 enum Acc {
@@ -255,11 +261,26 @@ void launch_dual_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list,
                        float *wa, cudaStream_t st);
 
 // warm start (mlp.cu, warmstart.cu)
-void mlp_infer(const float *p_dev, const float *X, int64_t M, float *Xn, float *h1, float *h2, float *out,
+// the BF16 image of the blob's weights that the tensor-core forward reads
+// (MLP_WB_ELEMS BF16 values), and inference: raw features (M x MLP_IN) ->
+// outputs (M x MLP_OUT) in the blob's output units; *err is set when a wait
+// of the kernel gives up
+void mlp_pack(const float *p_dev, void *wb, cudaStream_t st);
+void mlp_infer(const float *p_dev, const void *wb, const float *X, int64_t M, float *out, int *err,
                cudaStream_t st);
 void launch_distances(const uint8_t *X, int64_t ld, int N, int L, uint64_t *packed, int32_t *dist,
                       cudaStream_t st);
-void launch_knn(const int32_t *dist, int N, int k, int32_t *knn, cudaStream_t st);
+void launch_knn(const int32_t *dist, int N, int k, int32_t *knn, cudaStream_t st, int32_t *knn_d = nullptr);
+// dual form's learned start: per-sequence statistics of the target columns
+// cols + idx[g] * Nx (g < n) into feats [g][Nx][MLP_IN]; the network's
+// residual prediction into the R rows of slots[g]; and the start point from
+// the exact K rho of those rows
+void launch_dual_ws_feats(const uint8_t *cols, const int32_t *idx, int n, int N, int64_t Nx, int L, const double *w,
+                          const int32_t *knn, const int32_t *knn_d, float *feats, cudaStream_t st);
+void launch_dual_ws_r(const int32_t *slots, int n, int N, int64_t Nx, const float *out, const float *p_dev, float alpha,
+                      const float *w, float *R, cudaStream_t st);
+void launch_dual_ws_init(const Problem &P, const int32_t *list, int n, double c, double qscale, const int32_t *rq,
+                         const float2 *KR, float2 *dv, float2 *lbase, cudaStream_t st);
 void launch_ws_residual(const uint8_t *XT, int64_t Nx, int N, const int32_t *loci, int G, const double *w,
                         const int32_t *knn, int k, float eps, float *Rws, cudaStream_t st);
 void launch_ws_residual_split(const uint8_t *XT, int64_t Nx, int N, const int32_t *loci, const int32_t *slots, int G,

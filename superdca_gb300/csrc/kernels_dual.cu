@@ -39,8 +39,11 @@ __global__ void k_dual_kmat(const int32_t *__restrict__ dist, int N, int64_t Nx,
 }
 
 // rho_q = round(R * qscale) (R is FP32, so a single-precision product loses
-// nothing: the rounded value is the one every later step uses); class sums
-// csum[b][a][c] = sum over i with s_i(r) = a
+// nothing: the rounded value is the one every later step uses), with the
+// entry at the sequence's own state set to minus the sum of the other three,
+// so that every row sums to zero exactly (a residual w (p - onehot) does; the
+// K rho product then needs three columns); class sums csum[b][a][c] = sum
+// over i with s_i(r) = a
 __global__ void __launch_bounds__(256)
 k_dual_quant(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int N, int64_t Nx,
              const float4 *__restrict__ R, const uint8_t *__restrict__ rstate, float qscale, int4 *__restrict__ rq,
@@ -58,7 +61,12 @@ k_dual_quant(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, i
             const float4 v = R[(int64_t)b * Nx + i];
             q = make_int4(__float2int_rn(v.x * qscale), __float2int_rn(v.y * qscale), __float2int_rn(v.z * qscale),
                           __float2int_rn(v.w * qscale));
-            const int y = own ? (rstate[(int64_t)b * Nx + i] & 3) : -1;
+            const int ys = rstate[(int64_t)b * Nx + i] & 3;
+            if (ys == 0) q.x = -(q.y + q.z + q.w);
+            else if (ys == 1) q.y = -(q.x + q.z + q.w);
+            else if (ys == 2) q.z = -(q.x + q.y + q.w);
+            else q.w = -(q.x + q.y + q.z);
+            const int y = own ? ys : -1;
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
                 if (a != y) continue;
@@ -1138,6 +1146,28 @@ __global__ void k_dual_check_apply(DualCtl *__restrict__ ctl, DualSum *__restric
     write_summary(S, sum[b]);
 }
 
+// The learned start of a slot from its predicted residual rows (already
+// through k_dual_quant and the exact K rho product): a_x = c rho_q / qscale,
+// k_x = c K rho (KR is K rho / qscale), c = -1 / (2 lambda_J); the logits
+// start at k_x (eta = 0).  The pair (a_x, k_x) is consistent to the
+// double-float rounding of one product by c.
+__global__ void __launch_bounds__(256)
+k_dual_ws_init(const int32_t *__restrict__ list, int64_t Nx, int NV, double c, double inv_qscale,
+               const int32_t *__restrict__ rq, const float2 *__restrict__ KR, float2 *__restrict__ dv,
+               float2 *__restrict__ lbase)
+{
+    const int b = list[blockIdx.y];
+    const float2 cd = df_from_d(c), cq = df_from_d(c * inv_qscale);
+    float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = ax + Nx * 4;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Nx * 4; e += (int64_t)gridDim.x * blockDim.x) {
+        const float2 a = df_mul(cq, df_from_int(rq[(int64_t)b * Nx * 4 + e]));
+        const float2 k = df_mul(cd, KR[(int64_t)b * Nx * 4 + e]);
+        ax[e] = a;
+        kx[e] = k;
+        lbase[(int64_t)b * Nx * 4 + e] = k;
+    }
+}
+
 unsigned grid_for(int64_t elems, int per_block_elems, int cap)
 {
     const int64_t g = (elems + per_block_elems - 1) / per_block_elems;
@@ -1204,6 +1234,14 @@ void launch_dual_accept(const Problem &P, const DualCtl *ctl, const int32_t *lis
     if (n <= 0) return;
     dim3 g(grid_for(P.Nx * 2, 256 * 2, 64), n);
     k_dual_accept<<<g, 256, 0, st>>>(ctl, list, P.Nx, DV_S + 2 * P.ring, dv, u, lbase);
+}
+
+void launch_dual_ws_init(const Problem &P, const int32_t *list, int n, double c, double qscale, const int32_t *rq,
+                         const float2 *KR, float2 *dv, float2 *lbase, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 g(grid_for(P.Nx * 4, 256 * 4, 64), n);
+    k_dual_ws_init<<<g, 256, 0, st>>>(list, P.Nx, DV_S + 2 * P.ring, c, 1.0 / qscale, rq, KR, dv, lbase);
 }
 
 void launch_dual_to_r(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int which,

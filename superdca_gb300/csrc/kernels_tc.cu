@@ -36,6 +36,7 @@
 #include "df.cuh"
 #include "engine.h"
 #include "kernels_common.cuh"
+#include "tcgen05.cuh"
 
 namespace sdca {
 namespace tc {
@@ -45,7 +46,6 @@ constexpr int A_BYTES = BM * BK * 2;   // one 128-row one-hot subtile
 constexpr int B_BYTES = BN * BK * 2;   // one fp16 half (hi or lo) of the slot operand
 constexpr int RAW_BYTES = 2048;        // u8 states behind one subtile
 constexpr int THREADS = 192;
-constexpr long long WAIT_LIMIT = 1ll << 26;  // polls before a wait gives up
 
 // A CTA owns MSUB consecutive 128-row subtiles and reuses each staged B tile
 // for all of them: the slot operand is the traffic that the L2 has to carry,
@@ -60,71 +60,6 @@ template <int MSUB, int STG> struct Cfg {
 
 enum { MODE_FWD = 0, MODE_BWD = 1 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// bounded wait; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
-{
-    for (long long i = 0; i < WAIT_LIMIT; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *tm, int x, int y,
-                                            uint32_t bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar)
-        : "memory");
-}
-
-// tcgen05 shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row
-// groups 1024 bytes apart (SBO), descriptor version 1.
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr)
-{
-    uint64_t d = 0;
-    d |= (uint64_t)((addr >> 4) & 0x3FFF);          // start address
-    d |= (uint64_t)(0) << 16;                        // LBO (unused for swizzled K-major)
-    d |= (uint64_t)((1024 >> 4) & 0x3FFF) << 32;     // SBO
-    d |= (uint64_t)1 << 46;                          // version
-    d |= (uint64_t)2 << 61;                          // SWIZZLE_128B
-    return d;
-}
-
 // instruction descriptor, kind::f16: A = B = F16, D = F32, K-major, M = 128, N = 128
 constexpr uint32_t IDESC = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(BN >> 3) << 17) |
                            ((uint32_t)(BM >> 4) << 24);
@@ -138,43 +73,6 @@ __device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
         "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
         : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-                 : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
-{
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-          "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
-}
-
-// 16-byte chunk c of row r of a 128-byte-swizzled tile
-__device__ __forceinline__ uint32_t sw128(uint32_t base, int r, int c)
-{
-    return base + (uint32_t)r * 128u + ((uint32_t)(c ^ (r & 7)) << 4);
-}
-
-__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint4 v)
-{
-    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z),
-                 "r"(v.w)
-                 : "memory");
 }
 
 // fp16 1.0 in lane s of four 16-bit lanes
@@ -438,21 +336,38 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
 // sequences stays below 2^24, so each of the 12 digit-pair GEMMs is exact in
 // its FP32 TMEM accumulator; the epilogue combines them with their weights
 // 2^(6k + 7p) in 64-bit integers (modulo 2^64: the total is below 2^62).
+//
+// Every row of rho_q sums to zero (k_dual_quant makes it so exactly), so the
+// fourth column of K rho is minus the sum of the other three: only three
+// columns per slot enter the product.  A CTA takes 128 rows of K and 13
+// slots (39 columns; with one unused row, 40 rows per rho digit plane), the
+// most that the 12 accumulators leave room for in TMEM (3 K digits x 4 planes
+// x 40 columns = 480 of 512), so each K tile staged from L2 serves 13 slots.
+// The B operand of one MMA stacks the four planes' first 32 rows (4 x 4 KB)
+// and then their last 8 rows (4 x 1 KB): every plane's accumulator columns
+// start 32-aligned (x32 loads) and its tail 8-aligned (x8 loads).
 
-constexpr int KD_BM = 128, KD_BN = 32, KD_BK = 64;
+constexpr int KD_BM = 128, KD_BK = 64;
 constexpr int KD_KDIG = 3, KD_RDIG = 4;
-constexpr int KD_A_BYTES = KD_BM * KD_BK * 2;  // one K digit plane tile, 16 KB
-constexpr int KD_B_BYTES = KD_BN * KD_BK * 2;  // one rho digit plane tile, 4 KB
-constexpr int KD_STAGE = KD_KDIG * KD_A_BYTES + KD_RDIG * KD_B_BYTES;
+constexpr int KD_S = 13;                     // slots per CTA
+constexpr int KD_C = 3;                      // product columns per slot (the fourth follows)
+constexpr int KD_COLS = KD_S * KD_C;         // 39 live columns per plane
+constexpr int KD_BN = 40;                    // rows per rho digit plane in a B tile
+constexpr int KD_HEAD = 32, KD_TAIL = KD_BN - KD_HEAD;
+constexpr int KD_A_BYTES = KD_BM * KD_BK * 2;          // one K digit plane tile, 16 KB
+constexpr int KD_HEAD_BYTES = KD_HEAD * KD_BK * 2;     // 4 KB
+constexpr int KD_TAIL_BYTES = KD_TAIL * KD_BK * 2;     // 1 KB
+constexpr int KD_STAGE = KD_KDIG * KD_A_BYTES + KD_RDIG * (KD_HEAD_BYTES + KD_TAIL_BYTES);
 constexpr int KD_STG = 3;
 constexpr int KD_SMEM = KD_STG * KD_STAGE + 1024 + 256;
-constexpr uint32_t KD_TMEM_COLS = 512;  // 12 accumulators of 32 columns
-// one MMA per K digit covers all four rho digit planes: they are staged
-// back to back, a 128-row B operand, and fill 128 accumulator columns
-constexpr int KD_NB = KD_RDIG * KD_BN;
+constexpr uint32_t KD_TMEM_COLS = 512;
+constexpr int KD_NB = KD_RDIG * KD_BN;                 // 160 accumulator columns per K digit
 constexpr uint32_t IDESC_KD = (1u << 4) | ((uint32_t)(KD_NB >> 3) << 17) | ((uint32_t)(KD_BM >> 4) << 24);
 static_assert(KD_STAGE % 1024 == 0, "stage must keep 1024-byte alignment");
-static_assert(KD_KDIG * KD_RDIG * KD_BN <= (int)KD_TMEM_COLS, "accumulators fit TMEM");
+static_assert(KD_HEAD_BYTES % 1024 == 0 && KD_TAIL_BYTES % 1024 == 0, "TMA destinations 1024-aligned");
+static_assert(KD_KDIG * KD_NB <= (int)KD_TMEM_COLS, "accumulators fit TMEM");
+static_assert(KD_NB % 16 == 0 && KD_NB <= 256, "MMA N for M = 128");
+static_assert(KD_COLS < KD_BN, "one unused row per plane");
 
 __device__ __forceinline__ void mma_f16_kd(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
 {
@@ -467,7 +382,7 @@ __device__ __forceinline__ void mma_f16_kd(uint32_t tmem_d, uint64_t adesc, uint
 struct KdArgs {
     int kt_total;        // Nx / 64
     int nk_rows;         // rows per K digit plane (multiple of 128)
-    int nr_rows;         // rows per rho digit plane (multiple of 32)
+    int nr_rows;         // rows per rho digit plane (>= 3 x slots + 1)
     int N;
     int64_t Nx;
     int nlist;
@@ -480,7 +395,8 @@ struct KdArgs {
 };
 
 __global__ void __launch_bounds__(THREADS, 1)
-k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensorMap tmR, const KdArgs args)
+k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensorMap tmRh,
+       const __grid_constant__ CUtensorMap tmRt, const KdArgs args)
 {
     extern __shared__ uint8_t smem_raw[];
     const uint32_t sbase0 = smem_u32(smem_raw);
@@ -492,7 +408,8 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
     const uint32_t tmem_full = bars + 8u * (2 * KD_STG);
     const uint32_t tmem_slot = bars + 8u * (2 * KD_STG + 1);
     uint32_t *tmem_slot_gen = reinterpret_cast<uint32_t *>(sgen + KD_STG * KD_STAGE + 8 * (2 * KD_STG + 1));
-    constexpr uint32_t BOFF = KD_KDIG * KD_A_BYTES;
+    constexpr uint32_t BOFF = KD_KDIG * KD_A_BYTES;                      // plane heads
+    constexpr uint32_t TOFF = BOFF + KD_RDIG * KD_HEAD_BYTES;            // plane tails
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m_tile = blockIdx.x, n_tile = blockIdx.y;
@@ -520,6 +437,7 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
 
     if (warp == 0) {
         if (lane == 0) {
+            const int r0 = n_tile * KD_COLS;   // this CTA's first rho row in each plane
             for (int j = 0; j < nkt; ++j) {
                 const int s = j % KD_STG;
                 const uint32_t ph = (uint32_t)((j / KD_STG) & 1);
@@ -530,9 +448,11 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
                 for (int k = 0; k < KD_KDIG; ++k)
                     tma_load_2d(st + k * KD_A_BYTES, &tmK, j * KD_BK, k * args.nk_rows + m_tile * KD_BM, full(s));
 #pragma unroll
-                for (int p = 0; p < KD_RDIG; ++p)
-                    tma_load_2d(st + BOFF + p * KD_B_BYTES, &tmR, j * KD_BK, p * args.nr_rows + n_tile * KD_BN,
+                for (int p = 0; p < KD_RDIG; ++p) {
+                    tma_load_2d(st + BOFF + p * KD_HEAD_BYTES, &tmRh, j * KD_BK, p * args.nr_rows + r0, full(s));
+                    tma_load_2d(st + TOFF + p * KD_TAIL_BYTES, &tmRt, j * KD_BK, p * args.nr_rows + r0 + KD_HEAD,
                                 full(s));
+                }
             }
             for (int j = max(0, nkt - KD_STG); j < nkt; ++j)
                 if (!mbar_wait(full(j % KD_STG), (uint32_t)((j / KD_STG) & 1))) failed = true;
@@ -569,32 +489,43 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
         // in the FP32 accumulators): each is converted with a 32-bit
         // conversion and shifted into place in 64-bit integers (no 64-bit
         // conversion or multiply, which run on GB300's narrow FP64 pipe).
-        long long acc[KD_BN];
+        long long acc[KD_COLS];
 #pragma unroll
-        for (int c = 0; c < KD_BN; ++c) acc[c] = 0ll;
+        for (int c = 0; c < KD_COLS; ++c) acc[c] = 0ll;
         if (ok) {
+            const uint32_t lanes = (uint32_t)(q * 32) << 16;
 #pragma unroll 1
             for (int k = 0; k < KD_KDIG; ++k)
 #pragma unroll 1
                 for (int p = 0; p < KD_RDIG; ++p) {
-                    float v[32];
-                    tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)((k * KD_RDIG + p) * KD_BN), v);
                     const int sh = 6 * k + 7 * p;
+                    float v[32], t[8];
+                    tmem_ld32(tmem_base + lanes + (uint32_t)(k * KD_NB + p * KD_HEAD), v);
+                    tmem_ld8(tmem_base + lanes + (uint32_t)(k * KD_NB + KD_RDIG * KD_HEAD + p * KD_TAIL), t);
 #pragma unroll
-                    for (int c = 0; c < KD_BN; ++c) acc[c] += (long long)__float2int_rn(v[c]) << sh;
+                    for (int c = 0; c < KD_HEAD; ++c) acc[c] += (long long)__float2int_rn(v[c]) << sh;
+#pragma unroll
+                    for (int c = KD_HEAD; c < KD_COLS; ++c) acc[c] += (long long)__float2int_rn(t[c - KD_HEAD]) << sh;
                 }
 #pragma unroll
-            for (int cc = 0; cc < KD_BN; ++cc) {
-                const int P = n_tile * (KD_BN / 4) + cc / 4;
+            for (int s = 0; s < KD_S; ++s) {
+                const int P = n_tile * KD_S + s;
                 if (P >= args.nlist || row >= args.Nx) continue;
-                const int b = args.list[P], c = cc & 3;
-                float2 val = df_zero();
+                const int b = args.list[P];
+                float2 val[4] = {df_zero(), df_zero(), df_zero(), df_zero()};
                 if (row < args.N) {
                     const int y = args.rstate[(int64_t)b * args.Nx + row] & 3;
-                    const long long tot = acc[cc] - args.csum[(int64_t)b * 16 + y * 4 + c];
-                    val = df_mul(df_from_ll_fast(tot), iq);
+                    const long long *cs = args.csum + (int64_t)b * 16 + y * 4;
+                    long long tot[4];
+#pragma unroll
+                    for (int c = 0; c < KD_C; ++c) tot[c] = acc[KD_C * s + c] - cs[c];
+                    tot[3] = -(tot[0] + tot[1] + tot[2]);
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) val[c] = df_mul(df_from_ll_fast(tot[c]), iq);
                 }
-                args.KR[((int64_t)b * args.Nx + row) * 4 + c] = val;
+                float4 *o = reinterpret_cast<float4 *>(args.KR + ((int64_t)b * args.Nx + row) * 4);
+                o[0] = make_float4(val[0].x, val[0].y, val[1].x, val[1].y);
+                o[1] = make_float4(val[2].x, val[2].y, val[3].x, val[3].y);
             }
         }
     }
@@ -621,16 +552,17 @@ __global__ void k_kdig_split_k(const int32_t *__restrict__ K, int64_t Nx, int nk
     }
 }
 
-// rho_q of list position P (slot list[P]) -> four fp16 planes of balanced base-128 digits, rows P*4+c
+// rho_q of list position P (slot list[P]), its first three columns -> four
+// fp16 planes of balanced base-128 digits, rows P*3+c
 __global__ void k_kdig_split_r(const int32_t *__restrict__ list, int64_t Nx, int nr_rows,
                                const int4 *__restrict__ rq, __half *__restrict__ Rd)
 {
     const int P = blockIdx.y, b = list[P];
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < Nx; j += (int64_t)gridDim.x * blockDim.x) {
         const int4 q = rq[(int64_t)b * Nx + j];
-        const int qq[4] = {q.x, q.y, q.z, q.w};
+        const int qq[KD_C] = {q.x, q.y, q.z};
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
+        for (int c = 0; c < KD_C; ++c) {
             long long v = qq[c];
 #pragma unroll
             for (int p = 0; p < KD_RDIG; ++p) {
@@ -639,7 +571,7 @@ __global__ void k_kdig_split_r(const int32_t *__restrict__ list, int64_t Nx, int
                     d = ((v + 64) & 127) - 64;   // balanced digit, v - d divisible by 128
                     v = (v - d) / 128;
                 }
-                Rd[((int64_t)p * nr_rows + (int64_t)P * 4 + c) * Nx + j] = __int2half_rn((int)d);
+                Rd[((int64_t)p * nr_rows + (int64_t)P * KD_C + c) * Nx + j] = __int2half_rn((int)d);
             }
         }
     }
@@ -818,12 +750,18 @@ TcPlan *tc_plan_create(const Problem &P, const uint8_t *X, const uint8_t *XT, __
 void tc_plan_destroy(TcPlan *p) { delete p; }
 
 struct KdPlan {
-    CUtensorMap mK, mR;
+    CUtensorMap mK, mRh, mRt;   // K digits; rho digit plane heads (32 rows) and tails (8 rows)
     int nk_rows = 0, nr_rows = 0;
 };
 
 int kd_nk_rows(const Problem &P) { return (int)(((P.Nx + tc::KD_BM - 1) / tc::KD_BM) * tc::KD_BM); }
-int kd_nr_rows(const Problem &P) { return (int)(((4 * P.Bmax + tc::KD_BN - 1) / tc::KD_BN) * tc::KD_BN); }
+// rows per rho digit plane: 3 per slot for whole CTAs of 13 slots, one more
+// for the last CTA's unused row, rounded to 8
+int kd_nr_rows(const Problem &P)
+{
+    const int64_t slots = (P.Bmax + tc::KD_S - 1) / tc::KD_S * tc::KD_S;
+    return (int)((tc::KD_C * slots + 1 + 7) / 8 * 8);
+}
 
 KdPlan *tc_kdig_plan_create(const Problem &P, __half *Kd, __half *Rd)
 {
@@ -832,8 +770,10 @@ KdPlan *tc_kdig_plan_create(const Problem &P, __half *Kd, __half *Rd)
     p->nr_rows = kd_nr_rows(P);
     bool ok = make_map(&p->mK, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Kd, (uint64_t)P.Nx, (uint64_t)tc::KD_KDIG * p->nk_rows,
                        (uint64_t)P.Nx * 2, tc::KD_BK, tc::KD_BM, CU_TENSOR_MAP_SWIZZLE_128B);
-    ok &= make_map(&p->mR, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Rd, (uint64_t)P.Nx, (uint64_t)tc::KD_RDIG * p->nr_rows,
-                   (uint64_t)P.Nx * 2, tc::KD_BK, tc::KD_BN, CU_TENSOR_MAP_SWIZZLE_128B);
+    ok &= make_map(&p->mRh, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Rd, (uint64_t)P.Nx, (uint64_t)tc::KD_RDIG * p->nr_rows,
+                   (uint64_t)P.Nx * 2, tc::KD_BK, tc::KD_HEAD, CU_TENSOR_MAP_SWIZZLE_128B);
+    ok &= make_map(&p->mRt, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Rd, (uint64_t)P.Nx, (uint64_t)tc::KD_RDIG * p->nr_rows,
+                   (uint64_t)P.Nx * 2, tc::KD_BK, tc::KD_TAIL, CU_TENSOR_MAP_SWIZZLE_128B);
     if (!ok) {
         delete p;
         return nullptr;
@@ -872,8 +812,8 @@ cudaError_t tc_launch_kdig(const KdPlan *pl, const Problem &P, const int32_t *li
     a.inv_qscale = inv_qscale;
     a.KR = KR;
     a.err = err;
-    dim3 grid((unsigned)(pl->nk_rows / tc::KD_BM), (unsigned)((4 * n + tc::KD_BN - 1) / tc::KD_BN));
-    tc::k_kdig<<<grid, tc::THREADS, tc::KD_SMEM, st>>>(pl->mK, pl->mR, a);
+    dim3 grid((unsigned)(pl->nk_rows / tc::KD_BM), (unsigned)((n + tc::KD_S - 1) / tc::KD_S));
+    tc::k_kdig<<<grid, tc::THREADS, tc::KD_SMEM, st>>>(pl->mK, pl->mRh, pl->mRt, a);
     return cudaGetLastError();
 }
 

@@ -1,11 +1,18 @@
 // mlp.cu -- the learned warm start's network and its training on the GPU.
 //
-// A per-pair MLP, 40 -> 128 -> 128 -> 16 with ReLU, maps the statistics of a
-// locus pair (r, n) to an initial 4 x 4 coupling block J_rn (the inputs are
-// built in warmstart.cu).  Every layer, forward and backward, is one launch
-// of a tiled FP32 kernel C = op(A) op(B) written here; Adam and the loss are
-// elementwise kernels.  The parameter blob (MLP_* offsets in engine.h) holds
-// the input normalisation, the weights and the output scale.
+// An MLP, 40 -> 128 -> 128 -> 16 with ReLU, maps the statistics of a locus
+// pair (r, n), or of one sequence at a target column (the dual form's start),
+// to a starting point (the inputs are built in warmstart.cu).
+//
+// Inference, and the forward pass of training, is one fused tcgen05 kernel
+// (k_mlp_tc): BF16 weights and activations, FP32 accumulators in TMEM, all
+// three layers of a 128-row tile without leaving the SM.  The backward pass
+// is tiled FP32 kernels C = op(A) op(B) on the FP32 master weights from the
+// saved FP32 activations (mixed-precision training); Adam and the loss are
+// elementwise kernels.  sdca_mlp_grad takes the FP32 forward, the exact
+// derivative the CPU oracle checks.  The parameter blob (MLP_* offsets in
+// engine.h) holds the input normalisation, the FP32 weights and the output
+// scale; the BF16 weight image is made from it (k_mlp_pack).
 //
 // SuperDCA has no learned component: its solver starts every locus from
 // zero (SuperDCA/include/plmDCA.hpp:298).  The warm start only moves the
@@ -19,8 +26,11 @@
 #include <vector>
 
 #include "engine.h"
+#include <cuda_bf16.h>
+
 #include "kernels_common.cuh"
 #include "superdca_gb300.h"
+#include "tcgen05.cuh"
 
 namespace sdca {
 namespace {
@@ -182,6 +192,218 @@ __global__ void k_adam(int n, float *__restrict__ p, const float *__restrict__ g
     p[i] -= lr * (a / c1) / (sqrtf(b / c2) + eps);
 }
 
+// ---- the fused tensor-core forward (BF16 weights, FP32 accumulators)
+//
+// One CTA of 128 threads owns the three BF16 weight matrices in shared
+// memory (128-byte swizzled K-major tiles: W1 128 x 64 with the 40 inputs
+// zero-padded, W2 128 x 128 as two 64-column atoms, W3 16 x 128 likewise)
+// and walks 128-row tiles of the input.  Per tile: thread r normalises row
+// r, rounds it to BF16 into the A tile; one thread issues the layer's
+// tcgen05.mma (M128, K16 steps) into TMEM and commits to an mbarrier; every
+// thread reads its row's accumulators back (tcgen05.ld, TMEM lane = row),
+// adds the bias, applies ReLU and writes the next layer's BF16 A tile.
+// Layer 3 (N = 16) writes the outputs.  h1, h2 (optional) receive the FP32
+// activations for the backward pass.
+constexpr int MT_THREADS = 128;
+constexpr int MT_K1 = 64;                                       // layer-1 K, padded
+constexpr int MT_W1_ELEMS = MLP_H * MT_K1, MT_W2_ELEMS = MLP_H * MLP_H, MT_W3_ELEMS = MLP_OUT * MLP_H;
+constexpr int MT_WB_ELEMS = MT_W1_ELEMS + MT_W2_ELEMS + MT_W3_ELEMS;   // BF16 weight image
+constexpr uint32_t MT_SW1 = 0, MT_SW2 = 16384, MT_SW3 = 49152, MT_SA1 = 53248, MT_SA2 = 69632;
+constexpr uint32_t MT_SBAR = 102400;
+constexpr int MT_SMEM = (int)MT_SBAR + 64 + 1024;
+constexpr uint32_t MT_TMEM_COLS = 256;                          // layer 1/3 at 0, layer 2 at 128
+// kind::f16 instruction descriptor: D = F32, A = B = BF16, K-major, M = 128
+constexpr uint32_t mt_idesc(int n) { return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | (8u << 24); }
+static_assert(MLP_IN <= MT_K1 && MLP_H == 128 && MLP_OUT == 16, "tile shapes of k_mlp_tc");
+static_assert(MT_WB_ELEMS == MLP_WB_ELEMS, "weight image size");
+static_assert(MT_SW2 - MT_SW1 == 2 * MT_W1_ELEMS && MT_SW3 - MT_SW2 == 2 * MT_W2_ELEMS &&
+              MT_SA1 - MT_SW3 == 2 * MT_W3_ELEMS && MT_SBAR - MT_SA2 == 2 * 128 * 128,
+              "shared-memory map");
+
+__device__ __forceinline__ void mt_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ uint32_t bf2(float a, float b)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+// rows x (64 * atoms) BF16, row-major in global -> 128-byte swizzled atoms
+__device__ void mt_stage_weights(const __nv_bfloat16 *__restrict__ w, int rows, int atoms, uint32_t dst)
+{
+    for (int e = threadIdx.x; e < rows * atoms * 8; e += blockDim.x) {
+        const int c = e & 7, r = (e >> 3) % rows, a = (e >> 3) / rows;
+        const uint4 v = *reinterpret_cast<const uint4 *>(w + (int64_t)r * 64 * atoms + a * 64 + c * 8);
+        tc::st_shared_v4(tc::sw128(dst + (uint32_t)(a * rows * 128), r, c), v);
+    }
+}
+
+// 32 accumulator columns of this thread's row: + bias, ReLU, into the BF16 A
+// tile (4 chunks of 8 at column c0) and, when given, the FP32 activations
+__device__ __forceinline__ void mt_hidden(const float (&v)[32], const float *__restrict__ bias, int c0, uint32_t a2,
+                                         int r, float *__restrict__ h)
+{
+    float x[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) x[j] = fmaxf(v[j] + bias[c0 + j], 0.f);
+    if (h) {
+#pragma unroll
+        for (int j = 0; j < 32; j += 4)
+            *reinterpret_cast<float4 *>(h + c0 + j) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+    }
+    const int atom = c0 >> 6;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int c = ((c0 & 63) >> 3) + q;
+        tc::st_shared_v4(tc::sw128(a2 + (uint32_t)(atom * 16384), r, c),
+                         make_uint4(bf2(x[8 * q], x[8 * q + 1]), bf2(x[8 * q + 2], x[8 * q + 3]),
+                                    bf2(x[8 * q + 4], x[8 * q + 5]), bf2(x[8 * q + 6], x[8 * q + 7])));
+    }
+}
+
+__global__ void __launch_bounds__(MT_THREADS, 2)
+k_mlp_tc(int64_t M, const float *__restrict__ X, const float *__restrict__ p, const __nv_bfloat16 *__restrict__ wb,
+         float *__restrict__ out, float *__restrict__ h1, float *__restrict__ h2, int *__restrict__ err)
+{
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t s0 = tc::smem_u32(smem_raw);
+    const uint32_t sb = (s0 + 1023u) & ~1023u;
+    uint8_t *const sg = smem_raw + (sb - s0);
+    const uint32_t bar = sb + MT_SBAR, slot = bar + 8;
+    const int t = threadIdx.x, warp = t >> 5;
+    if (t == 0) {
+        tc::mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot),
+                     "r"(MT_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    mt_stage_weights(wb, MLP_H, 1, sb + MT_SW1);
+    mt_stage_weights(wb + MT_W1_ELEMS, MLP_H, 2, sb + MT_SW2);
+    mt_stage_weights(wb + MT_W1_ELEMS + MT_W2_ELEMS, MLP_OUT, 2, sb + MT_SW3);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *reinterpret_cast<const uint32_t *>(sg + MT_SBAR + 8);
+    const uint32_t lanes = (uint32_t)(warp * 32) << 16;
+    const float *b1 = p + MLP_B1, *b2 = p + MLP_B2, *b3 = p + MLP_B3;
+    uint32_t phase = 0;
+    bool failed = false;
+    // one layer: MMAs by thread 0, commit, bounded wait by every thread
+    auto layer = [&](uint32_t d, uint32_t a, uint32_t w, int atoms, int a_stride, int w_stride, int n) -> bool {
+        // the A tile's generic-proxy stores and this thread's TMEM reads come
+        // before the MMAs that read the tile and overwrite the accumulators
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        if (t == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int at = 0; at < atoms; ++at)
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk)
+                    mt_mma(tmem + d, tc::smem_desc_sw128(a + (uint32_t)(at * a_stride + kk * 32)),
+                           tc::smem_desc_sw128(w + (uint32_t)(at * w_stride + kk * 32)), mt_idesc(n),
+                           (at > 0 || kk > 0) ? 1u : 0u);
+            tc::mma_commit(bar);
+        }
+        const bool ok = tc::mbar_wait(bar, phase);
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        return __syncthreads_and(ok ? 1 : 0) != 0;
+    };
+    const int64_t tiles = (M + 127) / 128;
+    for (int64_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
+        const int64_t row = tile * 128 + t;
+        const bool live = row < M;
+        {
+            // input row -> normalised BF16, K padded to 64
+            float x[MT_K1];
+#pragma unroll
+            for (int k = 0; k < MT_K1; ++k) x[k] = 0.f;
+            if (live) {
+#pragma unroll
+                for (int k = 0; k < MLP_IN; k += 4) {
+                    const float4 v = *reinterpret_cast<const float4 *>(X + row * MLP_IN + k);
+                    x[k] = (v.x - p[MLP_IN_MEAN + k]) * p[MLP_IN_SCALE + k];
+                    x[k + 1] = (v.y - p[MLP_IN_MEAN + k + 1]) * p[MLP_IN_SCALE + k + 1];
+                    x[k + 2] = (v.z - p[MLP_IN_MEAN + k + 2]) * p[MLP_IN_SCALE + k + 2];
+                    x[k + 3] = (v.w - p[MLP_IN_MEAN + k + 3]) * p[MLP_IN_SCALE + k + 3];
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                tc::st_shared_v4(tc::sw128(sb + MT_SA1, t, c),
+                                 make_uint4(bf2(x[8 * c], x[8 * c + 1]), bf2(x[8 * c + 2], x[8 * c + 3]),
+                                            bf2(x[8 * c + 4], x[8 * c + 5]), bf2(x[8 * c + 6], x[8 * c + 7])));
+        }
+        if (!layer(0, sb + MT_SA1, sb + MT_SW1, 1, 0, 0, MLP_H)) { failed = true; break; }
+#pragma unroll 1
+        for (int c0 = 0; c0 < MLP_H; c0 += 32) {
+            float v[32];
+            tc::tmem_ld32(tmem + lanes + (uint32_t)c0, v);
+            mt_hidden(v, b1, c0, sb + MT_SA2, t, live && h1 ? h1 + row * MLP_H : nullptr);
+        }
+        if (!layer(128, sb + MT_SA2, sb + MT_SW2, 2, 16384, 16384, MLP_H)) { failed = true; break; }
+        // layer-2 activations replace layer-1's in the A tile (the MMA that read them is complete)
+#pragma unroll 1
+        for (int c0 = 0; c0 < MLP_H; c0 += 32) {
+            float v[32];
+            tc::tmem_ld32(tmem + lanes + (uint32_t)(128 + c0), v);
+            mt_hidden(v, b2, c0, sb + MT_SA2, t, live && h2 ? h2 + row * MLP_H : nullptr);
+        }
+        if (!layer(0, sb + MT_SA2, sb + MT_SW3, 2, 16384, 2048, MLP_OUT)) { failed = true; break; }
+        float v0[8], v1[8];
+        tc::tmem_ld8(tmem + lanes, v0);
+        tc::tmem_ld8(tmem + lanes + 8u, v1);
+        if (live) {
+            float4 *o = reinterpret_cast<float4 *>(out + row * MLP_OUT);
+            o[0] = make_float4(v0[0] + b3[0], v0[1] + b3[1], v0[2] + b3[2], v0[3] + b3[3]);
+            o[1] = make_float4(v0[4] + b3[4], v0[5] + b3[5], v0[6] + b3[6], v0[7] + b3[7]);
+            o[2] = make_float4(v1[0] + b3[8], v1[1] + b3[9], v1[2] + b3[10], v1[3] + b3[11]);
+            o[3] = make_float4(v1[4] + b3[12], v1[5] + b3[13], v1[6] + b3[14], v1[7] + b3[15]);
+        }
+        // the next tile overwrites the A tiles and layer 1's accumulators
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+    }
+    if (failed && t == 0 && err) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(MT_TMEM_COLS)
+                     : "memory");
+    }
+}
+
+// FP32 weights of the blob -> the BF16 image k_mlp_tc reads (W1 zero-padded to 64 inputs)
+__global__ void k_mlp_pack(const float *__restrict__ p, __nv_bfloat16 *__restrict__ wb)
+{
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < MT_WB_ELEMS; e += gridDim.x * blockDim.x) {
+        float v;
+        if (e < MT_W1_ELEMS) {
+            const int r = e / MT_K1, k = e % MT_K1;
+            v = k < MLP_IN ? p[MLP_W1 + r * MLP_IN + k] : 0.f;
+        } else if (e < MT_W1_ELEMS + MT_W2_ELEMS) {
+            v = p[MLP_W2 + (e - MT_W1_ELEMS)];
+        } else {
+            v = p[MLP_W3 + (e - MT_W1_ELEMS - MT_W2_ELEMS)];
+        }
+        wb[e] = __float2bfloat16_rn(v);
+    }
+}
+
 struct Dev {
     std::vector<void *> ptrs;
     bool ok = true;
@@ -250,20 +472,49 @@ int mfail(const std::string &m)
 int check_blob(const float *params)
 {
     if (!params) return SDCA_E_ARG;
-    if (params[MLP_VERSION] != (float)MLP_BLOB_VERSION) return SDCA_E_ARG;
+    // version 1 (per-pair start) and 2 (the dual form's per-sequence start) share the network
+    if (params[MLP_VERSION] != (float)MLP_BLOB_VERSION && params[MLP_VERSION] != (float)MLP_BLOB_VERSION_DUAL)
+        return SDCA_E_ARG;
     return SDCA_OK;
 }
 
 } // namespace
 
-// inference for the engine: raw features (M x MLP_IN) -> normalised outputs
-// (M x MLP_OUT); Xn, h1, h2 are scratch of M x {MLP_IN, MLP_H, MLP_H}
-void mlp_infer(const float *p_dev, const float *X, int64_t M, float *Xn, float *h1, float *h2, float *out,
-               cudaStream_t st)
+void mlp_pack(const float *p_dev, void *wb, cudaStream_t st)
+{
+    k_mlp_pack<<<(MT_WB_ELEMS + 255) / 256, 256, 0, st>>>(p_dev, static_cast<__nv_bfloat16 *>(wb));
+}
+
+namespace {
+
+cudaError_t mt_configure()
+{
+    static std::once_flag once;
+    static cudaError_t e = cudaSuccess;
+    std::call_once(once, [] { e = cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, MT_SMEM); });
+    return e;
+}
+
+// the fused forward over M rows: outputs, and the FP32 activations when h1, h2 are given
+void mt_forward(const float *p_dev, const void *wb, const float *X, int64_t M, float *out, float *h1, float *h2,
+                int *err, cudaStream_t st)
 {
     if (M <= 0) return;
-    k_normalise<<<(unsigned)((M * MLP_IN + 255) / 256), 256, 0, st>>>(M, X, p_dev, Xn);
-    forward(st, p_dev, Xn, M, Scratch{h1, h2, out});
+    if (mt_configure() != cudaSuccess) return;   // the caller's launch check reports it
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+    const int64_t tiles = (M + 127) / 128;
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, 2 * (int64_t)sms);
+    k_mlp_tc<<<grid, MT_THREADS, MT_SMEM, st>>>(M, X, p_dev, static_cast<const __nv_bfloat16 *>(wb), out, h1, h2,
+                                                  err);
+}
+
+} // namespace
+
+void mlp_infer(const float *p_dev, const void *wb, const float *X, int64_t M, float *out, int *err, cudaStream_t st)
+{
+    mt_forward(p_dev, wb, X, M, out, nullptr, nullptr, err, st);
 }
 
 } // namespace sdca
@@ -305,13 +556,19 @@ int sdca_mlp_predict(const float *params, const float *X, int64_t M, float *out)
 {
     if (check_blob(params) || !X || M < 1 || !out) return SDCA_E_ARG;
     Dev d;
-    float *p = d.alloc<float>(MLP_BLOB_SIZE), *x = d.alloc<float>(M * MLP_IN), *xn = d.alloc<float>(M * MLP_IN);
-    float *h1 = d.alloc<float>(M * MLP_H), *h2 = d.alloc<float>(M * MLP_H), *o = d.alloc<float>(M * MLP_OUT);
+    float *p = d.alloc<float>(MLP_BLOB_SIZE), *x = d.alloc<float>(M * MLP_IN), *o = d.alloc<float>(M * MLP_OUT);
+    __nv_bfloat16 *wb = d.alloc<__nv_bfloat16>(MT_WB_ELEMS);
+    int *err = d.alloc<int>(1);
     if (!d.ok) return mfail("device allocation failed"), SDCA_E_NOMEM;
     MK(cudaMemcpy(p, params, sizeof(float) * MLP_BLOB_SIZE, cudaMemcpyHostToDevice));
     MK(cudaMemcpy(x, X, sizeof(float) * M * MLP_IN, cudaMemcpyHostToDevice));
-    mlp_infer(p, x, M, xn, h1, h2, o, 0);
+    MK(cudaMemset(err, 0, sizeof(int)));
+    mlp_pack(p, wb, 0);
+    mlp_infer(p, wb, x, M, o, err, 0);
     MK(cudaGetLastError());
+    int e = 0;
+    MK(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) return mfail("tensor-core forward: a pipeline wait gave up");
     MK(cudaMemcpy(out, o, sizeof(float) * M * MLP_OUT, cudaMemcpyDeviceToHost));
     return SDCA_OK;
 }
@@ -331,7 +588,11 @@ int sdca_mlp_train(float *params, const float *X, const float *T, int64_t M, int
     float *g = d.alloc<float>(MLP_BLOB_SIZE), *m1 = d.alloc<float>(MLP_BLOB_SIZE), *m2 = d.alloc<float>(MLP_BLOB_SIZE);
     int32_t *perm_d = d.alloc<int32_t>(M);
     double *l = d.alloc<double>(1);
+    float *braw = d.alloc<float>(Bm * MLP_IN);
+    __nv_bfloat16 *wb = d.alloc<__nv_bfloat16>(MT_WB_ELEMS);
+    int *err = d.alloc<int>(1);
     if (!d.ok) return mfail("device allocation failed"), SDCA_E_NOMEM;
+    MK(cudaMemset(err, 0, sizeof(int)));
     MK(cudaMemcpy(p, params, sizeof(float) * MLP_BLOB_SIZE, cudaMemcpyHostToDevice));
     MK(cudaMemcpy(x, X, sizeof(float) * M * MLP_IN, cudaMemcpyHostToDevice));
     MK(cudaMemcpy(t, T, sizeof(float) * M * MLP_OUT, cudaMemcpyHostToDevice));
@@ -350,9 +611,13 @@ int sdca_mlp_train(float *params, const float *X, const float *T, int64_t M, int
         MK(cudaMemset(l, 0, sizeof(double)));
         int64_t nb = 0;
         for (int64_t b0 = 0; b0 + Bm <= M; b0 += Bm, ++nb) {
+            // forward on the tensor cores (BF16 image of the current weights),
+            // backward in FP32 from its saved activations
+            k_gather_rows<<<(unsigned)((Bm * MLP_IN + 255) / 256), 256, 0, st>>>(Bm, MLP_IN, perm_d + b0, x, braw);
             k_gather_rows<<<(unsigned)((Bm * MLP_IN + 255) / 256), 256, 0, st>>>(Bm, MLP_IN, perm_d + b0, xn, bx);
             k_gather_rows<<<(unsigned)((Bm * MLP_OUT + 255) / 256), 256, 0, st>>>(Bm, MLP_OUT, perm_d + b0, t, bt);
-            forward(st, p, bx, Bm, s);
+            mlp_pack(p, wb, st);
+            mt_forward(p, wb, braw, Bm, out, h1, h2, err, st);
             k_mse<<<(unsigned)std::min<int64_t>(1024, (Bm * MLP_OUT + 255) / 256), 256, 0, st>>>(Bm, out, bt, dout, l);
             MK(cudaMemsetAsync(g, 0, sizeof(float) * MLP_BLOB_SIZE, st));
             backward(st, p, bx, Bm, s, dout, d1, d2, g);
@@ -363,6 +628,9 @@ int sdca_mlp_train(float *params, const float *X, const float *T, int64_t M, int
                                                                        b1, b2, 1e-8f, 1.f - c1, 1.f - c2);
         }
         MK(cudaGetLastError());
+        int e = 0;
+        MK(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (e) return mfail("tensor-core forward: a pipeline wait gave up");
         double lsum = 0.0;
         MK(cudaMemcpy(&lsum, l, sizeof(double), cudaMemcpyDeviceToHost));
         if (losses) losses[ep] = nb ? lsum / (double)nb : 0.0;

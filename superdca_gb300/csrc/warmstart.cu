@@ -28,7 +28,8 @@ constexpr int WS_NB = 8;            // values of R per sequence: joint (4) and r
 __device__ __forceinline__ bool before(int d, int j, int d2, int j2) { return d < d2 || (d == d2 && j < j2); }
 
 // k nearest neighbours of each sequence (ties by lower index); one warp per row
-__global__ void k_knn(const int32_t *__restrict__ dist, int N, int k, int32_t *__restrict__ knn)
+__global__ void k_knn(const int32_t *__restrict__ dist, int N, int k, int32_t *__restrict__ knn,
+                      int32_t *__restrict__ knn_d)
 {
     const int i = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
@@ -59,7 +60,10 @@ __global__ void k_knn(const int32_t *__restrict__ dist, int N, int k, int32_t *_
             bd[k - 1] = INT_MAX;
             bj[k - 1] = INT_MAX;
         }
-        if (lane == 0) knn[(int64_t)i * k + t] = j == INT_MAX ? -1 : j;
+        if (lane == 0) {
+            knn[(int64_t)i * k + t] = j == INT_MAX ? -1 : j;
+            if (knn_d) knn_d[(int64_t)i * k + t] = j == INT_MAX ? -1 : d;
+        }
     }
 }
 
@@ -102,6 +106,95 @@ __device__ __forceinline__ void sequence_r(const uint8_t *__restrict__ y, int i,
         const float ph = (cnt[a] + eps * fr[a]) / ((float)kk + eps);
         v[a] = wi * oh;
         v[4 + a] = wi * (ph - oh);
+    }
+}
+
+// ---- the dual form's learned start (blob version 2).  From a zero start
+// the dual iteration's x is (Phi^T a, eta), and at the optimum a* = -rho* /
+// (2 lambda_J) with rho*_i = w_i (p*_i - onehot(y_i)), p*_i the fitted state
+// probabilities of sequence i at the target column.  The network predicts
+// p*_i - onehot(y_i) from statistics of the sequence and its DWS_K nearest
+// neighbours in Hamming distance; the start is a0 = -alpha rho^ / (2
+// lambda_J), eta0 = 0, with K a0 formed exactly (the K rho product of the
+// iteration).  Statistics per sequence i of target column y (MLP_IN = 40):
+//   [0, 4)   onehot(y_i)
+//   [4, 8)   weighted state frequencies of the column
+//   [8, 24)  state frequencies among the 1, 3, 8 and 16 nearest neighbours
+//   [24, 28) Hamming distances of neighbours 1, 3, 8 and 16, over L
+//   [28, 40) 0
+__global__ void __launch_bounds__(256)
+k_dual_ws_feats(const uint8_t *__restrict__ cols, const int32_t *__restrict__ idx, int N, int64_t Nx, int L,
+                const double *__restrict__ w, const int32_t *__restrict__ knn, const int32_t *__restrict__ knn_d,
+                float *__restrict__ feats)
+{
+    const int g = blockIdx.x;
+    const uint8_t *y = cols + (int64_t)idx[g] * Nx;
+    float fr[4];
+    locus_frequencies(y, N, w, fr);
+    const float invL = 1.f / (float)L;
+    for (int i = threadIdx.x; i < Nx; i += blockDim.x) {
+        float f[MLP_IN];
+#pragma unroll
+        for (int t = 0; t < MLP_IN; ++t) f[t] = 0.f;
+        if (i < N) {
+            const int yi = y[i] & 3;
+            float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                f[a] = a == yi ? 1.f : 0.f;
+                f[4 + a] = fr[a];
+            }
+            int kk = 0;
+            const int marks[4] = {1, 3, 8, 16};
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                for (; kk < marks[m]; ++kk) {
+                    const int j = knn[(int64_t)i * DWS_K + kk];
+                    if (j >= 0) {
+                        const int yj = y[j] & 3;
+#pragma unroll
+                        for (int a = 0; a < 4; ++a) c[a] += a == yj ? 1.f : 0.f;
+                    }
+                }
+#pragma unroll
+                for (int a = 0; a < 4; ++a) f[8 + 4 * m + a] = c[a] / (float)marks[m];
+                const int d = knn_d[(int64_t)i * DWS_K + marks[m] - 1];
+                f[24 + m] = d < 0 ? 1.f : (float)d * invL;
+            }
+        }
+        float4 *o4 = reinterpret_cast<float4 *>(feats + ((int64_t)g * Nx + i) * MLP_IN);
+#pragma unroll
+        for (int t = 0; t < MLP_IN / 4; ++t) o4[t] = make_float4(f[4 * t], f[4 * t + 1], f[4 * t + 2], f[4 * t + 3]);
+    }
+}
+
+// The predicted residual rows of slots[g]: R_i = alpha w_i c_i with c_i the
+// network's first four outputs in the blob's output units, centred (a
+// residual p - onehot sums to zero over the states) and scaled down to
+// max |c_ia| <= 1 where larger (a residual's entries lie in [-1, 1]), so that
+// |R| <= w_max keeps the exact K rho product in its digit range; rows
+// N..Nx-1 are zero
+__global__ void k_dual_ws_r(const int32_t *__restrict__ slots, int N, int64_t Nx, const float *__restrict__ out,
+                            const float *__restrict__ p, float alpha, const float *__restrict__ w,
+                            float4 *__restrict__ R)
+{
+    const int g = blockIdx.y, b = slots[g];
+    const float s0 = p[MLP_OUT_SCALE], s1 = p[MLP_OUT_SCALE + 1], s2 = p[MLP_OUT_SCALE + 2], s3 = p[MLP_OUT_SCALE + 3];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Nx; i += (int64_t)gridDim.x * blockDim.x) {
+        float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i < N) {
+            const float *o = out + ((int64_t)g * Nx + i) * MLP_OUT;
+            float c0 = o[0] * s0, c1 = o[1] * s1, c2 = o[2] * s2, c3 = o[3] * s3;
+            const float m = 0.25f * (c0 + c1 + c2 + c3);
+            c0 -= m;
+            c1 -= m;
+            c2 -= m;
+            c3 -= m;
+            const float mx = fmaxf(fmaxf(fabsf(c0), fabsf(c1)), fmaxf(fabsf(c2), fabsf(c3)));
+            const float c = alpha * w[i] / fmaxf(mx, 1.f);
+            r = isfinite(c * mx) ? make_float4(c * c0, c * c1, c * c2, c * c3) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        R[(int64_t)b * Nx + i] = r;
     }
 }
 
@@ -385,10 +478,25 @@ k_ws_hfit(int N, int64_t Nx, int64_t Dp, int L, double lambda_h, const int32_t *
 
 } // namespace
 
-void launch_knn(const int32_t *dist, int N, int k, int32_t *knn, cudaStream_t st)
+void launch_knn(const int32_t *dist, int N, int k, int32_t *knn, cudaStream_t st, int32_t *knn_d)
 {
     const int64_t threads = (int64_t)N * 32;
-    k_knn<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(dist, N, k, knn);
+    k_knn<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(dist, N, k, knn, knn_d);
+}
+
+void launch_dual_ws_feats(const uint8_t *cols, const int32_t *idx, int n, int N, int64_t Nx, int L, const double *w,
+                          const int32_t *knn, const int32_t *knn_d, float *feats, cudaStream_t st)
+{
+    if (n <= 0) return;
+    k_dual_ws_feats<<<n, 256, 0, st>>>(cols, idx, N, Nx, L, w, knn, knn_d, feats);
+}
+
+void launch_dual_ws_r(const int32_t *slots, int n, int N, int64_t Nx, const float *out, const float *p_dev, float alpha,
+                      const float *w, float *R, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 g((unsigned)((Nx + 255) / 256), (unsigned)n);
+    k_dual_ws_r<<<g, 256, 0, st>>>(slots, N, Nx, out, p_dev, alpha, w, reinterpret_cast<float4 *>(R));
 }
 
 void launch_ws_residual(const uint8_t *XT, int64_t Nx, int N, const int32_t *loci, int G, const double *w,

@@ -48,7 +48,8 @@ class Engine:
     the resident alignment and take loci from one queue, so one lane's host
     decisions overlap the other lanes' kernels.  form: FORM_GATHER (plain),
     FORM_TC (tensor-core contractions) or FORM_DUAL (the span of the
-    sequences, zero start only)."""
+    sequences; zero start, or the per-sequence learned start of a version-2
+    blob)."""
 
     def __init__(self, n_seqs: int, n_loci: int, *, lambda_h: float = -1.0,
                  lambda_J: float = -1.0, gradient_threshold: float = 1e-3,
@@ -189,6 +190,21 @@ class Engine:
         self._check(self.lib.sdca_ws_features(self.h, int(k), float(eps), _ptr(loci), n, _ptr(sel), sel.shape[1],
                                               _ptr(out)))
         return out
+
+    def ws_dual_data(self, loci):
+        """Training data of the dual form's per-sequence start: statistics
+        (n x N x 40) and converged residual rows w_i (p_i - onehot) (n x N x 4)
+        of the listed loci, with their solve statistics (sdca_ws_dual_data)."""
+        loci = np.ascontiguousarray(loci, dtype=np.uint32)
+        n = len(loci)
+        feats = np.zeros((n, self.N, 40), dtype=np.float32)
+        rho = np.zeros((n, self.N, 4), dtype=np.float32)
+        stats = (_lib.LocusStat * max(n, 1))()
+        self._check(self.lib.sdca_ws_dual_data(self.h, _ptr(loci), n, _ptr(feats), _ptr(rho),
+                                               C.cast(stats, C.c_void_p)))
+        st = stats[:n]
+        return feats, rho, dict(f=np.array([s.f for s in st]), iterations=np.array([s.iterations for s in st]),
+                                status=np.array([s.status for s in st]))
 
     def eval(self, r: int, x: np.ndarray, grad: bool = True):
         x = np.ascontiguousarray(x, dtype=np.float64)

@@ -1,4 +1,4 @@
-"""The learned warm start: training data, training and parameter blobs.
+"""The learned warm starts: training data, training and parameter blobs.
 
 SuperDCA starts every per-locus solve from zero (SuperDCA/include/plmDCA.hpp:
 298).  Here a per-pair MLP (csrc/mlp.cu), trained on the GPU on this engine's
@@ -129,9 +129,96 @@ def predict(blob: np.ndarray, X: np.ndarray) -> np.ndarray:
 
 def load(path: str) -> np.ndarray:
     blob = np.load(path).astype(np.float32)
-    if blob.shape != (SIZE,) or int(blob[0]) != VERSION:
+    if blob.shape != (SIZE,) or int(blob[0]) not in (VERSION, VERSION_DUAL):
         raise ValueError(f"{path} is not a warm-start parameter blob")
     return blob
+
+
+# ---- the dual form's per-sequence start (blob version 2)
+#
+# Inputs per (locus, sequence): the 28 statistics of sdca_ws_dual_data
+# (padded to 40); targets: the converged residual p_i - onehot(s_i(r)) (4
+# outputs; the other 12 are trained to 0).  The start is a0 = -alpha w_i
+# (predicted residual) / (2 lambda_J).
+
+VERSION_DUAL = 2
+DUAL_K = 16
+
+
+def new_blob_dual(X: np.ndarray, T4: np.ndarray, alpha: float, seed: int = 0) -> np.ndarray:
+    """A fresh version-2 blob: normalisation from the inputs X (M x 40),
+    output scale from the residual targets T4 (M x 4)."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros(SIZE, dtype=np.float32)
+    p[0], p[1], p[2], p[3] = VERSION_DUAL, DUAL_K, alpha, 0.0
+    p[IN_MEAN:IN_MEAN + N_IN] = X.mean(0)
+    p[IN_SCALE:IN_SCALE + N_IN] = 1.0 / np.maximum(X.std(0), 1e-6)
+    p[W1:B1] = rng.normal(0, np.sqrt(2.0 / N_IN), N_H * N_IN)
+    p[W2:B2] = rng.normal(0, np.sqrt(2.0 / N_H), N_H * N_H)
+    p[W3:B3] = rng.normal(0, np.sqrt(1.0 / N_H), N_OUT * N_H)
+    p[OUT_SCALE:] = 1.0
+    p[OUT_SCALE:OUT_SCALE + 4] = np.maximum(T4.std(0), 1e-6)
+    return p
+
+
+def dual_rows(engine, loci, weights, rows_per_locus: int = 0, rng=None, chunk: int = 1000):
+    """Training rows from converged solves of `loci` on a dual-form engine:
+    statistics (M x 40) and residual targets p - onehot (M x 4) of the
+    sequences with a positive weight (rows_per_locus > 0: that many of them
+    at random per locus), and the loci's solve statistics.  The loci are
+    solved in chunks so that host memory stays bounded."""
+    w = np.asarray(weights, dtype=np.float32)
+    live = np.flatnonzero(w > 0)
+    rng = rng or np.random.default_rng(0)
+    Xs, Ts, sts = [], [], []
+    loci = np.asarray(loci)
+    for c0 in range(0, len(loci), chunk):
+        feats, rho, st = engine.ws_dual_data(loci[c0:c0 + chunk])
+        for j in range(len(feats)):
+            rows = live if rows_per_locus <= 0 or rows_per_locus >= len(live) else \
+                np.sort(rng.choice(live, rows_per_locus, replace=False))
+            Xs.append(feats[j, rows])
+            Ts.append(rho[j, rows] / w[rows, None])
+        sts.append(st)
+    st = {k: np.concatenate([s[k] for s in sts]) for k in sts[0]}
+    return np.concatenate(Xs).astype(np.float32), np.concatenate(Ts).astype(np.float32), st
+
+
+def train_dual(X: np.ndarray, T4: np.ndarray, alpha: float, epochs: int = 15, batch: int = 8192,
+               lr: float = 1e-3, seed: int = 0):
+    """Train a version-2 blob on the GPU (the project's MLP kernels, csrc/mlp.cu)."""
+    blob = new_blob_dual(X, T4, alpha, seed=seed)
+    T = np.zeros((len(X), N_OUT), dtype=np.float32)
+    T[:, :4] = T4 / blob[OUT_SCALE:OUT_SCALE + 4][None, :]
+    return train(blob, X, T, epochs=epochs, batch=batch, lr=lr, seed=seed)
+
+
+def train_dual_on_workload(name: str, seeds, loci_per_seed: int, *, alpha: float = 0.4, epochs: int = 15,
+                           lr: float = 1e-3, sizes: dict | None = None, batch_slots: int = 256,
+                           rows_per_locus: int = 0, log=print):
+    """Train the dual form's start on converged solves of synthetic
+    alignments (workload `name` at the given seeds), unit weights."""
+    from . import synthetic
+    from .engine import Engine
+
+    rng = np.random.default_rng(4321)
+    Xs, Ts = [], []
+    for seed in seeds:
+        states, _, _ = synthetic.workload(name, seed=seed, **(sizes or {}))
+        N, L = states.shape
+        w = np.ones(N)
+        with Engine(N, L, form=_lib.FORM_DUAL, batch=batch_slots) as E:
+            E.set_alignment(states, w)
+            loci = rng.choice(L, size=min(loci_per_seed, L), replace=False)
+            X, T4, st = dual_rows(E, loci, w, rows_per_locus, rng)
+        log(f"seed {seed}: {N} x {L}, {len(loci)} loci solved, median iterations {np.median(st['iterations']):.0f}")
+        Xs.append(X)
+        Ts.append(T4)
+    X = np.concatenate(Xs)
+    T4 = np.concatenate(Ts)
+    blob, losses = train_dual(X, T4, alpha, epochs=epochs, lr=lr)
+    log(f"trained on {len(X)} sequence rows: loss {losses[0]:.4f} -> {losses[-1]:.4f}")
+    return blob, losses
 
 
 def train_on_workload(name: str, seeds, loci_per_seed: int, pairs: int, *, epochs: int = 20, batch: int = 4096,
@@ -174,10 +261,17 @@ def main(argv=None):
     ap.add_argument("--pairs", type=int, default=2048, help="training pairs per solved locus")
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--dual", action="store_true", help="the dual form's per-sequence start (version 2)")
+    ap.add_argument("--alpha", type=float, default=0.4, help="dual: shrinkage of the predicted residuals")
+    ap.add_argument("--rows-per-locus", type=int, default=0, help="dual: sequences sampled per locus (0: all)")
     ap.add_argument("--out", required=True)
     a = ap.parse_args(argv)
     sizes = {k: v for k, v in (("N", a.N), ("L", a.L)) if v is not None}
-    blob, _ = train_on_workload(a.workload, a.seeds, a.loci, a.pairs, epochs=a.epochs, lr=a.lr, sizes=sizes)
+    if a.dual:
+        blob, _ = train_dual_on_workload(a.workload, a.seeds, a.loci, alpha=a.alpha, epochs=a.epochs, lr=a.lr,
+                                         sizes=sizes, rows_per_locus=a.rows_per_locus)
+    else:
+        blob, _ = train_on_workload(a.workload, a.seeds, a.loci, a.pairs, epochs=a.epochs, lr=a.lr, sizes=sizes)
     np.save(a.out, blob)
     print("wrote", a.out)
 

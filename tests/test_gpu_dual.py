@@ -83,7 +83,10 @@ def test_dual_tree_subset_against_oracle(oracle_mod):
         assert np.abs(g).max() < 1.05e-3
 
 
-def test_dual_refuses_start_points_and_warm_start():
+def test_dual_refuses_start_points_and_per_pair_blobs():
+    """The dual form keeps every iterate in the span of the sequences: it
+    refuses an arbitrary start point and the per-pair network (version 1);
+    its own start comes from the per-sequence network (version 2)."""
     from superdca_gb300 import _lib, synthetic
     from superdca_gb300 import warmstart as W
     from superdca_gb300._lib import EngineError

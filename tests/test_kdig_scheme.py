@@ -97,3 +97,24 @@ def test_solution_digit_planes_are_exact():
         J = int(G[0]) * (1 << 22) + int(G[1]) * (1 << 11) + int(G[2])
         assert J == int(A[m].sum())
     assert 16383 * 1024 < 2 ** 24
+
+
+def test_three_columns_give_the_fourth():
+    """Rows of rho_q made to sum to zero exactly (the own-state entry set to
+    minus the sum of the others, as the quantiser does): the product needs
+    three columns, the fourth of K rho - csum is minus their sum."""
+    rng = np.random.default_rng(3)
+    N, L = 500, 3000
+    y = rng.integers(0, 4, size=N)
+    p = rng.dirichlet(np.ones(4), size=N)
+    R = p - np.eye(4)[y]
+    q = np.rint(R * 2 ** 27).astype(np.int64)
+    q[np.arange(N), y] = 0
+    q[np.arange(N), y] = -q.sum(1)
+    assert np.all(q.sum(1) == 0) and np.abs(q).max() <= 2 ** 27 + 2
+    K = rng.integers(0, L, size=(N, N), dtype=np.int64)
+    csum = np.stack([q[y == a].sum(0) for a in range(4)])
+    full = K @ q - csum[y]
+    three = K @ q[:, :3] - csum[y][:, :3]
+    np.testing.assert_array_equal(full[:, :3], three)
+    np.testing.assert_array_equal(full[:, 3], -three.sum(1))
