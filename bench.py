@@ -4,11 +4,12 @@
 Workload: the seeded 3000-sequence x 94,000-locus coalescent-tree alignment
 (synthetic stand-in for a genome alignment of that shape), unit sequence
 weights (SuperDCA's --no-reweighting path), automatic lambdas, gradient
-threshold 1e-3, zero start.  A step solves one batch of target loci to
-convergence (L-BFGS + More-Thuente, every locus independent); steps take
-disjoint loci.  --form picks the engine form: dual (default: the iteration
-kept in the span of the sequences), tc (tensor-core contractions, with the
-learned warm start) or gather (plain).  A step's working set (alignment
+threshold 1e-3, learned start (--warm-start none: zero start).  A step
+solves one batch of target loci to convergence (L-BFGS + More-Thuente, every
+locus independent); steps take disjoint loci.  --form picks the engine
+form: dual (default: the iteration kept in the span of the sequences, with
+the per-sequence learned start), tc (tensor-core contractions, with the
+per-pair learned start) or gather (plain).  A step's working set (alignment
 282 MB, agreement digits 54 MB, per-slot solver state) is larger than the
 129 MB L2, so no L2 flush is needed between steps.
 
@@ -25,8 +26,11 @@ learned warm start) or gather (plain).  A step's working set (alignment
               returned parameters, for a seeded sample of the first timed
               step's loci (relative objective error; SuperDCA stops at
               max|g| < 1e-3)
-  vs_plain    the plain GPU form (FP32 gather contractions) timed on loci of
-              the same step in the same process, and value / its loci/s
+  vs_plain    the plain GPU form (FP32 gather contractions, zero start) timed
+              on loci of the same step in the same process, and value / its
+              loci/s
+  warm_start_effect  the first timed step's loci solved again from zero:
+              loci/s and mean iterations with and without the learned start
   cpu_baseline the FP64 C oracle on this host's cores (rank 0, N=1)
 --impl reference times the CPU reference path (the FP64 C oracle restating
 SuperDCA's solve) on all host cores, on rank 0 only.
@@ -48,6 +52,12 @@ sys.path.insert(0, ROOT)
 
 Q = 4
 METRIC = "loci/s at N=3000,L=94k: mixed+batched+warm-start vs plain GPU at <=1e-6 rel obj"
+# committed learned-start blobs: the dual form's per-sequence network was
+# trained on 20,000 loci of 3000 x 10,000 tree alignments (seeds 1-4), the
+# per-pair network on 3000 x 94,000 tree alignments (seeds 1, 2); the bench
+# alignment is seed 0 (held out)
+WS_DEFAULT = {"dual": "warmstart_dual_tree-3000x10000.npy", "tc": "warmstart_tree-3000x94000.npy",
+              "gather": "warmstart_tree-3000x94000.npy"}
 
 
 def parse():
@@ -64,8 +74,10 @@ def parse():
     ap.add_argument("--loci-per-step", type=int, default=0, help="default: 2 x batch x lanes")
     ap.add_argument("--form", default="dual", choices=["gather", "tc", "dual"])
     ap.add_argument("--history-bf16", action="store_true")
-    ap.add_argument("--warm-start", default=os.path.join(ROOT, "superdca_gb300", "warmstart_tree-3000x94000.npy"),
-                    help="learned warm-start parameter blob ('none': zero start)")
+    ap.add_argument("--warm-start", default="auto",
+                    help="learned warm-start parameter blob ('none': zero start; 'auto': the committed blob of "
+                         "the form: per-sequence for dual, per-pair otherwise)")
+    ap.add_argument("--no-zero-start", action="store_true", help="skip the zero-start comparison")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form arm")
     ap.add_argument("--plain-loci", type=int, default=64, help="loci timed in the plain-form arm")
@@ -186,12 +198,22 @@ def load_workload(args):
 NCU_TRAFFIC_PER_UNIT = {("tree-3000x94000", "direction"): (542.68e6 + 42.05e6) / 128}
 
 
+def mean_history(iterations, m):
+    """Mean live L-BFGS history length over a solve of `iterations`
+    iterations: the direction of iteration i combines min(i, m) pairs."""
+    it = max(1, int(iterations))
+    return sum(min(i, m) for i in range(it)) / it
+
+
 def roofline_dual(prof_tot, N, L, m, cls=None):
     """Roofline of the dual form's dominant kernel class.
 
-    Work per unit (one target locus through one launch of the class):
-      forward (K rho, exact on the tensor cores): 2 N^2 q FLOP, counted once
-        (the digit expansion issues 12 fp16 products of it on the pipe);
+    m: the mean live history length (mean_history).  Work per unit (one
+    target locus through one launch of the class):
+      forward (K rho, exact on the tensor cores): 2 N^2 (q - 1) FLOP -- the
+        rows of rho sum to zero, so three of the four columns determine the
+        product -- counted once (the digit expansion issues 12 fp16
+        products of it on the pipe);
       backward (one-hot contraction X^T a on the tensor cores: max-norm
         checks and the final J): 2 N L q^2 FLOP, as in the other forms;
       history dots: 2k + 1 vectors of N x q doubles read (32 N bytes each);
@@ -211,7 +233,7 @@ def roofline_dual(prof_tot, N, L, m, cls=None):
     if units[cls] == 0 or t <= 0:
         return None, cls
     if cls == "forward":
-        ach = 2.0 * N * N * Q * units[cls] / t / 1e12
+        ach = 2.0 * N * N * (Q - 1) * units[cls] / t / 1e12
         return dict(bound="tensor", achieved=round(ach, 3), peak=tflops, unit="TFLOP/s", frac=round(ach / tflops, 5),
                     traffic=None, kernel="k_kdig (K rho)", issued_factor=12, peak_source=src), cls
     if cls == "backward":
@@ -387,7 +409,9 @@ def engine_arm(args):
     per_step = args.loci_per_step or 2 * B * lanes   # slots refill once per step
     E = Engine(N, L, batch=B, device=local, form=form, history_bf16=args.history_bf16, lanes=lanes)
     E.set_alignment(st, w)
-    ws = None if args.warm_start in ("", "none") or args.form == "dual" else args.warm_start
+    ws = None if args.warm_start in ("", "none") else args.warm_start
+    if ws == "auto":
+        ws = os.path.join(ROOT, "superdca_gb300", WS_DEFAULT[args.form])
     if ws:
         from superdca_gb300 import warmstart
         E.set_warm_start(warmstart.load(ws))
@@ -414,9 +438,12 @@ def engine_arm(args):
     barrier()
     clocks.start()
     t0 = time.time()
+    first = None
     for s in range(args.steps):
         res = E.solve(loci_for(args.warmup + s), want_scores=True)
         p = E.profile()
+        if first is None:
+            first = (res, p["solve_ms"])
         walls.append(time.time() - t0 - sum(walls))
         dev_ms += p["solve_ms"]
         launches += p["gpu_launches"]
@@ -491,9 +518,12 @@ def engine_arm(args):
         iso = {k: p1[k] for k in ("kernel_ms", "kernel_units", "kernel_launches")}
     if args.form == "dual":
         dom_cls = max(iso["kernel_ms"], key=lambda k: iso["kernel_ms"][k]) if iso else None
-        rf, dom = roofline_dual(tot, N, L, 10, dom_cls)
+        m_mean = mean_history(np.median(iters), 10)
+        rf, dom = roofline_dual(tot, N, L, m_mean, dom_cls)
+        if rf is not None:
+            rf["mean_history"] = round(m_mean, 3)
         if rf is not None and iso is not None:
-            ri, _ = roofline_dual(iso, N, L, 10, dom)
+            ri, _ = roofline_dual(iso, N, L, m_mean, dom)
             if ri is not None:
                 rf["isolated"] = {"achieved": ri["achieved"], "frac": ri["frac"], "lanes": 1,
                                   "avg_launch_ms": round(iso["kernel_ms"][dom] /
@@ -525,6 +555,23 @@ def engine_arm(args):
                             "the engine's returned parameters; max_oracle_gnorm: the oracle's max|g| there "
                             "(SuperDCA's stop test is max|g| < 1e-3); sampled from the first timed step's loci, "
                             "re-solved after the timed region in the same queue")}
+    # what the learned start gains: the first timed step's loci solved again
+    # from zero (same engine and queue), against the timed warm-started solve
+    ws_effect = None
+    if ws and not args.no_zero_start and first is not None:
+        E.set_warm_start(None)
+        rz = E.solve(loci_for(args.warmup), want_scores=True)
+        pz = E.profile()
+        rw_, ms_w = first
+        ws_effect = {"warm_loci_s": round(per_step / (ms_w / 1e3), 4),
+                     "zero_start_loci_s": round(per_step / (pz["solve_ms"] / 1e3), 4),
+                     "speedup": round(pz["solve_ms"] / ms_w, 4),
+                     "warm_mean_iterations": round(float(rw_.iterations.mean()), 2),
+                     "zero_mean_iterations": round(float(rz.iterations.mean()), 2),
+                     "max_rel_f_diff": float(np.max(np.abs(rw_.f - rz.f) / np.abs(rz.f))),
+                     "zero_status_counts": {str(k): int((rz.status == k).sum()) for k in sorted(set(rz.status.tolist()))},
+                     "how": ("the first timed step's loci solved again with the warm start disabled, after the "
+                             "timed region; device time of each solve (CUDA events)")}
     E.close()
 
     # the plain GPU form (FP32 gather contractions, FP32 L-BFGS history,
@@ -577,7 +624,8 @@ def engine_arm(args):
                           f"{B * lanes} slots)"),
                    "parallelism": f"loci sharded over {world} rank(s)"},
         "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": rf,
-        "accuracy": accuracy, "vs_plain": vs_plain, "autotune": tune, "reweighting": rw,
+        "accuracy": accuracy, "vs_plain": vs_plain, "warm_start_effect": ws_effect, "autotune": tune,
+        "reweighting": rw,
         "kernel_ms": {k: round(v, 2) for k, v in tot["kernel_ms"].items()},
         "kernel_launches": dict(tot["kernel_launches"]), "kernel_units": dict(tot["kernel_units"]),
         "solver": {"median_nfeval": float(np.median(nfe)), "median_iterations": float(np.median(iters)),
