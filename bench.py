@@ -52,11 +52,11 @@ sys.path.insert(0, ROOT)
 
 Q = 4
 METRIC = "loci/s at N=3000,L=94k: mixed+batched+warm-start vs plain GPU at <=1e-6 rel obj"
-# committed learned-start blobs: the dual form's per-sequence network was
-# trained on 20,000 loci of 3000 x 10,000 tree alignments (seeds 1-4), the
-# per-pair network on 3000 x 94,000 tree alignments (seeds 1, 2); the bench
+# committed learned-start blobs, trained on the GPU on converged solves of
+# 3000 x 94,000 tree alignments: the dual form's per-sequence network on
+# seeds 1-4 (384 loci each), the per-pair network on seeds 1, 2; the bench
 # alignment is seed 0 (held out)
-WS_DEFAULT = {"dual": "warmstart_dual_tree-3000x10000.npy", "tc": "warmstart_tree-3000x94000.npy",
+WS_DEFAULT = {"dual": "warmstart_dual_tree-3000x94000.npy", "tc": "warmstart_tree-3000x94000.npy",
               "gather": "warmstart_tree-3000x94000.npy"}
 
 
