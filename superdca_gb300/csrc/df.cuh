@@ -120,27 +120,26 @@ __device__ __forceinline__ float2 df_warp_sum(float2 v)
 }
 
 // Sum K per-thread double-float values over the block and add them to
-// dst[idx[k]] (FP64 atomics): warp sums in double-float, one conversion per
-// warp, the warps' sums in FP64 by the first warp.
+// dst[idx[k]] (FP64 atomics): warp sums in double-float, the warps' sums in
+// double-float by the first warp, one conversion and one atomic per value
+// (GB300's FP64 pipe is narrow: only the conversion and the atomic use it).
 template <int K>
 __device__ __forceinline__ void block_sum_df(float2 (&v)[K], double *dst, const int *idx)
 {
-    __shared__ double red_df[32][K];
+    __shared__ float2 red_df[32][K];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const float2 s = df_warp_sum(v[k]);
-        if (lane == 0) red_df[wid][k] = df_to_d(s);
+        if (lane == 0) red_df[wid][k] = s;
     }
     __syncthreads();
     if (wid == 0) {
         const int nw = blockDim.x >> 5;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-            double t = lane < nw ? red_df[lane][k] : 0.0;
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
-            if (lane == 0 && t != 0.0) atomicAdd(dst + idx[k], t);
+            const float2 t = df_warp_sum(lane < nw ? red_df[lane][k] : df_zero());
+            if (lane == 0 && (t.x != 0.f || t.y != 0.f)) atomicAdd(dst + idx[k], df_to_d(t));
         }
     }
     __syncthreads();
