@@ -72,6 +72,13 @@ __device__ __forceinline__ float2 df_from_d(double x)
 
 __device__ __forceinline__ double df_to_d(float2 a) { return (double)a.x + (double)a.y; }
 
+// the same split on the host, for kernel arguments
+__host__ __device__ __forceinline__ float2 df_host(double x)
+{
+    const float hi = (float)x;
+    return make_float2(hi, (float)(x - (double)hi));
+}
+
 // exact for |v| < 2^31
 __device__ __forceinline__ float2 df_from_int(int v)
 {

@@ -135,7 +135,7 @@ struct DualCtl {
     // [0, m) coefS, [MAXHIST, MAXHIST + m) coefY, [2 MAXHIST] coef_g,
     // [2 MAXHIST + 1, + Q) eta_d
     float2 cdf[2 * MAXHIST + 1 + Q];
-    int32_t cdf_pad_[2];
+    float2 stp_df;          // stp as double-float (the accept kernel's step)
 };
 
 // What the host reads of each slot after a round (a copy of DualCtl fields).

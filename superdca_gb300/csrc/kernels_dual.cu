@@ -168,14 +168,13 @@ __device__ __forceinline__ void df2_store(float2 *p, int64_t t, const float2 (&v
 // J-part sums: g.g, x.x, s.y, y.y, s.s; max |a_g| and max |a_x|
 __global__ void __launch_bounds__(256)
 k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
-            double lambda_J, const int32_t *__restrict__ rq, double inv_qscale, const float2 *__restrict__ KR,
+            float2 l2, const int32_t *__restrict__ rq, float2 iq, const float2 *__restrict__ KR,
             float2 *__restrict__ dv, double *__restrict__ acc, double *__restrict__ amax)
 {
     const int b = list[blockIdx.y];
     const DualCtl &S = ctl[b];
     if (S.phase == DC_STOP) return;
     const bool push = S.push && S.ring_new >= 0;
-    const float2 l2 = df_from_d(2.0 * lambda_J), iq = df_from_d(inv_qscale);
     const int64_t part = Nx * 4;
     const float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = ax + part;
     const float2 *ago = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kgo = ago + part;
@@ -487,9 +486,8 @@ k_dual_accept(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list,
     const int b = list[blockIdx.y];
     const DualCtl &S = ctl[b];
     if (S.phase != DC_STEP) return;
-    const double stp = S.stp;
     const bool push = S.push && S.ring_new >= 0;
-    const float2 sf = df_from_d(stp);
+    const float2 sf = S.stp_df;
     const int64_t part = Nx * 4;
     float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = ax + part;
     const float2 *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = ad + part;
@@ -897,6 +895,7 @@ k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
             }
             if (done) {
                 S.stp = stp;   // the accepted point is the last trial
+                S.stp_df = stpd;
                 S.f = ff;
                 double *ac = acc + (int64_t)b * NACC;
                 for (int a = 0; a < 4; ++a) ac[ACC_RS0 + a] = tot[2 + a];
@@ -1207,7 +1206,8 @@ void launch_dual_grad(const Problem &P, const DualCtl *ctl, const int32_t *list,
     if (n <= 0) return;
     const int NV = DV_S + 2 * P.ring;
     dim3 gg(grid_for(P.Nx * 2, 256 * 2, 64), n);
-    k_dual_grad<<<gg, 256, 0, st>>>(ctl, list, P.Nx, NV, P.ring, P.lambda_J, rq, 1.0 / qscale, KR, dv, acc, amax);
+    k_dual_grad<<<gg, 256, 0, st>>>(ctl, list, P.Nx, NV, P.ring, df_host(2.0 * P.lambda_J), rq, df_host(1.0 / qscale),
+                                    KR, dv, acc, amax);
 }
 
 void launch_dual_dots(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int newg, const float2 *dv,
