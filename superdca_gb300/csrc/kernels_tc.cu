@@ -49,13 +49,17 @@ constexpr int THREADS = 192;
 
 // A CTA owns MSUB consecutive 128-row subtiles and reuses each staged B tile
 // for all of them: the slot operand is the traffic that the L2 has to carry,
-// once per CTA per k-step.  TMEM holds one 128-column accumulator per subtile.
-template <int MSUB, int STG> struct Cfg {
+// once per CTA per k-step.  TMEM holds one 128-column accumulator per subtile
+// and N tile.  NT = 2 (slot operands exact in fp16, no lo half): the stage's
+// lo slot carries a second N tile, so every expanded one-hot tile feeds two
+// MMAs per K16 step, as it does for hi + lo.
+template <int MSUB, int STG, int NT = 1> struct Cfg {
     static constexpr int STAGE_BYTES = MSUB * A_BYTES + 2 * B_BYTES + MSUB * RAW_BYTES;
     static constexpr int SMEM_BYTES = STG * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-    static constexpr uint32_t TMEM_COLS = MSUB * BN;
+    static constexpr uint32_t TMEM_COLS = MSUB * BN * NT;
     static_assert(STAGE_BYTES % 1024 == 0, "stage must keep 1024-byte alignment");
-    static_assert(MSUB * BN <= 512, "TMEM holds 512 columns");
+    static_assert(MSUB * BN * NT <= 512, "TMEM holds 512 columns");
+    static_assert(NT == 1 || NT == 2, "one or two N tiles per CTA");
 };
 
 enum { MODE_FWD = 0, MODE_BWD = 1 };
@@ -151,12 +155,12 @@ struct GemmArgs {
     int *err;
 };
 
-template <int MSUB, int STG>
+template <int MSUB, int STG, int NT>
 __global__ void __launch_bounds__(THREADS, 1)
 k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtensorMap tmBhi,
        const __grid_constant__ CUtensorMap tmBlo, const GemmArgs args)
 {
-    using C = Cfg<MSUB, STG>;
+    using C = Cfg<MSUB, STG, NT>;
     constexpr int SB = C::STAGE_BYTES;
     extern __shared__ uint8_t smem_raw[];
     const uint32_t sbase0 = smem_u32(smem_raw);
@@ -175,7 +179,7 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
     uint32_t *tmem_slot_gen = reinterpret_cast<uint32_t *>(sgen + STG * SB + 8 * (3 * STG + 1));
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m_group = blockIdx.x, n_tile = blockIdx.y, split = blockIdx.z;
+    const int m_group = blockIdx.x, n_tile = blockIdx.y * NT, split = blockIdx.z;   // first N tile
     const int kt0 = split * args.kt_begin_stride;
     const int kt1 = min(args.kt_total, kt0 + args.kt_begin_stride);
     const int nkt = max(0, kt1 - kt0);
@@ -208,7 +212,7 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
                 const uint32_t ph = (uint32_t)((j / STG) & 1);
                 if (!mbar_wait(empty(s), ph ^ 1u)) { failed = true; break; }
                 const uint32_t st = sbase + (uint32_t)s * SB;
-                mbar_expect_tx(full_raw(s), MSUB * RAW_BYTES + (args.hi_only ? 1 : 2) * B_BYTES);
+                mbar_expect_tx(full_raw(s), MSUB * RAW_BYTES + (NT == 2 || !args.hi_only ? 2 : 1) * B_BYTES);
                 const int kt = kt0 + j;
 #pragma unroll
                 for (int ms = 0; ms < MSUB; ++ms) {
@@ -219,7 +223,10 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
                         tma_load_2d(st + RAW + ms * RAW_BYTES, &tmRaw, kt * BK, mt * 32, full_raw(s));
                 }
                 tma_load_2d(st + BHI, &tmBhi, kt * BK, n_tile * BN, full_raw(s));
-                if (!args.hi_only) tma_load_2d(st + BLO, &tmBlo, kt * BK, n_tile * BN, full_raw(s));
+                if (NT == 2)   // the second N tile (rows past the operand's end read as zero)
+                    tma_load_2d(st + BLO, &tmBhi, kt * BK, (n_tile + 1) * BN, full_raw(s));
+                else if (!args.hi_only)
+                    tma_load_2d(st + BLO, &tmBlo, kt * BK, n_tile * BN, full_raw(s));
             }
             // loads still in flight land before the block retires
             for (int j = max(0, nkt - STG); j < nkt; ++j)
@@ -242,7 +249,10 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
                         const uint64_t ad = smem_desc_sw128(st + a_off(ms) + kk * 32);
                         const uint32_t td = tmem_base + (uint32_t)(ms * BN);
                         mma_f16(td, ad, bh, (j > 0 || kk > 0) ? 1u : 0u);
-                        if (!args.hi_only) mma_f16(td, ad, bl, 1u);
+                        if (NT == 2)
+                            mma_f16(td + (uint32_t)(MSUB * BN), ad, bl, (j > 0 || kk > 0) ? 1u : 0u);
+                        else if (!args.hi_only)
+                            mma_f16(td, ad, bl, 1u);
                     }
                 }
                 mma_commit(empty(s));
@@ -273,8 +283,9 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
         const int q = warp & 3;  // TMEM lane quadrant of this warp
         const int r = q * 32 + lane;
 #pragma unroll 1
-        for (int ms = 0; ms < MSUB; ++ms) {
-            const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(ms * BN);
+        for (int nm = 0; nm < NT * MSUB; ++nm) {
+            const int nt = nm / MSUB, ms = nm % MSUB;
+            const uint32_t tbase = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(nm * BN);
             const int row = (m_group * MSUB + ms) * BM + r;
 #pragma unroll 1
             for (int cj = 0; cj < BN / 32; ++cj) {
@@ -283,7 +294,7 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
                 if (!ok) continue;
 #pragma unroll
                 for (int tt = 0; tt < 8; ++tt) {
-                    const int P = (n_tile * BN + cj * 32) / 4 + tt;
+                    const int P = ((n_tile + nt) * BN + cj * 32) / 4 + tt;
                     if (P >= args.nlist) continue;
                     const int b = args.planes > 1 ? args.list[P % args.nslot] : args.list[P];
                     if (args.mode == MODE_FWD) {
@@ -681,16 +692,22 @@ int msub_choice()
     return v;
 }
 
-template <int MSUB, int STG>
+template <int MSUB, int STG, int NT = 1>
 void launch_gemm(dim3 grid, const CUtensorMap &a, const CUtensorMap &bh, const CUtensorMap &bl,
                  const tc::GemmArgs &args, cudaStream_t st)
 {
-    tc::k_gemm<MSUB, STG><<<grid, tc::THREADS, tc::Cfg<MSUB, STG>::SMEM_BYTES, st>>>(a, bh, bl, args);
+    tc::k_gemm<MSUB, STG, NT><<<grid, tc::THREADS, tc::Cfg<MSUB, STG, NT>::SMEM_BYTES, st>>>(a, bh, bl, args);
 }
 
 void launch_gemm_any(int msub, int m_tiles, int n_tiles, int splits, const CUtensorMap &a, const CUtensorMap &bh,
                      const CUtensorMap &bl, const tc::GemmArgs &args, cudaStream_t st)
 {
+    if (args.hi_only && args.mode == tc::MODE_BWD) {
+        // exact fp16 operands: two N tiles per CTA, two subtiles, three stages
+        const dim3 grid((unsigned)((m_tiles + 1) / 2), (unsigned)((n_tiles + 1) / 2), (unsigned)splits);
+        launch_gemm<2, 3, 2>(grid, a, bh, bl, args, st);
+        return;
+    }
     const dim3 grid((unsigned)((m_tiles + msub - 1) / msub), (unsigned)n_tiles, (unsigned)splits);
     if (msub == 4) launch_gemm<4, 2>(grid, a, bh, bl, args, st);
     else if (msub == 2) launch_gemm<2, 3>(grid, a, bh, bl, args, st);
@@ -883,13 +900,16 @@ cudaError_t tc_launch_bwd(const TcPlan *pl, const Problem &P, const SlotDev *sd,
 
 cudaError_t tc_configure()
 {
-    cudaError_t e = cudaFuncSetAttribute(tc::k_gemm<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(tc::k_gemm<4, 2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          tc::Cfg<4, 2>::SMEM_BYTES);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(tc::k_gemm<2, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(tc::k_gemm<2, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc::Cfg<2, 3, 2>::SMEM_BYTES);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(tc::k_gemm<2, 3, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  tc::Cfg<2, 3>::SMEM_BYTES);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(tc::k_gemm<1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(tc::k_gemm<1, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  tc::Cfg<1, 4>::SMEM_BYTES);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(tc::k_kdig, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::KD_SMEM);
