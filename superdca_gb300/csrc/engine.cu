@@ -1329,13 +1329,12 @@ int dual_convert(sdca_handle *h, bool force)
     int rc = upload_slots(h, fin);
     if (rc) return rc;
     if (per_pass >= 1) {
-        Timed t(h, SDCA_K_BACKWARD, 5, 3 * (int64_t)fin.size());
+        Timed t(h, SDCA_K_BACKWARD, 4, 3 * (int64_t)fin.size());
         const int nf = (int)fin.size();
         launch_dual_digits3(P, h->sd, h->list, nf, h->dv, h->Rchk, h->stream);
         CK(tc_launch_bwd(h->tc, P, h->sd, h->list, nf, h->Rchk, 1.0f, h->Rhi, h->Rlo, h->gpool, h->tc_err,
                          h->stream, true, nullptr, 0, 3));   // digits |D| <= 2^10: exact in fp16
-        launch_dual_digit_acc3(P, h->list, nf, h->gpool, h->J64, h->stream);
-        launch_dual_to_wa(P, h->sd, h->list, nf, h->J64, h->wa, h->stream);
+        launch_dual_planes_to_wa(P, h->sd, h->list, nf, h->gpool, h->wa, h->stream);
     } else {
         Timed t(h, SDCA_K_BACKWARD, 3 * 4 + 1, 3 * (int64_t)fin.size());
         for (int d = 0; d < 3; ++d) {

@@ -255,8 +255,8 @@ void launch_dual_digit_acc(const Problem &P, const SlotDev *sd, const int32_t *l
 // combination from gpool buffers d n + s
 void launch_dual_digits3(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float2 *dv, float *R,
                          cudaStream_t st);
-void launch_dual_digit_acc3(const Problem &P, const int32_t *list, int n, const float *gpool, double *J64,
-                            cudaStream_t st);
+void launch_dual_planes_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *gpool,
+                              float *wa, cudaStream_t st);
 void launch_dual_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *J64,
                        float *wa, cudaStream_t st);
 

@@ -592,17 +592,46 @@ __global__ void k_dual_digits3(const SlotDev *__restrict__ sd, const int32_t *__
     }
 }
 
-// J = 2^22 X^T D0 + 2^11 X^T D1 + X^T D2 in 64-bit integers, the three
-// products from gpool buffers s, n + s, 2n + s
-__global__ void k_dual_digit_acc3(const int32_t *__restrict__ list, int n, int64_t Dp, const float *__restrict__ gpool,
-                                  long long *__restrict__ J64)
+// The solution from its three digit planes in one pass: J = (2^22 X^T D0 +
+// 2^11 X^T D1 + X^T D2) / tc_scale, the integer sum exact in 64 bits (below
+// 2^47), converted to double-float exactly, scaled in double-float and
+// rounded once to FP32 (no FP64 arithmetic: GB300's FP64 pipe is narrow);
+// J_rr = 0, h = eta, padding 0.  The products come from gpool buffers s,
+// n + s, 2n + s.
+__global__ void k_dual_planes_to_wa(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int n, int L,
+                                    int64_t Dp, const float *__restrict__ gpool, float *__restrict__ wa)
 {
     const int s = blockIdx.y, b = list[s];
+    const SlotDev &S = sd[b];
+    __shared__ float2 s_inv;
+    if (threadIdx.x == 0) s_inv = df_from_d(1.0 / S.tc_scale);   // one FP64 division per block
+    __syncthreads();
+    const float2 inv = s_inv;
     const float *g0 = gpool + (int64_t)s * Dp, *g1 = gpool + (int64_t)(n + s) * Dp, *g2 = gpool + (int64_t)(2 * n + s) * Dp;
-    long long *o = J64 + (int64_t)b * Dp;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < Dp; e += (int64_t)gridDim.x * blockDim.x)
-        o[e] = ((long long)__float2int_rn(g0[e]) << 22) + ((long long)__float2int_rn(g1[e]) << 11) +
-               (long long)__float2int_rn(g2[e]);
+    const int64_t nJ = (int64_t)QQ * L, own0 = (int64_t)S.locus * QQ;
+    float *o = wa + (int64_t)b * Dp;
+    for (int64_t e4 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e4 < Dp / 4; e4 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = 4 * e4;   // Dp and nJ are multiples of 4: a float4 is all J, all h or all padding
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (e < nJ) {
+            if (e < own0 || e >= own0 + QQ) {
+                const float4 a = reinterpret_cast<const float4 *>(g0)[e4], bb = reinterpret_cast<const float4 *>(g1)[e4],
+                             c = reinterpret_cast<const float4 *>(g2)[e4];
+                const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {bb.x, bb.y, bb.z, bb.w}, cv[4] = {c.x, c.y, c.z, c.w};
+                float r[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const long long J = ((long long)__float2int_rn(av[k]) << 22) +
+                                        ((long long)__float2int_rn(bv[k]) << 11) + (long long)__float2int_rn(cv[k]);
+                    r[k] = df_f(df_mul(df_from_ll_fast(J), inv));
+                }
+                v = make_float4(r[0], r[1], r[2], r[3]);
+            }
+        } else if (e < nJ + Q) {
+            v = make_float4((float)S.eta[0], (float)S.eta[1], (float)S.eta[2], (float)S.eta[3]);
+        }
+        reinterpret_cast<float4 *>(o)[e4] = v;
+    }
 }
 
 // J (=, or +=) 2^(22, 11, 0) (X^T D) in 64-bit integers: every X^T D is an
@@ -1279,12 +1308,12 @@ void launch_dual_digits3(const Problem &P, const SlotDev *sd, const int32_t *lis
                                       reinterpret_cast<float4 *>(R));
 }
 
-void launch_dual_digit_acc3(const Problem &P, const int32_t *list, int n, const float *gpool, double *J64,
-                            cudaStream_t st)
+void launch_dual_planes_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *gpool,
+                              float *wa, cudaStream_t st)
 {
     if (n <= 0) return;
-    dim3 g(grid_for(P.Dp, 256 * 16, 256), n);
-    k_dual_digit_acc3<<<g, 256, 0, st>>>(list, n, P.Dp, gpool, reinterpret_cast<long long *>(J64));
+    dim3 g(grid_for(P.Dp / 4, 256 * 8, 256), n);
+    k_dual_planes_to_wa<<<g, 256, 0, st>>>(sd, list, n, (int)P.L, P.Dp, gpool, wa);
 }
 
 void launch_dual_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const double *J64,
