@@ -86,7 +86,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the autotuner (default when --batch/--lanes are not given: measure them on a "
                          "probe list of loci outside the timed steps)")
-    ap.add_argument("--tune-loci", type=int, default=16384, help="loci the autotuner may solve as probes")
+    ap.add_argument("--tune-loci", type=int, default=36864, help="loci the autotuner may solve as probes")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the skewed 616 x 78,700 workload measured after the headline")
     ap.add_argument("--no-cpu", action="store_true")
@@ -348,7 +348,7 @@ def secondary_skewed(args, local, steps=3, warmup=1, seed=2):
     with Engine(N, L, batch=64, device=local, form=FORM_DUAL) as E0:
         w = E0.compute_weights(st, 0.9)
     order = (np.arange(L) * 7919) % L
-    tr = autotune(st, w, order[L - min(16384, L // 4):], form=FORM_DUAL, max_fraction=1.0, device=local,
+    tr = autotune(st, w, order[L - min(36864, L // 2):], form=FORM_DUAL, max_fraction=1.0, device=local,
                   want_scores=False)
     B, lanes = (tr.batch, tr.lanes) if tr.batch > 0 else (512, 4)
     per_step = 2 * B * lanes

@@ -36,7 +36,9 @@ struct Candidate {
 std::vector<Candidate> candidates(int form)
 {
     if (form == SDCA_FORM_DUAL)
-        return {{512, 4}, {512, 2}, {1024, 2}, {256, 4}, {768, 3}, {1024, 1}, {512, 1}, {256, 2}};
+        // largest first: on a small list the ones its probe budget cannot fill are skipped
+        return {{1280, 3}, {1024, 3}, {1024, 4}, {1536, 2}, {768, 3}, {1024, 2}, {512, 4},
+                {512, 2}, {256, 4}, {256, 2}, {512, 1}};
     return {{64, 1}, {32, 2}, {64, 2}, {128, 1}, {32, 1}};
 }
 

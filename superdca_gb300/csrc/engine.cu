@@ -526,7 +526,7 @@ int slot_begin(sdca_handle *h, int b, int64_t k, int32_t locus, const float *x0_
     }
     else
         CK(cudaMemsetAsync(wab, 0, sizeof(float) * P.Dp, h->stream));
-    CK(cudaMemsetAsync(h->d + (int64_t)b * P.Dp, 0, sizeof(float) * P.Dp, h->stream));
+    if (h->d) CK(cudaMemsetAsync(h->d + (int64_t)b * P.Dp, 0, sizeof(float) * P.Dp, h->stream));
     CK(cudaMemcpyAsync(h->rstate + (int64_t)b * P.Nx, (h->scan ? h->TT : h->XT) + (int64_t)locus * P.Nx, P.Nx,
                        cudaMemcpyDeviceToDevice, h->stream));
     if (!x0_engine)
@@ -1916,11 +1916,18 @@ static int create_lane(const sdca_config *cfg, const sdca_handle *owner, sdca_ha
         h->Kmat = owner->Kmat;
         h->Kd = owner->Kd;
     }
+    // The dual form keeps its iteration in N x 4 vectors: of the D-vectors it
+    // needs x (the formed solution, wa) per slot, gradient buffers for its
+    // one-hot contractions (the digit planes of up to B / 3 slots, or two per
+    // slot below 3 slots, which also serve sdca_eval) and the FP64 solution
+    // image only below 3 slots; no primal direction and no forward operand.
+    const bool dual_small = dual && B < 3;
+    const size_t n_d = dual ? 0 : B, n_gpool = dual && !dual_small ? std::max<size_t>(B, 2) : 2 * B;
     if ((!shared && ((rc = dalloc(h, &h->X, (size_t)P.N * P.Lx)) || (rc = dalloc(h, &h->XT, (size_t)P.L * P.Nx)) ||
                      (rc = dalloc(h, &h->w, (size_t)P.Nx)) || (rc = dalloc(h, &h->wf, (size_t)P.Nx)))) ||
         (rc = dalloc(h, &h->rstate, B * P.Nx)) ||
-        (rc = dalloc(h, &h->wa, B * P.Dp)) || (rc = dalloc(h, &h->d, B * P.Dp)) ||
-        (rc = dalloc(h, &h->gpool, 2 * B * P.Dp)) || (rc = dalloc(h, &h->u, B * P.Nx * 4)) ||
+        (rc = dalloc(h, &h->wa, B * P.Dp)) || (n_d && (rc = dalloc(h, &h->d, n_d * P.Dp))) ||
+        (rc = dalloc(h, &h->gpool, n_gpool * P.Dp)) || (rc = dalloc(h, &h->u, B * P.Nx * 4)) ||
         (rc = dalloc(h, &h->R, B * P.Nx * 4)) || (rc = dalloc(h, &h->lbase, B * P.Nx * 4)) ||
         (rc = dalloc(h, &h->partial, (size_t)P.C * B * P.Nx * 4)) ||
         (rc = dalloc(h, &h->partial64, (size_t)P.Cg * B * P.Nx * 4)) ||
@@ -1939,15 +1946,15 @@ static int create_lane(const sdca_config *cfg, const sdca_handle *owner, sdca_ha
                   (rc = dalloc(h, &h->dv, B * NV * 2 * P.Nx * 4)) || (rc = dalloc(h, &h->udf, B * P.Nx * 4)) ||
                   (rc = dalloc(h, &h->KR, B * P.Nx * 4)) || (rc = dalloc(h, &h->amax, 2 * B)) ||
                   (rc = dalloc(h, &h->rq, B * P.Nx * 4)) || (rc = dalloc(h, &h->csum, 16 * B)) ||
-                  (rc = dalloc(h, &h->Rchk, B * P.Nx * 4)) || (rc = dalloc(h, &h->J64, B * P.Dp)) ||
+                  (rc = dalloc(h, &h->Rchk, B * P.Nx * 4)) || (dual_small && (rc = dalloc(h, &h->J64, B * P.Dp))) ||
                   (rc = dalloc(h, &h->P0, B * P.Nx * 4)) || (rc = dalloc(h, &h->ud, B * P.Nx * 4)) ||
                   (!shared && (rc = dalloc(h, &h->Kmat, (size_t)P.Nx * P.Nx))) ||
                   (P.N <= 4000 && P.L < (1 << 18) &&
                    ((!shared && (rc = dalloc(h, &h->Kd, (size_t)3 * kd_nk_rows(P) * P.Nx))) ||
                     (rc = dalloc(h, &h->Rd, (size_t)4 * kd_nr_rows(P) * P.Nx)))))) ||
         (tcres &&
-         ((rc = dalloc(h, &h->Dhi, 4 * B * (size_t)round_up(4 * P.L, 64))) ||
-          (rc = dalloc(h, &h->Dlo, 4 * B * (size_t)round_up(4 * P.L, 64))) ||
+         ((!dual && (rc = dalloc(h, &h->Dhi, 4 * B * (size_t)round_up(4 * P.L, 64)))) ||
+          (!dual && (rc = dalloc(h, &h->Dlo, 4 * B * (size_t)round_up(4 * P.L, 64)))) ||
           (rc = dalloc(h, &h->Rhi, 4 * B * (size_t)P.Nx)) || (rc = dalloc(h, &h->Rlo, 4 * B * (size_t)P.Nx)) ||
           (rc = dalloc(h, &h->tc_err, 4))))) {
         std::string msg = h->err;

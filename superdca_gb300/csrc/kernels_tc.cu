@@ -673,6 +673,7 @@ bool make_map(CUtensorMap *m, CUtensorMapDataType dt, void *base, uint64_t cols,
 
 struct TcPlan {
     CUtensorMap mX, mXT, mDhi, mDlo, mRhi, mRlo;
+    bool has_fwd = false;   // the forward's slot operand (null for the dual form, which has no forward GEMM)
     int64_t Kp = 0;
     int fwd_splits = 1;
 };
@@ -749,10 +750,13 @@ TcPlan *tc_plan_create(const Problem &P, const uint8_t *X, const uint8_t *XT, __
                    (uint64_t)P.N, (uint64_t)P.Lx, 16, 128, CU_TENSOR_MAP_SWIZZLE_NONE);
     ok &= make_map(&p->mXT, CU_TENSOR_MAP_DATA_TYPE_UINT8, const_cast<uint8_t *>(XT), (uint64_t)P.Nx,
                    (uint64_t)P.L, (uint64_t)P.Nx, 64, 32, CU_TENSOR_MAP_SWIZZLE_NONE);
-    ok &= make_map(&p->mDhi, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Dhi, (uint64_t)Kp, (uint64_t)4 * P.Bmax,
-                   (uint64_t)Kp * 2, 64, 128, CU_TENSOR_MAP_SWIZZLE_128B);
-    ok &= make_map(&p->mDlo, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Dlo, (uint64_t)Kp, (uint64_t)4 * P.Bmax,
-                   (uint64_t)Kp * 2, 64, 128, CU_TENSOR_MAP_SWIZZLE_128B);
+    p->has_fwd = Dhi && Dlo;
+    if (p->has_fwd) {
+        ok &= make_map(&p->mDhi, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Dhi, (uint64_t)Kp, (uint64_t)4 * P.Bmax,
+                       (uint64_t)Kp * 2, 64, 128, CU_TENSOR_MAP_SWIZZLE_128B);
+        ok &= make_map(&p->mDlo, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Dlo, (uint64_t)Kp, (uint64_t)4 * P.Bmax,
+                       (uint64_t)Kp * 2, 64, 128, CU_TENSOR_MAP_SWIZZLE_128B);
+    }
     ok &= make_map(&p->mRhi, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Rhi, (uint64_t)P.Nx, (uint64_t)4 * P.Bmax,
                    (uint64_t)P.Nx * 2, 64, 128, CU_TENSOR_MAP_SWIZZLE_128B);
     ok &= make_map(&p->mRlo, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Rlo, (uint64_t)P.Nx, (uint64_t)4 * P.Bmax,
@@ -838,6 +842,7 @@ cudaError_t tc_launch_fwd(const TcPlan *pl, const Problem &P, const SlotDev *sd,
                           const float *vecs, __half *Dhi, __half *Dlo, float *partial, int splits, int *err,
                           cudaStream_t st)
 {
+    if (!pl->has_fwd) return cudaErrorInvalidValue;   // a plan without the forward's operand
     if (n <= 0) return cudaSuccess;
     {
         dim3 g((unsigned)std::min<int64_t>((4 * P.L + 255) / 256, 1024), (unsigned)n);
