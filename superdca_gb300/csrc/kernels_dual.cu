@@ -19,6 +19,7 @@
 // are taken in 64-bit integers; QB keeps them below 2^62.  K = K_all minus
 // the agreement at r itself, a class sum per state of r.
 #include <cstdint>
+#include <cstdlib>
 #include <new>
 
 #include "df.cuh"
@@ -725,7 +726,10 @@ __device__ __forceinline__ double dot4d(const double *a, const double *b)
     return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3];
 }
 
-constexpr int LS_THREADS = 256;
+// Threads per search block (LS_THREADS, 128 by default): the search is
+// latency-bound (short passes over the slot's sequences between block
+// reductions and the FP64 state machine of one thread), so smaller blocks
+// let more searches share an SM.
 
 // The whole line search of one slot in one thread block (SuperDCA: the
 // More-Thuente search of CppNumericalSolvers' LbfgsSolver, one
@@ -745,7 +749,8 @@ constexpr int LS_THREADS = 256;
 //   3. Trials until the search accepts one: the accepted point is the last
 //      trial, so R holds its residual rows, acc[ACC_RS*] their sums and the
 //      slot's f, stp the point's objective and step.
-__global__ void __launch_bounds__(LS_THREADS, 3)
+template <int LS_THREADS>
+__global__ void __launch_bounds__(LS_THREADS, 768 / LS_THREADS)
 k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int N, int64_t Nx, int NV,
                   double lambda_J, double lambda_h, const double *__restrict__ dacc, float2 *__restrict__ dv,
                   const float2 *__restrict__ lbase, float2 *__restrict__ u, float4 *__restrict__ ud,
@@ -977,12 +982,16 @@ k_dual_control(DualCtl *__restrict__ ctl, DualSum *__restrict__ sum, const int32
 {
     const int b = list[blockIdx.x];
     __shared__ DualCtl S;
+    __shared__ double s_eg[Q], s_dt[2 * MAXHIST], s_R[MAXHIST * MAXHIST], s_YY[MAXHIST * MAXHIST];
+    __shared__ int s_go;
     {
         const unsigned long long *src = reinterpret_cast<const unsigned long long *>(ctl + b);
         unsigned long long *dst = reinterpret_cast<unsigned long long *>(&S);
         for (int k = threadIdx.x; k < CTL_WORDS; k += 32) dst[k] = src[k];
     }
+    if (threadIdx.x == 0) s_go = 0;
     __syncwarp();
+    int &go = s_go;
     if (threadIdx.x == 0 && S.phase != DC_STOP) {
         const double *ac = acc + (int64_t)b * NACC;
         const bool init = S.phase == DC_EVAL0;
@@ -1060,72 +1069,81 @@ k_dual_control(DualCtl *__restrict__ ctl, DualSum *__restrict__ sum, const int32
             const bool near = S.chk_ratio > 0.0 && S.chk_ratio * gnorm < 1.1 * gtol;
             S.want_check = (due || near || gnorm < gtol || S.releps_stop) ? 1 : 0;
             S.chk_wait = S.want_check ? S.chk_wait + 1 : 0;
-            // compact-form coefficients of the next direction
-            const int k = S.nhist;
             S.coef_g = -1.0;
-            if (k > 0) {
-                const double *dp = dots + (int64_t)b * 4 * MAXHIST;
-                double dt[2 * MAXHIST];
-                for (int j = 0; j < k; ++j) {
-                    const int pj = S.hist[j];
-                    dt[j] = dp[pj] + dot4d(S.eta_s[pj], eg);
-                    dt[MAXHIST + j] = dp[DOT_Y + pj] + dot4d(S.eta_y[pj], eg);
-                }
-                if (S.ring_new >= 0) {
-                    // the newest pair's column: s_j.y = s_j.g - s_j.g_old, y_j.y likewise,
-                    // and its own s.y, y.y from the gradient pass
-                    const int pn = S.ring_new;
-                    for (int j = 0; j < k; ++j) {
-                        const int pj = S.hist[j];
-                        const double syj = pj == pn ? S.sy_new : dt[j] - S.sg_prev[pj];
-                        const double yyj = pj == pn ? S.yy_new : dt[MAXHIST + j] - S.yg_prev[pj];
-                        S.SY[pj][pn] = syj;
-                        S.YY[pj][pn] = yyj;
-                        S.YY[pn][pj] = yyj;
-                    }
-                }
-                for (int j = 0; j < k; ++j) {
-                    S.sg_prev[S.hist[j]] = dt[j];
-                    S.yg_prev[S.hist[j]] = dt[MAXHIST + j];
-                }
-                double Rm[MAXHIST * MAXHIST], YYm[MAXHIST * MAXHIST], sg[MAXHIST], yg[MAXHIST];
+            for (int a = 0; a < Q; ++a) s_eg[a] = eg[a];
+            go = 1;
+        }
+    }
+    __syncwarp();
+    // compact-form coefficients of the next direction: the per-pair work on
+    // the warp's lanes (lane j: history pair j), the small triangular solve
+    // on one thread
+    if (go) {
+        const int lane = threadIdx.x, k = S.nhist;
+        const double *dp = dots + (int64_t)b * 4 * MAXHIST;
+        if (lane < k) {
+            const int pj = S.hist[lane];
+            s_dt[lane] = dp[pj] + dot4d(S.eta_s[pj], s_eg);
+            s_dt[MAXHIST + lane] = dp[DOT_Y + pj] + dot4d(S.eta_y[pj], s_eg);
+        }
+        __syncwarp();
+        if (lane < k) {
+            const int pj = S.hist[lane];
+            if (S.ring_new >= 0) {
+                // the newest pair's column: s_j.y = s_j.g - s_j.g_old, y_j.y likewise,
+                // and its own s.y, y.y from the gradient pass
+                const int pn = S.ring_new;
+                const double syj = pj == pn ? S.sy_new : s_dt[lane] - S.sg_prev[pj];
+                const double yyj = pj == pn ? S.yy_new : s_dt[MAXHIST + lane] - S.yg_prev[pj];
+                S.SY[pj][pn] = syj;
+                S.YY[pj][pn] = yyj;
+                S.YY[pn][pj] = yyj;
+            }
+        }
+        __syncwarp();
+        if (lane < k) {
+            S.sg_prev[S.hist[lane]] = s_dt[lane];
+            S.yg_prev[S.hist[lane]] = s_dt[MAXHIST + lane];
+        }
+        for (int e = lane; e < k * k; e += 32) {
+            const int ra = e / k, rc = e % k;
+            s_R[e] = (ra <= rc) ? S.SY[S.hist[ra]][S.hist[rc]] : 0.0;
+            s_YY[e] = S.YY[S.hist[ra]][S.hist[rc]];
+        }
+        __syncwarp();
+        if (lane == 0 && k > 0) {
+            double cg, cS[MAXHIST], cY[MAXHIST];
+            if (lbfgs_compact_coeffs(k, s_R, s_YY, s_dt, s_dt + MAXHIST, S.gamma, &cg, cS, cY)) {
+                S.coef_g = cg;
                 for (int a = 0; a < k; ++a) {
-                    sg[a] = dt[a];
-                    yg[a] = dt[MAXHIST + a];
-                    for (int c = 0; c < k; ++c) {
-                        Rm[a * k + c] = (a <= c) ? S.SY[S.hist[a]][S.hist[c]] : 0.0;
-                        YYm[a * k + c] = S.YY[S.hist[a]][S.hist[c]];
-                    }
+                    S.coefS[a] = cS[a];
+                    S.coefY[a] = cY[a];
                 }
-                double cg, cS[MAXHIST], cY[MAXHIST];
-                if (lbfgs_compact_coeffs(k, Rm, YYm, sg, yg, S.gamma, &cg, cS, cY)) {
-                    S.coef_g = cg;
-                    for (int a = 0; a < k; ++a) {
-                        S.coefS[a] = cS[a];
-                        S.coefY[a] = cY[a];
-                    }
-                } else {
-                    S.nhist = 0;
-                    S.iter = 0;
-                }
+            } else {
+                S.nhist = 0;
+                S.iter = 0;
             }
-            for (int a = 0; a < Q; ++a) {
-                double v = S.coef_g * eg[a];
-                for (int j = 0; j < S.nhist; ++j)
-                    v += S.coefS[j] * S.eta_s[S.hist[j]][a] + S.coefY[j] * S.eta_y[S.hist[j]][a];
-                S.eta_d[a] = v;
-            }
-            for (int j = 0; j < S.nhist; ++j) {
-                S.cdf[j] = df_from_d(S.coefS[j]);
-                S.cdf[MAXHIST + j] = df_from_d(S.coefY[j]);
-            }
+        }
+        __syncwarp();
+        const int kk = S.nhist;
+        if (lane < Q) {
+            double v = S.coef_g * s_eg[lane];
+            for (int j = 0; j < kk; ++j)
+                v += S.coefS[j] * S.eta_s[S.hist[j]][lane] + S.coefY[j] * S.eta_y[S.hist[j]][lane];
+            S.eta_d[lane] = v;
+            S.cdf[2 * MAXHIST + 1 + lane] = df_from_d(v);
+        }
+        if (lane < kk) {
+            S.cdf[lane] = df_from_d(S.coefS[lane]);
+            S.cdf[MAXHIST + lane] = df_from_d(S.coefY[lane]);
+        }
+        if (lane == 0) {
             S.cdf[2 * MAXHIST] = df_from_d(S.coef_g);
-            for (int a = 0; a < Q; ++a) S.cdf[2 * MAXHIST + 1 + a] = df_from_d(S.eta_d[a]);
             // the next accepted step fills a ring position outside the live history
             int pos = 0;
             for (bool used = true; used;) {
                 used = false;
-                for (int j = 0; j < S.nhist; ++j) used = used || S.hist[j] == pos;
+                for (int j = 0; j < kk; ++j) used = used || S.hist[j] == pos;
                 if (used) ++pos;
             }
             S.ring_new = pos;
@@ -1329,10 +1347,19 @@ void launch_dual_linesearch(const Problem &P, DualCtl *ctl, const int32_t *list,
                             const float *w, const float *P0, float *R, double *acc, cudaStream_t st)
 {
     if (n <= 0) return;
-    k_dual_linesearch<<<n, LS_THREADS, 0, st>>>(ctl, list, (int)P.N, P.Nx, DV_S + 2 * P.ring, P.lambda_J,
-                                               P.lambda_h, dacc, dv, lbase, u, reinterpret_cast<float4 *>(ud),
-                                               rstate, w, reinterpret_cast<const float4 *>(P0),
-                                               reinterpret_cast<float4 *>(R), acc);
+    static const int threads = [] {
+        const char *e = std::getenv("SDCA_LS_THREADS");
+        const int v = e ? std::atoi(e) : 128;
+        return (v == 64 || v == 256) ? v : 128;
+    }();
+#define SDCA_LS_LAUNCH(T)                                                                                          \
+    k_dual_linesearch<T><<<n, T, 0, st>>>(ctl, list, (int)P.N, P.Nx, DV_S + 2 * P.ring, P.lambda_J, P.lambda_h,   \
+                                          dacc, dv, lbase, u, reinterpret_cast<float4 *>(ud), rstate, w,          \
+                                          reinterpret_cast<const float4 *>(P0), reinterpret_cast<float4 *>(R), acc)
+    if (threads == 64) SDCA_LS_LAUNCH(64);
+    else if (threads == 256) SDCA_LS_LAUNCH(256);
+    else SDCA_LS_LAUNCH(128);
+#undef SDCA_LS_LAUNCH
 }
 
 void launch_dual_control(const Problem &P, DualCtl *ctl, DualSum *sum, const int32_t *list, int n,
