@@ -390,39 +390,6 @@ __device__ __forceinline__ void mma_f16_kd(uint32_t tmem_d, uint64_t adesc, uint
         : "memory");
 }
 
-// cluster helpers (the multicast K rho product pairs two CTAs)
-__device__ __forceinline__ uint32_t cluster_rank()
-{
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-    return r;
-}
-
-__device__ __forceinline__ void cluster_sync()
-{
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
-// TMA tile load delivered to the same shared-memory offset (and completing
-// on the same mbarrier offset) in every CTA of the mask
-__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap *tm, int x, int y, uint32_t bar,
-                                               uint16_t mask)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-        " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar), "h"(mask)
-        : "memory");
-}
-
-// MMA completion arriving on the same mbarrier offset in every CTA of the mask
-__device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
-                 ::"r"(bar), "h"(mask)
-                 : "memory");
-}
-
 struct KdArgs {
     int kt_total;        // Nx / 64
     int nk_rows;         // rows per K digit plane (multiple of 128)
@@ -438,14 +405,6 @@ struct KdArgs {
     int *err;
 };
 
-// MC: the CTA pair of a cluster (same 128 rows of K, consecutive groups of
-// 13 slots) shares the K digit tiles: each CTA loads 64 of the 128 rows of
-// every plane and multicasts them to both (tmK then has a 64-row box), and a
-// stage is free once both CTAs' MMAs have read it (the empty barriers count
-// two arrivals, one multicast commit from each CTA).  The pair synchronises
-// after initialising its barriers and before leaving, so that no multicast
-// copy or remote arrival reaches a CTA that has not started or has ended.
-template <bool MC>
 __global__ void __launch_bounds__(THREADS, 1)
 k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensorMap tmRh,
        const __grid_constant__ CUtensorMap tmRt, const KdArgs args)
@@ -470,7 +429,7 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
     if (threadIdx.x == 0) {
         for (int s = 0; s < KD_STG; ++s) {
             mbar_init(full(s), 1);
-            mbar_init(empty(s), MC ? 2 : 1);
+            mbar_init(empty(s), 1);
         }
         mbar_init(tmem_full, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -483,11 +442,9 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (MC) cluster_sync();   // the peer's barriers are initialised before any multicast reaches them
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem_base = *tmem_slot_gen;
     bool failed = false;
-    const uint32_t crank = MC ? cluster_rank() : 0u;
 
     if (warp == 0) {
         if (lane == 0) {
@@ -499,14 +456,8 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
                 const uint32_t st = sbase + (uint32_t)s * KD_STAGE;
                 mbar_expect_tx(full(s), KD_STAGE);
 #pragma unroll
-                for (int k = 0; k < KD_KDIG; ++k) {
-                    if (MC)   // this CTA's half of the rows, to both CTAs of the pair
-                        tma_load_2d_mc(st + k * KD_A_BYTES + crank * (KD_A_BYTES / 2), &tmK, j * KD_BK,
-                                       k * args.nk_rows + m_tile * KD_BM + (int)crank * (KD_BM / 2), full(s),
-                                       (uint16_t)0x3);
-                    else
-                        tma_load_2d(st + k * KD_A_BYTES, &tmK, j * KD_BK, k * args.nk_rows + m_tile * KD_BM, full(s));
-                }
+                for (int k = 0; k < KD_KDIG; ++k)
+                    tma_load_2d(st + k * KD_A_BYTES, &tmK, j * KD_BK, k * args.nk_rows + m_tile * KD_BM, full(s));
 #pragma unroll
                 for (int p = 0; p < KD_RDIG; ++p) {
                     tma_load_2d(st + BOFF + p * KD_HEAD_BYTES, &tmRh, j * KD_BK, p * args.nr_rows + r0, full(s));
@@ -534,8 +485,7 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
                         mma_f16_kd(tmem_base + (uint32_t)(k * KD_NB), ad, bd, (j > 0 || kk > 0) ? 1u : 0u);
                     }
                 }
-                if (MC) mma_commit_mc(empty(s), (uint16_t)0x3);   // the stage is free in both CTAs' view
-                else mma_commit(empty(s));
+                mma_commit(empty(s));
             }
             mma_commit(tmem_full);
         }
@@ -593,9 +543,6 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
     if (failed) atomicExch(args.err, 1);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    // every MMA of both CTAs has completed (each waited on its tmem_full), so
-    // no multicast copy or commit is still on its way to either CTA
-    if (MC) cluster_sync();
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(KD_TMEM_COLS)
@@ -824,19 +771,9 @@ TcPlan *tc_plan_create(const Problem &P, const uint8_t *X, const uint8_t *XT, __
 void tc_plan_destroy(TcPlan *p) { delete p; }
 
 struct KdPlan {
-    CUtensorMap mK, mKh, mRh, mRt;   // K digits (128- and 64-row boxes); rho digit plane heads (32 rows) and tails (8 rows)
+    CUtensorMap mK, mRh, mRt;   // K digits; rho digit plane heads (32 rows) and tails (8 rows)
     int nk_rows = 0, nr_rows = 0;
 };
-
-// the K rho product with CTA pairs sharing the K tiles (default); SDCA_KDIG_MC=0 selects one CTA per tile
-bool kdig_multicast()
-{
-    static const bool v = [] {
-        const char *e = std::getenv("SDCA_KDIG_MC");
-        return !(e && e[0] == '0');
-    }();
-    return v;
-}
 
 int kd_nk_rows(const Problem &P) { return (int)(((P.Nx + tc::KD_BM - 1) / tc::KD_BM) * tc::KD_BM); }
 // rows per rho digit plane: 3 per slot for whole CTAs of 13 slots, one more
@@ -854,8 +791,6 @@ KdPlan *tc_kdig_plan_create(const Problem &P, __half *Kd, __half *Rd)
     p->nr_rows = kd_nr_rows(P);
     bool ok = make_map(&p->mK, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Kd, (uint64_t)P.Nx, (uint64_t)tc::KD_KDIG * p->nk_rows,
                        (uint64_t)P.Nx * 2, tc::KD_BK, tc::KD_BM, CU_TENSOR_MAP_SWIZZLE_128B);
-    ok &= make_map(&p->mKh, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Kd, (uint64_t)P.Nx, (uint64_t)tc::KD_KDIG * p->nk_rows,
-                   (uint64_t)P.Nx * 2, tc::KD_BK, tc::KD_BM / 2, CU_TENSOR_MAP_SWIZZLE_128B);
     ok &= make_map(&p->mRh, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Rd, (uint64_t)P.Nx, (uint64_t)tc::KD_RDIG * p->nr_rows,
                    (uint64_t)P.Nx * 2, tc::KD_BK, tc::KD_HEAD, CU_TENSOR_MAP_SWIZZLE_128B);
     ok &= make_map(&p->mRt, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Rd, (uint64_t)P.Nx, (uint64_t)tc::KD_RDIG * p->nr_rows,
@@ -898,25 +833,8 @@ cudaError_t tc_launch_kdig(const KdPlan *pl, const Problem &P, const int32_t *li
     a.inv_qscale = inv_qscale;
     a.KR = KR;
     a.err = err;
-    const unsigned ntiles = (unsigned)((n + tc::KD_S - 1) / tc::KD_S);
-    if (kdig_multicast()) {
-        // CTA pairs along the slot groups (an odd last group gets an idle partner)
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3((unsigned)(pl->nk_rows / tc::KD_BM), (ntiles + 1) & ~1u, 1);
-        cfg.blockDim = dim3(tc::THREADS, 1, 1);
-        cfg.dynamicSmemBytes = tc::KD_SMEM;
-        cfg.stream = st;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = 1;
-        attr[0].val.clusterDim.y = 2;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        return cudaLaunchKernelEx(&cfg, tc::k_kdig<true>, pl->mKh, pl->mRh, pl->mRt, a);
-    }
-    dim3 grid((unsigned)(pl->nk_rows / tc::KD_BM), ntiles);
-    tc::k_kdig<false><<<grid, tc::THREADS, tc::KD_SMEM, st>>>(pl->mK, pl->mRh, pl->mRt, a);
+    dim3 grid((unsigned)(pl->nk_rows / tc::KD_BM), (unsigned)((n + tc::KD_S - 1) / tc::KD_S));
+    tc::k_kdig<<<grid, tc::THREADS, tc::KD_SMEM, st>>>(pl->mK, pl->mRh, pl->mRt, a);
     return cudaGetLastError();
 }
 
@@ -999,9 +917,7 @@ cudaError_t tc_configure()
         e = cudaFuncSetAttribute(tc::k_gemm<1, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  tc::Cfg<1, 4>::SMEM_BYTES);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(tc::k_kdig<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::KD_SMEM);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(tc::k_kdig<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::KD_SMEM);
+        e = cudaFuncSetAttribute(tc::k_kdig, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::KD_SMEM);
     return e;
 }
 
