@@ -224,27 +224,27 @@ void launch_trial_dual(const Problem &P, const SlotDev *sd, const int32_t *list,
 // dual form (kernels_dual.cu)
 void launch_dual_kmat(const int32_t *dist, int N, int64_t Nx, int L, int32_t *K, cudaStream_t st);
 void launch_dual_quant(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *R,
-                       const uint8_t *rstate, double qscale, int32_t *rq, long long *csum, cudaStream_t st);
+                       const uint8_t *rstate, double qscale, int32_t *rq, long long *csum, cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8_t *rstate, const int32_t *K,
-                       double qscale, const int32_t *rq, const long long *csum, float2 *KR, cudaStream_t st);
+                       double qscale, const int32_t *rq, const long long *csum, float2 *KR, cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_grad(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, double qscale,
-                      const int32_t *rq, const float2 *KR, float2 *dv, double *acc, double *amax, cudaStream_t st);
+                      const int32_t *rq, const float2 *KR, float2 *dv, double *acc, double *amax, cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_dots(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int newg, const float2 *dv,
-                      double *dots, cudaStream_t st);
+                      double *dots, cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_direction(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
                            const float2 *lbase, float *P0, const float *w, const uint8_t *rstate, float2 *u,
-                           float *ud, double *dacc, cudaStream_t st);
+                           float *ud, double *dacc, cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_accept(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
-                        const float2 *u, float2 *lbase, cudaStream_t st);
+                        const float2 *u, float2 *lbase, cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_to_r(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int which,
                       const float2 *dv, float *R, cudaStream_t st);
 // the per-iteration decisions of the dual form on the device
 void launch_dual_linesearch(const Problem &P, DualCtl *ctl, const int32_t *list, int n, const double *dacc,
                             float2 *dv, const float2 *lbase, float2 *u, float *ud, const uint8_t *rstate,
-                            const float *w, const float *P0, float *R, double *acc, cudaStream_t st);
+                            const float *w, const float *P0, float *R, double *acc, cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_control(const Problem &P, DualCtl *ctl, DualSum *sum, const int32_t *list, int n,
                          int max_iterations, double gtol, const double *acc, const double *amax, const double *dots,
-                         cudaStream_t st);
+                         cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_check_apply(DualCtl *ctl, DualSum *sum, const int32_t *list, int n, double gtol, const double *acc,
                              cudaStream_t st);
 void launch_dual_digits(const Problem &P, const SlotDev *sd, const int32_t *list, int n, int d, const float2 *dv,
@@ -280,7 +280,7 @@ void launch_dual_ws_feats(const uint8_t *cols, const int32_t *idx, int n, int N,
 void launch_dual_ws_r(const int32_t *slots, int n, int N, int64_t Nx, const float *out, const float *p_dev, float alpha,
                       const float *w, float *R, cudaStream_t st);
 void launch_dual_ws_init(const Problem &P, const int32_t *list, int n, double c, double qscale, const int32_t *rq,
-                         const float2 *KR, float2 *dv, float2 *lbase, cudaStream_t st);
+                         const float2 *KR, float2 *dv, float2 *lbase, cudaStream_t st, const int *cnt = nullptr);
 void launch_ws_residual(const uint8_t *XT, int64_t Nx, int N, const int32_t *loci, int G, const double *w,
                         const int32_t *knn, int k, float eps, float *Rws, cudaStream_t st);
 void launch_ws_residual_split(const uint8_t *XT, int64_t Nx, int N, const int32_t *loci, const int32_t *slots, int G,
@@ -328,6 +328,6 @@ void tc_kdig_plan_destroy(KdPlan *p);
 void tc_kdig_fill_k(const KdPlan *pl, const Problem &P, const int32_t *K, __half *Kd, cudaStream_t st);
 cudaError_t tc_launch_kdig(const KdPlan *pl, const Problem &P, const int32_t *list, int n, const int32_t *rq,
                            const uint8_t *rstate, const long long *csum, double inv_qscale, __half *Rd, float2 *KR,
-                           int *err, cudaStream_t st);
+                           int *err, cudaStream_t st, const int *cnt = nullptr);
 
 } // namespace sdca

@@ -48,8 +48,9 @@ __global__ void k_dual_kmat(const int32_t *__restrict__ dist, int N, int64_t Nx,
 __global__ void __launch_bounds__(256)
 k_dual_quant(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int N, int64_t Nx,
              const float4 *__restrict__ R, const uint8_t *__restrict__ rstate, float qscale, int4 *__restrict__ rq,
-             unsigned long long *__restrict__ csum)
+             unsigned long long *__restrict__ csum, const int *__restrict__ cnt)
 {
+    if (cnt && (int)blockIdx.y >= *cnt) return;
     const int b = list[blockIdx.y];
     const bool own = sd[b].locus >= 0;   // scan mode: no own-agreement correction
     __shared__ unsigned long long red[16];
@@ -96,8 +97,12 @@ constexpr int KP_J = 16;   // sequences j per shared-memory stage
 __global__ void __launch_bounds__(256)
 k_dual_kprod(const int32_t *__restrict__ K, int64_t Nx, int N, const int32_t *__restrict__ list, int nlist,
              const int4 *__restrict__ rq, const long long *__restrict__ csum, const uint8_t *__restrict__ rstate,
-             double inv_qscale, float2 *__restrict__ KR)
+             double inv_qscale, float2 *__restrict__ KR, const int *__restrict__ cnt)
 {
+    if (cnt) {
+        nlist = *cnt;
+        if ((int)blockIdx.y * KP_S >= nlist) return;
+    }
     __shared__ __align__(16) int32_t sK[KP_J][KP_M];
     __shared__ __align__(16) int32_t sR[KP_J][KP_S * 4];
     const int t = threadIdx.x;
@@ -170,8 +175,9 @@ __device__ __forceinline__ void df2_store(float2 *p, int64_t t, const float2 (&v
 __global__ void __launch_bounds__(256)
 k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
             float2 l2, const int32_t *__restrict__ rq, float2 iq, const float2 *__restrict__ KR,
-            float2 *__restrict__ dv, double *__restrict__ acc, double *__restrict__ amax)
+            float2 *__restrict__ dv, double *__restrict__ acc, double *__restrict__ amax, const int *__restrict__ cnt)
 {
+    if (cnt && (int)blockIdx.y >= *cnt) return;
     const int b = list[blockIdx.y];
     const DualCtl &S = ctl[b];
     if (S.phase == DC_STOP) return;
@@ -248,8 +254,9 @@ constexpr int DOT_CHUNK = 2048;
 
 __global__ void __launch_bounds__(256)
 k_dual_dots(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
-            int newg, const float2 *__restrict__ dv, double *__restrict__ dots)
+            int newg, const float2 *__restrict__ dv, double *__restrict__ dots, const int *__restrict__ cnt)
 {
+    if (cnt && (int)blockIdx.y >= *cnt) return;
     const int b = list[blockIdx.y];
     const DualCtl &S = ctl[b];
     if (S.phase == DC_STOP) return;
@@ -365,8 +372,9 @@ __global__ void __launch_bounds__(DIR_THREADS, 5)
 k_dual_direction(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int N, int NV,
                  int ring, float2 *__restrict__ dv, const float2 *__restrict__ lbase, float *__restrict__ P0,
                  const float *__restrict__ w, const uint8_t *__restrict__ rstate, float2 *__restrict__ u,
-                 float *__restrict__ ud, double *__restrict__ dacc)
+                 float *__restrict__ ud, double *__restrict__ dacc, const int *__restrict__ cnt)
 {
+    if (cnt && (int)blockIdx.y >= *cnt) return;
     const int b = list[blockIdx.y];
     const DualCtl &S = ctl[b];
     if (S.phase == DC_STOP) return;
@@ -482,8 +490,10 @@ k_dual_direction(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ li
 // logits lbase += stp u
 __global__ void __launch_bounds__(256)
 k_dual_accept(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int NV,
-              float2 *__restrict__ dv, const float2 *__restrict__ u, float2 *__restrict__ lbase)
+              float2 *__restrict__ dv, const float2 *__restrict__ u, float2 *__restrict__ lbase,
+              const int *__restrict__ cnt)
 {
+    if (cnt && (int)blockIdx.y >= *cnt) return;
     const int b = list[blockIdx.y];
     const DualCtl &S = ctl[b];
     if (S.phase != DC_STEP) return;
@@ -755,8 +765,9 @@ k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
                   double lambda_J, double lambda_h, const double *__restrict__ dacc, float2 *__restrict__ dv,
                   const float2 *__restrict__ lbase, float2 *__restrict__ u, float4 *__restrict__ ud,
                   const uint8_t *__restrict__ rstate, const float *__restrict__ w, const float4 *__restrict__ P0,
-                  float4 *__restrict__ R, double *__restrict__ acc)
+                  float4 *__restrict__ R, double *__restrict__ acc, const int *__restrict__ cnt)
 {
+    if (cnt && (int)blockIdx.x >= *cnt) return;
     const int b = list[blockIdx.x];
     DualCtl &S = ctl[b];
     if (S.phase != DC_STEP) return;   // (the same for the whole block)
@@ -978,8 +989,9 @@ __device__ void write_summary(const DualCtl &S, DualSum &o)
 __global__ void __launch_bounds__(32)
 k_dual_control(DualCtl *__restrict__ ctl, DualSum *__restrict__ sum, const int32_t *__restrict__ list, int m,
                int max_iterations, double gtol, double lambda_J, double lambda_h, const double *__restrict__ acc,
-               const double *__restrict__ amax, const double *__restrict__ dots)
+               const double *__restrict__ amax, const double *__restrict__ dots, const int *__restrict__ cnt)
 {
+    if (cnt && (int)blockIdx.x >= *cnt) return;
     const int b = list[blockIdx.x];
     __shared__ DualCtl S;
     __shared__ double s_eg[Q], s_dt[2 * MAXHIST], s_R[MAXHIST * MAXHIST], s_YY[MAXHIST * MAXHIST];
@@ -1200,8 +1212,9 @@ __global__ void k_dual_check_apply(DualCtl *__restrict__ ctl, DualSum *__restric
 __global__ void __launch_bounds__(256)
 k_dual_ws_init(const int32_t *__restrict__ list, int64_t Nx, int NV, double c, double inv_qscale,
                const int32_t *__restrict__ rq, const float2 *__restrict__ KR, float2 *__restrict__ dv,
-               float2 *__restrict__ lbase)
+               float2 *__restrict__ lbase, const int *__restrict__ cnt)
 {
+    if (cnt && (int)blockIdx.y >= *cnt) return;
     const int b = list[blockIdx.y];
     const float2 cd = df_from_d(c), cq = df_from_d(c * inv_qscale);
     float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = ax + Nx * 4;
@@ -1228,67 +1241,70 @@ void launch_dual_kmat(const int32_t *dist, int N, int64_t Nx, int L, int32_t *K,
 }
 
 void launch_dual_quant(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *R,
-                       const uint8_t *rstate, double qscale, int32_t *rq, long long *csum, cudaStream_t st)
+                       const uint8_t *rstate, double qscale, int32_t *rq, long long *csum, cudaStream_t st,
+                       const int *cnt)
 {
     if (n <= 0) return;
     dim3 gq(grid_for(P.Nx, 256 * 4, 64), n);
     k_dual_quant<<<gq, 256, 0, st>>>(sd, list, (int)P.N, P.Nx, reinterpret_cast<const float4 *>(R), rstate,
-                                     (float)qscale,
-                                     reinterpret_cast<int4 *>(rq), reinterpret_cast<unsigned long long *>(csum));
+                                     (float)qscale, reinterpret_cast<int4 *>(rq),
+                                     reinterpret_cast<unsigned long long *>(csum), cnt);
 }
 
 // K rho on the CUDA cores (64-bit integer multiply-adds): any N
 void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8_t *rstate, const int32_t *K,
-                       double qscale, const int32_t *rq, const long long *csum, float2 *KR, cudaStream_t st)
+                       double qscale, const int32_t *rq, const long long *csum, float2 *KR, cudaStream_t st,
+                       const int *cnt)
 {
     if (n <= 0) return;
     dim3 gk((unsigned)(P.Nx / KP_M), (unsigned)((n + KP_S - 1) / KP_S));
     k_dual_kprod<<<gk, 256, 0, st>>>(K, P.Nx, (int)P.N, list, n, reinterpret_cast<const int4 *>(rq), csum, rstate,
-                                     1.0 / qscale, KR);
+                                     1.0 / qscale, KR, cnt);
 }
 
 void launch_dual_grad(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, double qscale,
-                      const int32_t *rq, const float2 *KR, float2 *dv, double *acc, double *amax, cudaStream_t st)
+                      const int32_t *rq, const float2 *KR, float2 *dv, double *acc, double *amax, cudaStream_t st,
+                      const int *cnt)
 {
     if (n <= 0) return;
     const int NV = DV_S + 2 * P.ring;
     dim3 gg(grid_for(P.Nx * 2, 256 * 2, 64), n);
     k_dual_grad<<<gg, 256, 0, st>>>(ctl, list, P.Nx, NV, P.ring, df_host(2.0 * P.lambda_J), rq, df_host(1.0 / qscale),
-                                    KR, dv, acc, amax);
+                                    KR, dv, acc, amax, cnt);
 }
 
 void launch_dual_dots(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int newg, const float2 *dv,
-                      double *dots, cudaStream_t st)
+                      double *dots, cudaStream_t st, const int *cnt)
 {
     if (n <= 0) return;
     dim3 g((unsigned)((P.Nx * 4 + DOT_CHUNK - 1) / DOT_CHUNK), n);
-    k_dual_dots<<<g, 256, 0, st>>>(ctl, list, P.Nx, DV_S + 2 * P.ring, P.ring, newg, dv, dots);
+    k_dual_dots<<<g, 256, 0, st>>>(ctl, list, P.Nx, DV_S + 2 * P.ring, P.ring, newg, dv, dots, cnt);
 }
 
 void launch_dual_direction(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
                            const float2 *lbase, float *P0, const float *w, const uint8_t *rstate, float2 *u,
-                           float *ud, double *dacc, cudaStream_t st)
+                           float *ud, double *dacc, cudaStream_t st, const int *cnt)
 {
     if (n <= 0) return;
     dim3 g((unsigned)((P.Nx * 2 + DIR_THREADS - 1) / DIR_THREADS), n);
     k_dual_direction<<<g, DIR_THREADS, 0, st>>>(ctl, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, P.ring, dv, lbase, P0,
-                                                w, rstate, u, ud, dacc);
+                                                w, rstate, u, ud, dacc, cnt);
 }
 
 void launch_dual_accept(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
-                        const float2 *u, float2 *lbase, cudaStream_t st)
+                        const float2 *u, float2 *lbase, cudaStream_t st, const int *cnt)
 {
     if (n <= 0) return;
     dim3 g(grid_for(P.Nx * 2, 256 * 2, 64), n);
-    k_dual_accept<<<g, 256, 0, st>>>(ctl, list, P.Nx, DV_S + 2 * P.ring, dv, u, lbase);
+    k_dual_accept<<<g, 256, 0, st>>>(ctl, list, P.Nx, DV_S + 2 * P.ring, dv, u, lbase, cnt);
 }
 
 void launch_dual_ws_init(const Problem &P, const int32_t *list, int n, double c, double qscale, const int32_t *rq,
-                         const float2 *KR, float2 *dv, float2 *lbase, cudaStream_t st)
+                         const float2 *KR, float2 *dv, float2 *lbase, cudaStream_t st, const int *cnt)
 {
     if (n <= 0) return;
     dim3 g(grid_for(P.Nx * 4, 256 * 4, 64), n);
-    k_dual_ws_init<<<g, 256, 0, st>>>(list, P.Nx, DV_S + 2 * P.ring, c, 1.0 / qscale, rq, KR, dv, lbase);
+    k_dual_ws_init<<<g, 256, 0, st>>>(list, P.Nx, DV_S + 2 * P.ring, c, 1.0 / qscale, rq, KR, dv, lbase, cnt);
 }
 
 void launch_dual_to_r(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int which,
@@ -1344,7 +1360,7 @@ void launch_dual_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list,
 
 void launch_dual_linesearch(const Problem &P, DualCtl *ctl, const int32_t *list, int n, const double *dacc,
                             float2 *dv, const float2 *lbase, float2 *u, float *ud, const uint8_t *rstate,
-                            const float *w, const float *P0, float *R, double *acc, cudaStream_t st)
+                            const float *w, const float *P0, float *R, double *acc, cudaStream_t st, const int *cnt)
 {
     if (n <= 0) return;
     static const int threads = [] {
@@ -1355,7 +1371,8 @@ void launch_dual_linesearch(const Problem &P, DualCtl *ctl, const int32_t *list,
 #define SDCA_LS_LAUNCH(T)                                                                                          \
     k_dual_linesearch<T><<<n, T, 0, st>>>(ctl, list, (int)P.N, P.Nx, DV_S + 2 * P.ring, P.lambda_J, P.lambda_h,   \
                                           dacc, dv, lbase, u, reinterpret_cast<float4 *>(ud), rstate, w,          \
-                                          reinterpret_cast<const float4 *>(P0), reinterpret_cast<float4 *>(R), acc)
+                                          reinterpret_cast<const float4 *>(P0), reinterpret_cast<float4 *>(R), acc, \
+                                          cnt)
     if (threads == 64) SDCA_LS_LAUNCH(64);
     else if (threads == 256) SDCA_LS_LAUNCH(256);
     else SDCA_LS_LAUNCH(128);
@@ -1364,11 +1381,11 @@ void launch_dual_linesearch(const Problem &P, DualCtl *ctl, const int32_t *list,
 
 void launch_dual_control(const Problem &P, DualCtl *ctl, DualSum *sum, const int32_t *list, int n,
                          int max_iterations, double gtol, const double *acc, const double *amax, const double *dots,
-                         cudaStream_t st)
+                         cudaStream_t st, const int *cnt)
 {
     if (n <= 0) return;
     k_dual_control<<<n, 32, 0, st>>>(ctl, sum, list, P.m, max_iterations, gtol, P.lambda_J, P.lambda_h, acc, amax,
-                                     dots);
+                                     dots, cnt);
 }
 
 void launch_dual_check_apply(DualCtl *ctl, DualSum *sum, const int32_t *list, int n, double gtol, const double *acc,

@@ -403,6 +403,7 @@ struct KdArgs {
     double inv_qscale;
     float2 *KR;                  // K rho / qscale in double-float
     int *err;
+    const int *ncount;           // list length in device memory (the grid covers the most slots), or null
 };
 
 __global__ void __launch_bounds__(THREADS, 1)
@@ -425,6 +426,8 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m_tile = blockIdx.x, n_tile = blockIdx.y;
     const int nkt = args.kt_total;
+    const int nlist = args.ncount ? *args.ncount : args.nlist;
+    if (n_tile * KD_S >= nlist) return;   // (the whole CTA, before any barrier or TMEM allocation)
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < KD_STG; ++s) {
@@ -521,7 +524,7 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
 #pragma unroll
             for (int s = 0; s < KD_S; ++s) {
                 const int P = n_tile * KD_S + s;
-                if (P >= args.nlist || row >= args.Nx) continue;
+                if (P >= nlist || row >= args.Nx) continue;
                 const int b = args.list[P];
                 float2 val[4] = {df_zero(), df_zero(), df_zero(), df_zero()};
                 if (row < args.N) {
@@ -566,8 +569,9 @@ __global__ void k_kdig_split_k(const int32_t *__restrict__ K, int64_t Nx, int nk
 // rho_q of list position P (slot list[P]), its first three columns -> four
 // fp16 planes of balanced base-128 digits, rows P*3+c
 __global__ void k_kdig_split_r(const int32_t *__restrict__ list, int64_t Nx, int nr_rows,
-                               const int4 *__restrict__ rq, __half *__restrict__ Rd)
+                               const int4 *__restrict__ rq, __half *__restrict__ Rd, const int *__restrict__ cnt)
 {
+    if (cnt && (int)blockIdx.y >= *cnt) return;
     const int P = blockIdx.y, b = list[P];
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < Nx; j += (int64_t)gridDim.x * blockDim.x) {
         const int4 q = rq[(int64_t)b * Nx + j];
@@ -813,12 +817,12 @@ void tc_kdig_fill_k(const KdPlan *pl, const Problem &P, const int32_t *K, __half
 
 cudaError_t tc_launch_kdig(const KdPlan *pl, const Problem &P, const int32_t *list, int n, const int32_t *rq,
                            const uint8_t *rstate, const long long *csum, double inv_qscale, __half *Rd, float2 *KR,
-                           int *err, cudaStream_t st)
+                           int *err, cudaStream_t st, const int *cnt)
 {
     if (n <= 0) return cudaSuccess;
     {
         dim3 g((unsigned)std::min<int64_t>((P.Nx + 255) / 256, 64), (unsigned)n);
-        tc::k_kdig_split_r<<<g, 256, 0, st>>>(list, P.Nx, pl->nr_rows, reinterpret_cast<const int4 *>(rq), Rd);
+        tc::k_kdig_split_r<<<g, 256, 0, st>>>(list, P.Nx, pl->nr_rows, reinterpret_cast<const int4 *>(rq), Rd, cnt);
     }
     tc::KdArgs a{};
     a.kt_total = (int)(P.Nx / tc::KD_BK);
@@ -833,6 +837,7 @@ cudaError_t tc_launch_kdig(const KdPlan *pl, const Problem &P, const int32_t *li
     a.inv_qscale = inv_qscale;
     a.KR = KR;
     a.err = err;
+    a.ncount = cnt;
     dim3 grid((unsigned)(pl->nk_rows / tc::KD_BM), (unsigned)((n + tc::KD_S - 1) / tc::KD_S));
     tc::k_kdig<<<grid, tc::THREADS, tc::KD_SMEM, st>>>(pl->mK, pl->mRh, pl->mRt, a);
     return cudaGetLastError();
