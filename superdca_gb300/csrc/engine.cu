@@ -102,6 +102,28 @@ struct ProfRec {
 
 } // namespace
 
+// Per-class timing of one replay of the dual form's iteration core: the
+// events recorded by its event nodes and, per class, the list (counts index)
+// whose length gives the units.
+struct GraphRec {
+    int cls, kernels, cidx;
+    cudaEvent_t a, b;
+};
+
+// The round's list lengths, in the order they follow the lists in device
+// memory: searching slots, gradient pass, K rho pass (gradient pass and
+// learned starts), learned starts
+enum { DC_T = 0, DC_G = 1, DC_GW = 2, DC_W = 3, DC_N = 4 };
+
+struct DualGraph {
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev_round = nullptr;     // recorded after the summary copy (the host waits on it)
+    std::vector<cudaEvent_t> ev;        // timing events of the event nodes
+    std::vector<GraphRec> recs;
+    bool pending = false;               // replayed, its timings not collected yet
+    int64_t counts[DC_N] = {};          // the list lengths of that replay
+};
+
 struct sdca_handle {
     sdca_config cfg{};
     std::string err;
@@ -159,8 +181,13 @@ struct sdca_handle {
     DualCtl *ctl = nullptr;        // per-slot solver state, owned by the device while a slot iterates
     DualSum *sum = nullptr, *sum_h = nullptr;   // per-slot summary the host reads after each round
     double *dacc = nullptr;        // direction sums for the next line search
-    int32_t *dlist = nullptr;      // the round's slot lists: [evaluations | searching | gradient pass]
+    int32_t *dlist = nullptr;      // the round's slot lists: [evaluations | searching | gradient pass + starts |
+                                   // starts], then their lengths (DualCounts)
     cudaEvent_t ev_round = nullptr;   // end of a round's control kernel
+    // the iteration core of a round as two alternating CUDA graphs (DualGraph)
+    DualGraph dgraph[2];
+    int dgraph_next = 0;
+    bool dgraph_off = false;       // SDCA_DUAL_GRAPH=0, or a capture failed: launch the kernels one by one
     std::vector<int64_t> rows_pending;   // list positions whose score rows are on their way to rows_h
     KdPlan *kd = nullptr;          // exact K rho on the tensor cores (N <= 4000), else CUDA cores
     __half *Kd = nullptr, *Rd = nullptr;
@@ -1458,6 +1485,196 @@ int dual_ws_rows(sdca_handle *h, int nW, const int32_t *l_W)
     return SDCA_OK;
 }
 
+// The iteration core of a round (dual_round has written the lists and their
+// lengths): the line search and accept of the searching slots, the K rho
+// pass over the gradient pass and the learned starts, the starts
+// themselves, the gradient, history-dot and control kernels, the summary
+// copy and the event `ev`, then the directions.  dev: every grid covers
+// Bmax slots and the kernels read the list lengths from device memory -- the
+// form captured in a CUDA graph and replayed every round, its classes timed
+// by event nodes into `g`; otherwise the grids are the host's list lengths
+// and the classes are timed as usual.
+int dual_core(sdca_handle *h, const int64_t (&n)[DC_N], bool dev, cudaEvent_t ev, DualGraph *g)
+{
+    const Problem &P = h->P;
+    const int B = (int)P.Bmax;
+    const double gtol = h->cfg.gradient_threshold;
+    const int32_t *l_T = h->dlist + B, *l_G = h->dlist + 2 * B, *l_W = h->dlist + 3 * B;
+    const int *cnt = h->dlist + 4 * (size_t)B;
+    auto len = [&](int i) { return dev ? B : (int)n[i]; };
+    auto dcnt = [&](int i) -> const int * { return dev ? cnt + i : nullptr; };
+    // one profile class: Timed, or an event pair recorded by the graph
+    auto region = [&](int cls, int kernels, int cidx, auto &&fn) -> int {
+        if (!dev) {
+            if (n[cidx] <= 0) return SDCA_OK;
+            Timed t(h, cls, kernels, n[cidx]);
+            return fn();
+        }
+        const size_t k = 2 * g->recs.size();
+        if (k + 1 >= g->ev.size()) return fn();   // (no event pair left: untimed)
+        GraphRec r{cls, kernels, cidx, g->ev[k], g->ev[k + 1]};
+        CK(cudaEventRecord(r.a, h->stream));
+        const int rc = fn();
+        CK(cudaEventRecord(r.b, h->stream));
+        g->recs.push_back(r);
+        return rc;
+    };
+    int rc;
+    // Profile classes of this form: "forward" is K rho (a coefficient vector's
+    // logit image, as X d is in the other forms), "backward" the one-hot
+    // contractions X^T a (max-norm checks, final J), "accept" the iterate
+    // update and gradient assembly, "other" the control kernel and the
+    // learned starts.
+    if ((rc = region(SDCA_K_LINESEARCH, 1, DC_T, [&] {
+             launch_dual_linesearch(P, h->ctl, l_T, len(DC_T), h->dacc, h->dv, lbase_df(h), h->udf, h->ud, h->rstate,
+                                    h->wf, h->P0, h->R, h->acc, h->stream, dcnt(DC_T));
+             return SDCA_OK;
+         })))
+        return rc;
+    if ((rc = region(SDCA_K_ACCEPT, 1, DC_T, [&] {
+             launch_dual_accept(P, h->ctl, l_T, len(DC_T), h->dv, h->udf, lbase_df(h), h->stream, dcnt(DC_T));
+             return SDCA_OK;
+         })))
+        return rc;
+    CKL();
+    if (dev || n[DC_GW] > 0) {
+        CK(cudaMemsetAsync(h->csum, 0, sizeof(long long) * 16 * P.Bmax, h->stream));
+        CK(cudaMemsetAsync(h->amax, 0, sizeof(double) * 2 * P.Bmax, h->stream));
+        CK(cudaMemsetAsync(h->dots, 0, sizeof(double) * 4 * MAXHIST * P.Bmax, h->stream));
+    }
+    if ((rc = region(SDCA_K_ACCEPT, 1, DC_GW, [&] {
+             launch_dual_quant(P, h->sd, l_G, len(DC_GW), h->R, h->rstate, h->qscale, h->rq, h->csum, h->stream,
+                               dcnt(DC_GW));
+             return SDCA_OK;
+         })))
+        return rc;
+    if ((rc = region(SDCA_K_FORWARD, h->kd ? 2 : 1, DC_GW, [&] {
+             if (h->kd)
+                 CK(tc_launch_kdig(h->kd, P, l_G, len(DC_GW), h->rq, h->rstate, h->csum, 1.0 / h->qscale, h->Rd,
+                                   h->KR, h->tc_err, h->stream, dcnt(DC_GW)));
+             else
+                 launch_dual_kprod(P, l_G, len(DC_GW), h->rstate, h->Kmat, h->qscale, h->rq, h->csum, h->KR,
+                                   h->stream, dcnt(DC_GW));
+             return SDCA_OK;
+         })))
+        return rc;
+    if (!dev || h->ws_dual) {
+        // the learned start: a_x = -rho^ / (2 lambda_J), K a_x exactly from the pass above
+        if ((rc = region(SDCA_K_OTHER, 1, DC_W, [&] {
+                 launch_dual_ws_init(P, l_W, len(DC_W), -0.5 / P.lambda_J, h->qscale, h->rq, h->KR, h->dv,
+                                     lbase_df(h), h->stream, dcnt(DC_W));
+                 return SDCA_OK;
+             })))
+            return rc;
+    }
+    if ((rc = region(SDCA_K_ACCEPT, 1, DC_G, [&] {
+             launch_dual_grad(P, h->ctl, l_G, len(DC_G), h->qscale, h->rq, h->KR, h->dv, h->acc, h->amax, h->stream,
+                              dcnt(DC_G));
+             return SDCA_OK;
+         })))
+        return rc;
+    if ((rc = region(SDCA_K_HISTORY, 1, DC_G, [&] {
+             launch_dual_dots(P, h->ctl, l_G, len(DC_G), 1, h->dv, h->dots, h->stream, dcnt(DC_G));
+             return SDCA_OK;
+         })))
+        return rc;
+    if ((rc = region(SDCA_K_OTHER, 1, DC_G, [&] {
+             launch_dual_control(P, h->ctl, h->sum, l_G, len(DC_G), h->cfg.max_iterations, gtol, h->acc, h->amax,
+                                 h->dots, h->stream, dcnt(DC_G));
+             return SDCA_OK;
+         })))
+        return rc;
+    CKL();
+    CK(cudaMemcpyAsync(h->sum_h, h->sum, sizeof(DualSum) * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(h->acc_h, h->acc, sizeof(double) * NACC * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
+    if (h->tc_err) CK(cudaMemcpyAsync(h->flag_h + 1, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    if (h->ws_err && (dev ? h->ws_dual : n[DC_W] > 0))
+        CK(cudaMemcpyAsync(h->flag_h + 2, h->ws_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaEventRecord(ev, h->stream));
+    if (dev || n[DC_G] > 0) CK(cudaMemsetAsync(h->dacc, 0, sizeof(double) * NDACC * P.Bmax, h->stream));
+    if ((rc = region(SDCA_K_DIRECTION, 1, DC_G, [&] {
+             launch_dual_direction(P, h->ctl, l_G, len(DC_G), h->dv, lbase_df(h), h->P0, h->wf, h->rstate, h->udf,
+                                   h->ud, h->dacc, h->stream, dcnt(DC_G));
+             return SDCA_OK;
+         })))
+        return rc;
+    CKL();
+    return SDCA_OK;
+}
+
+// Capture the iteration core into g's CUDA graph (on the lane's stream, in
+// this thread's capture mode) and instantiate it.
+int dual_graph_build(sdca_handle *h, DualGraph &g)
+{
+    if (!g.ev_round) CK(cudaEventCreateWithFlags(&g.ev_round, cudaEventDisableTiming));
+    while (g.ev.size() < 24) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        g.ev.push_back(e);
+    }
+    g.recs.clear();
+    const int64_t any[DC_N] = {1, 1, 1, 1};
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = dual_core(h, any, true, g.ev_round, &g);
+    const cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+    if (rc || e != cudaSuccess || !graph) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        g.recs.clear();
+        return rc ? rc : SDCA_E_CUDA;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+        g.exec = nullptr;
+        cudaGetLastError();
+        return SDCA_E_CUDA;
+    }
+    return SDCA_OK;
+}
+
+// A completed replay's class timings into the profile (units: the list
+// lengths of that replay).
+void dual_graph_collect(sdca_handle *h, DualGraph &g)
+{
+    if (!g.pending) return;
+    for (const GraphRec &r : g.recs) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            h->prof.kernel_ms[r.cls] += ms;
+            h->prof.kernel_launches[r.cls] += r.kernels;
+            h->prof.kernel_units[r.cls] += g.counts[r.cidx];
+        }
+        h->prof.gpu_launches += r.kernels;
+    }
+    g.pending = false;
+}
+
+// Drop the lane's graphs (the alignment, the targets or the learned start
+// changed, or the handle ends); they are captured again at the next round.
+void dual_graph_reset(sdca_handle *h)
+{
+    for (DualGraph &g : h->dgraph) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        g.recs.clear();
+        g.pending = false;
+    }
+    h->dgraph_next = 0;
+}
+
+void dual_graph_free(sdca_handle *h)
+{
+    dual_graph_reset(h);
+    for (DualGraph &g : h->dgraph) {
+        for (cudaEvent_t e : g.ev) cudaEventDestroy(e);
+        g.ev.clear();
+        if (g.ev_round) cudaEventDestroy(g.ev_round);
+        g.ev_round = nullptr;
+    }
+}
+
 // One round: start/final evaluations, line searches, accepts, the gradient
 // pass and the control kernel for every slot, then the directions.
 int dual_round(sdca_handle *h, Queue &Qu)
@@ -1475,15 +1692,18 @@ int dual_round(sdca_handle *h, Queue &Qu)
     for (int b : ef)
         if (h->slots[b].phase == PH_INIT) G.push_back(b);
     if (ef.empty() && G.empty() && W.empty()) return dual_convert(h, true);
-    // the lists: [ef | T | G, W] in one upload (the K rho pass takes G and W)
-    const int32_t *l_ef = h->dlist, *l_T = h->dlist + P.Bmax, *l_G = h->dlist + 2 * P.Bmax;
-    const int32_t *l_W = l_G + G.size();
+    // the lists [ef | T | G, W | W] and their lengths in one upload
+    const int32_t *l_ef = h->dlist, *l_W = h->dlist + 3 * P.Bmax;
+    const int64_t counts[DC_N] = {(int64_t)T.size(), (int64_t)G.size(), (int64_t)(G.size() + W.size()),
+                                  (int64_t)W.size()};
     {
-        std::vector<int32_t> all(3 * (size_t)P.Bmax, 0);
+        std::vector<int32_t> all(4 * (size_t)P.Bmax + DC_N, 0);
         std::copy(ef.begin(), ef.end(), all.begin());
         std::copy(T.begin(), T.end(), all.begin() + P.Bmax);
         std::copy(G.begin(), G.end(), all.begin() + 2 * P.Bmax);
         std::copy(W.begin(), W.end(), all.begin() + 2 * P.Bmax + G.size());
+        std::copy(W.begin(), W.end(), all.begin() + 3 * P.Bmax);
+        for (int i = 0; i < DC_N; ++i) all[4 * (size_t)P.Bmax + i] = (int32_t)counts[i];
         for (int b : W) h->sd_h[b].locus = h->scan ? -1 : h->slots[b].locus;
         for (int b : ef) {
             h->sd_h[b].locus = h->scan ? -1 : h->slots[b].locus;
@@ -1503,73 +1723,29 @@ int dual_round(sdca_handle *h, Queue &Qu)
         launch_trial_dual(P, h->sd, l_ef, (int)ef.size(), lbase_df(h), h->udf, h->rstate, h->w, h->R, h->acc,
                           h->stream);
     }
-    if (!T.empty()) {
-        {
-            Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)T.size());
-            launch_dual_linesearch(P, h->ctl, l_T, (int)T.size(), h->dacc, h->dv, lbase_df(h), h->udf, h->ud,
-                                   h->rstate, h->wf, h->P0, h->R, h->acc, h->stream);
-        }
-        Timed t(h, SDCA_K_ACCEPT, 1, (int64_t)T.size());
-        launch_dual_accept(P, h->ctl, l_T, (int)T.size(), h->dv, h->udf, lbase_df(h), h->stream);
-    }
     CKL();
-    const int nG = (int)G.size(), nGW = nG + (int)W.size();
-    if (nGW > 0) {
-        CK(cudaMemsetAsync(h->csum, 0, sizeof(long long) * 16 * P.Bmax, h->stream));
-        CK(cudaMemsetAsync(h->amax, 0, sizeof(double) * 2 * P.Bmax, h->stream));
-        CK(cudaMemsetAsync(h->dots, 0, sizeof(double) * 4 * MAXHIST * P.Bmax, h->stream));
-        // Profile classes of this form: "forward" is K rho (a coefficient
-        // vector's logit image, as X d is in the other forms), "backward" the
-        // one-hot contractions X^T a (max-norm checks, final J), "accept" the
-        // iterate update and gradient assembly, "other" the control kernel.
-        {
-            Timed t(h, SDCA_K_ACCEPT, 1, nGW);
-            launch_dual_quant(P, h->sd, l_G, nGW, h->R, h->rstate, h->qscale, h->rq, h->csum, h->stream);
+    // the iteration core: a replay of this lane's CUDA graph, or the kernels one by one
+    cudaEvent_t ev_sum = h->ev_round;
+    DualGraph *other = nullptr;
+    if (!h->dgraph_off) {
+        DualGraph &g = h->dgraph[h->dgraph_next];
+        if (!g.exec && dual_graph_build(h, g) != SDCA_OK) {
+            h->dgraph_off = true;   // fall back to the direct launches for the rest of the handle's life
+            cudaGetLastError();
         }
-        {
-            Timed t(h, SDCA_K_FORWARD, h->kd ? 2 : 1, nGW);
-            if (h->kd)
-                CK(tc_launch_kdig(h->kd, P, l_G, nGW, h->rq, h->rstate, h->csum, 1.0 / h->qscale, h->Rd, h->KR,
-                                  h->tc_err, h->stream));
-            else
-                launch_dual_kprod(P, l_G, nGW, h->rstate, h->Kmat, h->qscale, h->rq, h->csum, h->KR, h->stream);
-        }
-        if (!W.empty()) {
-            // the learned start: a_x = -rho^ / (2 lambda_J), K a_x exactly from the pass above
-            Timed t(h, SDCA_K_OTHER, 1, (int64_t)W.size());
-            launch_dual_ws_init(P, l_W, (int)W.size(), -0.5 / P.lambda_J, h->qscale, h->rq, h->KR, h->dv, lbase_df(h),
-                                h->stream);
+        if (!h->dgraph_off) {
+            CK(cudaGraphLaunch(g.exec, h->stream));
+            std::copy(counts, counts + DC_N, g.counts);
+            g.pending = true;
+            ev_sum = g.ev_round;
+            other = &h->dgraph[1 - h->dgraph_next];
+            h->dgraph_next = 1 - h->dgraph_next;
         }
     }
-    if (nG > 0) {
-        {
-            Timed t(h, SDCA_K_ACCEPT, 1, nG);
-            launch_dual_grad(P, h->ctl, l_G, nG, h->qscale, h->rq, h->KR, h->dv, h->acc, h->amax, h->stream);
-        }
-        {
-            Timed t(h, SDCA_K_HISTORY, 1, nG);
-            launch_dual_dots(P, h->ctl, l_G, nG, 1, h->dv, h->dots, h->stream);
-        }
-        {
-            Timed t(h, SDCA_K_OTHER, 1, nG);
-            launch_dual_control(P, h->ctl, h->sum, l_G, nG, h->cfg.max_iterations, gtol, h->acc, h->amax, h->dots,
-                                h->stream);
-        }
-        CKL();
-    }
-    CK(cudaMemcpyAsync(h->sum_h, h->sum, sizeof(DualSum) * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(h->acc_h, h->acc, sizeof(double) * NACC * P.Bmax, cudaMemcpyDeviceToHost, h->stream));
-    if (h->tc_err) CK(cudaMemcpyAsync(h->flag_h + 1, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    if (!W.empty()) CK(cudaMemcpyAsync(h->flag_h + 2, h->ws_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaEventRecord(h->ev_round, h->stream));
-    if (nG > 0) {
-        CK(cudaMemsetAsync(h->dacc, 0, sizeof(double) * NDACC * P.Bmax, h->stream));
-        Timed t(h, SDCA_K_DIRECTION, 1, nG);
-        launch_dual_direction(P, h->ctl, l_G, nG, h->dv, lbase_df(h), h->P0, h->wf, h->rstate, h->udf, h->ud,
-                              h->dacc, h->stream);
-    }
-    CKL();
-    CK(cudaEventSynchronize(h->ev_round));
+    if (h->dgraph_off && (rc = dual_core(h, counts, false, h->ev_round, nullptr))) return rc;
+    CK(cudaEventSynchronize(ev_sum));
+    // the previous round's replay has completed: its timings can be read
+    if (other) dual_graph_collect(h, *other);
     // every staged host-to-device copy was queued before the event
     h->stage_off = 0;
     if (h->tc_err && h->flag_h[1])
@@ -1668,6 +1844,7 @@ int solve_lane(sdca_handle *h, Queue &Qu, cudaEvent_t t0_common)
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, t0, t1));
     h->prof.solve_ms = ms;
+    for (DualGraph &g : h->dgraph) dual_graph_collect(h, g);
     prof_collect(h);
     return SDCA_OK;
 }
@@ -1942,7 +2119,7 @@ static int create_lane(const sdca_config *cfg, const sdca_handle *owner, sdca_ha
         (rc = halloc(h, &h->stage, (h->stage_cap = 64 * (((sizeof(SlotDev) + 4) * B + 1024 + 255) & ~(size_t)255)))) ||
         (dual && ((rc = halloc(h, &h->amax_h, 2 * B)) || (rc = halloc(h, &h->sum_h, B)) ||
                   (rc = dalloc(h, &h->ctl, B)) || (rc = dalloc(h, &h->sum, B)) ||
-                  (rc = dalloc(h, &h->dacc, B * NDACC)) || (rc = dalloc(h, &h->dlist, 3 * B)) ||
+                  (rc = dalloc(h, &h->dacc, B * NDACC)) || (rc = dalloc(h, &h->dlist, 4 * B + DC_N)) ||
                   (rc = dalloc(h, &h->dv, B * NV * 2 * P.Nx * 4)) || (rc = dalloc(h, &h->udf, B * P.Nx * 4)) ||
                   (rc = dalloc(h, &h->KR, B * P.Nx * 4)) || (rc = dalloc(h, &h->amax, 2 * B)) ||
                   (rc = dalloc(h, &h->rq, B * P.Nx * 4)) || (rc = dalloc(h, &h->csum, 16 * B)) ||
@@ -1969,6 +2146,11 @@ static int create_lane(const sdca_config *cfg, const sdca_handle *owner, sdca_ha
         if (h->own_stream) cudaStreamDestroy(h->stream);
         delete h;
         return fail(nullptr, SDCA_E_CUDA, "initialisation failed");
+    }
+    {
+        // the dual form replays its iteration core as a CUDA graph unless SDCA_DUAL_GRAPH=0
+        const char *e = std::getenv("SDCA_DUAL_GRAPH");
+        h->dgraph_off = !dual || (e && e[0] == '0');
     }
     if (tcres) {
         int major = 0, minor = 0;
@@ -1998,7 +2180,9 @@ int sdca_set_alignment(sdca_handle *h, const uint8_t *states, const double *weig
     if (!h) return SDCA_E_ARG;
     h->knn_k = 0;
     h->scan = false;
+    dual_graph_reset(h);
     for (sdca_handle *s : h->sub) {
+        dual_graph_reset(s);
         s->has_alignment = false;
         s->knn_k = 0;
         s->scan = false;
@@ -2283,6 +2467,8 @@ int sdca_set_targets(sdca_handle *h, const uint8_t *targets, int64_t n_target_lo
 {
     if (!h) return SDCA_E_ARG;
     if (!h->has_alignment) return fail(h, SDCA_E_STATE, "sdca_set_alignment must come first");
+    dual_graph_reset(h);
+    for (sdca_handle *s : h->sub) dual_graph_reset(s);
     if (h->TT) {
         cudaFree(h->TT);
         h->TT = nullptr;
@@ -2337,6 +2523,8 @@ int sdca_set_targets(sdca_handle *h, const uint8_t *targets, int64_t n_target_lo
 int sdca_set_warm_start(sdca_handle *h, const float *params, size_t n_params)
 {
     if (!h) return SDCA_E_ARG;
+    dual_graph_reset(h);   // the dual form's graph holds the learned start's kernels or not
+    for (sdca_handle *s : h->sub) dual_graph_reset(s);
     if (!params) {
         h->ws_on = false;
         h->ws_dual = false;
@@ -2452,6 +2640,7 @@ int sdca_destroy(sdca_handle *h)
     if (h->ev_lanes) cudaEventDestroy(h->ev_lanes);
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->ev_round) cudaEventDestroy(h->ev_round);
+    dual_graph_free(h);
     for (auto e : h->ev_pool) cudaEventDestroy(e);
     if (h->tc) tc_plan_destroy(h->tc);
     if (h->kd) tc_kdig_plan_destroy(h->kd);
