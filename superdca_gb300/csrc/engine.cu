@@ -1513,9 +1513,10 @@ int dual_core(sdca_handle *h, const int64_t (&n)[DC_N], bool dev, cudaEvent_t ev
         const size_t k = 2 * g->recs.size();
         if (k + 1 >= g->ev.size()) return fn();   // (no event pair left: untimed)
         GraphRec r{cls, kernels, cidx, g->ev[k], g->ev[k + 1]};
-        CK(cudaEventRecord(r.a, h->stream));
+        // (external: event nodes that record the event at every replay)
+        CK(cudaEventRecordWithFlags(r.a, h->stream, cudaEventRecordExternal));
         const int rc = fn();
-        CK(cudaEventRecord(r.b, h->stream));
+        CK(cudaEventRecordWithFlags(r.b, h->stream, cudaEventRecordExternal));
         g->recs.push_back(r);
         return rc;
     };
@@ -1590,7 +1591,8 @@ int dual_core(sdca_handle *h, const int64_t (&n)[DC_N], bool dev, cudaEvent_t ev
     if (h->tc_err) CK(cudaMemcpyAsync(h->flag_h + 1, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     if (h->ws_err && (dev ? h->ws_dual : n[DC_W] > 0))
         CK(cudaMemcpyAsync(h->flag_h + 2, h->ws_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaEventRecord(ev, h->stream));
+    if (dev) CK(cudaEventRecordWithFlags(ev, h->stream, cudaEventRecordExternal));
+    else CK(cudaEventRecord(ev, h->stream));
     if (dev || n[DC_G] > 0) CK(cudaMemsetAsync(h->dacc, 0, sizeof(double) * NDACC * P.Bmax, h->stream));
     if ((rc = region(SDCA_K_DIRECTION, 1, DC_G, [&] {
              launch_dual_direction(P, h->ctl, l_G, len(DC_G), h->dv, lbase_df(h), h->P0, h->wf, h->rstate, h->udf,
