@@ -77,6 +77,8 @@ const char *USAGE =
     "                                     (default: autotuned; 4 dual, 1 otherwise without it).\n"
     "  --gpu-no-autotune                  Do not measure batch and lanes on the first loci.\n"
     "  --gpu-tune-cache arg               File that keeps the autotuner's choice per shape.\n"
+    "  --gpu-warm-start arg               Learned start: a parameter blob (.npy of float32, or raw\n"
+    "                                     float32), per-sequence for the dual form, per-pair otherwise.\n"
     "  --gpu-history arg (=fp32)          L-BFGS history storage: fp32 or bf16.\n"
     "  --gpu-chunk arg (=4096)            Loci per solve call (bounds host memory).\n"
     "  --gpu-top-k arg (=0)               Write only the K strongest pairs, strongest first.\n"
@@ -101,13 +103,49 @@ struct Options {
     bool history_bf16 = false, binary_output = false;
     long chunk = 4096, top_k = 0;
     bool no_autotune = false;
-    std::string tune_cache;
+    std::string tune_cache, warm_start;
 };
 
 [[noreturn]] void fail(const std::string &msg)
 {
     std::cerr << "superdca-gb300 error: " << msg << "\n";
     std::exit(EXIT_FAILURE);
+}
+
+// A learned-start parameter blob: a NumPy .npy file of little-endian float32
+// (format versions 1-3, C order), or raw float32 values.
+std::vector<float> read_blob(const std::string &path)
+{
+    std::FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f) fail("cannot open \"" + path + "\"");
+    std::vector<unsigned char> bytes;
+    unsigned char buf[1 << 16];
+    size_t got;
+    while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0) bytes.insert(bytes.end(), buf, buf + got);
+    std::fclose(f);
+    size_t off = 0;
+    if (bytes.size() >= 10 && std::memcmp(bytes.data(), "\x93NUMPY", 6) == 0) {
+        const int major = bytes[6];
+        size_t hlen = 0, hoff = 0;
+        if (major == 1) {
+            hlen = (size_t)bytes[8] | ((size_t)bytes[9] << 8);
+            hoff = 10;
+        } else if ((major == 2 || major == 3) && bytes.size() >= 12) {
+            hlen = (size_t)bytes[8] | ((size_t)bytes[9] << 8) | ((size_t)bytes[10] << 16) | ((size_t)bytes[11] << 24);
+            hoff = 12;
+        } else {
+            fail("\"" + path + "\": unknown .npy format version");
+        }
+        if (hoff + hlen > bytes.size()) fail("\"" + path + "\": truncated .npy header");
+        const std::string header(bytes.begin() + (long)hoff, bytes.begin() + (long)(hoff + hlen));
+        if (header.find("'<f4'") == std::string::npos || header.find("'fortran_order': False") == std::string::npos)
+            fail("\"" + path + "\": expected a C-ordered little-endian float32 array");
+        off = hoff + hlen;
+    }
+    if ((bytes.size() - off) % 4 != 0) fail("\"" + path + "\": size is not a whole number of float32 values");
+    std::vector<float> v((bytes.size() - off) / 4);
+    std::memcpy(v.data(), bytes.data() + off, v.size() * 4);
+    return v;
 }
 
 template <typename T> T parse_number(const std::string &opt, const std::string &v)
@@ -194,6 +232,7 @@ Options parse_options(int argc, char **argv)
         else if (name == "gpu-batch") o.batch = parse_number<int>(opt, value);
         else if (name == "gpu-lanes") o.lanes = parse_number<int>(opt, value);
         else if (name == "gpu-tune-cache") o.tune_cache = value;
+        else if (name == "gpu-warm-start") o.warm_start = value;
         else if (name == "gpu-chunk") o.chunk = parse_number<long>(opt, value);
         else if (name == "gpu-top-k") o.top_k = parse_number<long>(opt, value);
         else if (name == "gpu-form") {
@@ -773,6 +812,11 @@ int main(int argc, char **argv)
 
     check(sdca_set_alignment(H.h, states.data(), weights.data()), H.h, "alignment upload failed");
     if (scan) check(sdca_set_targets(H.h, states1.data(), L1), H.h, "target upload failed");
+    std::vector<float> blob;
+    if (!o.warm_start.empty()) {
+        blob = read_blob(o.warm_start);
+        check(sdca_set_warm_start(H.h, blob.data(), blob.size()), H.h, "learned start rejected");
+    }
     if (o.verbose) {
         double lh, lJ, beff;
         sdca_get_lambdas(H.h, &lh, &lJ, &beff);
@@ -835,8 +879,10 @@ int main(int argc, char **argv)
     // Without --gpu-batch / --gpu-lanes the first loci (at most a quarter of
     // the list, and at most 4 GB of score rows) are solved with candidate
     // configurations in turn, and the rest with the fastest.  Norm-of-mean
-    // scoring needs every solution, which the probes do not return.
-    if (!o.no_autotune && o.batch <= 0 && o.lanes <= 0 && !o.norm_of_mean) {
+    // scoring needs every solution, which the probes do not return; in the
+    // scan mode the loci index the second alignment, which the probes do not
+    // hold.
+    if (!o.no_autotune && o.batch <= 0 && o.lanes <= 0 && !o.norm_of_mean && !scan) {
         const size_t prefix = std::min(n / 4, (size_t)((1ull << 30) / (uint64_t)L));
         rows.resize(prefix * (size_t)L);
         stats.resize(std::max<size_t>(prefix, 1));
@@ -866,6 +912,8 @@ int main(int argc, char **argv)
             cfg = best;
             check(sdca_create(&cfg, &H.h), nullptr, "engine set-up failed");
             check(sdca_set_alignment(H.h, states.data(), weights.data()), H.h, "alignment upload failed");
+            if (!blob.empty())
+                check(sdca_set_warm_start(H.h, blob.data(), blob.size()), H.h, "learned start rejected");
         }
         start = done;
     }

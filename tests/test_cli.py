@@ -164,6 +164,30 @@ def test_gpu_cli_couplings_match_oracle(cli, tmp_path, oracle_mod):
     np.testing.assert_allclose(vals, [v for v, _, _ in want], rtol=0, atol=1e-4)
 
 
+@pytest.mark.gpu
+def test_gpu_cli_warm_start_same_couplings(cli, tmp_path):
+    """--gpu-warm-start with the committed per-sequence blob: the optimum of
+    each locus is unique, so the coupling file matches the zero-start run's
+    (same lines and order, values within 1e-4)."""
+    import shutil
+    nuc, _ = synthetic.independent(N=200, L=300, seed=8)
+    A.write_fasta(str(tmp_path / "a.fasta"), nuc, width=60)
+    shutil.copy(tmp_path / "a.fasta", tmp_path / "b.fasta")
+    blob = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "superdca_gb300",
+                        "warmstart_dual_tree-3000x94000.npy")
+    r0 = run(cli, ["--gpu-batch", "32", "a.fasta"], tmp_path)
+    r1 = run(cli, ["--gpu-batch", "32", "--gpu-warm-start", blob, "b.fasta"], tmp_path)
+    assert r0.returncode == 0 and r1.returncode == 0, r0.stderr + r1.stderr
+    z = (tmp_path / "a.SuperDCA_couplings.1-based.all").read_text().splitlines()
+    w = (tmp_path / "b.SuperDCA_couplings.1-based.all").read_text().splitlines()
+    assert len(z) == len(w) == 300 * 299 // 2
+    assert [l.split()[1:] for l in z] == [l.split()[1:] for l in w]
+    np.testing.assert_allclose([float(l.split()[0]) for l in w], [float(l.split()[0]) for l in z], rtol=0, atol=1e-4)
+    (tmp_path / "bad.bin").write_bytes(b"\x00" * 12)
+    r2 = run(cli, ["--gpu-batch", "32", "--gpu-warm-start", "bad.bin", "a.fasta"], tmp_path)
+    assert r2.returncode == 1 and "learned start rejected" in r2.stderr
+
+
 def _gauge(M):
     """SuperDCA's ising_gauge as it evaluates (row means spread along columns),
     in single precision."""

@@ -122,3 +122,32 @@ def test_skewed_workload_subset(oracle_mod, form):
     for k in range(3):
         g = P.objective(int(loci[k]), res.x[k])[1]
         assert np.abs(g).max() < 1.05e-3
+
+
+def test_dual_graph_rounds_match_direct_launches():
+    """Each round's iteration core replayed as a CUDA graph (the default)
+    against the same kernels launched one by one (SDCA_DUAL_GRAPH=0): the same
+    optimum per locus and the same statuses, with slots refilled; and the
+    graph's class timings are collected."""
+    import os
+    from superdca_gb300 import _lib, synthetic
+    from superdca_gb300.engine import Engine
+    states, _, _ = synthetic.workload("tree-3000x10000", seed=5, N=400, L=900)
+    n, L = states.shape
+    loci = np.random.default_rng(2).choice(L, 40, replace=False)
+    out = {}
+    for mode in ("1", "0"):
+        os.environ["SDCA_DUAL_GRAPH"] = mode
+        try:
+            with Engine(n, L, form=_lib.FORM_DUAL, batch=12, lanes=2) as E:
+                E.set_alignment(states, np.ones(n))
+                out[mode] = (E.solve(loci), E.profile())
+        finally:
+            os.environ.pop("SDCA_DUAL_GRAPH", None)
+    (rg, pg), (rd, pd) = out["1"], out["0"]
+    assert np.all(rg.status == 0) and np.all(rd.status == 0)
+    np.testing.assert_allclose(rg.f, rd.f, rtol=1e-9)
+    np.testing.assert_allclose(rg.scores, rd.scores, atol=1e-5, equal_nan=True)
+    assert abs(rg.iterations.mean() - rd.iterations.mean()) <= 0.05 * rd.iterations.mean()
+    for cls in ("forward", "direction", "history", "linesearch"):
+        assert pg["kernel_ms"][cls] > 0 and pg["kernel_units"][cls] > 0
