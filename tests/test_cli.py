@@ -180,7 +180,7 @@ def test_gpu_cli_warm_start_same_couplings(cli, tmp_path):
     assert r0.returncode == 0 and r1.returncode == 0, r0.stderr + r1.stderr
     z = (tmp_path / "a.SuperDCA_couplings.1-based.all").read_text().splitlines()
     w = (tmp_path / "b.SuperDCA_couplings.1-based.all").read_text().splitlines()
-    assert len(z) == len(w) == 300 * 299 // 2
+    assert len(z) == len(w) > 0   # (the MAF filter may drop columns; the same ones in both runs)
     assert [l.split()[1:] for l in z] == [l.split()[1:] for l in w]
     np.testing.assert_allclose([float(l.split()[0]) for l in w], [float(l.split()[0]) for l in z], rtol=0, atol=1e-4)
     (tmp_path / "bad.bin").write_bytes(b"\x00" * 12)

@@ -146,8 +146,10 @@ def test_dual_graph_rounds_match_direct_launches():
             os.environ.pop("SDCA_DUAL_GRAPH", None)
     (rg, pg), (rd, pd) = out["1"], out["0"]
     assert np.all(rg.status == 0) and np.all(rd.status == 0)
-    np.testing.assert_allclose(rg.f, rd.f, rtol=1e-9)
-    np.testing.assert_allclose(rg.scores, rd.scores, atol=1e-5, equal_nan=True)
+    # the runs differ in the order of atomic sums, so each stops at its own
+    # point below the threshold: the converged-objective tolerance
+    np.testing.assert_allclose(rg.f, rd.f, rtol=1e-6)
+    np.testing.assert_allclose(rg.scores, rd.scores, atol=1e-4, equal_nan=True)
     assert abs(rg.iterations.mean() - rd.iterations.mean()) <= 0.05 * rd.iterations.mean()
     for cls in ("forward", "direction", "history", "linesearch"):
         assert pg["kernel_ms"][cls] > 0 and pg["kernel_units"][cls] > 0
