@@ -376,6 +376,7 @@ constexpr int KD_NB = KD_RDIG * KD_BN;                 // 160 accumulator column
 constexpr uint32_t IDESC_KD = (1u << 4) | ((uint32_t)(KD_NB >> 3) << 17) | ((uint32_t)(KD_BM >> 4) << 24);
 static_assert(KD_STAGE % 1024 == 0, "stage must keep 1024-byte alignment");
 static_assert(KD_HEAD_BYTES % 1024 == 0 && KD_TAIL_BYTES % 1024 == 0, "TMA destinations 1024-aligned");
+static_assert(KD_TAIL == 0 || KD_TAIL == 8, "plane tails of 8 rows (or none)");
 static_assert(KD_KDIG * KD_NB <= (int)KD_TMEM_COLS, "accumulators fit TMEM");
 static_assert(KD_NB % 16 == 0 && KD_NB <= 256, "MMA N for M = 128");
 static_assert(KD_COLS < KD_BN, "one unused row per plane");
@@ -464,8 +465,9 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
 #pragma unroll
                 for (int p = 0; p < KD_RDIG; ++p) {
                     tma_load_2d(st + BOFF + p * KD_HEAD_BYTES, &tmRh, j * KD_BK, p * args.nr_rows + r0, full(s));
-                    tma_load_2d(st + TOFF + p * KD_TAIL_BYTES, &tmRt, j * KD_BK, p * args.nr_rows + r0 + KD_HEAD,
-                                full(s));
+                    if (KD_TAIL > 0)
+                        tma_load_2d(st + TOFF + p * KD_TAIL_BYTES, &tmRt, j * KD_BK, p * args.nr_rows + r0 + KD_HEAD,
+                                    full(s));
                 }
             }
             for (int j = max(0, nkt - KD_STG); j < nkt; ++j)
@@ -513,11 +515,13 @@ k_kdig(const __grid_constant__ CUtensorMap tmK, const __grid_constant__ CUtensor
 #pragma unroll 1
                 for (int p = 0; p < KD_RDIG; ++p) {
                     const int sh = 6 * k + 7 * p;
-                    float v[32], t[8];
+                    float v[32], t[8] = {};
                     tmem_ld32(tmem_base + lanes + (uint32_t)(k * KD_NB + p * KD_HEAD), v);
-                    tmem_ld8(tmem_base + lanes + (uint32_t)(k * KD_NB + KD_RDIG * KD_HEAD + p * KD_TAIL), t);
+                    if (KD_TAIL > 0)
+                        tmem_ld8(tmem_base + lanes + (uint32_t)(k * KD_NB + KD_RDIG * KD_HEAD + p * KD_TAIL), t);
 #pragma unroll
-                    for (int c = 0; c < KD_HEAD; ++c) acc[c] += (long long)__float2int_rn(v[c]) << sh;
+                    for (int c = 0; c < (KD_HEAD < KD_COLS ? KD_HEAD : KD_COLS); ++c)
+                        acc[c] += (long long)__float2int_rn(v[c]) << sh;
 #pragma unroll
                     for (int c = KD_HEAD; c < KD_COLS; ++c) acc[c] += (long long)__float2int_rn(t[c - KD_HEAD]) << sh;
                 }
@@ -797,8 +801,9 @@ KdPlan *tc_kdig_plan_create(const Problem &P, __half *Kd, __half *Rd)
                        (uint64_t)P.Nx * 2, tc::KD_BK, tc::KD_BM, CU_TENSOR_MAP_SWIZZLE_128B);
     ok &= make_map(&p->mRh, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Rd, (uint64_t)P.Nx, (uint64_t)tc::KD_RDIG * p->nr_rows,
                    (uint64_t)P.Nx * 2, tc::KD_BK, tc::KD_HEAD, CU_TENSOR_MAP_SWIZZLE_128B);
-    ok &= make_map(&p->mRt, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Rd, (uint64_t)P.Nx, (uint64_t)tc::KD_RDIG * p->nr_rows,
-                   (uint64_t)P.Nx * 2, tc::KD_BK, tc::KD_TAIL, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (tc::KD_TAIL > 0)
+        ok &= make_map(&p->mRt, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, Rd, (uint64_t)P.Nx, (uint64_t)tc::KD_RDIG * p->nr_rows,
+                       (uint64_t)P.Nx * 2, tc::KD_BK, tc::KD_TAIL > 0 ? tc::KD_TAIL : 8, CU_TENSOR_MAP_SWIZZLE_128B);
     if (!ok) {
         delete p;
         return nullptr;
