@@ -40,3 +40,11 @@ def test_roofline_dual_picks_the_requested_class():
     # per unit: (4k + 3) + 4 vectors of 32 N bytes plus 32 N more, over 1 ms for 10 units
     per = ((4 * 10 + 3) + 2 + 1 + 1) * 32 * 3000 + 32 * 3000
     assert abs(rf["achieved"] - round(per * 10 / 1e-3 / 1e9, 1)) < 0.2
+
+
+def test_top_overlap_counts_shared_strongest_pairs():
+    a = [(float(v), 1, 2) for v in [5, 4, 3, 2, 1]]
+    b = [(float(v), 1, 2) for v in [5, 4, 0, 2, 3]]
+    assert bench.top_overlap(a, b, k=2) == 1.0          # {0, 1} in both
+    assert bench.top_overlap(a, b, k=3) == 2 / 3        # {0, 1, 2} vs {0, 1, 4}
+    assert bench.top_overlap(a, a, k=10) == 1.0         # k above the length: all pairs

@@ -7,6 +7,8 @@ Tolerances: the engine contracts in FP32 and reduces the objective in FP64.
   converged objective vs optimum  rel 1e-6
   coupling scores                 abs 1e-4
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -99,6 +101,12 @@ def test_scores_and_topk_small_workload(engine_lib, oracle_mod, cfg_small):
     sub = np.arange(0, L, 5)
     osc, _ = P.solve(sub, threads=8, gtol=1e-5)
     np.testing.assert_allclose(res.scores[sub], osc, atol=1e-4, equal_nan=True)
+    # the 10,000 strongest pairs against the oracle's (every locus solved)
+    import bench
+    oall, _ = P.solve(loci, threads=os.cpu_count() or 1, gtol=1e-5)
+    ov = bench.top_overlap(coupling_lines(res.scores, loci), coupling_lines(oall, loci))
+    print(f"\n[200 x 500] top-10k pair overlap with the oracle: {ov:.5f}")
+    assert ov >= 0.99
     # planted pairs lead the ranking
     lines = coupling_lines(res.scores, loci)
     top = sorted(lines, reverse=True)[:len(pairs)]
