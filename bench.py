@@ -32,6 +32,9 @@ per-pair learned start) or gather (plain).  A step's working set (alignment
   warm_start_effect  the first timed step's loci solved again from zero:
               loci/s and mean iterations with and without the learned start
   cpu_baseline the FP64 C oracle on this host's cores (rank 0, N=1)
+  parity_small every locus of the 200 x 500 workload solved by the engine and
+              by the FP64 oracle: objective and coupling agreement, and the
+              overlap of the 10,000 strongest pairs (rank 0, N=1)
 --impl reference times the CPU reference path (the FP64 C oracle restating
 SuperDCA's solve) on all host cores, on rank 0 only.
 """
