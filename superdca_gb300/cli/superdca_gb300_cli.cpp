@@ -15,6 +15,7 @@
 // three-allele envelope) are the ones of superdca_gb300/alignment.py, which
 // the tests hold this program to.
 #include <algorithm>
+#include <atomic>
 #include <cctype>
 #include <charconv>
 #include <cmath>
@@ -25,6 +26,7 @@
 #include <fstream>
 #include <iostream>
 #include <memory>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <sys/stat.h>
@@ -69,6 +71,8 @@ const char *USAGE =
     "  --no-coupling-output               Don't write coupling scores to file.\n"
     "GPU:\n"
     "  --gpu-device arg (=0)              CUDA device.\n"
+    "  --gpu-devices arg                  Comma-separated CUDA devices (e.g. 0,1,2,3): one engine\n"
+    "                                     per device, each solving a contiguous share of the loci.\n"
     "  --gpu-form arg (=dual)             Engine form: dual (span of the sequences), tc (tensor-core\n"
     "                                     contractions) or plain.\n"
     "  --gpu-batch arg                    Loci solved together per lane (default: autotuned;\n"
@@ -100,6 +104,7 @@ struct Options {
     double gradient_threshold = 1e-3, lambda_h = -1.0, lambda_J = -1.0;
     bool no_dca = false, no_coupling_output = false;
     int device = 0, batch = 0, lanes = 0, form = SDCA_FORM_DUAL;
+    std::vector<int> devices;       // --gpu-devices; empty: {device}
     bool history_bf16 = false, binary_output = false;
     long chunk = 4096, top_k = 0;
     bool no_autotune = false;
@@ -229,6 +234,17 @@ Options parse_options(int argc, char **argv)
         else if (name == "lambda-h") o.lambda_h = parse_number<double>(opt, value);
         else if (name == "lambda-J") o.lambda_J = parse_number<double>(opt, value);
         else if (name == "gpu-device") o.device = parse_number<int>(opt, value);
+        else if (name == "gpu-devices") {
+            o.devices.clear();
+            size_t p = 0;
+            while (p <= value.size()) {
+                const size_t q = std::min(value.find(',', p), value.size());
+                const int d = parse_number<int>(opt, value.substr(p, q - p));
+                if (d < 0) fail("--gpu-devices entries must be >= 0");
+                o.devices.push_back(d);
+                p = q + 1;
+            }
+        }
         else if (name == "gpu-batch") o.batch = parse_number<int>(opt, value);
         else if (name == "gpu-lanes") o.lanes = parse_number<int>(opt, value);
         else if (name == "gpu-tune-cache") o.tune_cache = value;
@@ -768,6 +784,7 @@ int main(int argc, char **argv)
     }
 
     const bool need_gpu = !o.no_reweighting || !o.no_dca;
+    const std::vector<int> devices = o.devices.empty() ? std::vector<int>{o.device} : o.devices;
     Handle H;
     sdca_config cfg;
     sdca_config_default(&cfg);
@@ -787,7 +804,7 @@ int main(int argc, char **argv)
         cfg.batch = o.batch > 0 ? o.batch : (dual ? 512 : 64);
         cfg.lanes = o.lanes > 0 ? o.lanes : (dual ? 4 : 1);
         cfg.flags = o.history_bf16 ? SDCA_FLAG_HISTORY_BF16 : 0;
-        cfg.device = o.device;
+        cfg.device = devices[0];
         check(sdca_create(&cfg, &H.h), nullptr, "engine set-up failed");
     }
 
@@ -810,23 +827,83 @@ int main(int argc, char **argv)
         return EXIT_SUCCESS;
     }
 
-    check(sdca_set_alignment(H.h, states.data(), weights.data()), H.h, "alignment upload failed");
-    if (scan) check(sdca_set_targets(H.h, states1.data(), L1), H.h, "target upload failed");
     std::vector<float> blob;
-    if (!o.warm_start.empty()) {
-        blob = read_blob(o.warm_start);
-        check(sdca_set_warm_start(H.h, blob.data(), blob.size()), H.h, "learned start rejected");
-    }
+    if (!o.warm_start.empty()) blob = read_blob(o.warm_start);
+    // alignment, weights, targets and learned start of one engine
+    auto prepare = [&](sdca_handle *h) {
+        check(sdca_set_alignment(h, states.data(), weights.data()), h, "alignment upload failed");
+        if (scan) check(sdca_set_targets(h, states1.data(), L1), h, "target upload failed");
+        if (!blob.empty()) check(sdca_set_warm_start(h, blob.data(), blob.size()), h, "learned start rejected");
+    };
+    prepare(H.h);
     if (o.verbose) {
         double lh, lJ, beff;
         sdca_get_lambdas(H.h, &lh, &lJ, &beff);
         std::cout << "superdca-gb300: B_eff = " << beff << ", lambda_h = " << lh << ", lambda_J = " << lJ << "\n";
     }
 
+    // One engine per further device of --gpu-devices, with the configuration
+    // of the first (after autotuning) and its own copy of the alignment.
+    std::vector<std::unique_ptr<Handle>> extra;
+    std::vector<sdca_handle *> hs;
+    auto open_devices = [&] {
+        hs.assign(1, H.h);
+        for (size_t d = 1; d < devices.size(); ++d) {
+            sdca_config c = cfg;
+            c.device = devices[d];
+            extra.push_back(std::make_unique<Handle>());
+            check(sdca_create(&c, &extra.back()->h), nullptr,
+                  ("engine set-up failed on device " + std::to_string(devices[d])).c_str());
+            prepare(extra.back()->h);
+            hs.push_back(extra.back()->h);
+        }
+        if (o.verbose && hs.size() > 1) {
+            std::cout << "superdca-gb300: " << hs.size() << " engines, on devices";
+            for (int d : devices) std::cout << ' ' << d;
+            std::cout << "\n";
+        }
+    };
+
+    // Solve loci[lo, hi) over the engines: engine d takes the d-th of
+    // hs.size() contiguous ranges and solves it in calls of at most `chunk`
+    // loci on its own host thread.  take(k0, m, rows, xs, stats) receives
+    // each solved call; the ranges are disjoint, so it may write row k0 + k
+    // of shared output without a lock.
+    const int64_t D = 16 * L + 4;
+    auto solve_sharded = [&](size_t lo, size_t hi, size_t chunk, bool want_x, const auto &take) {
+        const size_t nd = hs.size();
+        std::vector<std::string> err(nd);
+        std::vector<std::thread> pool;
+        for (size_t d = 0; d < nd; ++d)
+            pool.emplace_back([&, d] {
+                const size_t b0 = lo + (hi - lo) * d / nd, b1 = lo + (hi - lo) * (d + 1) / nd;
+                std::vector<float> rows;
+                std::vector<double> xs;
+                std::vector<sdca_locus_stat> stats;
+                for (size_t k0 = b0; k0 < b1; k0 += chunk) {
+                    const size_t m = std::min(b1 - k0, chunk);
+                    rows.resize(m * (size_t)L);
+                    stats.resize(m);
+                    if (want_x) xs.resize(m * (size_t)D);
+                    if (sdca_solve_ex(hs[d], loci.data() + k0, m, nullptr, want_x ? xs.data() : nullptr, rows.data(),
+                                      stats.data()) != SDCA_OK) {
+                        err[d] = sdca_last_error(hs[d]);
+                        return;
+                    }
+                    take(k0, m, rows.data(), xs.data(), stats.data());
+                }
+            });
+        for (auto &t : pool) t.join();
+        for (size_t d = 0; d < nd; ++d)
+            if (!err[d].empty()) fail("solve failed on device " + std::to_string(devices[d]) + ": " + err[d]);
+    };
+    std::atomic<size_t> not_converged{0};
+
     if (scan) {
         // lines "S[r][n] r n" for r over the target list and every feature
         // locus n (plmDCA.hpp:638-645, 673-680); the norm-of-mean mode prints
         // the same norm of the untransposed block
+        open_devices();
         std::FILE *f = nullptr;
         std::string path;
         if (!o.no_coupling_output) {
@@ -836,20 +913,21 @@ int main(int argc, char **argv)
             if (!f) fail("cannot open \"" + path + "\" for writing");
         }
         std::vector<float> rows;
-        std::vector<sdca_locus_stat> stats;
         std::string out;
         char tmp[64];
-        size_t not_converged = 0;
-        for (size_t k0 = 0; k0 < loci.size(); k0 += (size_t)o.chunk) {
-            const size_t m = std::min(loci.size() - k0, (size_t)o.chunk);
+        // each chunk of the target list is shared out over the engines, then
+        // written in list order
+        for (size_t c0 = 0; c0 < loci.size(); c0 += (size_t)o.chunk) {
+            const size_t m = std::min(loci.size() - c0, (size_t)o.chunk);
             rows.resize(m * (size_t)L);
-            stats.resize(m);
-            check(sdca_solve(H.h, loci.data() + k0, m, rows.data(), stats.data()), H.h, "solve failed");
-            for (size_t k = 0; k < m; ++k) {
-                not_converged += stats[k].status != 0;
-                if (!f) continue;
+            solve_sharded(c0, c0 + m, m, false,
+                          [&](size_t k0, size_t mm, const float *r, const double *, const sdca_locus_stat *st) {
+                              std::memcpy(rows.data() + (k0 - c0) * (size_t)L, r, mm * (size_t)L * sizeof(float));
+                              for (size_t k = 0; k < mm; ++k) not_converged += st[k].status != 0;
+                          });
+            for (size_t k = 0; k < m && f; ++k) {
                 out.clear();
-                const std::string rs = std::to_string(translation[loci[k0 + k]] + o.out_base);
+                const std::string rs = std::to_string(translation[loci[c0 + k]] + o.out_base);
                 for (int64_t nn = 0; nn < L; ++nn) {
                     char *p = std::to_chars(tmp, tmp + sizeof tmp, (double)rows[k * (size_t)L + nn],
                                             std::chars_format::fixed, 8).ptr;
@@ -865,27 +943,22 @@ int main(int argc, char **argv)
         return EXIT_SUCCESS;
     }
 
-    // Solve the loci list in chunks; keep the scores of the listed columns
-    // (and, for norm-of-mean scoring, their 4 x 4 blocks).
+    // Solve the loci list; keep the scores of the listed columns (and, for
+    // norm-of-mean scoring, their 4 x 4 blocks).
     const size_t n = loci.size();
-    const int64_t D = 16 * L + 4;
     std::vector<float> S(n * n), blocks;
     if (o.norm_of_mean) blocks.assign(n * n * 16, 0.f);
-    std::vector<float> rows;
-    std::vector<double> xs;
-    std::vector<sdca_locus_stat> stats;
-    size_t not_converged = 0;
     size_t start = 0;
     // Without --gpu-batch / --gpu-lanes the first loci (at most a quarter of
     // the list, and at most 4 GB of score rows) are solved with candidate
-    // configurations in turn, and the rest with the fastest.  Norm-of-mean
-    // scoring needs every solution, which the probes do not return; in the
-    // scan mode the loci index the second alignment, which the probes do not
-    // hold.
-    if (!o.no_autotune && o.batch <= 0 && o.lanes <= 0 && !o.norm_of_mean && !scan) {
+    // configurations in turn on the first device, and the rest with the
+    // fastest.  Norm-of-mean scoring needs every solution, which the probes
+    // do not return; in the scan mode the loci index the second alignment,
+    // which the probes do not hold.
+    if (!o.no_autotune && o.batch <= 0 && o.lanes <= 0 && !o.norm_of_mean) {
         const size_t prefix = std::min(n / 4, (size_t)((1ull << 30) / (uint64_t)L));
-        rows.resize(prefix * (size_t)L);
-        stats.resize(std::max<size_t>(prefix, 1));
+        std::vector<float> rows(prefix * (size_t)L);
+        std::vector<sdca_locus_stat> stats(std::max<size_t>(prefix, 1));
         sdca_config best;
         size_t done = 0;
         sdca_tune_entry ents[SDCA_TUNE_MAX_ENTRIES];
@@ -911,36 +984,34 @@ int main(int argc, char **argv)
             H.h = nullptr;
             cfg = best;
             check(sdca_create(&cfg, &H.h), nullptr, "engine set-up failed");
-            check(sdca_set_alignment(H.h, states.data(), weights.data()), H.h, "alignment upload failed");
-            if (!blob.empty())
-                check(sdca_set_warm_start(H.h, blob.data(), blob.size()), H.h, "learned start rejected");
+            prepare(H.h);
         }
         start = done;
     }
-    // solutions are D doubles per locus: keep a chunk of them under ~1 GB
+    open_devices();
+    // solutions are D doubles per locus: keep a call's worth under ~1 GB
     const size_t chunk = o.norm_of_mean ? std::max<size_t>(1, std::min<size_t>((size_t)o.chunk, (1ull << 27) / D))
                                         : (size_t)o.chunk;
-    for (size_t k0 = start; k0 < n; k0 += chunk) {
-        const size_t m = std::min(n - k0, chunk);
-        rows.resize(m * (size_t)L);
-        stats.resize(m);
-        if (o.norm_of_mean) xs.resize(m * (size_t)D);
-        check(sdca_solve_ex(H.h, loci.data() + k0, m, nullptr, o.norm_of_mean ? xs.data() : nullptr, rows.data(),
-                            stats.data()),
-              H.h, "solve failed");
-        for (size_t k = 0; k < m; ++k) {
-            for (size_t j = 0; j < n; ++j) S[(k0 + k) * n + j] = rows[k * (size_t)L + loci[j]];
-            not_converged += stats[k].status != 0;
-            if (o.norm_of_mean)
-                for (size_t j = 0; j < n; ++j) {
-                    if (loci[j] == loci[k0 + k]) continue;
-                    stored_block(xs.data() + k * D, L, loci[k0 + k], loci[j],
-                                 reinterpret_cast<float(*)[4]>(&blocks[((k0 + k) * n + j) * 16]));
-                }
-        }
-        if (o.verbose)
-            std::cout << "superdca-gb300: solved " << k0 + m << " of " << n << " loci\n" << std::flush;
-    }
+    std::mutex progress;
+    size_t solved = start;
+    solve_sharded(start, n, chunk, o.norm_of_mean,
+                  [&](size_t k0, size_t m, const float *rows, const double *xs, const sdca_locus_stat *stats) {
+                      for (size_t k = 0; k < m; ++k) {
+                          for (size_t j = 0; j < n; ++j) S[(k0 + k) * n + j] = rows[k * (size_t)L + loci[j]];
+                          not_converged += stats[k].status != 0;
+                          if (o.norm_of_mean)
+                              for (size_t j = 0; j < n; ++j) {
+                                  if (loci[j] == loci[k0 + k]) continue;
+                                  stored_block(xs + k * D, L, loci[k0 + k], loci[j],
+                                               reinterpret_cast<float(*)[4]>(&blocks[((k0 + k) * n + j) * 16]));
+                              }
+                      }
+                      if (o.verbose) {
+                          std::lock_guard<std::mutex> g(progress);
+                          solved += m;
+                          std::cout << "superdca-gb300: solved " << solved << " of " << n << " loci\n" << std::flush;
+                      }
+                  });
     if (not_converged)
         std::cerr << "superdca-gb300: " << not_converged << " loci stopped before the gradient threshold\n";
 

@@ -70,6 +70,11 @@ def test_cli_help_and_option_errors(cli, tmp_path):
     assert r.returncode == 1 and "invalid value" in r.stderr
     r = run(cli, ["missing.fasta"], tmp_path)
     assert r.returncode == 1 and "cannot open" in r.stderr
+    for bad in ("0,,1", "0,x", "", "0,"):
+        r = run(cli, ["--gpu-devices", bad, "x.fasta"], tmp_path)
+        assert r.returncode == 1 and "invalid value" in r.stderr, bad
+    r = run(cli, ["--gpu-devices", "0,-1", "x.fasta"], tmp_path)
+    assert r.returncode == 1 and "--gpu-devices entries must be >= 0" in r.stderr
     (tmp_path / "bad.fasta").write_text(">a\nACGT\n>b\nACG\n")
     r = run(cli, ["bad.fasta"], tmp_path)
     assert r.returncode == 1 and "has length 3, expected 4" in r.stderr
@@ -186,6 +191,32 @@ def test_gpu_cli_warm_start_same_couplings(cli, tmp_path):
     (tmp_path / "bad.bin").write_bytes(b"\x00" * 12)
     r2 = run(cli, ["--gpu-batch", "32", "--gpu-warm-start", "bad.bin", "a.fasta"], tmp_path)
     assert r2.returncode == 1 and "learned start rejected" in r2.stderr
+
+
+@pytest.mark.gpu
+def test_gpu_cli_devices_share_the_loci(cli, tmp_path):
+    """--gpu-devices: one engine per listed device, each solving a contiguous
+    share of the loci list on its own host thread.  Two engines on device 0
+    give the single-engine coupling file: the same lines in the same order,
+    values within 1e-4 (a slot's exact stop test waits for a few slots to
+    want one, so the iterate a locus stops at, below the gradient threshold
+    either way, depends on the loci it shares a batch with).  Small calls
+    (--gpu-chunk 13) make each engine solve several."""
+    import shutil
+    nuc, _ = synthetic.independent(N=180, L=260, seed=9)
+    A.write_fasta(str(tmp_path / "one.fasta"), nuc, width=60)
+    shutil.copy(tmp_path / "one.fasta", tmp_path / "two.fasta")
+    flags = ["--gpu-batch", "24", "--gpu-lanes", "2", "--gpu-chunk", "13"]
+    r1 = run(cli, [*flags, "one.fasta"], tmp_path)
+    r2 = run(cli, ["-v", *flags, "--gpu-devices", "0,0", "two.fasta"], tmp_path)
+    assert r1.returncode == 0 and r2.returncode == 0, r1.stderr + r2.stderr
+    assert "2 engines, on devices 0 0" in r2.stdout
+    one = (tmp_path / "one.SuperDCA_couplings.1-based.all").read_text().splitlines()
+    two = (tmp_path / "two.SuperDCA_couplings.1-based.all").read_text().splitlines()
+    assert len(one) == len(two) > 0
+    assert [l.split()[1:] for l in one] == [l.split()[1:] for l in two]
+    np.testing.assert_allclose([float(l.split()[0]) for l in two], [float(l.split()[0]) for l in one],
+                               rtol=0, atol=1e-4)
 
 
 def _gauge(M):

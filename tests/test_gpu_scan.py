@@ -91,3 +91,14 @@ def test_cli_scan_mode(oracle_mod, tmp_path):
             k += 1
             assert (int(a), int(b)) == (cA[rr] + 1, cB[nn] + 1)
             assert abs(float(v) - sc[rr, nn]) < 1e-4
+    # two engines on device 0, each taking part of every 7-target call:
+    # the same lines in the same order, values within the oracle tolerance
+    # (the stop iterate of a locus depends on its batch neighbours)
+    (tmp_path / "tgt2.fasta").write_bytes((tmp_path / "tgt.fasta").read_bytes())
+    r = subprocess.run([cli, "--gpu-devices", "0,0", "--gpu-chunk", "7", "tgt2.fasta", "feat.fasta"], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    two = (tmp_path / "tgt2_scan.SuperDCA_couplings.1-based.all").read_text().splitlines()
+    assert [l.split()[1:] for l in two] == [l.split()[1:] for l in lines]
+    np.testing.assert_allclose([float(l.split()[0]) for l in two], [float(l.split()[0]) for l in lines],
+                               rtol=0, atol=1e-4)
