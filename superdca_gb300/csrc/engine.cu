@@ -1306,7 +1306,7 @@ int phase_step(sdca_handle *h)
 
 // ---- dual form: device-driven rounds.  The L-BFGS iteration of every slot
 // runs on the device (k_dual_linesearch: restart test, More-Thuente search
-// and its trials; k_dual_accept; the gradient through K rho; k_dual_control:
+// and its trials; K rho; k_dual_grad: the accept and the gradient; k_dual_control:
 // history, tests and the next direction's coefficients; k_dual_direction).
 // The host, once per round, reads a summary of every slot (one stream
 // event, taken before the direction kernel so that the host's work overlaps
@@ -1486,9 +1486,9 @@ int dual_ws_rows(sdca_handle *h, int nW, const int32_t *l_W)
 }
 
 // The iteration core of a round (dual_round has written the lists and their
-// lengths): the line search and accept of the searching slots, the K rho
-// pass over the gradient pass and the learned starts, the starts
-// themselves, the gradient, history-dot and control kernels, the summary
+// lengths): the line search of the searching slots, the K rho pass over
+// the gradient pass and the learned starts, the starts themselves, the
+// accept and gradient, history-dot and control kernels, the summary
 // copy and the event `ev`, then the directions.  dev: every grid covers
 // Bmax slots and the kernels read the list lengths from device memory -- the
 // form captured in a CUDA graph and replayed every round, its classes timed
@@ -1532,11 +1532,6 @@ int dual_core(sdca_handle *h, const int64_t (&n)[DC_N], bool dev, cudaEvent_t ev
              return SDCA_OK;
          })))
         return rc;
-    if ((rc = region(SDCA_K_ACCEPT, 1, DC_T, [&] {
-             launch_dual_accept(P, h->ctl, l_T, len(DC_T), h->dv, h->udf, lbase_df(h), h->stream, dcnt(DC_T));
-             return SDCA_OK;
-         })))
-        return rc;
     CKL();
     if (dev || n[DC_GW] > 0) {
         CK(cudaMemsetAsync(h->csum, 0, sizeof(long long) * 16 * P.Bmax, h->stream));
@@ -1569,8 +1564,8 @@ int dual_core(sdca_handle *h, const int64_t (&n)[DC_N], bool dev, cudaEvent_t ev
             return rc;
     }
     if ((rc = region(SDCA_K_ACCEPT, 1, DC_G, [&] {
-             launch_dual_grad(P, h->ctl, l_G, len(DC_G), h->qscale, h->rq, h->KR, h->dv, h->acc, h->amax, h->stream,
-                              dcnt(DC_G));
+             launch_dual_grad(P, h->ctl, l_G, len(DC_G), h->qscale, h->rq, h->KR, h->dv, h->udf, lbase_df(h), h->acc,
+                              h->amax, h->stream, dcnt(DC_G));
              return SDCA_OK;
          })))
         return rc;

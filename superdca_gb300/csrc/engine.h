@@ -227,15 +227,16 @@ void launch_dual_quant(const Problem &P, const SlotDev *sd, const int32_t *list,
                        const uint8_t *rstate, double qscale, int32_t *rq, long long *csum, cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8_t *rstate, const int32_t *K,
                        double qscale, const int32_t *rq, const long long *csum, float2 *KR, cudaStream_t st, const int *cnt = nullptr);
+// the accept (x += stp d, s push, logits += stp u) of the slots that searched
+// this round, then the gradient at the new point (y push, sums)
 void launch_dual_grad(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, double qscale,
-                      const int32_t *rq, const float2 *KR, float2 *dv, double *acc, double *amax, cudaStream_t st, const int *cnt = nullptr);
+                      const int32_t *rq, const float2 *KR, float2 *dv, const float2 *u, float2 *lbase, double *acc,
+                      double *amax, cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_dots(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int newg, const float2 *dv,
                       double *dots, cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_direction(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
                            const float2 *lbase, float *P0, const float *w, const uint8_t *rstate, float2 *u,
                            float *ud, double *dacc, cudaStream_t st, const int *cnt = nullptr);
-void launch_dual_accept(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
-                        const float2 *u, float2 *lbase, cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_to_r(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int which,
                       const float2 *dv, float *R, cudaStream_t st);
 // the per-iteration decisions of the dual form on the device

@@ -169,38 +169,78 @@ __device__ __forceinline__ void df2_store(float2 *p, int64_t t, const float2 (&v
     reinterpret_cast<float4 *>(p)[t] = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
 }
 
-// new gradient (a, k) = (rho_q / qscale + 2 lambda_J a_x, K rho + 2 lambda_J k_x),
-// y = g_new - g_old into the history when the slot pushes a pair;
-// J-part sums: g.g, x.x, s.y, y.y, s.s; max |a_g| and max |a_x|
+// The accept of a slot that searched this round and the gradient pass at
+// its new point, in one pass over the slot's vectors (a slot entering
+// with its start point has no accept):
+//   accept: x += stp d (a and k parts), s = x_new - x_old into the history
+//   on a push, logits lbase += stp u;
+//   gradient (a, k) = (rho_q / qscale + 2 lambda_J a_x, K rho + 2 lambda_J k_x),
+//   y = g_new - g_old into the history on a push;
+//   J-part sums: g.g, x.x, s.y, y.y, s.s; max |a_g| and max |a_x|.
+// Nothing between the line search and this kernel reads x or the logits of
+// a searching slot (the residual quantiser and K rho take the search's R
+// rows), so the accept can wait until here.
 __global__ void __launch_bounds__(256)
 k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
             float2 l2, const int32_t *__restrict__ rq, float2 iq, const float2 *__restrict__ KR,
-            float2 *__restrict__ dv, double *__restrict__ acc, double *__restrict__ amax, const int *__restrict__ cnt)
+            float2 *__restrict__ dv, const float2 *__restrict__ u, float2 *__restrict__ lbase,
+            double *__restrict__ acc, double *__restrict__ amax, const int *__restrict__ cnt)
 {
     if (cnt && (int)blockIdx.y >= *cnt) return;
     const int b = list[blockIdx.y];
     const DualCtl &S = ctl[b];
     if (S.phase == DC_STOP) return;
+    const bool step = S.phase == DC_STEP;   // searched this round: accept first
     const bool push = S.push && S.ring_new >= 0;
+    const float2 sf = S.stp_df;
     const int64_t part = Nx * 4;
-    const float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = ax + part;
+    float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = ax + part;
+    const float2 *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = ad + part;
     const float2 *ago = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kgo = ago + part;
     float2 *agn = dv + dvo(b, DV_G + 1 - S.gcur, 0, NV, Nx), *kgn = agn + part;
     const int ps = push ? S.ring_new : 0;
-    const float2 *as = dv + dvo(b, DV_S + ps, 0, NV, Nx), *ks = as + part;
+    float2 *as = dv + dvo(b, DV_S + ps, 0, NV, Nx), *ks = as + part;
     float2 *ay = dv + dvo(b, DV_S + ring + ps, 0, NV, Nx), *ky = ay + part;
     const int2 *rq2 = reinterpret_cast<const int2 *>(rq + (int64_t)b * Nx * 4);
     const float2 *KRb = KR + (int64_t)b * Nx * 4;
+    const float2 *ub = u + (int64_t)b * Nx * 4;
+    float2 *lb = lbase + (int64_t)b * Nx * 4;
     float2 g2 = df_zero(), x2 = df_zero(), sy = df_zero(), yy = df_zero(), ss = df_zero();
     float mg = 0.f, mx = 0.f;
     // entry pairs (2t, 2t+1): 16-byte loads of every stream
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < Nx * 2; t += (int64_t)gridDim.x * blockDim.x) {
-        float2 a_x[2], k_x[2], kr[2], a_g[2], k_g[2];
+        float2 a_x[2], k_x[2], kr[2], a_g[2], k_g[2], a_s[2], k_s[2];
         df2_load(ax, t, a_x);
         df2_load(kx, t, k_x);
         df2_load(KRb, t, kr);
         const int2 r2 = rq2[t];
         const int rr[2] = {r2.x, r2.y};
+        if (step) {
+            float2 a_d[2], k_d[2], uu[2], l[2];
+            df2_load(ad, t, a_d);
+            df2_load(kd, t, k_d);
+            df2_load(ub, t, uu);
+            df2_load(lb, t, l);
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const float2 a1 = df_fma(sf, a_d[q], a_x[q]), k1 = df_fma(sf, k_d[q], k_x[q]);
+                a_s[q] = df_sub(a1, a_x[q]);
+                k_s[q] = df_sub(k1, k_x[q]);
+                a_x[q] = a1;
+                k_x[q] = k1;
+                l[q] = df_fma(sf, uu[q], l[q]);
+            }
+            df2_store(ax, t, a_x);
+            df2_store(kx, t, k_x);
+            df2_store(lb, t, l);
+            if (push) {
+                df2_store(as, t, a_s);
+                df2_store(ks, t, k_s);
+            }
+        } else if (push) {
+            df2_load(as, t, a_s);
+            df2_load(ks, t, k_s);
+        }
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             a_g[q] = df_fma(l2, a_x[q], df_mul(df_from_int(rr[q]), iq));
@@ -211,11 +251,9 @@ k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
             mx = fmaxf(mx, fabsf(a_x[q].x));
         }
         if (push) {
-            float2 a_o[2], k_o[2], a_s[2], k_s[2], a_y[2], k_y[2];
+            float2 a_o[2], k_o[2], a_y[2], k_y[2];
             df2_load(ago, t, a_o);
             df2_load(kgo, t, k_o);
-            df2_load(as, t, a_s);
-            df2_load(ks, t, k_s);
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
                 a_y[q] = df_sub(a_g[q], a_o[q]);
@@ -293,11 +331,20 @@ k_dual_dots(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
 // double-float logits without FP64 arithmetic: l1 = l0 + stp u in
 // double-float, each log-sum-exp shifted by its largest high part and taken
 // in FP32 (the shifted terms are O(1)), the change of w (lse(l) - l_y)
-// assembled in double-float.  Adds to fbig, dgbig and writes the residual
-// row r.
-__device__ __noinline__ void trial_big(const float2 *lb, const float2 *up, float2 stp, int y, float wi,
-                                       const float (&p0)[4], float (&r)[4], float2 &fbig, float2 &dgbig)
+// assembled in double-float.  Returns the change of w (lse - l_y), the
+// slope change and the residual row r (by value: nothing of the common path
+// has to live in memory for this rare call).
+struct BigTrial {
+    float4 r;
+    float2 df, ddg;
+};
+
+__device__ __noinline__ BigTrial trial_big(const float2 *lb, const float2 *up, float2 stp, int y, float wi,
+                                           float4 p0v)
 {
+    const float p0[4] = {p0v.x, p0v.y, p0v.z, p0v.w};
+    float r[4];
+    float2 fbig = df_zero(), dgbig = df_zero();
     float2 l0[4], l1[4], uu[4];
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
@@ -338,6 +385,11 @@ __device__ __noinline__ void trial_big(const float2 *lb, const float2 *up, float
 #pragma unroll
     for (int a = 0; a < 4; ++a)
         if (a == y) r[a] = -ro;
+    BigTrial o;
+    o.r = make_float4(r[0], r[1], r[2], r[3]);
+    o.df = fbig;
+    o.ddg = dgbig;
+    return o;
 }
 
 // A line-search trial as a change from the current point.  With p0 the base
@@ -486,55 +538,6 @@ k_dual_direction(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ li
     block_sum_df<4>(v, dacc + (int64_t)b * NDACC, idx);
 }
 
-// x += stp d (a and k parts), s = x_new - x_old into the history on a push,
-// logits lbase += stp u
-__global__ void __launch_bounds__(256)
-k_dual_accept(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int NV,
-              float2 *__restrict__ dv, const float2 *__restrict__ u, float2 *__restrict__ lbase,
-              const int *__restrict__ cnt)
-{
-    if (cnt && (int)blockIdx.y >= *cnt) return;
-    const int b = list[blockIdx.y];
-    const DualCtl &S = ctl[b];
-    if (S.phase != DC_STEP) return;
-    const bool push = S.push && S.ring_new >= 0;
-    const float2 sf = S.stp_df;
-    const int64_t part = Nx * 4;
-    float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = ax + part;
-    const float2 *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = ad + part;
-    float2 *as = dv + dvo(b, DV_S + (push ? S.ring_new : 0), 0, NV, Nx), *ks = as + part;
-    const float2 *ub = u + (int64_t)b * Nx * 4;
-    float2 *lb = lbase + (int64_t)b * Nx * 4;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < Nx * 2; t += (int64_t)gridDim.x * blockDim.x) {
-        float2 a0[2], k0[2], a_d[2], k_d[2], a1[2], k1[2], uu[2], l[2];
-        df2_load(ax, t, a0);
-        df2_load(kx, t, k0);
-        df2_load(ad, t, a_d);
-        df2_load(kd, t, k_d);
-        df2_load(ub, t, uu);
-        df2_load(lb, t, l);
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            a1[q] = df_fma(sf, a_d[q], a0[q]);
-            k1[q] = df_fma(sf, k_d[q], k0[q]);
-            l[q] = df_fma(sf, uu[q], l[q]);
-        }
-        df2_store(ax, t, a1);
-        df2_store(kx, t, k1);
-        df2_store(lb, t, l);
-        if (push) {
-            float2 sa[2], sk[2];
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                sa[q] = df_sub(a1[q], a0[q]);
-                sk[q] = df_sub(k1[q], k0[q]);
-            }
-            df2_store(as, t, sa);
-            df2_store(ks, t, sk);
-        }
-    }
-}
-
 // FP32 copy of a vector's a part (the current gradient, or x) as the R rows
 // of a tensor-core backward contraction, scaled by `scale`
 __global__ void k_dual_to_r(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int N,
@@ -680,21 +683,38 @@ __global__ void k_dual_to_wa(const SlotDev *__restrict__ sd, const int32_t *__re
 
 // ---- the per-iteration decisions on the device
 
+// What a step trial reads of one sequence: u_a - u_y, the base
+// probabilities, the state at r and the weight (constant through a search).
+struct TrialIn {
+    float4 du, p0;
+    int y;
+    float w;
+};
+
+__device__ __forceinline__ TrialIn trial_load(int64_t o, int i, const float4 *__restrict__ ud,
+                                              const uint8_t *__restrict__ rstate, const float *__restrict__ w,
+                                              const float4 *__restrict__ P0)
+{
+    TrialIn t;
+    t.du = ud[o];
+    t.p0 = P0[o];
+    t.y = rstate[o] & 3;
+    t.w = w[i];
+    return t;
+}
+
 // One sequence of a step trial as a change from the current point (the
 // derivation above): adds w dl, the slope change and the new residual row's
 // sums, and writes the row.
-__device__ __forceinline__ void trial_seq(int64_t o, int i, float2 stp, float stpf, const float2 *__restrict__ lbase,
-                                          const float2 *__restrict__ u, const float4 *__restrict__ ud,
-                                          const uint8_t *__restrict__ rstate, const float *__restrict__ w,
-                                          const float4 *__restrict__ P0, float4 *__restrict__ R, float &f, float &dg,
-                                          float (&rs)[4], float2 &fbig, float2 &dgbig)
+__device__ __forceinline__ void trial_seq(int64_t o, const TrialIn &in, float2 stp, float stpf,
+                                          const float2 *__restrict__ lbase, const float2 *__restrict__ u,
+                                          float4 *__restrict__ R, float &f, float &dg, float (&rs)[4], float2 &fbig,
+                                          float2 &dgbig)
 {
-    const float4 dv4 = ud[o];
-    const float du[4] = {dv4.x, dv4.y, dv4.z, dv4.w};   // u_a - u_y
-    const int y = rstate[o] & 3;
-    const float wi = w[i];
-    const float4 pv = P0[o];
-    const float p0[4] = {pv.x, pv.y, pv.z, pv.w};
+    const float du[4] = {in.du.x, in.du.y, in.du.z, in.du.w};   // u_a - u_y
+    const int y = in.y;
+    const float wi = in.w;
+    const float p0[4] = {in.p0.x, in.p0.y, in.p0.z, in.p0.w};
     float t[4], tmax = 0.f;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
@@ -724,7 +744,13 @@ __device__ __forceinline__ void trial_seq(int64_t o, int i, float2 stp, float st
         for (int a = 0; a < 4; ++a)
             if (a == y) r[a] = -ro;
     } else {
-        trial_big(lbase + o * 4, u + o * 4, stp, y, wi, p0, r, fbig, dgbig);
+        const BigTrial bt = trial_big(lbase + o * 4, u + o * 4, stp, y, wi, in.p0);
+        r[0] = bt.r.x;
+        r[1] = bt.r.y;
+        r[2] = bt.r.z;
+        r[3] = bt.r.w;
+        fbig = df_add(fbig, bt.df);
+        dgbig = df_add(dgbig, bt.ddg);
     }
 #pragma unroll
     for (int a = 0; a < 4; ++a) rs[a] += r[a];
@@ -896,9 +922,19 @@ k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
         const float stpf = stpd.x + stpd.y;
         float f = 0.f, dg = 0.f, rs[4] = {0.f, 0.f, 0.f, 0.f};
         float2 fbig = df_zero(), dgbig = df_zero();
+        // two sequences per pass, both sequences' loads in flight before
+        // either is computed (the search has few warps per SM to hide
+        // latency with)
 #pragma unroll 1
-        for (int i = tid; i < N; i += LS_THREADS)
-            trial_seq((int64_t)b * Nx + i, i, stpd, stpf, lbase, u, ud, rstate, w, P0, R, f, dg, rs, fbig, dgbig);
+        for (int i0 = tid; i0 < N; i0 += 2 * LS_THREADS) {
+            const int i1 = i0 + LS_THREADS;
+            const bool two = i1 < N;
+            const int64_t o0 = (int64_t)b * Nx + i0, o1 = (int64_t)b * Nx + (two ? i1 : i0);
+            const TrialIn t0 = trial_load(o0, i0, ud, rstate, w, P0);
+            const TrialIn t1 = trial_load(o1, two ? i1 : i0, ud, rstate, w, P0);
+            trial_seq(o0, t0, stpd, stpf, lbase, u, R, f, dg, rs, fbig, dgbig);
+            if (two) trial_seq(o1, t1, stpd, stpf, lbase, u, R, f, dg, rs, fbig, dgbig);
+        }
         // FP32 sums per warp (each lane's value is an FP32 partial over a few
         // sequences), double-float for the large-step terms, FP64 across warps
         const float v[6] = {warp_sum_f(f), warp_sum_f(dg), warp_sum_f(rs[0]), warp_sum_f(rs[1]), warp_sum_f(rs[2]),
@@ -1268,14 +1304,14 @@ void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8
 }
 
 void launch_dual_grad(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, double qscale,
-                      const int32_t *rq, const float2 *KR, float2 *dv, double *acc, double *amax, cudaStream_t st,
-                      const int *cnt)
+                      const int32_t *rq, const float2 *KR, float2 *dv, const float2 *u, float2 *lbase, double *acc,
+                      double *amax, cudaStream_t st, const int *cnt)
 {
     if (n <= 0) return;
     const int NV = DV_S + 2 * P.ring;
     dim3 gg(grid_for(P.Nx * 2, 256 * STREAM_PASSES, 64), n);
     k_dual_grad<<<gg, 256, 0, st>>>(ctl, list, P.Nx, NV, P.ring, df_host(2.0 * P.lambda_J), rq, df_host(1.0 / qscale),
-                                    KR, dv, acc, amax, cnt);
+                                    KR, dv, u, lbase, acc, amax, cnt);
 }
 
 void launch_dual_dots(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int newg, const float2 *dv,
@@ -1296,13 +1332,6 @@ void launch_dual_direction(const Problem &P, const DualCtl *ctl, const int32_t *
                                                 w, rstate, u, ud, dacc, cnt);
 }
 
-void launch_dual_accept(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
-                        const float2 *u, float2 *lbase, cudaStream_t st, const int *cnt)
-{
-    if (n <= 0) return;
-    dim3 g(grid_for(P.Nx * 2, 256 * STREAM_PASSES, 64), n);
-    k_dual_accept<<<g, 256, 0, st>>>(ctl, list, P.Nx, DV_S + 2 * P.ring, dv, u, lbase, cnt);
-}
 
 void launch_dual_ws_init(const Problem &P, const int32_t *list, int n, double c, double qscale, const int32_t *rq,
                          const float2 *KR, float2 *dv, float2 *lbase, cudaStream_t st, const int *cnt)
