@@ -57,7 +57,7 @@ Q = 4
 METRIC = "loci/s at N=3000,L=94k: mixed+batched+warm-start vs plain GPU at <=1e-6 rel obj"
 # committed learned-start blobs, trained on the GPU on converged solves of
 # 3000 x 94,000 tree alignments: the dual form's per-sequence network on
-# seeds 1-4 (384 loci each), the per-pair network on seeds 1, 2; the bench
+# seeds 1-4 (1024 loci each), the per-pair network on seeds 1, 2; the bench
 # alignment is seed 0 (held out)
 WS_DEFAULT = {"dual": "warmstart_dual_tree-3000x94000.npy", "tc": "warmstart_tree-3000x94000.npy",
               "gather": "warmstart_tree-3000x94000.npy"}
@@ -107,11 +107,13 @@ def dist():
 
 
 class Clocks:
-    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+    """nvidia-smi samples of SM clock, throttle reasons and kernel occupancy
+    (utilization.gpu: the share of each sample period in which at least one
+    kernel ran) during a region."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
 
     def __init__(self, device):
         self.device = device
@@ -164,9 +166,12 @@ class Clocks:
                 if r[5 + k].lower().startswith("active"):
                     reasons.add(nm)
         load = sm[sm > 0.5 * np.nanmax(sm)] if np.isfinite(sm).any() else sm
+        util = np.array([num(r[9]) for r in rows if len(r) >= 10])
+        util = util[np.isfinite(util)]
         return {"sm_mhz": float(np.nanmedian(load)) if len(load) else None,
                 "sm_max_mhz": float(np.nanmax(mx)) if np.isfinite(mx).any() else None,
-                "reasons": sorted(reasons), "samples": len(rows)}
+                "reasons": sorted(reasons), "samples": len(rows),
+                "gpu_util_pct": {"median": float(np.median(util)), "min": float(util.min())} if len(util) else None}
 
 
 def measured_peaks():
@@ -251,6 +256,31 @@ def roofline_dual(prof_tot, N, L, m, cls=None):
     ach = per * units[cls] / t / 1e9
     return dict(bound="hbm", achieved=round(ach, 1), peak=hbm, unit="GB/s", frac=round(ach / hbm, 4),
                 traffic=None, kernel=cls, peak_source=src), cls
+
+
+def whole_solve_dual(prof_tot, N, L, m, trials, t_dev):
+    """The whole timed solve against both roofs: every dual-form class's
+    algorithmic HBM bytes and tensor FLOP over the timed device time.
+    Per slot-iteration (one history-dot launch unit), in parts of N x q
+    double-float values (32 N bytes): history dots 2k + 1; direction
+    (4k + 3) + 2 + 1 + 1 + 1; accept and gradient 18.5 (x, d, u, logits, K rho,
+    rho_q, old g read; x, logits, s, g, y written); quantiser 1; line search
+    1.5 + 9/32 per trial (P0, u - u_y, R written; states and weights).
+    Tensor work: 2 N^2 (q - 1) per K rho unit, 2 N L q^2 per one-hot
+    contraction unit (counted once, as in the class rooflines)."""
+    hbm, tflops, src = measured_peaks()
+    units = prof_tot["kernel_units"]
+    its = units["history"]
+    parts = (2 * m + 1) + (4 * m + 8) + 18.5 + 1 + trials * (1.5 + 9 / 32)
+    nbytes = its * parts * 32 * N
+    flop = units["forward"] * 2.0 * N * N * (Q - 1) + units["backward"] * 2.0 * N * L * Q * Q
+    gbs = nbytes / t_dev / 1e9
+    tf = flop / t_dev / 1e12
+    return dict(hbm_bytes_per_slot_iteration=round(parts * 32 * N), slot_iterations=int(its),
+                hbm_achieved_gbs=round(gbs, 1), hbm_frac=round(gbs / hbm, 4), tensor_achieved_tflops=round(tf, 2),
+                tensor_frac=round(tf / tflops, 4), peak_source=src,
+                how="algorithmic bytes and FLOP of every class over the timed device time (the kernels of "
+                    "different lanes overlap, so the two fractions share the same seconds)")
 
 
 def roofline(prof_tot, N, L, Dp, m, hist_bytes):
@@ -582,6 +612,9 @@ def engine_arm(args):
                                   "avg_launch_ms": round(iso["kernel_ms"][dom] /
                                                          max(1, iso["kernel_launches"][dom]), 4),
                                   "measured": f"one untimed step of {B} loci on a single lane"}
+        if rf is not None:
+            trials = float(np.median(nfe)) / max(1.0, float(np.median(iters)))
+            rf["whole_solve"] = whole_solve_dual(tot, N, L, m_mean, trials, dev_ms / 1e3)
     else:
         rf, dom = roofline(tot, N, L, Dp, 10, 2 if args.history_bf16 else 4)
     # accuracy: the FP64 oracle's objective and gradient at the parameters

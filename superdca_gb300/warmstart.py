@@ -264,14 +264,18 @@ def main(argv=None):
     ap.add_argument("--dual", action="store_true", help="the dual form's per-sequence start (version 2)")
     ap.add_argument("--alpha", type=float, default=0.4, help="dual: shrinkage of the predicted residuals")
     ap.add_argument("--rows-per-locus", type=int, default=0, help="dual: sequences sampled per locus (0: all)")
+    ap.add_argument("--batch-slots", type=int, default=0,
+                    help="slots of the engine that solves the training loci (default: 256 dual, 64 otherwise)")
     ap.add_argument("--out", required=True)
     a = ap.parse_args(argv)
     sizes = {k: v for k, v in (("N", a.N), ("L", a.L)) if v is not None}
     if a.dual:
         blob, _ = train_dual_on_workload(a.workload, a.seeds, a.loci, alpha=a.alpha, epochs=a.epochs, lr=a.lr,
-                                         sizes=sizes, rows_per_locus=a.rows_per_locus)
+                                         sizes=sizes, rows_per_locus=a.rows_per_locus,
+                                         batch_slots=a.batch_slots or 256)
     else:
-        blob, _ = train_on_workload(a.workload, a.seeds, a.loci, a.pairs, epochs=a.epochs, lr=a.lr, sizes=sizes)
+        blob, _ = train_on_workload(a.workload, a.seeds, a.loci, a.pairs, epochs=a.epochs, lr=a.lr, sizes=sizes,
+                                    batch_slots=a.batch_slots or 64)
     np.save(a.out, blob)
     print("wrote", a.out)
 
