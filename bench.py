@@ -201,10 +201,12 @@ def load_workload(args):
 
 # DRAM bytes per unit (one target locus through one launch) from one ncu
 # capture, scaled to a launch by its units (the traffic grows with the slots):
-#   ncu --set full --clock-control none -k regex:k_dual_direction -s 40 -c 2 ... \
-#       python bench.py --steps 1 --warmup 0 --batch 128 --lanes 1 --loci-per-step 128 --no-cpu --no-e2e
-#   dram__bytes_read.sum 542.7 MB + dram__bytes_write.sum 42.0 MB per launch of 128 slots
-NCU_TRAFFIC_PER_UNIT = {("tree-3000x94000", "direction"): (542.68e6 + 42.05e6) / 128}
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none \
+#       -k regex:k_dual_direction -s 40 -c 2 python bench.py --steps 1 --warmup 0 --batch 128 --lanes 1 \
+#       --loci-per-step 128 --no-cpu --no-e2e --no-plain --no-secondary --no-autotune --no-parity \
+#       --accuracy-sample 0 --no-zero-start
+#   dram__bytes_read.sum 542.70 MB + dram__bytes_write.sum 29.29 MB per launch of 128 slots (mean of 2)
+NCU_TRAFFIC_PER_UNIT = {("tree-3000x94000", "direction"): (542.70e6 + 29.29e6) / 128}
 
 
 def mean_history(iterations, m):
@@ -226,9 +228,10 @@ def roofline_dual(prof_tot, N, L, m, cls=None):
       backward (one-hot contraction X^T a on the tensor cores: max-norm
         checks and the final J): 2 N L q^2 FLOP, as in the other forms;
       history dots: 2k + 1 vectors of N x q doubles read (32 N bytes each);
-      direction: (4k + 3) vectors read, 2 written, u (32 N) and its
-        single-precision differences (16 N) written, the logits read (32 N)
-        and the base probabilities written (16 N);
+      direction: (4k + 3) vectors read (history, g, a_x), 2 written (d),
+        the k part of x read (32 N: the logits are k_x + eta_x), the
+        single-precision differences u - u_y (16 N) and the base
+        probabilities (16 N) written;
       line search (step trials): base probabilities, u differences, R
         (16 N each), states, w.
     With several solver lanes the classes of different lanes overlap in
@@ -249,7 +252,7 @@ def roofline_dual(prof_tot, N, L, m, cls=None):
         ach = 2.0 * N * L * Q * Q * units[cls] / t / 1e12
         return dict(bound="tensor", achieved=round(ach, 3), peak=tflops, unit="TFLOP/s", frac=round(ach / tflops, 5),
                     traffic=None, kernel="k_gemm (X^T a)", peak_source=src), cls
-    per = {"history": (2 * m + 1) * 32 * N, "direction": ((4 * m + 3) + 2 + 1 + 1) * 32 * N + 32 * N,
+    per = {"history": (2 * m + 1) * 32 * N, "direction": ((4 * m + 3) + 2 + 1 + 1) * 32 * N,
            "linesearch": 16 * N * 3 + 9 * N}.get(cls)
     if per is None:
         return None, cls
@@ -263,15 +266,15 @@ def whole_solve_dual(prof_tot, N, L, m, trials, t_dev):
     algorithmic HBM bytes and tensor FLOP over the timed device time.
     Per slot-iteration (one history-dot launch unit), in parts of N x q
     double-float values (32 N bytes): history dots 2k + 1; direction
-    (4k + 3) + 2 + 1 + 1 + 1; accept and gradient 18.5 (x, d, u, logits, K rho,
-    rho_q, old g read; x, logits, s, g, y written); quantiser 1; line search
-    1.5 + 9/32 per trial (P0, u - u_y, R written; states and weights).
+    (4k + 3) + 2 + 1 + 1; accept and gradient 15.5 (x, d, K rho, rho_q, old g
+    read; x, s, g, y written); quantiser 1; line search 1.5 + 9/32 per trial
+    (P0, u - u_y, R written; states and weights).
     Tensor work: 2 N^2 (q - 1) per K rho unit, 2 N L q^2 per one-hot
     contraction unit (counted once, as in the class rooflines)."""
     hbm, tflops, src = measured_peaks()
     units = prof_tot["kernel_units"]
     its = units["history"]
-    parts = (2 * m + 1) + (4 * m + 8) + 18.5 + 1 + trials * (1.5 + 9 / 32)
+    parts = (2 * m + 1) + (4 * m + 7) + 15.5 + 1 + trials * (1.5 + 9 / 32)
     nbytes = its * parts * 32 * N
     flop = units["forward"] * 2.0 * N * N * (Q - 1) + units["backward"] * 2.0 * N * L * Q * Q
     gbs = nbytes / t_dev / 1e9

@@ -171,7 +171,6 @@ struct sdca_handle {
 
     // dual form (kernels_dual.cu)
     float2 *dv = nullptr, *KR = nullptr;   // coefficient vectors and K rho, double-float (df.cuh)
-    float2 *udf = nullptr;                 // logits direction (the dual form's logits are lbase as double-float)
     double *amax = nullptr, *J64 = nullptr, *amax_h = nullptr;
     int32_t *rq = nullptr, *Kmat = nullptr;
     long long *csum = nullptr;
@@ -262,7 +261,6 @@ int fail(sdca_handle *h, int code, const std::string &msg)
 int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
 
 // the dual form keeps its logits in double-float: the same 8 bytes per value
-float2 *lbase_df(sdca_handle *h) { return reinterpret_cast<float2 *>(h->lbase); }
 
 cudaEvent_t take_event(sdca_handle *h)
 {
@@ -561,7 +559,6 @@ int slot_begin(sdca_handle *h, int b, int64_t k, int32_t locus, const float *x0_
     if (h->form == SDCA_FORM_DUAL) {
         const size_t NV = DV_S + 2 * (size_t)P.ring;
         CK(cudaMemsetAsync(h->dv + (size_t)b * NV * 2 * P.Nx * 4, 0, sizeof(double) * NV * 2 * P.Nx * 4, h->stream));
-        CK(cudaMemsetAsync(h->udf + (size_t)b * P.Nx * 4, 0, sizeof(float2) * P.Nx * 4, h->stream));
         const int rc = dual_ctl_begin(h, b);
         if (rc) return rc;
     }
@@ -1527,7 +1524,7 @@ int dual_core(sdca_handle *h, const int64_t (&n)[DC_N], bool dev, cudaEvent_t ev
     // update and gradient assembly, "other" the control kernel and the
     // learned starts.
     if ((rc = region(SDCA_K_LINESEARCH, 1, DC_T, [&] {
-             launch_dual_linesearch(P, h->ctl, l_T, len(DC_T), h->dacc, h->dv, lbase_df(h), h->udf, h->ud, h->rstate,
+             launch_dual_linesearch(P, h->ctl, l_T, len(DC_T), h->dacc, h->dv, h->ud, h->rstate,
                                     h->wf, h->P0, h->R, h->acc, h->stream, dcnt(DC_T));
              return SDCA_OK;
          })))
@@ -1558,14 +1555,14 @@ int dual_core(sdca_handle *h, const int64_t (&n)[DC_N], bool dev, cudaEvent_t ev
         // the learned start: a_x = -rho^ / (2 lambda_J), K a_x exactly from the pass above
         if ((rc = region(SDCA_K_OTHER, 1, DC_W, [&] {
                  launch_dual_ws_init(P, l_W, len(DC_W), -0.5 / P.lambda_J, h->qscale, h->rq, h->KR, h->dv,
-                                     lbase_df(h), h->stream, dcnt(DC_W));
+                                     h->stream, dcnt(DC_W));
                  return SDCA_OK;
              })))
             return rc;
     }
     if ((rc = region(SDCA_K_ACCEPT, 1, DC_G, [&] {
-             launch_dual_grad(P, h->ctl, l_G, len(DC_G), h->qscale, h->rq, h->KR, h->dv, h->udf, lbase_df(h), h->acc,
-                              h->amax, h->stream, dcnt(DC_G));
+             launch_dual_grad(P, h->ctl, l_G, len(DC_G), h->qscale, h->rq, h->KR, h->dv, h->acc, h->amax, h->stream,
+                              dcnt(DC_G));
              return SDCA_OK;
          })))
         return rc;
@@ -1590,8 +1587,8 @@ int dual_core(sdca_handle *h, const int64_t (&n)[DC_N], bool dev, cudaEvent_t ev
     else CK(cudaEventRecord(ev, h->stream));
     if (dev || n[DC_G] > 0) CK(cudaMemsetAsync(h->dacc, 0, sizeof(double) * NDACC * P.Bmax, h->stream));
     if ((rc = region(SDCA_K_DIRECTION, 1, DC_G, [&] {
-             launch_dual_direction(P, h->ctl, l_G, len(DC_G), h->dv, lbase_df(h), h->P0, h->wf, h->rstate, h->udf,
-                                   h->ud, h->dacc, h->stream, dcnt(DC_G));
+             launch_dual_direction(P, h->ctl, l_G, len(DC_G), h->dv, h->P0, h->wf, h->rstate, h->ud, h->dacc,
+                                   h->stream, dcnt(DC_G));
              return SDCA_OK;
          })))
         return rc;
@@ -1707,6 +1704,10 @@ int dual_round(sdca_handle *h, Queue &Qu)
             h->sd_h[b].gcur = 0;
             h->sd_h[b].stp = 0.0;
             h->sd_h[b].flags = 0;
+            // the evaluation's logits are k_x + eta: eta is zero at a start
+            // (zero or learned) and eta_x at the end (set by dual_convert)
+            if (h->slots[b].phase == PH_INIT)
+                for (int a = 0; a < Q; ++a) h->sd_h[b].eta[a] = 0.0;
         }
         int rc = staged_h2d(h, h->sd, h->sd_h, sizeof(SlotDev) * P.Bmax);
         if (rc) return rc;
@@ -1717,8 +1718,7 @@ int dual_round(sdca_handle *h, Queue &Qu)
     if ((rc = zero_acc(h))) return rc;
     if (!ef.empty()) {
         Timed t(h, SDCA_K_LINESEARCH, 1, (int64_t)ef.size());
-        launch_trial_dual(P, h->sd, l_ef, (int)ef.size(), lbase_df(h), h->udf, h->rstate, h->w, h->R, h->acc,
-                          h->stream);
+        launch_dual_eval(P, h->sd, l_ef, (int)ef.size(), h->dv, h->rstate, h->w, h->R, h->acc, h->stream);
     }
     CKL();
     // the iteration core: a replay of this lane's CUDA graph, or the kernels one by one
@@ -2117,7 +2117,7 @@ static int create_lane(const sdca_config *cfg, const sdca_handle *owner, sdca_ha
         (dual && ((rc = halloc(h, &h->amax_h, 2 * B)) || (rc = halloc(h, &h->sum_h, B)) ||
                   (rc = dalloc(h, &h->ctl, B)) || (rc = dalloc(h, &h->sum, B)) ||
                   (rc = dalloc(h, &h->dacc, B * NDACC)) || (rc = dalloc(h, &h->dlist, 4 * B + DC_N)) ||
-                  (rc = dalloc(h, &h->dv, B * NV * 2 * P.Nx * 4)) || (rc = dalloc(h, &h->udf, B * P.Nx * 4)) ||
+                  (rc = dalloc(h, &h->dv, B * NV * 2 * P.Nx * 4)) ||
                   (rc = dalloc(h, &h->KR, B * P.Nx * 4)) || (rc = dalloc(h, &h->amax, 2 * B)) ||
                   (rc = dalloc(h, &h->rq, B * P.Nx * 4)) || (rc = dalloc(h, &h->csum, 16 * B)) ||
                   (rc = dalloc(h, &h->Rchk, B * P.Nx * 4)) || (dual_small && (rc = dalloc(h, &h->J64, B * P.Dp))) ||

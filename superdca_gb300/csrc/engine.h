@@ -215,12 +215,6 @@ void launch_direction(const Problem &P, const SlotDev *sd, const int32_t *list, 
 void launch_score(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
                   const float *wa, int gap, float *rows, cudaStream_t st);
 
-// sequence reweighting (kernels_weights.cu)
-// the dual form's FP64 evaluation from its double-float logits (start and final points)
-void launch_trial_dual(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
-                       const float2 *lbase, const float2 *u, const uint8_t *rstate, const double *w,
-                       float *R, double *acc, cudaStream_t st);
-
 // dual form (kernels_dual.cu)
 void launch_dual_kmat(const int32_t *dist, int N, int64_t Nx, int L, int32_t *K, cudaStream_t st);
 void launch_dual_quant(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float *R,
@@ -230,18 +224,21 @@ void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8
 // the accept (x += stp d, s push, logits += stp u) of the slots that searched
 // this round, then the gradient at the new point (y push, sums)
 void launch_dual_grad(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, double qscale,
-                      const int32_t *rq, const float2 *KR, float2 *dv, const float2 *u, float2 *lbase, double *acc,
-                      double *amax, cudaStream_t st, const int *cnt = nullptr);
+                      const int32_t *rq, const float2 *KR, float2 *dv, double *acc, double *amax, cudaStream_t st,
+                      const int *cnt = nullptr);
 void launch_dual_dots(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int newg, const float2 *dv,
                       double *dots, cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_direction(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
-                           const float2 *lbase, float *P0, const float *w, const uint8_t *rstate, float2 *u,
-                           float *ud, double *dacc, cudaStream_t st, const int *cnt = nullptr);
+                           float *P0, const float *w, const uint8_t *rstate, float *ud, double *dacc,
+                           cudaStream_t st, const int *cnt = nullptr);
+// start and final evaluations of the dual form (logits k_x + eta, FP64 log-sum-exp)
+void launch_dual_eval(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float2 *dv,
+                      const uint8_t *rstate, const double *w, float *R, double *acc, cudaStream_t st);
 void launch_dual_to_r(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int which,
                       const float2 *dv, float *R, cudaStream_t st);
 // the per-iteration decisions of the dual form on the device
 void launch_dual_linesearch(const Problem &P, DualCtl *ctl, const int32_t *list, int n, const double *dacc,
-                            float2 *dv, const float2 *lbase, float2 *u, float *ud, const uint8_t *rstate,
+                            float2 *dv, float *ud, const uint8_t *rstate,
                             const float *w, const float *P0, float *R, double *acc, cudaStream_t st, const int *cnt = nullptr);
 void launch_dual_control(const Problem &P, DualCtl *ctl, DualSum *sum, const int32_t *list, int n,
                          int max_iterations, double gtol, const double *acc, const double *amax, const double *dots,
@@ -281,7 +278,7 @@ void launch_dual_ws_feats(const uint8_t *cols, const int32_t *idx, int n, int N,
 void launch_dual_ws_r(const int32_t *slots, int n, int N, int64_t Nx, const float *out, const float *p_dev, float alpha,
                       const float *w, float *R, cudaStream_t st);
 void launch_dual_ws_init(const Problem &P, const int32_t *list, int n, double c, double qscale, const int32_t *rq,
-                         const float2 *KR, float2 *dv, float2 *lbase, cudaStream_t st, const int *cnt = nullptr);
+                         const float2 *KR, float2 *dv, cudaStream_t st, const int *cnt = nullptr);
 void launch_ws_residual(const uint8_t *XT, int64_t Nx, int N, const int32_t *loci, int G, const double *w,
                         const int32_t *knn, int k, float eps, float *Rws, cudaStream_t st);
 void launch_ws_residual_split(const uint8_t *XT, int64_t Nx, int N, const int32_t *loci, const int32_t *slots, int G,

@@ -173,18 +173,18 @@ __device__ __forceinline__ void df2_store(float2 *p, int64_t t, const float2 (&v
 // its new point, in one pass over the slot's vectors (a slot entering
 // with its start point has no accept):
 //   accept: x += stp d (a and k parts), s = x_new - x_old into the history
-//   on a push, logits lbase += stp u;
+//   on a push (the logits k_x + eta_x follow with x);
 //   gradient (a, k) = (rho_q / qscale + 2 lambda_J a_x, K rho + 2 lambda_J k_x),
 //   y = g_new - g_old into the history on a push;
 //   J-part sums: g.g, x.x, s.y, y.y, s.s; max |a_g| and max |a_x|.
-// Nothing between the line search and this kernel reads x or the logits of
-// a searching slot (the residual quantiser and K rho take the search's R
-// rows), so the accept can wait until here.
+// Nothing between the line search and this kernel reads x of a searching
+// slot (the residual quantiser and K rho take the search's R rows), so the
+// accept can wait until here.
 __global__ void __launch_bounds__(256)
 k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
             float2 l2, const int32_t *__restrict__ rq, float2 iq, const float2 *__restrict__ KR,
-            float2 *__restrict__ dv, const float2 *__restrict__ u, float2 *__restrict__ lbase,
-            double *__restrict__ acc, double *__restrict__ amax, const int *__restrict__ cnt)
+            float2 *__restrict__ dv, double *__restrict__ acc, double *__restrict__ amax,
+            const int *__restrict__ cnt)
 {
     if (cnt && (int)blockIdx.y >= *cnt) return;
     const int b = list[blockIdx.y];
@@ -203,8 +203,6 @@ k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
     float2 *ay = dv + dvo(b, DV_S + ring + ps, 0, NV, Nx), *ky = ay + part;
     const int2 *rq2 = reinterpret_cast<const int2 *>(rq + (int64_t)b * Nx * 4);
     const float2 *KRb = KR + (int64_t)b * Nx * 4;
-    const float2 *ub = u + (int64_t)b * Nx * 4;
-    float2 *lb = lbase + (int64_t)b * Nx * 4;
     float2 g2 = df_zero(), x2 = df_zero(), sy = df_zero(), yy = df_zero(), ss = df_zero();
     float mg = 0.f, mx = 0.f;
     // entry pairs (2t, 2t+1): 16-byte loads of every stream
@@ -216,11 +214,9 @@ k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
         const int2 r2 = rq2[t];
         const int rr[2] = {r2.x, r2.y};
         if (step) {
-            float2 a_d[2], k_d[2], uu[2], l[2];
+            float2 a_d[2], k_d[2];
             df2_load(ad, t, a_d);
             df2_load(kd, t, k_d);
-            df2_load(ub, t, uu);
-            df2_load(lb, t, l);
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
                 const float2 a1 = df_fma(sf, a_d[q], a_x[q]), k1 = df_fma(sf, k_d[q], k_x[q]);
@@ -228,11 +224,9 @@ k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
                 k_s[q] = df_sub(k1, k_x[q]);
                 a_x[q] = a1;
                 k_x[q] = k1;
-                l[q] = df_fma(sf, uu[q], l[q]);
             }
             df2_store(ax, t, a_x);
             df2_store(kx, t, k_x);
-            df2_store(lb, t, l);
             if (push) {
                 df2_store(as, t, a_s);
                 df2_store(ks, t, k_s);
@@ -328,8 +322,8 @@ k_dual_dots(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
 }
 
 // A step trial of one sequence with a large step (|t| >= 30), from its
-// double-float logits without FP64 arithmetic: l1 = l0 + stp u in
-// double-float, each log-sum-exp shifted by its largest high part and taken
+// double-float logits without FP64 arithmetic: l0 = k_x + eta_x,
+// u = k_d + eta_d, l1 = l0 + stp u in double-float, each log-sum-exp shifted by its largest high part and taken
 // in FP32 (the shifted terms are O(1)), the change of w (lse(l) - l_y)
 // assembled in double-float.  Returns the change of w (lse - l_y), the
 // slope change and the residual row r (by value: nothing of the common path
@@ -339,8 +333,8 @@ struct BigTrial {
     float2 df, ddg;
 };
 
-__device__ __noinline__ BigTrial trial_big(const float2 *lb, const float2 *up, float2 stp, int y, float wi,
-                                           float4 p0v)
+__device__ __noinline__ BigTrial trial_big(const float2 *kx, const float2 *kd, const float2 *ex, const float2 *ed,
+                                           float2 stp, int y, float wi, float4 p0v)
 {
     const float p0[4] = {p0v.x, p0v.y, p0v.z, p0v.w};
     float r[4];
@@ -348,8 +342,8 @@ __device__ __noinline__ BigTrial trial_big(const float2 *lb, const float2 *up, f
     float2 l0[4], l1[4], uu[4];
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-        l0[a] = lb[a];
-        uu[a] = up[a];
+        l0[a] = df_add(kx[a], ex[a]);
+        uu[a] = df_add(kd[a], ed[a]);
         l1[a] = df_fma(stp, uu[a], l0[a]);
     }
     const float m0 = fmaxf(fmaxf(l0[0].x, l0[1].x), fmaxf(l0[2].x, l0[3].x));
@@ -408,9 +402,10 @@ __device__ __noinline__ BigTrial trial_big(const float2 *lb, const float2 *up, f
 // the sums of w dl, of the slope change and of R(stp), and the rows
 // R <- R(stp) = w (p(stp) - onehot(y)), the y entry as minus the sum of the
 // others (trial_seq, in the line-search kernel below).
-// d = coef_g g + sum_j coefS_j s_j + coefY_j y_j (a and k parts); trial
-// logits direction u = k_d + eta_d; the base probabilities P0 of the step
-// trials from the double-float logits at the current point (fresh every iteration,
+// d = coef_g g + sum_j coefS_j s_j + coefY_j y_j (a and k parts); the trial
+// logits direction u = k_d + eta_d, kept only as its single-precision
+// differences u - u_y; the base probabilities P0 of the step trials from the
+// double-float logits k_x + eta_x at the current point (fresh every iteration,
 // so that rounding does not carry from one iteration to the next); sums g.d,
 // d.d, x.d (J parts) and the slope of the search line at 0 from the trials'
 // own numbers, sum_i w_i sum_c p0_ic (u_ic - u_iy).
@@ -422,9 +417,9 @@ constexpr int DIR_THREADS = 256;
 
 __global__ void __launch_bounds__(DIR_THREADS, 5)
 k_dual_direction(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int N, int NV,
-                 int ring, float2 *__restrict__ dv, const float2 *__restrict__ lbase, float *__restrict__ P0,
-                 const float *__restrict__ w, const uint8_t *__restrict__ rstate, float2 *__restrict__ u,
-                 float *__restrict__ ud, double *__restrict__ dacc, const int *__restrict__ cnt)
+                 int ring, float2 *__restrict__ dv, float *__restrict__ P0, const float *__restrict__ w,
+                 const uint8_t *__restrict__ rstate, float *__restrict__ ud, double *__restrict__ dacc,
+                 const int *__restrict__ cnt)
 {
     if (cnt && (int)blockIdx.y >= *cnt) return;
     const int b = list[blockIdx.y];
@@ -432,8 +427,10 @@ k_dual_direction(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ li
     if (S.phase == DC_STOP) return;
     const int k = S.nhist;
     __shared__ float2 cf[2 * MAXHIST + 1 + Q];   // the slot's coefficients and eta_d (double-float)
+    __shared__ float2 ex[Q];                     // eta_x (double-float): logits = k_x + eta_x
     __shared__ int64_t hoff[2 * MAXHIST];        // history vector offsets (a parts; k part at + Nx*4)
     if (threadIdx.x < 2 * MAXHIST + 1 + Q) cf[threadIdx.x] = S.cdf[threadIdx.x];
+    if (threadIdx.x < Q) ex[threadIdx.x] = df_from_d(S.eta_x[threadIdx.x]);
     if (threadIdx.x < k) {
         hoff[threadIdx.x] = dvo(b, DV_S + S.hist[threadIdx.x], 0, NV, Nx);
         hoff[MAXHIST + threadIdx.x] = dvo(b, DV_S + ring + S.hist[threadIdx.x], 0, NV, Nx);
@@ -497,7 +494,7 @@ k_dual_direction(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ li
         df2_store(kd, t, kk);
         float2 x_a[2], l[2];
         df2_load(ax, t, x_a);
-        df2_load(lbase + (int64_t)b * Nx * 4, t, l);
+        df2_load(ax + part, t, l);
         const int c0 = (int)((2 * t) & 3);        // state of the first entry: 0 or 2
         const int64_t i = t >> 1;                  // the sequence
         float2 uu[2];
@@ -507,8 +504,8 @@ k_dual_direction(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ li
             dd = df_fma(a[q], kk[q], dd);
             xd = df_fma(x_a[q], kk[q], xd);
             uu[q] = df_add(kk[q], cf[2 * MAXHIST + 1 + c0 + q]);
+            l[q] = df_add(l[q], ex[c0 + q]);       // logits k_x + eta_x
         }
-        df2_store(u + (int64_t)b * Nx * 4, t, uu);
         // u at the sequence's own state y, from whichever lane of the pair holds it
         const int y = rstate[(int64_t)b * Nx + i] & 3;
         const float2 mine = (y & 1) ? uu[1] : uu[0];
@@ -706,10 +703,10 @@ __device__ __forceinline__ TrialIn trial_load(int64_t o, int i, const float4 *__
 // One sequence of a step trial as a change from the current point (the
 // derivation above): adds w dl, the slope change and the new residual row's
 // sums, and writes the row.
-__device__ __forceinline__ void trial_seq(int64_t o, const TrialIn &in, float2 stp, float stpf,
-                                          const float2 *__restrict__ lbase, const float2 *__restrict__ u,
-                                          float4 *__restrict__ R, float &f, float &dg, float (&rs)[4], float2 &fbig,
-                                          float2 &dgbig)
+__device__ __forceinline__ void trial_seq(int64_t o, int i, const TrialIn &in, float2 stp, float stpf,
+                                          const float2 *__restrict__ kx, const float2 *__restrict__ kd,
+                                          const float2 *ex, const float2 *ed, float4 *__restrict__ R, float &f,
+                                          float &dg, float (&rs)[4], float2 &fbig, float2 &dgbig)
 {
     const float du[4] = {in.du.x, in.du.y, in.du.z, in.du.w};   // u_a - u_y
     const int y = in.y;
@@ -744,7 +741,7 @@ __device__ __forceinline__ void trial_seq(int64_t o, const TrialIn &in, float2 s
         for (int a = 0; a < 4; ++a)
             if (a == y) r[a] = -ro;
     } else {
-        const BigTrial bt = trial_big(lbase + o * 4, u + o * 4, stp, y, wi, in.p0);
+        const BigTrial bt = trial_big(kx + 4 * (int64_t)i, kd + 4 * (int64_t)i, ex, ed, stp, y, wi, in.p0);
         r[0] = bt.r.x;
         r[1] = bt.r.y;
         r[2] = bt.r.z;
@@ -789,7 +786,7 @@ template <int LS_THREADS>
 __global__ void __launch_bounds__(LS_THREADS, 768 / LS_THREADS)
 k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int N, int64_t Nx, int NV,
                   double lambda_J, double lambda_h, const double *__restrict__ dacc, float2 *__restrict__ dv,
-                  const float2 *__restrict__ lbase, float2 *__restrict__ u, float4 *__restrict__ ud,
+                  float4 *__restrict__ ud,
                   const uint8_t *__restrict__ rstate, const float *__restrict__ w, const float4 *__restrict__ P0,
                   float4 *__restrict__ R, double *__restrict__ acc, const int *__restrict__ cnt)
 {
@@ -803,6 +800,7 @@ k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
     __shared__ float2 s_stp_df;
     __shared__ double s_tot[8];
     __shared__ int s_restart, s_done;
+    __shared__ float2 s_ex[Q], s_ed[Q];   // eta_x, eta_d as double-float (the h parts of the logits and of u)
     MoreThuente &mt = *reinterpret_cast<MoreThuente *>(mt_raw);
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const double *da = dacc + (int64_t)b * NDACC;
@@ -844,7 +842,6 @@ k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
                 ad[4 * i + c] = a_d;
                 kd[4 * i + c] = k_d;
                 uu[c] = df_add(k_d, ed[c]);
-                u[o * 4 + c] = uu[c];
                 xd = df_fma(ax[4 * i + c], k_d, xd);
             }
             const int y = rstate[o] & 3;
@@ -892,6 +889,10 @@ k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
         __syncthreads();
     }
     if (tid == 0) {
+        for (int c = 0; c < Q; ++c) {
+            s_ex[c] = df_from_d(S.eta_x[c]);
+            s_ed[c] = df_from_d(S.eta_d[c]);
+        }
         xdH = dot4d(S.eta_x, S.eta_d);
         x2H = dot4d(S.eta_x, S.eta_x);
         const double l20 = lambda_J * S.x2J + lambda_h * x2H;
@@ -922,6 +923,7 @@ k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
         const float stpf = stpd.x + stpd.y;
         float f = 0.f, dg = 0.f, rs[4] = {0.f, 0.f, 0.f, 0.f};
         float2 fbig = df_zero(), dgbig = df_zero();
+        const float2 *kxs = dv + dvo(b, DV_X, 1, NV, Nx), *kds = dv + dvo(b, DV_D, 1, NV, Nx);
         // two sequences per pass, both sequences' loads in flight before
         // either is computed (the search has few warps per SM to hide
         // latency with)
@@ -932,8 +934,8 @@ k_dual_linesearch(DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
             const int64_t o0 = (int64_t)b * Nx + i0, o1 = (int64_t)b * Nx + (two ? i1 : i0);
             const TrialIn t0 = trial_load(o0, i0, ud, rstate, w, P0);
             const TrialIn t1 = trial_load(o1, two ? i1 : i0, ud, rstate, w, P0);
-            trial_seq(o0, t0, stpd, stpf, lbase, u, R, f, dg, rs, fbig, dgbig);
-            if (two) trial_seq(o1, t1, stpd, stpf, lbase, u, R, f, dg, rs, fbig, dgbig);
+            trial_seq(o0, i0, t0, stpd, stpf, kxs, kds, s_ex, s_ed, R, f, dg, rs, fbig, dgbig);
+            if (two) trial_seq(o1, i1, t1, stpd, stpf, kxs, kds, s_ex, s_ed, R, f, dg, rs, fbig, dgbig);
         }
         // FP32 sums per warp (each lane's value is an FP32 partial over a few
         // sequences), double-float for the large-step terms, FP64 across warps
@@ -1243,12 +1245,12 @@ __global__ void k_dual_check_apply(DualCtl *__restrict__ ctl, DualSum *__restric
 // The learned start of a slot from its predicted residual rows (already
 // through k_dual_quant and the exact K rho product): a_x = c rho_q / qscale,
 // k_x = c K rho (KR is K rho / qscale), c = -1 / (2 lambda_J); the logits
-// start at k_x (eta = 0).  The pair (a_x, k_x) is consistent to the
-// double-float rounding of one product by c.
+// are k_x (eta = 0).  The pair (a_x, k_x) is consistent to the double-float
+// rounding of one product by c.
 __global__ void __launch_bounds__(256)
 k_dual_ws_init(const int32_t *__restrict__ list, int64_t Nx, int NV, double c, double inv_qscale,
                const int32_t *__restrict__ rq, const float2 *__restrict__ KR, float2 *__restrict__ dv,
-               float2 *__restrict__ lbase, const int *__restrict__ cnt)
+               const int *__restrict__ cnt)
 {
     if (cnt && (int)blockIdx.y >= *cnt) return;
     const int b = list[blockIdx.y];
@@ -1259,8 +1261,49 @@ k_dual_ws_init(const int32_t *__restrict__ list, int64_t Nx, int NV, double c, d
         const float2 k = df_mul(cd, KR[(int64_t)b * Nx * 4 + e]);
         ax[e] = a;
         kx[e] = k;
-        lbase[(int64_t)b * Nx * 4 + e] = k;
     }
+}
+
+// The start and final evaluations of the dual form: objective terms, R rows
+// and their sums at the slot's current point, from the logits k_x + eta
+// (eta: the SlotDev field, the h part of x; zero at a start) with an FP64
+// log-sum-exp (SuperDCA's objective, plmDCA_objective.hpp:86-151, at x).
+constexpr int EVAL_THREADS = 256;
+
+__global__ void __launch_bounds__(EVAL_THREADS)
+k_dual_eval(const SlotDev *__restrict__ sd, const int32_t *__restrict__ list, int N, int64_t Nx, int NV,
+            const float2 *__restrict__ dv, const uint8_t *__restrict__ rstate, const double *__restrict__ w,
+            float4 *__restrict__ R, double *__restrict__ acc)
+{
+    const int b = list[blockIdx.y];
+    const SlotDev &S = sd[b];
+    const double eta[4] = {S.eta[0], S.eta[1], S.eta[2], S.eta[3]};
+    const float2 *kx = dv + dvo(b, DV_X, 1, NV, Nx);
+    double f = 0, rs0 = 0, rs1 = 0, rs2 = 0, rs3 = 0;
+    for (int i = blockIdx.x * EVAL_THREADS + threadIdx.x; i < N; i += gridDim.x * EVAL_THREADS) {
+        const int64_t o = (int64_t)b * Nx + i;
+        double l[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) l[a] = df_to_d(kx[4 * (int64_t)i + a]) + eta[a];
+        const double mx = fmax(fmax(l[0], l[1]), fmax(l[2], l[3]));
+        double e[4], z = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            e[a] = exp(l[a] - mx);
+            z += e[a];
+        }
+        const int sr = rstate[o] & 3;
+        const double wi = w[i];
+        f += wi * (mx + log(z) - l[sr]);
+        double r[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) r[a] = wi * (e[a] / z) - (a == sr ? wi : 0.0);
+        rs0 += r[0]; rs1 += r[1]; rs2 += r[2]; rs3 += r[3];
+        R[o] = make_float4((float)r[0], (float)r[1], (float)r[2], (float)r[3]);
+    }
+    double v[6] = {f, 0.0, rs0, rs1, rs2, rs3};
+    const int idx[6] = {ACC_F, ACC_DG, ACC_RS0, ACC_RS1, ACC_RS2, ACC_RS3};
+    block_sum_atomic<6>(v, acc + (int64_t)b * NACC, idx);
 }
 
 unsigned grid_for(int64_t elems, int per_block_elems, int cap)
@@ -1304,14 +1347,14 @@ void launch_dual_kprod(const Problem &P, const int32_t *list, int n, const uint8
 }
 
 void launch_dual_grad(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, double qscale,
-                      const int32_t *rq, const float2 *KR, float2 *dv, const float2 *u, float2 *lbase, double *acc,
-                      double *amax, cudaStream_t st, const int *cnt)
+                      const int32_t *rq, const float2 *KR, float2 *dv, double *acc, double *amax, cudaStream_t st,
+                      const int *cnt)
 {
     if (n <= 0) return;
     const int NV = DV_S + 2 * P.ring;
     dim3 gg(grid_for(P.Nx * 2, 256 * STREAM_PASSES, 64), n);
     k_dual_grad<<<gg, 256, 0, st>>>(ctl, list, P.Nx, NV, P.ring, df_host(2.0 * P.lambda_J), rq, df_host(1.0 / qscale),
-                                    KR, dv, u, lbase, acc, amax, cnt);
+                                    KR, dv, acc, amax, cnt);
 }
 
 void launch_dual_dots(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int newg, const float2 *dv,
@@ -1323,22 +1366,31 @@ void launch_dual_dots(const Problem &P, const DualCtl *ctl, const int32_t *list,
 }
 
 void launch_dual_direction(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, float2 *dv,
-                           const float2 *lbase, float *P0, const float *w, const uint8_t *rstate, float2 *u,
-                           float *ud, double *dacc, cudaStream_t st, const int *cnt)
+                           float *P0, const float *w, const uint8_t *rstate, float *ud, double *dacc,
+                           cudaStream_t st, const int *cnt)
 {
     if (n <= 0) return;
     dim3 g((unsigned)((P.Nx * 2 + DIR_THREADS - 1) / DIR_THREADS), n);
-    k_dual_direction<<<g, DIR_THREADS, 0, st>>>(ctl, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, P.ring, dv, lbase, P0,
-                                                w, rstate, u, ud, dacc, cnt);
+    k_dual_direction<<<g, DIR_THREADS, 0, st>>>(ctl, list, P.Nx, (int)P.N, DV_S + 2 * P.ring, P.ring, dv, P0, w,
+                                                rstate, ud, dacc, cnt);
+}
+
+void launch_dual_eval(const Problem &P, const SlotDev *sd, const int32_t *list, int n, const float2 *dv,
+                      const uint8_t *rstate, const double *w, float *R, double *acc, cudaStream_t st)
+{
+    if (n <= 0) return;
+    dim3 g(grid_for(P.N, EVAL_THREADS, 32), n);
+    k_dual_eval<<<g, EVAL_THREADS, 0, st>>>(sd, list, (int)P.N, P.Nx, DV_S + 2 * P.ring, dv, rstate, w,
+                                            reinterpret_cast<float4 *>(R), acc);
 }
 
 
 void launch_dual_ws_init(const Problem &P, const int32_t *list, int n, double c, double qscale, const int32_t *rq,
-                         const float2 *KR, float2 *dv, float2 *lbase, cudaStream_t st, const int *cnt)
+                         const float2 *KR, float2 *dv, cudaStream_t st, const int *cnt)
 {
     if (n <= 0) return;
     dim3 g(grid_for(P.Nx * 4, 256 * 4, 64), n);
-    k_dual_ws_init<<<g, 256, 0, st>>>(list, P.Nx, DV_S + 2 * P.ring, c, 1.0 / qscale, rq, KR, dv, lbase, cnt);
+    k_dual_ws_init<<<g, 256, 0, st>>>(list, P.Nx, DV_S + 2 * P.ring, c, 1.0 / qscale, rq, KR, dv, cnt);
 }
 
 void launch_dual_to_r(const Problem &P, const DualCtl *ctl, const int32_t *list, int n, int which,
@@ -1393,7 +1445,7 @@ void launch_dual_to_wa(const Problem &P, const SlotDev *sd, const int32_t *list,
 }
 
 void launch_dual_linesearch(const Problem &P, DualCtl *ctl, const int32_t *list, int n, const double *dacc,
-                            float2 *dv, const float2 *lbase, float2 *u, float *ud, const uint8_t *rstate,
+                            float2 *dv, float *ud, const uint8_t *rstate,
                             const float *w, const float *P0, float *R, double *acc, cudaStream_t st, const int *cnt)
 {
     if (n <= 0) return;
@@ -1404,7 +1456,7 @@ void launch_dual_linesearch(const Problem &P, DualCtl *ctl, const int32_t *list,
     }();
 #define SDCA_LS_LAUNCH(T)                                                                                          \
     k_dual_linesearch<T><<<n, T, 0, st>>>(ctl, list, (int)P.N, P.Nx, DV_S + 2 * P.ring, P.lambda_J, P.lambda_h,   \
-                                          dacc, dv, lbase, u, reinterpret_cast<float4 *>(ud), rstate, w,          \
+                                          dacc, dv, reinterpret_cast<float4 *>(ud), rstate, w,                    \
                                           reinterpret_cast<const float4 *>(P0), reinterpret_cast<float4 *>(R), acc, \
                                           cnt)
     if (threads == 64) SDCA_LS_LAUNCH(64);

@@ -20,8 +20,7 @@ namespace {
 
 constexpr int TRIAL_THREADS = 256;
 
-// the direction's logits u and the base logits: float4 / FP64 (contraction
-// forms) or double-float (dual form)
+// the direction's logits u and the base logits: float4 / FP64
 __device__ __forceinline__ double4 load4(const float4 *u, int64_t o)
 {
     const float4 v = u[o];
@@ -32,13 +31,6 @@ __device__ __forceinline__ double4 load4(const double *v, int64_t o)
     const double2 a = reinterpret_cast<const double2 *>(v + o * 4)[0];
     const double2 b = reinterpret_cast<const double2 *>(v + o * 4)[1];
     return make_double4(a.x, a.y, b.x, b.y);
-}
-__device__ __forceinline__ double4 load4(const float2 *v, int64_t o)
-{
-    const float4 a = reinterpret_cast<const float4 *>(v + o * 4)[0];
-    const float4 b = reinterpret_cast<const float4 *>(v + o * 4)[1];
-    return make_double4(df_to_d(make_float2(a.x, a.y)), df_to_d(make_float2(a.z, a.w)),
-                        df_to_d(make_float2(b.x, b.y)), df_to_d(make_float2(b.z, b.w)));
 }
 
 template <typename UT, typename LT>
@@ -399,18 +391,6 @@ void launch_trial(const Problem &P, const SlotDev *sd, const int32_t *list, int 
     dim3 grid((unsigned)gx, (unsigned)n);
     k_trial<float4, double><<<grid, TRIAL_THREADS, 0, st>>>(sd, list, (int)P.N, P.Nx, lbase,
                                                     reinterpret_cast<const float4 *>(u), rstate, w,
-                                                    reinterpret_cast<float4 *>(R), acc);
-}
-
-void launch_trial_dual(const Problem &P, const SlotDev *sd, const int32_t *list, int n,
-                       const float2 *lbase, const float2 *u, const uint8_t *rstate, const double *w,
-                       float *R, double *acc, cudaStream_t st)
-{
-    if (n <= 0) return;
-    int gx = (int)((P.N + TRIAL_THREADS - 1) / TRIAL_THREADS);
-    if (gx > 32) gx = 32;
-    dim3 grid((unsigned)gx, (unsigned)n);
-    k_trial<float2, float2><<<grid, TRIAL_THREADS, 0, st>>>(sd, list, (int)P.N, P.Nx, lbase, u, rstate, w,
                                                     reinterpret_cast<float4 *>(R), acc);
 }
 

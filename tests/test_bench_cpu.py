@@ -37,8 +37,9 @@ def test_roofline_dual_picks_the_requested_class():
     assert cls == "linesearch"
     rf, cls = bench.roofline_dual(tot, 3000, 94000, 10, "direction")
     assert cls == "direction" and rf["bound"] == "hbm" and rf["kernel"] == "direction"
-    # per unit: (4k + 3) + 4 vectors of 32 N bytes plus 32 N more, over 1 ms for 10 units
-    per = ((4 * 10 + 3) + 2 + 1 + 1) * 32 * 3000 + 32 * 3000
+    # per unit: (4k + 3) vectors read, d written, k_x read, u - u_y with P0
+    # written: (4k + 7) parts of 32 N bytes, over 1 ms for 10 units
+    per = ((4 * 10 + 3) + 2 + 1 + 1) * 32 * 3000
     assert abs(rf["achieved"] - round(per * 10 / 1e-3 / 1e9, 1)) < 0.2
 
 
