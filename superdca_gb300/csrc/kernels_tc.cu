@@ -53,12 +53,25 @@ constexpr int THREADS = 192;
 // and N tile.  NT = 2 (slot operands exact in fp16, no lo half): the stage's
 // lo slot carries a second N tile, so every expanded one-hot tile feeds two
 // MMAs per K16 step, as it does for hi + lo.
-template <int MSUB, int STG, int NT = 1> struct Cfg {
-    static constexpr int STAGE_BYTES = MSUB * A_BYTES + 2 * B_BYTES + MSUB * RAW_BYTES;
+//
+// AT (backward only): the one-hot A tiles live in TMEM instead of shared
+// memory.  The expansion warps write them with tcgen05.st (row m of a
+// subtile in TMEM lane m, sequence pairs (2j, 2j+1) in column j as the low
+// and high halves) and the MMAs read A from TMEM, so shared memory carries
+// only the slot operand and the u8 state tiles: an M128 N128 K16 MMA with
+// both operands in shared memory reads 8 KB per 64 cycles, which with the
+// expansion's stores and the TMA writes is more than the 128 bytes per
+// cycle shared memory delivers.  TMEM then holds the accumulators
+// (MSUB x NT x 128 columns) and STG stages of MSUB A subtiles (32 columns
+// each: 64 sequences).
+template <int MSUB, int STG, int NT = 1, bool AT = false> struct Cfg {
+    static constexpr int STAGE_BYTES = (AT ? 0 : MSUB * A_BYTES) + 2 * B_BYTES + MSUB * RAW_BYTES;
     static constexpr int SMEM_BYTES = STG * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-    static constexpr uint32_t TMEM_COLS = MSUB * BN * NT;
+    static constexpr uint32_t ACC_COLS = MSUB * BN * NT;
+    static constexpr uint32_t A_COLS = AT ? MSUB * (BK / 2) * STG : 0;
+    static constexpr uint32_t TMEM_COLS = AT ? 512 : ACC_COLS;
     static_assert(STAGE_BYTES % 1024 == 0, "stage must keep 1024-byte alignment");
-    static_assert(MSUB * BN * NT <= 512, "TMEM holds 512 columns");
+    static_assert(ACC_COLS + A_COLS <= 512, "TMEM holds 512 columns");
     static_assert(NT == 1 || NT == 2, "one or two N tiles per CTA");
 };
 
@@ -76,6 +89,41 @@ __device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
         "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+        : "memory");
+}
+
+// the same MMA with A read from TMEM (column tmem_a, lanes 0-127) and the
+// instruction descriptor given (its N fitted to the tile's live columns)
+__device__ __forceinline__ void mma_f16_ts(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc,
+                                           uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// kind::f16 descriptor with N = the live columns of a tile rounded up to 16
+// (at most BN): a partly filled last N tile issues only the MMA work it needs
+__device__ __forceinline__ uint32_t idesc_fit(int cols)
+{
+    const int n = cols >= BN ? BN : (cols < 16 ? 16 : (cols + 15) / 16 * 16);
+    return (IDESC & ~(0x3Fu << 17)) | ((uint32_t)(n >> 3) << 17);
+}
+
+// 32 consecutive TMEM columns of this warp's 32 lanes from 32 registers per thread
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32])
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+        "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+        "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+        "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+        "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]),
+        "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]),
+        "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
         : "memory");
 }
 
@@ -107,6 +155,29 @@ __device__ __forceinline__ uint2 eq_halves(uint32_t bytes, uint32_t s4)
     const uint32_t a = __byte_perm(m, 0u, 0x1404) & 0x3C003C00u;
     const uint32_t b = __byte_perm(m, 0u, 0x3424) & 0x3C003C00u;
     return make_uint2(a, b);
+}
+
+// backward, A in TMEM: row t's 64 one-hot values as 32 sequence pairs
+// (low half: the even sequence), the column order of the TMEM A operand
+__device__ __forceinline__ void expand_bwd_regs(const uint8_t *raw, int t, uint32_t (&o)[32])
+{
+    const int nl = t >> 2;
+    const uint32_t s4 = (uint32_t)(t & 3) * 0x01010101u;
+    const uint4 *rp = reinterpret_cast<const uint4 *>(raw + nl * 64);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const uint4 w = rp[q];
+        const uint2 e0 = eq_halves(w.x, s4), e1 = eq_halves(w.y, s4);
+        const uint2 e2 = eq_halves(w.z, s4), e3 = eq_halves(w.w, s4);
+        o[8 * q + 0] = e0.x;
+        o[8 * q + 1] = e0.y;
+        o[8 * q + 2] = e1.x;
+        o[8 * q + 3] = e1.y;
+        o[8 * q + 4] = e2.x;
+        o[8 * q + 5] = e2.y;
+        o[8 * q + 6] = e3.x;
+        o[8 * q + 7] = e3.y;
+    }
 }
 
 // backward: raw = 32 loci x 64 sequences (u8); A row r = locus*4+state, K = sequence
@@ -155,21 +226,21 @@ struct GemmArgs {
     int *err;
 };
 
-template <int MSUB, int STG, int NT>
+template <int MSUB, int STG, int NT, bool AT = false>
 __global__ void __launch_bounds__(THREADS, 1)
 k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtensorMap tmBhi,
        const __grid_constant__ CUtensorMap tmBlo, const GemmArgs args)
 {
-    using C = Cfg<MSUB, STG, NT>;
+    using C = Cfg<MSUB, STG, NT, AT>;
     constexpr int SB = C::STAGE_BYTES;
     extern __shared__ uint8_t smem_raw[];
     const uint32_t sbase0 = smem_u32(smem_raw);
     const uint32_t sbase = (sbase0 + 1023u) & ~1023u;
     uint8_t *const sgen = smem_raw + (sbase - sbase0);
     const uint32_t bars = sbase + STG * SB;
-    // stage layout: [A subtiles | B hi | B lo | raw u8 tiles]
+    // stage layout: [A subtiles (not with AT) | B hi | B lo | raw u8 tiles]
     auto a_off = [](int ms) { return (uint32_t)(ms * A_BYTES); };
-    constexpr uint32_t BHI = MSUB * A_BYTES, BLO = BHI + B_BYTES, RAW = BLO + B_BYTES;
+    constexpr uint32_t BHI = AT ? 0 : MSUB * A_BYTES, BLO = BHI + B_BYTES, RAW = BLO + B_BYTES;
     // barrier layout: full_raw[STG], full_a[STG], empty[STG], tmem_full, tmem addr
     auto full_raw = [&](int s) { return bars + 8u * s; };
     auto full_a = [&](int s) { return bars + 8u * (STG + s); };
@@ -234,6 +305,9 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
         }
     } else if (warp == 1) {
         if (lane == 0) {
+            // live columns of this CTA's N tiles (4 per list position)
+            const int cols0 = 4 * args.nlist - n_tile * BN, cols1 = cols0 - BN;
+            const uint32_t id0 = idesc_fit(cols0), id1 = idesc_fit(cols1);
             for (int j = 0; j < nkt; ++j) {
                 const int s = j % STG;
                 const uint32_t ph = (uint32_t)((j / STG) & 1);
@@ -246,13 +320,26 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
                     const uint64_t bl = smem_desc_sw128(st + BLO + kk * 32);
 #pragma unroll
                     for (int ms = 0; ms < MSUB; ++ms) {
-                        const uint64_t ad = smem_desc_sw128(st + a_off(ms) + kk * 32);
                         const uint32_t td = tmem_base + (uint32_t)(ms * BN);
-                        mma_f16(td, ad, bh, (j > 0 || kk > 0) ? 1u : 0u);
-                        if (NT == 2)
-                            mma_f16(td + (uint32_t)(MSUB * BN), ad, bl, (j > 0 || kk > 0) ? 1u : 0u);
-                        else if (!args.hi_only)
-                            mma_f16(td, ad, bl, 1u);
+                        if (AT) {
+                            // K16 step kk: 8 of the subtile's 32 A columns
+                            const uint32_t ta =
+                                tmem_base + C::ACC_COLS + (uint32_t)((s * MSUB + ms) * (BK / 2) + kk * 8);
+                            mma_f16_ts(td, ta, bh, id0, (j > 0 || kk > 0) ? 1u : 0u);
+                            if (NT == 2) {
+                                if (cols1 > 0)   // (a second tile with no live column is not computed)
+                                    mma_f16_ts(td + (uint32_t)(MSUB * BN), ta, bl, id1, (j > 0 || kk > 0) ? 1u : 0u);
+                            } else if (!args.hi_only) {
+                                mma_f16_ts(td, ta, bl, id0, 1u);
+                            }
+                        } else {
+                            const uint64_t ad = smem_desc_sw128(st + a_off(ms) + kk * 32);
+                            mma_f16(td, ad, bh, (j > 0 || kk > 0) ? 1u : 0u);
+                            if (NT == 2)
+                                mma_f16(td + (uint32_t)(MSUB * BN), ad, bl, (j > 0 || kk > 0) ? 1u : 0u);
+                            else if (!args.hi_only)
+                                mma_f16(td, ad, bl, 1u);
+                        }
                     }
                 }
                 mma_commit(empty(s));
@@ -261,19 +348,36 @@ k_gemm(const __grid_constant__ CUtensorMap tmRaw, const __grid_constant__ CUtens
             mma_commit(tmem_full);
         }
     } else {
-        const int t = threadIdx.x - 64;  // 0..127
+        // with AT a warp writes only its TMEM lane quadrant: row = 32 (warp % 4) + lane
+        const int t = AT ? 32 * (warp & 3) + lane : threadIdx.x - 64;  // 0..127
         for (int j = 0; j < nkt; ++j) {
             const int s = j % STG;
             const uint32_t ph = (uint32_t)((j / STG) & 1);
+            // (full_raw(s) completes only after the producer saw empty(s): the
+            // MMAs that read this stage's A before have retired)
             if (!mbar_wait(full_raw(s), ph)) { failed = true; break; }
             const uint32_t st = sbase + (uint32_t)s * SB;
 #pragma unroll
             for (int ms = 0; ms < MSUB; ++ms) {
                 const uint8_t *raw = sgen + s * SB + RAW + ms * RAW_BYTES;
-                if (args.mode == MODE_FWD) expand_fwd(raw, st + a_off(ms), t);
-                else expand_bwd(raw, st + a_off(ms), t);
+                if (AT) {
+                    uint32_t o[32];
+                    expand_bwd_regs(raw, t, o);
+                    tmem_st32(tmem_base + ((uint32_t)(32 * (warp & 3)) << 16) + C::ACC_COLS +
+                                  (uint32_t)((s * MSUB + ms) * (BK / 2)),
+                              o);
+                } else if (args.mode == MODE_FWD) {
+                    expand_fwd(raw, st + a_off(ms), t);
+                } else {
+                    expand_bwd(raw, st + a_off(ms), t);
+                }
             }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            if (AT) {
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            } else {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            }
             mbar_arrive(full_a(s));
         }
         // epilogue
@@ -701,16 +805,40 @@ int msub_choice()
     return v;
 }
 
-template <int MSUB, int STG, int NT = 1>
+template <int MSUB, int STG, int NT = 1, bool AT = false>
 void launch_gemm(dim3 grid, const CUtensorMap &a, const CUtensorMap &bh, const CUtensorMap &bl,
                  const tc::GemmArgs &args, cudaStream_t st)
 {
-    tc::k_gemm<MSUB, STG, NT><<<grid, tc::THREADS, tc::Cfg<MSUB, STG, NT>::SMEM_BYTES, st>>>(a, bh, bl, args);
+    tc::k_gemm<MSUB, STG, NT, AT>
+        <<<grid, tc::THREADS, tc::Cfg<MSUB, STG, NT, AT>::SMEM_BYTES, st>>>(a, bh, bl, args);
+}
+
+// The backward with hi + lo operands (the tensor-core form's gradient, the
+// dual form's max-norm checks) keeps its one-hot A in TMEM: two subtiles,
+// four stages of 36 KB, the MMAs' N fitted to the live columns.  Measured
+// with ncu on the 3000 x 94,000 workload (192-slot check launches): 337-375
+// against 426-439 us for A in shared memory.  Exact (hi-only) operands -- the
+// dual form's solution digit planes, two N tiles per CTA -- stay with A in
+// shared memory: the TMEM form with one subtile and six stages took 689
+// against 607 us there.  SDCA_TC_BWD_SMEM_A=1 keeps A in shared memory
+// everywhere.
+bool bwd_tmem_a()
+{
+    static const bool v = [] {
+        const char *e = std::getenv("SDCA_TC_BWD_SMEM_A");
+        return !(e && e[0] == '1');
+    }();
+    return v;
 }
 
 void launch_gemm_any(int msub, int m_tiles, int n_tiles, int splits, const CUtensorMap &a, const CUtensorMap &bh,
                      const CUtensorMap &bl, const tc::GemmArgs &args, cudaStream_t st)
 {
+    if (args.mode == tc::MODE_BWD && !args.hi_only && bwd_tmem_a()) {
+        const dim3 grid((unsigned)((m_tiles + 1) / 2), (unsigned)n_tiles, (unsigned)splits);
+        launch_gemm<2, 4, 1, true>(grid, a, bh, bl, args, st);
+        return;
+    }
     if (args.hi_only && args.mode == tc::MODE_BWD) {
         // exact fp16 operands: two N tiles per CTA, two subtiles, three stages
         const dim3 grid((unsigned)((m_tiles + 1) / 2), (unsigned)((n_tiles + 1) / 2), (unsigned)splits);
@@ -926,6 +1054,9 @@ cudaError_t tc_configure()
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(tc::k_gemm<1, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  tc::Cfg<1, 4>::SMEM_BYTES);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(tc::k_gemm<2, 4, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc::Cfg<2, 4, 1, true>::SMEM_BYTES);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(tc::k_kdig, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::KD_SMEM);
     return e;
