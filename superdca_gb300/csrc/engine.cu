@@ -1328,11 +1328,14 @@ int dual_ctl_begin(sdca_handle *h, int b)
 // the logits K a_x are O(1) while sum_j |K_ij a_j| is hundreds, so a
 // rounding of a in the last bits of single precision would move the gradient
 // at the reported x by far more than the threshold.  A tensor-core pass
-// costs the same for 1 and for 32 slots, so stopped slots wait until 16 of
-// them are ready or no slot is still iterating (`force`: now).
+// costs about the same for 1 and for 21 slots (its CTAs take two 128-column
+// N tiles, 64 slot-planes: 21 slots' three planes), so stopped slots wait
+// until 21 of them are ready or no slot is still iterating (`force`: now),
+// and a pass takes whole groups of 21 while it can.
 int dual_convert(sdca_handle *h, bool force)
 {
     const Problem &P = h->P;
+    constexpr int GROUP = 21;
     std::vector<int32_t> fin;
     int active = 0;
     for (int b = 0; b < P.Bmax; ++b) {
@@ -1340,11 +1343,12 @@ int dual_convert(sdca_handle *h, bool force)
         if (ph == PH_CONVERT) fin.push_back(b);
         else if (ph != PH_EMPTY && ph != PH_FINALIZE) ++active;
     }
-    if (fin.empty() || (!force && active > 0 && (int)fin.size() < std::min(16, P.Bmax))) return SDCA_OK;
+    if (fin.empty() || (!force && active > 0 && (int)fin.size() < std::min(GROUP, P.Bmax))) return SDCA_OK;
     // the three digit planes of up to Bmax / 3 slots go through one tensor-core
     // pass (the one-hot operand is streamed once for all of them)
     const int per_pass = P.Bmax / 3;
     if (per_pass >= 1 && (int)fin.size() > per_pass) fin.resize(per_pass);
+    if (!force && active > 0 && (int)fin.size() > GROUP) fin.resize(fin.size() / GROUP * GROUP);
     for (int b : fin) {
         const SlotHost &S = h->slots[b];
         h->sd_h[b].tc_scale = S.amax_x > 0.0 ? std::ldexp(1.0, 32) / S.amax_x : 1.0;
