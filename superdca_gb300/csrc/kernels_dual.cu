@@ -279,10 +279,14 @@ k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
 // formed (buffer 1 - gcur) instead of the accepted one.  (The dots with the
 // newest y follow in the control kernel from these and the previous
 // iteration's: S^T y = S^T g - S^T g_old.)
-// A block takes DOT_CHUNK entries of one slot: k_g staged in shared memory,
-// each warp one history vector at a time, 16-byte loads (one accumulator
-// per lane).
+// A block takes DOT_CHUNK entries of one slot: k_g staged in shared memory;
+// the work is cut into (history vector, quarter of the chunk) units, taken
+// by the warps in turn, so every warp gets the same number of units whatever
+// the history length (8k units for 8 warps); 16-byte loads, eight in flight
+// per lane, one accumulator per lane.
 constexpr int DOT_CHUNK = 2048;
+constexpr int DOT_SUBS = 4;                       // units per vector and chunk
+constexpr int DOT_SUB_Q = DOT_CHUNK / 2 / DOT_SUBS;   // float4 pairs per unit (256)
 
 __global__ void __launch_bounds__(256)
 k_dual_dots(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, int64_t Nx, int NV, int ring,
@@ -303,14 +307,16 @@ k_dual_dots(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
     for (int t = threadIdx.x; t < nq; t += blockDim.x) g[t] = reinterpret_cast<const float4 *>(kg)[t];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int qv = warp; qv < 2 * k; qv += nw) {
+    for (int u = warp; u < 2 * k * DOT_SUBS; u += nw) {
+        const int qv = u / DOT_SUBS, t0 = (u % DOT_SUBS) * DOT_SUB_Q;
         const bool isy = qv >= k;
         const int j = isy ? qv - k : qv;
         const int pos = j < S.nhist ? S.hist[j] : S.ring_new;
         const float4 *v = reinterpret_cast<const float4 *>(dv + dvo(b, DV_S + (isy ? ring : 0) + pos, 0, NV, Nx) + e0);
+        const int t1 = min(nq, t0 + DOT_SUB_Q);
         float2 acc = df_zero();
 #pragma unroll 8
-        for (int t = lane; t < nq; t += 32) {
+        for (int t = t0 + lane; t < t1; t += 32) {
             const float4 x = v[t], y = g[t];
             acc = df_fma(make_float2(x.x, x.y), make_float2(y.x, y.y), acc);
             acc = df_fma(make_float2(x.z, x.w), make_float2(y.z, y.w), acc);
