@@ -1,12 +1,14 @@
 """Parity at the headline shape: the 3000-sequence x 94,000-locus tree
-workload, solved with the bench's own configuration (dual form, 4 solver
-lanes x 512 slots), against the FP64 oracle.
+workload, solved in the dual form against the FP64 oracle, from zero with 4
+solver lanes x 512 slots, and with the bench's default configuration: the
+committed learned start and 3 lanes x 1280 slots (the shape the autotuner
+picks there).
 
 SuperDCA solves each locus from zero to max|g| < 1e-3
 (SuperDCA/include/plmDCA.hpp:298-307).  Eight loci whose FP64 oracle solves
 are committed (oracle/nfeval_tree-3000x94000.json: objective at the oracle's
-own optimum) sit late in a queue of 2560 loci, so they enter slots that
-earlier loci have left (retire and refill).  For each: the FP64 oracle's
+own optimum) sit late in a queue of 1.25 x the slots, so they enter slots
+that earlier loci have left (retire and refill).  For each: the FP64 oracle's
 objective at the engine's returned parameters equals the engine's reported
 objective within 1e-6 relative; the oracle's gradient there has max-norm
 below 1.05e-3; and the objective lies within 1e-5 relative of the oracle's
@@ -23,7 +25,8 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def test_headline_shape_against_fp64_oracle():
+@pytest.mark.parametrize("batch,lanes,learned", [(512, 4, False), (1280, 3, True)])
+def test_headline_shape_against_fp64_oracle(batch, lanes, learned):
     from concurrent.futures import ThreadPoolExecutor
 
     from oracle import oracle as O
@@ -36,18 +39,22 @@ def test_headline_shape_against_fp64_oracle():
     assert (N, L) == (ref["N"], ref["L"])
     w = np.ones(N)
     target = np.array(ref["loci"], dtype=np.int64)
-    # a queue of 2560 loci (the 4 x 512 slots fill once, then refill), the
-    # checked loci at positions past the first fill
+    # a queue of 1.25 x the slots (they fill once, then refill), the checked
+    # loci at positions past the first fill
+    slots = batch * lanes
+    nq = slots + slots // 4
     rng = np.random.default_rng(11)
-    others = rng.choice(np.setdiff1d(np.arange(L), target), 2560 - len(target), replace=False)
-    pos = np.sort(rng.choice(np.arange(2100, 2560), len(target), replace=False))
-    queue = np.empty(2560, dtype=np.int64)
-    mask = np.zeros(2560, dtype=bool)
+    others = rng.choice(np.setdiff1d(np.arange(L), target), nq - len(target), replace=False)
+    pos = np.sort(rng.choice(np.arange(slots + 20, nq), len(target), replace=False))
+    queue = np.empty(nq, dtype=np.int64)
+    mask = np.zeros(nq, dtype=bool)
     mask[pos] = True
     queue[mask] = target
     queue[~mask] = others
-    with Engine(N, L, batch=512, lanes=4, form=FORM_DUAL) as E:
+    with Engine(N, L, batch=batch, lanes=lanes, form=FORM_DUAL) as E:
         E.set_alignment(states, w)
+        if learned:
+            E.set_warm_start(np.load(os.path.join(ROOT, "superdca_gb300", "warmstart_dual_tree-3000x94000.npy")))
         res = E.solve(queue, x_positions=pos, want_scores=False)
         lh, lJ, _ = E.lambdas()
     assert np.all(res.status == 0), np.unique(res.status, return_counts=True)
@@ -65,7 +72,7 @@ def test_headline_shape_against_fp64_oracle():
     f_opt = np.array(ref["f"])
     rel_x = np.abs(f_eng - f_orc) / np.abs(f_orc)
     rel_opt = np.abs(f_eng - f_opt) / np.abs(f_opt)
-    print(f"\nheadline shape: max rel |f - f_oracle(x)| {rel_x.max():.2e}, max oracle |g| {gmax.max():.3e}, "
+    print(f"\nheadline shape ({lanes} x {batch}, learned start {learned}): max rel |f - f_oracle(x)| {rel_x.max():.2e}, max oracle |g| {gmax.max():.3e}, "
           f"max rel |f - f_oracle_opt| {rel_opt.max():.2e}, iterations {res.iterations[pos].tolist()} "
           f"(oracle {ref['iterations']})")
     assert rel_x.max() <= 1e-6
