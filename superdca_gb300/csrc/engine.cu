@@ -167,7 +167,6 @@ struct sdca_handle {
     double refresh_factor = 8.0;
     int refresh_every = 30;
     int tc_refresh_every = 5;   // tensor-core form: recompute logits every this many accepted steps
-    std::vector<int> trace_loci;  // SDCA_TRACE=<locus>[,<locus>...]: per-iteration solver state on stderr
 
     // dual form (kernels_dual.cu)
     float2 *dv = nullptr, *KR = nullptr;   // coefficient vectors and K rho, double-float (df.cuh)
@@ -2068,13 +2067,6 @@ static int create_lane(const sdca_config *cfg, const sdca_handle *owner, sdca_ha
     if (const char *e = std::getenv("SDCA_REFRESH_EVERY")) h->refresh_every = std::max(1, std::atoi(e));
     if (const char *e = std::getenv("SDCA_REFRESH_FACTOR")) h->refresh_factor = std::atof(e);
     if (const char *e = std::getenv("SDCA_TC_REFRESH_EVERY")) h->tc_refresh_every = std::max(1, std::atoi(e));
-    if (const char *e = std::getenv("SDCA_TRACE")) {
-        for (const char *p = e; *p;) {
-            h->trace_loci.push_back(std::atoi(p));
-            while (*p && *p != ',') ++p;
-            if (*p == ',') ++p;
-        }
-    }
     h->slots.resize(P.Bmax);
     int rc = SDCA_OK;
     const size_t B = P.Bmax;
