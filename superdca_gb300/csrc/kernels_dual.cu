@@ -193,30 +193,40 @@ k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
     const bool step = S.phase == DC_STEP;   // searched this round: accept first
     const bool push = S.push && S.ring_new >= 0;
     const float2 sf = S.stp_df;
-    const int64_t part = Nx * 4;
-    float2 *ax = dv + dvo(b, DV_X, 0, NV, Nx), *kx = ax + part;
-    const float2 *ad = dv + dvo(b, DV_D, 0, NV, Nx), *kd = ad + part;
-    const float2 *ago = dv + dvo(b, DV_G + S.gcur, 0, NV, Nx), *kgo = ago + part;
-    float2 *agn = dv + dvo(b, DV_G + 1 - S.gcur, 0, NV, Nx), *kgn = agn + part;
+    // the slot's vectors as entry pairs (float4) from one base, each part at
+    // a 32-bit offset (a part; its k part follows at + P): fewer registers
+    // than a pointer per stream, so more blocks fit on an SM
+    const int P = (int)(Nx * 2);
+    float4 *base = reinterpret_cast<float4 *>(dv + dvo(b, 0, 0, NV, Nx));
     const int ps = push ? S.ring_new : 0;
-    float2 *as = dv + dvo(b, DV_S + ps, 0, NV, Nx), *ks = as + part;
-    float2 *ay = dv + dvo(b, DV_S + ring + ps, 0, NV, Nx), *ky = ay + part;
+    const int o_x = DV_X * 2 * P, o_d = DV_D * 2 * P, o_go = (DV_G + S.gcur) * 2 * P,
+              o_gn = (DV_G + 1 - S.gcur) * 2 * P, o_s = (DV_S + ps) * 2 * P, o_y = (DV_S + ring + ps) * 2 * P;
     const int2 *rq2 = reinterpret_cast<const int2 *>(rq + (int64_t)b * Nx * 4);
-    const float2 *KRb = KR + (int64_t)b * Nx * 4;
+    const float4 *KRb = reinterpret_cast<const float4 *>(KR + (int64_t)b * Nx * 4);
+    auto ld = [&](int o, int t, float2 (&v)[2]) {
+        const float4 q = base[o + t];
+        v[0] = make_float2(q.x, q.y);
+        v[1] = make_float2(q.z, q.w);
+    };
+    auto st = [&](int o, int t, const float2 (&v)[2]) { base[o + t] = make_float4(v[0].x, v[0].y, v[1].x, v[1].y); };
     float2 g2 = df_zero(), x2 = df_zero(), sy = df_zero(), yy = df_zero(), ss = df_zero();
     float mg = 0.f, mx = 0.f;
     // entry pairs (2t, 2t+1): 16-byte loads of every stream
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < Nx * 2; t += (int64_t)gridDim.x * blockDim.x) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x) {
         float2 a_x[2], k_x[2], kr[2], a_g[2], k_g[2], a_s[2], k_s[2];
-        df2_load(ax, t, a_x);
-        df2_load(kx, t, k_x);
-        df2_load(KRb, t, kr);
+        ld(o_x, t, a_x);
+        ld(o_x + P, t, k_x);
+        {
+            const float4 q = KRb[t];
+            kr[0] = make_float2(q.x, q.y);
+            kr[1] = make_float2(q.z, q.w);
+        }
         const int2 r2 = rq2[t];
         const int rr[2] = {r2.x, r2.y};
         if (step) {
             float2 a_d[2], k_d[2];
-            df2_load(ad, t, a_d);
-            df2_load(kd, t, k_d);
+            ld(o_d, t, a_d);
+            ld(o_d + P, t, k_d);
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
                 const float2 a1 = df_fma(sf, a_d[q], a_x[q]), k1 = df_fma(sf, k_d[q], k_x[q]);
@@ -225,15 +235,15 @@ k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
                 a_x[q] = a1;
                 k_x[q] = k1;
             }
-            df2_store(ax, t, a_x);
-            df2_store(kx, t, k_x);
+            st(o_x, t, a_x);
+            st(o_x + P, t, k_x);
             if (push) {
-                df2_store(as, t, a_s);
-                df2_store(ks, t, k_s);
+                st(o_s, t, a_s);
+                st(o_s + P, t, k_s);
             }
         } else if (push) {
-            df2_load(as, t, a_s);
-            df2_load(ks, t, k_s);
+            ld(o_s, t, a_s);
+            ld(o_s + P, t, k_s);
         }
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
@@ -246,8 +256,8 @@ k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
         }
         if (push) {
             float2 a_o[2], k_o[2], a_y[2], k_y[2];
-            df2_load(ago, t, a_o);
-            df2_load(kgo, t, k_o);
+            ld(o_go, t, a_o);
+            ld(o_go + P, t, k_o);
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
                 a_y[q] = df_sub(a_g[q], a_o[q]);
@@ -256,11 +266,11 @@ k_dual_grad(const DualCtl *__restrict__ ctl, const int32_t *__restrict__ list, i
                 yy = df_fma(a_y[q], k_y[q], yy);
                 ss = df_fma(a_s[q], k_s[q], ss);
             }
-            df2_store(ay, t, a_y);
-            df2_store(ky, t, k_y);
+            st(o_y, t, a_y);
+            st(o_y + P, t, k_y);
         }
-        df2_store(agn, t, a_g);
-        df2_store(kgn, t, k_g);
+        st(o_gn, t, a_g);
+        st(o_gn + P, t, k_g);
     }
     float2 v[5] = {g2, x2, sy, yy, ss};
     const int idx[5] = {ACC_G2, ACC_X2J, ACC_SY, ACC_YY, ACC_SS};
