@@ -49,3 +49,24 @@ def test_top_overlap_counts_shared_strongest_pairs():
     assert bench.top_overlap(a, b, k=2) == 1.0          # {0, 1} in both
     assert bench.top_overlap(a, b, k=3) == 2 / 3        # {0, 1, 2} vs {0, 1, 4}
     assert bench.top_overlap(a, a, k=10) == 1.0         # k above the length: all pairs
+
+
+def test_whole_solve_roofline_counts_every_class():
+    """The whole-solve figure sums the HBM classes' algorithmic bytes per
+    slot-iteration ((2k + 1) + (4k + 7) + 15.5 + 1 + trials x (1.5 + 9/32)
+    parts of 32 N bytes) and the tensor classes' FLOP, over the device time."""
+    keys = ["forward", "backward", "linesearch", "history", "direction", "accept", "score", "other"]
+    tot = {"kernel_ms": {k: 1.0 for k in keys}, "kernel_units": {k: 0 for k in keys},
+           "kernel_launches": {k: 1 for k in keys}}
+    N, L, m, trials = 3000, 94000, 10, 6.0
+    tot["kernel_units"]["history"] = 100
+    tot["kernel_units"]["forward"] = 100
+    tot["kernel_units"]["backward"] = 2
+    ws = bench.whole_solve_dual(tot, N, L, m, trials, 2.0)
+    parts = (2 * m + 1) + (4 * m + 7) + 15.5 + 1 + trials * (1.5 + 9 / 32)
+    assert ws["hbm_bytes_per_slot_iteration"] == round(parts * 32 * N)
+    assert abs(ws["hbm_achieved_gbs"] - round(100 * parts * 32 * N / 2.0 / 1e9, 1)) < 0.11
+    flop = 100 * 2.0 * N * N * 3 + 2 * 2.0 * N * L * 16
+    assert abs(ws["tensor_achieved_tflops"] - round(flop / 2.0 / 1e12, 2)) < 0.011
+    hbm, tflops, _ = bench.measured_peaks()
+    assert abs(ws["hbm_frac"] - ws["hbm_achieved_gbs"] / hbm) < 1e-3
