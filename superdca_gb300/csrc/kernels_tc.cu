@@ -16,11 +16,15 @@
 //     128-byte-swizzled K-major layout the MMA reads (the one-hot matrix never
 //     exists in HBM: 1 byte per locus is read instead of 8), fence to the async
 //     proxy, arrive on full_a[s];
-//   * warp 1, one thread: tcgen05.mma kind::f16 (M128 N256 K16, FP32
-//     accumulators in TMEM): the B tile stacks B_hi on B_lo, so one MMA forms
-//     A x B_hi and A x B_lo side by side; tcgen05.commit frees the stage;
+//   * warp 1, one thread: tcgen05.mma kind::f16 (M128 N128 K16, FP32
+//     accumulators in TMEM): A x B_hi and then A x B_lo into the same
+//     accumulator (or, with exact fp16 operands, a second N tile in the lo
+//     slot); tcgen05.commit frees the stage;
 //   * warps 2-5 again: tcgen05.ld the accumulator and store it, scaled back
 //     by the per-slot power of two.
+// With hi + lo operands the backward keeps the expanded A tiles in TMEM
+// instead (tcgen05.st by the expansion warps, MMAs reading A from TMEM; see
+// Cfg below).
 // B is split as hi + lo fp16 halves of (value * 2^e) so that the product keeps
 // about 22 significant bits; the one-hot A is exact in fp16.
 //
