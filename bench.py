@@ -89,7 +89,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the autotuner (default when --batch/--lanes are not given: measure them on a "
                          "probe list of loci outside the timed steps)")
-    ap.add_argument("--tune-loci", type=int, default=46080, help="loci the autotuner may solve as probes")
+    ap.add_argument("--tune-loci", type=int, default=57856, help="loci the autotuner may solve as probes")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the skewed 616 x 78,700 workload measured after the headline")
     ap.add_argument("--no-cpu", action="store_true")

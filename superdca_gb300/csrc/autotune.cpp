@@ -37,8 +37,8 @@ std::vector<Candidate> candidates(int form)
 {
     if (form == SDCA_FORM_DUAL)
         // largest first: on a small list the ones its probe budget cannot fill are skipped
-        return {{1536, 3}, {1280, 3}, {1024, 3}, {1024, 4}, {1536, 2}, {768, 3}, {1024, 2}, {512, 4},
-                {512, 2}, {256, 4}, {256, 2}, {512, 1}};
+        return {{2048, 4}, {2048, 3}, {1536, 4}, {1536, 3}, {1280, 3}, {1024, 3}, {1024, 4}, {1536, 2}, {768, 3},
+                {1024, 2}, {512, 4}, {512, 2}, {256, 4}, {256, 2}, {512, 1}};
     return {{64, 1}, {32, 2}, {64, 2}, {128, 1}, {32, 1}};
 }
 
