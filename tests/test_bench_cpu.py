@@ -70,3 +70,30 @@ def test_whole_solve_roofline_counts_every_class():
     assert abs(ws["tensor_achieved_tflops"] - round(flop / 2.0 / 1e12, 2)) < 0.011
     hbm, tflops, _ = bench.measured_peaks()
     assert abs(ws["hbm_frac"] - ws["hbm_achieved_gbs"] / hbm) < 1e-3
+
+
+def test_clocks_summary_reads_throttle_reasons_and_utilisation(tmp_path):
+    """The nvidia-smi sampler's summary: median SM clock under load, the
+    throttle reasons seen, and the kernel-occupancy column (utilization.gpu)."""
+
+    class Done:
+        def terminate(self):
+            pass
+
+        def wait(self, timeout=None):
+            return 0
+
+        def kill(self):
+            pass
+
+    path = tmp_path / "clocks.csv"
+    path.write_text("0, 2070, 2070, 900.5, 0x0, Not Active, Not Active, Not Active, Not Active, 100\n"
+                    "0, 2070, 2070, 1390.0, 0x4, Not Active, Not Active, Not Active, Active, 93\n"
+                    "0, 600, 2070, 120.0, 0x0, Not Active, Not Active, Not Active, Not Active, 0\n")
+    c = bench.Clocks(0)
+    c.proc, c.path = Done(), str(path)
+    out = c.stop()
+    assert out["sm_mhz"] == 2070.0 and out["sm_max_mhz"] == 2070.0 and out["samples"] == 3
+    assert out["reasons"] == ["sw_power_cap"]
+    assert out["gpu_util_pct"] == {"median": 93.0, "min": 0.0}
+    assert not path.exists()
