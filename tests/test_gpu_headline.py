@@ -1,8 +1,7 @@
 """Parity at the headline shape: the 3000-sequence x 94,000-locus tree
 workload, solved in the dual form against the FP64 oracle, from zero with 4
-solver lanes x 512 slots, and with the bench's default configuration: the
-committed learned start and 3 lanes x 1280 slots (the shape the autotuner
-picks there).
+solver lanes x 512 slots, and as the bench runs it: the committed learned
+start, 3 lanes x 1280 slots (one of the shapes the autotuner picks there).
 
 SuperDCA solves each locus from zero to max|g| < 1e-3
 (SuperDCA/include/plmDCA.hpp:298-307).  Eight loci whose FP64 oracle solves
