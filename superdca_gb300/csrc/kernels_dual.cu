@@ -11,7 +11,7 @@
 // image is K a_v + eta_v and inner products are a_v . K a_w + eta_v . eta_w.
 // So the same iteration runs on N x 4 coefficients; a vector is kept as the
 // pair (a, k = K a) in double-float (df.cuh: ~48 bits on the FP32 pipe) and
-// its eta on the host.
+// its eta (4 values, FP64) in the slot's device state (DualCtl).
 //
 // The one product per iteration, K rho, is exact: rho is rounded to integers
 // rho_q = round(rho * 2^QB / w_max) (the rounded value is the one used, so
